@@ -1,0 +1,160 @@
+/*
+ * wbgpu.h -- C ABI of the GB300 (sm_103a) distance library.
+ *
+ * Drop-in boundary for wildboar's distance hot path.  Each entry point
+ * replaces one Cython driver of the reference (wildboar src/wildboar/distance/
+ * _cdistance.pyx) and is reached from Python through ctypes
+ * (wildboar_gb300/_lib.py).  Plain pointers and sizes only.
+ *
+ * Conventions
+ *  - Every function returns an int status (WB_OK = 0); the message of the
+ *    last failure on the calling thread is wb_last_error().
+ *  - Series are (n, n_dims, n_timestep) row-major arrays, as produced by the
+ *    reference's _check_ts_array (utils/validation.py:594-620).  `on_device`
+ *    says whether `data` is a host pointer (copied in by the library) or a
+ *    CUDA device pointer (used in place).
+ *  - Outputs follow `out_on_device` the same way.  Host outputs are complete
+ *    when the call returns; device outputs are ordered on `stream`.
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).
+ *  - The caller owns every buffer it passes.  The library owns a per-stream
+ *    device workspace that grows on demand and is released by
+ *    wb_release_workspace().
+ */
+#ifndef WBGPU_H
+#define WBGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define WB_OK 0
+#define WB_EINVAL 1      /* bad argument: maps to ValueError */
+#define WB_ENOMEM 2      /* device allocation failed: maps to MemoryError */
+#define WB_ECUDA 3       /* CUDA runtime error: maps to RuntimeError */
+#define WB_ETIMEOUT 4    /* a bounded device wait gave up */
+#define WB_EUNSUPPORTED 5
+
+/* metric ids (same numbering as the oracle) */
+#define WB_EUCLIDEAN 0
+#define WB_DTW 1
+#define WB_WDTW 2
+#define WB_DDTW 3
+#define WB_WDDTW 4
+#define WB_ADTW 5
+#define WB_LCSS 6
+#define WB_WLCSS 7
+#define WB_EDR 8
+#define WB_ERP 9
+#define WB_MSM 10
+#define WB_TWE 11
+#define WB_SCALED_EUCLIDEAN 32
+
+/* dtypes */
+#define WB_F64 0
+#define WB_F32 1
+
+typedef struct wb_series {
+    const void *data;   /* (n, n_dims, n_timestep) row-major */
+    int64_t n;
+    int64_t n_dims;
+    int64_t n_timestep;
+    int32_t dtype;      /* WB_F64 (the drop-in) or WB_F32 (batched forms) */
+    int32_t on_device;  /* 0: host pointer, 1: device pointer */
+} wb_series;
+
+/* Union of the reference metric constructor arguments
+ * (distance/_elastic.pyx:3133-4006).  Unused fields are ignored. */
+typedef struct wb_params {
+    double r;          /* band as a fraction of the shorter length, [0, 1] */
+    double g;          /* wdtw/wddtw/wlcss weight steepness; erp gap value */
+    double p;          /* adtw penalty */
+    double epsilon;    /* lcss/edr match threshold; NaN = edr per-pair default */
+    double c;          /* msm split/merge cost */
+    double penalty;    /* twe penalty (lambda) */
+    double stiffness;  /* twe stiffness (nu) */
+} wb_params;
+
+/*
+ * pairwise distance of every x[i, dim] and y[j, dim]: out is (x.n, y.n).
+ * y == NULL is the reference's singleton path (x is y): strict upper
+ * triangle computed, mirrored, zero diagonal.
+ * Replaces _pairwise_distance / _singleton_pairwise_distance
+ * (distance/_cdistance.pyx:1184-1267) and the per-pair Metric.distance calls
+ * of the elastic metric classes (distance/_elastic.pyx:3126-4082) and
+ * EuclideanMetric (distance/_metric.pyx:381-409).
+ */
+int wb_pairwise_distance(const wb_series *x, const wb_series *y, int64_t dim,
+                         int32_t metric, const wb_params *params, double *out,
+                         int32_t out_on_device, void *stream);
+
+/*
+ * paired distance of x[i, dim] and y[i, dim]: out is (x.n,).  As in the
+ * reference the metric receives (y[i], x[i]): the rows of the recurrence come
+ * from the second argument.  Replaces _paired_distance
+ * (distance/_cdistance.pyx:1597-1652).
+ */
+int wb_paired_distance(const wb_series *x, const wb_series *y, int64_t dim,
+                       int32_t metric, const wb_params *params, double *out,
+                       int32_t out_on_device, void *stream);
+
+/*
+ * k nearest y rows of every x row (dim must be 0 in the public API; any dim is
+ * accepted here).  indices/distances are (x.n, k) in the reference's heap
+ * order, including its early-abandoning decisions.  lower_bound is NULL or a
+ * (x.n, y.n) matrix on the same side as the outputs.  Replaces
+ * _argmin_distance (distance/_cdistance.pyx:1270-1378) and the Heap of
+ * utils/_misc.pyx:18-107.
+ */
+int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_t dim,
+                       int32_t metric, const wb_params *params, int64_t k,
+                       const double *lower_bound, int64_t *indices, double *distances,
+                       int32_t out_on_device, void *stream);
+
+/*
+ * minimum subsequence distance and first argmin window of every shapelet
+ * against every x[i, dim]: out_dist / out_idx are (x.n, m).  Shapelets are
+ * packed float64 values; offsets/lengths index them.  means/stds are the
+ * np.mean / np.std of each shapelet (std <= 1e-13 given as 0), used by the
+ * scaled metric only.  metric is WB_EUCLIDEAN or WB_SCALED_EUCLIDEAN.
+ * Shapelet arrays live on the same side as x.  Replaces
+ * _pairwise_subsequence_distance (distance/_cdistance.pyx:956-1037) with
+ * euclidean_distance / scaled_euclidean_distance (distance/_metric.pyx:561-682).
+ */
+int wb_pairwise_subsequence_distance(const double *shapelets, const int64_t *offsets,
+                                     const int64_t *lengths, const double *means,
+                                     const double *stds, int64_t m, const wb_series *x,
+                                     int64_t dim, int32_t metric, double *out_dist,
+                                     int64_t *out_idx, int32_t out_on_device,
+                                     void *stream);
+
+/* message of the last failed call on this thread ("" if none) */
+const char *wb_last_error(void);
+
+/* library ABI version */
+int32_t wb_version(void);
+
+/* free the workspace the library holds for `stream` (NULL: all streams) */
+int wb_release_workspace(void *stream);
+
+/* number of kernel launches issued by this process (diagnostics) */
+int64_t wb_launch_count(void);
+
+/* Diagnostics (no counterpart in the reference): when enabled, the main
+ * kernel of each call is bracketed by CUDA events on the call's stream and
+ * wb_profile_last() returns its device time in ms (-1 if none). */
+int wb_profile_enable(int32_t on);
+int wb_profile_last(double *ms);
+
+/* Diagnostics: sustained add+mul throughput of the FP64 (dtype WB_F64) or
+ * FP32 (WB_F32) pipes of the current device, in operations per second; the
+ * roofline peak of the ALU-bound recurrence kernels. */
+int wb_alu_probe(int32_t dtype, int32_t iters, double *ops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WBGPU_H */

@@ -1,0 +1,249 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+Loaded by tests/, ``__graft_entry__.smoke()`` and bench.py's CPU legs; the
+product package never imports this module.  The functions mirror the
+reference's Cython entry points (``_pairwise_distance``,
+``_singleton_pairwise_distance``, ``_paired_distance``, ``_argmin_distance``,
+``_pairwise_subsequence_distance`` in wildboar's distance/_cdistance.pyx) on
+(n_samples, n_dims, n_timestep) float64 arrays.
+"""
+
+import ctypes
+import math
+import os
+
+import numpy as np
+
+from . import build as _build
+
+METRIC_IDS = {
+    "euclidean": 0,
+    "dtw": 1,
+    "wdtw": 2,
+    "ddtw": 3,
+    "wddtw": 4,
+    "adtw": 5,
+    "lcss": 6,
+    "wlcss": 7,
+    "edr": 8,
+    "erp": 9,
+    "msm": 10,
+    "twe": 11,
+    "scaled_euclidean": 32,
+}
+
+# Constructor defaults of the reference metric classes
+# (distance/_elastic.pyx:3133, 3231, 3325, 3407, 3347, 3440, 3545, 3574, 3681,
+# 3895, 3995).
+DEFAULTS = {
+    "euclidean": {},
+    "dtw": {"r": 1.0},
+    "ddtw": {"r": 1.0},
+    "wdtw": {"r": 1.0, "g": 0.05},
+    "wddtw": {"r": 1.0, "g": 0.05},
+    "adtw": {"r": 1.0, "p": 1.0},
+    "lcss": {"r": 1.0, "epsilon": 1.0},
+    "wlcss": {"r": 1.0, "epsilon": 1.0, "g": 0.05},
+    "erp": {"r": 1.0, "g": 0.0},
+    "edr": {"r": 1.0, "epsilon": math.nan},
+    "msm": {"r": 1.0, "c": 1.0},
+    "twe": {"r": 1.0, "penalty": 1.0, "stiffness": 0.001},
+    "scaled_euclidean": {},
+}
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("r", ctypes.c_double),
+        ("g", ctypes.c_double),
+        ("p", ctypes.c_double),
+        ("epsilon", ctypes.c_double),
+        ("c", ctypes.c_double),
+        ("penalty", ctypes.c_double),
+        ("stiffness", ctypes.c_double),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = ctypes.CDLL(path)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int64)
+        i64 = ctypes.c_int64
+        pp = ctypes.POINTER(Params)
+        L.wbo_pairwise.argtypes = [dp, i64, i64, i64, dp, i64, i64, i64, i64,
+                                   ctypes.c_int, pp, dp, ctypes.c_int]
+        L.wbo_paired.argtypes = [dp, dp, i64, i64, i64, i64, i64, ctypes.c_int, pp,
+                                 dp, ctypes.c_int]
+        L.wbo_argmin.argtypes = [dp, i64, i64, i64, dp, i64, i64, i64, i64,
+                                 ctypes.c_int, pp, i64, dp, ip, dp, ctypes.c_int]
+        L.wbo_subsequence.argtypes = [dp, ip, ip, dp, dp, i64, dp, i64, i64, i64, i64,
+                                      ctypes.c_int, dp, ip, ctypes.c_int]
+        L.wbo_distance_1d.argtypes = [dp, i64, dp, i64, ctypes.c_int, pp]
+        L.wbo_distance_1d.restype = ctypes.c_double
+        L.wbo_fast_mean_std.argtypes = [dp, i64, dp, dp]
+        L.wbo_dtw_alignment.argtypes = [dp, i64, dp, i64, i64, dp, dp]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+
+def make_params(metric, metric_params=None):
+    p = dict(DEFAULTS[metric])
+    p.update(metric_params or {})
+    s = Params()
+    s.r = p.get("r", 1.0)
+    s.g = p.get("g", 0.0)
+    s.p = p.get("p", 1.0)
+    s.epsilon = p.get("epsilon", math.nan)
+    s.c = p.get("c", 1.0)
+    s.penalty = p.get("penalty", 1.0)
+    s.stiffness = p.get("stiffness", 0.001)
+    return s
+
+
+def _ts(x):
+    x = np.asarray(x, dtype=np.float64)
+    if x.ndim == 1:
+        x = x.reshape(1, 1, -1)
+    elif x.ndim == 2:
+        x = x.reshape(x.shape[0], 1, x.shape[1])
+    return np.ascontiguousarray(x)
+
+
+def n_threads_default():
+    return os.cpu_count() or 1
+
+
+def pairwise(x, y=None, *, dim=0, metric="dtw", metric_params=None, n_threads=1):
+    """One-dim pairwise distance matrix; y=None is the singleton (x is y) path."""
+    X = _ts(x)
+    p = make_params(metric, metric_params)
+    if y is None:
+        out = np.zeros((X.shape[0], X.shape[0]))
+        lib().wbo_pairwise(_dp(X), X.shape[0], X.shape[1], X.shape[2], None, 0, 0, 0,
+                           dim, METRIC_IDS[metric], ctypes.byref(p), _dp(out), n_threads)
+        return out
+    Y = _ts(y)
+    out = np.empty((X.shape[0], Y.shape[0]))
+    lib().wbo_pairwise(_dp(X), X.shape[0], X.shape[1], X.shape[2], _dp(Y), Y.shape[0],
+                       Y.shape[1], Y.shape[2], dim, METRIC_IDS[metric], ctypes.byref(p),
+                       _dp(out), n_threads)
+    return out
+
+
+def paired(x, y, *, dim=0, metric="dtw", metric_params=None, n_threads=1):
+    A = _ts(x)
+    B = _ts(y)
+    p = make_params(metric, metric_params)
+    out = np.empty(A.shape[0])
+    lib().wbo_paired(_dp(A), _dp(B), A.shape[0], A.shape[1], A.shape[2], B.shape[2], dim,
+                     METRIC_IDS[metric], ctypes.byref(p), _dp(out), n_threads)
+    return out
+
+
+def argmin(x, y, *, k=1, dim=0, metric="dtw", metric_params=None, lower_bound=None,
+           n_threads=1):
+    X = _ts(x)
+    Y = _ts(y)
+    k = min(k, Y.shape[0])
+    p = make_params(metric, metric_params)
+    idx = np.zeros((X.shape[0], k), dtype=np.int64)
+    dist = np.zeros((X.shape[0], k))
+    lb = None
+    if lower_bound is not None:
+        lb = np.ascontiguousarray(lower_bound, dtype=np.float64)
+    lib().wbo_argmin(_dp(X), X.shape[0], X.shape[1], X.shape[2], _dp(Y), Y.shape[0],
+                     Y.shape[1], Y.shape[2], dim, METRIC_IDS[metric], ctypes.byref(p), k,
+                     _dp(lb), _ip(idx), _dp(dist), n_threads)
+    return idx, dist
+
+
+def subsequence(shapelets, x, *, dim=0, metric="euclidean", n_threads=1):
+    """(n_samples, n_shapelets) min distance and first argmin index."""
+    X = _ts(x)
+    shp = [np.asarray(s, dtype=np.float64).ravel() for s in shapelets]
+    lens = np.array([s.shape[0] for s in shp], dtype=np.int64)
+    offs = np.zeros(len(shp), dtype=np.int64)
+    offs[1:] = np.cumsum(lens)[:-1]
+    packed = np.ascontiguousarray(np.concatenate(shp))
+    # ScaledSubsequenceMetric.from_array: distance/_cdistance.pyx:453-467
+    smean = np.array([np.mean(s) for s in shp])
+    sstd = np.array([np.std(s) for s in shp])
+    sstd[sstd <= 1e-13] = 0.0
+    dist = np.empty((X.shape[0], len(shp)))
+    idx = np.empty((X.shape[0], len(shp)), dtype=np.int64)
+    lib().wbo_subsequence(_dp(packed), _ip(offs), _ip(lens), _dp(smean), _dp(sstd),
+                          len(shp), _dp(X), X.shape[0], X.shape[1], X.shape[2], dim,
+                          METRIC_IDS[metric], _dp(dist), _ip(idx), n_threads)
+    return dist, idx
+
+
+def distance_1d(x, y, *, metric="dtw", metric_params=None):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    p = make_params(metric, metric_params)
+    return lib().wbo_distance_1d(_dp(x), x.shape[0], _dp(y), y.shape[0],
+                                 METRIC_IDS[metric], ctypes.byref(p))
+
+
+def fast_mean_std(x):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    m = ctypes.c_double()
+    s = ctypes.c_double()
+    lib().wbo_fast_mean_std(_dp(x), x.shape[0], ctypes.byref(m), ctypes.byref(s))
+    return m.value, s.value
+
+
+def dtw_alignment(x, y, *, r=1.0, weights=None):
+    """distance/dtw.py:246-290 followed by _dtw_alignment (_elastic.pyx:1011-1073).
+
+    Cells outside the band are NaN here (the reference leaves np.empty garbage).
+    """
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    n, m = x.shape[0], y.shape[0]
+    warp = max(int(math.floor(max(n, m) * r)), 1)
+    out = np.full((n, m), np.nan)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    rc = lib().wbo_dtw_alignment(_dp(x), n, _dp(y), m, warp, _dp(w), _dp(out))
+    if rc != 0:
+        raise ValueError("invalid r")
+    return out
+
+
+def dtw_mapping(alignment):
+    """Traceback of distance/dtw.py:362-426: ties prefer diag, then up, then left."""
+    a = alignment
+    n, m = a.shape
+    i, j = n - 1, m - 1
+    path = [(i, j)]
+    while i > 0 or j > 0:
+        if i == 0:
+            j -= 1
+        elif j == 0:
+            i -= 1
+        else:
+            cand = [a[i - 1, j - 1], a[i - 1, j], a[i, j - 1]]
+            c = int(np.argmin(cand))
+            if c == 0:
+                i -= 1
+                j -= 1
+            elif c == 1:
+                i -= 1
+            else:
+                j -= 1
+        path.append((i, j))
+    return path[::-1]

@@ -1,0 +1,906 @@
+/*
+ * wb_oracle.c -- CPU restatement of wildboar's distance hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle and the timed CPU
+ * baseline.  Only tests/, __graft_entry__.smoke() and bench.py's CPU legs may
+ * load it; the product path (wildboar_gb300) never links or calls it.
+ *
+ * Every routine restates the algorithm of the reference file/line cited beside
+ * it, in plain C99, double precision, built with -O2 -ffp-contract=off so that
+ * every multiply and add rounds on its own (as gcc -O2 on x86-64 does for the
+ * Cython-generated C of the reference).
+ *
+ * Citations are to wildboar (src/wildboar/...).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <pthread.h>
+
+#define INF ((double)INFINITY)
+
+typedef int64_t idx_t;
+
+/* metric ids; the same numbering is used by include/wbgpu.h */
+enum {
+    WBO_EUCLIDEAN = 0,
+    WBO_DTW = 1,
+    WBO_WDTW = 2,
+    WBO_DDTW = 3,
+    WBO_WDDTW = 4,
+    WBO_ADTW = 5,
+    WBO_LCSS = 6,
+    WBO_WLCSS = 7,
+    WBO_EDR = 8,
+    WBO_ERP = 9,
+    WBO_MSM = 10,
+    WBO_TWE = 11,
+    /* subsequence-only */
+    WBO_SCALED_EUCLIDEAN = 32,
+};
+
+typedef struct {
+    double r, g, p, epsilon, c, penalty, stiffness;
+} wbo_params;
+
+static inline idx_t imax(idx_t a, idx_t b) { return a > b ? a : b; }
+static inline idx_t imin(idx_t a, idx_t b) { return a < b ? a : b; }
+/* Cython lowers builtin min/max on C doubles to "b < a ? b : a" */
+static inline double dmin(double a, double b) { return b < a ? b : a; }
+static inline double dmax(double a, double b) { return b > a ? b : a; }
+
+/* _compute_r: distance/_elastic.pyx:1924-1925 */
+static idx_t compute_r(idx_t length, double r)
+{
+    double v = floor((double)length * r);
+    return (idx_t)(v > 1.0 ? v : 1.0);
+}
+
+/* fast_mean_std: utils/_stats.pyx:22-42 (ex2 accumulates libm pow(x, 2.0)) */
+static void fast_mean_std(const double *x, idx_t n, double *mean, double *std)
+{
+    double ex = 0, ex2 = 0;
+    for (idx_t i = 0; i < n; i++) {
+        double v = x[i];
+        ex += v;
+        ex2 = ex2 + pow(v, 2.0);
+    }
+    *mean = ex / (double)n;
+    ex2 = ex2 / (double)n - *mean * *mean;
+    *std = ex2 > 1e-13 ? sqrt(ex2) : 0.0;
+}
+
+/* average_slope: distance/_elastic.pyx:3220-3225 */
+static void average_slope(const double *q, idx_t len, double *d)
+{
+    idx_t j = 0;
+    for (idx_t i = 1; i < len - 1; i++) {
+        d[j] = ((q[i] - q[i - 1]) + ((q[i + 1] - q[i - 1]) / 2)) / 2;
+        j++;
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+/* Elastic kernels: two-row band recurrences                              */
+/* ---------------------------------------------------------------------- */
+
+/* dtw_distance: distance/_elastic.pyx:869-940 (also WDTW/DDTW via w, inputs) */
+static double dtw_rows(const double *X, idx_t xl, const double *Y, idx_t yl, idx_t r,
+                       double *cost, double *cost_prev, const double *wv, double min_dist)
+{
+    idx_t mx = imax(0, yl - xl) + r;
+    idx_t mn = imax(0, xl - yl);
+    double v, w = 1.0;
+    v = X[0] - Y[0];
+    if (wv) w = wv[0];
+    cost_prev[0] = v * v * w;
+    for (idx_t i = 1; i < imin(yl, mx); i++) {
+        v = X[0] - Y[i];
+        if (wv) w = wv[i - 1];
+        cost_prev[i] = cost_prev[i - 1] + v * v * w;
+    }
+    if (mx < yl) cost_prev[mx] = INF;
+    for (idx_t i = 1; i < xl; i++) {
+        idx_t js = imax(0, i - mn - r + 1);
+        idx_t je = imin(yl, i + mx);
+        if (js > 0) cost[js - 1] = INF;
+        double min_cost = INF;
+        for (idx_t j = js; j < je; j++) {
+            double x = cost_prev[j], y, z;
+            if (j > 0) { y = cost[j - 1]; z = cost_prev[j - 1]; }
+            else { y = INF; z = INF; }
+            v = X[i] - Y[j];
+            if (wv) w = wv[labs((long)(i - j))];
+            cost[j] = dmin(dmin(x, y), z) + v * v * w;
+            if (cost[j] < min_cost) min_cost = cost[j];
+        }
+        if (min_cost > min_dist) return INF;
+        if (je < yl) cost[je] = INF;
+        double *t = cost; cost = cost_prev; cost_prev = t;
+    }
+    return cost_prev[yl - 1];
+}
+
+/* adtw_distance: distance/_elastic.pyx:943-1008 */
+static double adtw_rows(const double *X, idx_t xl, const double *Y, idx_t yl, idx_t r,
+                        double *cost, double *cost_prev, double penalty, double min_dist)
+{
+    idx_t mx = imax(0, yl - xl) + r;
+    idx_t mn = imax(0, xl - yl);
+    double v = X[0] - Y[0];
+    cost_prev[0] = v * v;
+    for (idx_t i = 1; i < imin(yl, mx); i++) {
+        v = X[0] - Y[i];
+        cost_prev[i] = cost_prev[i - 1] + v * v;
+    }
+    if (mx < yl) cost_prev[mx] = INF;
+    for (idx_t i = 1; i < xl; i++) {
+        idx_t js = imax(0, i - mn - r + 1);
+        idx_t je = imin(yl, i + mx);
+        if (js > 0) cost[js - 1] = INF;
+        double prev_cost = INF, min_cost = INF;
+        for (idx_t j = js; j < je; j++) {
+            double x = cost_prev[j] + penalty, y, z;
+            if (j > 0) { y = prev_cost + penalty; z = cost_prev[j - 1]; }
+            else { y = INF; z = INF; }
+            v = X[i] - Y[j];
+            cost[j] = dmin(dmin(x, y), z) + v * v;
+            if (cost[j] < min_cost) min_cost = cost[j];
+            prev_cost = cost[j];
+        }
+        if (min_cost > min_dist) return INF;
+        if (je < yl) cost[je] = INF;
+        double *t = cost; cost = cost_prev; cost_prev = t;
+    }
+    return cost_prev[yl - 1];
+}
+
+/* lcss_distance: distance/_elastic.pyx:1118-1183 */
+static double lcss_rows(const double *X, idx_t xl, const double *Y, idx_t yl, idx_t r,
+                        double eps, double *cost, double *cost_prev, const double *wv,
+                        double min_dist)
+{
+    idx_t mx = imax(0, yl - xl) + r;
+    idx_t mn = imax(0, xl - yl);
+    double w = 1.0;
+    for (idx_t i = 0; i < imin(yl, mx); i++) cost_prev[i] = 0;
+    if (mx < yl) cost_prev[mx] = 0;
+    for (idx_t i = 0; i < xl; i++) {
+        idx_t js = imax(0, i - mn - r + 1);
+        idx_t je = imin(yl, i + mx);
+        if (js > 0) cost[js - 1] = 0;
+        double min_cost = INF;
+        for (idx_t j = js; j < je; j++) {
+            double x = cost_prev[j], y, z;
+            if (j > 0) { y = cost_prev[j - 1]; z = cost[j - 1]; }
+            else { y = 0; z = 0; }
+            double v = fabs(X[i] - Y[j]);
+            if (wv) w = wv[labs((long)(i - j))];
+            if (v <= eps) cost[j] = w + y;
+            else cost[j] = dmax(z, x);
+            if (cost[j] < min_cost) min_cost = cost[j];
+        }
+        if (min_cost > min_dist) return INF;
+        if (je < yl) cost[je] = 0;
+        double *t = cost; cost = cost_prev; cost_prev = t;
+    }
+    return 1 - (cost_prev[yl - 1] / (double)imin(xl, yl));
+}
+
+/* erp_distance: distance/_elastic.pyx:1273-1347 */
+static double erp_rows(const double *X, idx_t xl, const double *Y, idx_t yl, idx_t r,
+                       double g, double *gX, double *gY, double *cost, double *cost_prev,
+                       double min_dist)
+{
+    double gx_sum = 0, gy_sum = 0;
+    for (idx_t i = 0; i < xl; i++) { double v = fabs(X[i] - g); gX[i] = v; gx_sum += v; }
+    for (idx_t i = 0; i < yl; i++) { double v = fabs(Y[i] - g); gY[i] = v; gy_sum += v; }
+    idx_t mx = imax(0, yl - xl) + r;
+    idx_t mn = imax(0, xl - yl);
+    for (idx_t i = 0; i < imin(yl, mx); i++) cost_prev[i] = gy_sum;
+    if (mx < yl) cost_prev[mx] = gy_sum;
+    for (idx_t i = 0; i < xl; i++) {
+        idx_t js = imax(0, i - mn - r + 1);
+        idx_t je = imin(yl, i + mx);
+        if (js > 0) cost[js - 1] = 0;
+        double min_cost = INF;
+        for (idx_t j = js; j < je; j++) {
+            double x = cost_prev[j], y, z;
+            if (j > 0) { y = cost_prev[j - 1]; z = cost[j - 1]; }
+            else { y = (i == 0) ? 0 : gx_sum; z = gx_sum; }
+            double v = fabs(X[i] - Y[j]);
+            cost[j] = dmin(y + v, dmin(x + gX[i], z + gY[j]));
+            if (cost[j] < min_cost) min_cost = cost[j];
+        }
+        if (min_cost > min_dist) return INF;
+        if (je < yl) cost[je] = 0;
+        double *t = cost; cost = cost_prev; cost_prev = t;
+    }
+    return cost_prev[yl - 1];
+}
+
+/* edr_distance: distance/_elastic.pyx:1437-1497 */
+static double edr_rows(const double *X, idx_t xl, const double *Y, idx_t yl, idx_t r,
+                       double eps, double *cost, double *cost_prev, double min_dist)
+{
+    idx_t mx = imax(0, yl - xl) + r;
+    idx_t mn = imax(0, xl - yl);
+    for (idx_t i = 0; i < imin(yl, mx); i++) cost_prev[i] = 0;
+    if (mx < yl) cost_prev[mx] = 0;
+    for (idx_t i = 0; i < xl; i++) {
+        idx_t js = imax(0, i - mn - r + 1);
+        idx_t je = imin(yl, i + mx);
+        if (js > 0) cost[js - 1] = 0;
+        double min_cost = INF;
+        for (idx_t j = js; j < je; j++) {
+            double x = cost_prev[j], y, z;
+            if (j > 0) { y = cost_prev[j - 1]; z = cost[j - 1]; }
+            else { y = 0; z = 0; }
+            double v = fabs(X[i] - Y[j]);
+            /* Cython 3-arg min: keep the first of equal values */
+            double a = y + (v < eps ? 0.0 : 1.0), b = x + 1, c = z + 1;
+            double m = a;
+            if (b < m) m = b;
+            if (c < m) m = c;
+            cost[j] = m;
+            if (cost[j] < min_cost) min_cost = cost[j];
+        }
+        if (min_cost > min_dist) return INF;
+        if (je < yl) cost[je] = 0;
+        double *t = cost; cost = cost_prev; cost_prev = t;
+    }
+    return cost_prev[yl - 1] / (double)imax(xl, yl);
+}
+
+/* _msm_cost: distance/_elastic.pyx:1583-1587 (arguments narrowed to float) */
+static inline double msm_cost(float x, float y, float z, float c)
+{
+    if ((y <= x && x <= z) || (y >= x && x >= z)) return c;
+    double a = fabs((double)(float)(x - y));
+    double b = fabs((double)(float)(x - z));
+    return (double)c + dmin(a, b);
+}
+
+/* msm_distance: distance/_elastic.pyx:1592-1647 */
+static double msm_rows(const double *X, idx_t xl, const double *Y, idx_t yl, idx_t r,
+                       double c, double *cost, double *cost_prev, double *cost_y,
+                       double min_dist)
+{
+    float cf = (float)c;
+    idx_t mx = imax(0, yl - xl) + r;
+    idx_t mn = imax(0, xl - yl);
+    cost_prev[0] = fabs(X[0] - Y[0]);
+    for (idx_t i = 1; i < imin(yl, mx); i++)
+        cost_prev[i] = cost_prev[i - 1] + msm_cost((float)Y[i], (float)Y[i - 1], (float)X[0], cf);
+    if (mx < yl)
+        cost_prev[mx] = cost_prev[mx - 1] + msm_cost((float)Y[mx], (float)Y[mx - 1], (float)X[0], cf);
+    cost_y[0] = cost_prev[0];
+    for (idx_t i = 1; i < xl; i++)
+        cost_y[i] = cost_y[i - 1] + msm_cost((float)X[i], (float)X[i - 1], (float)Y[0], cf);
+    for (idx_t i = 1; i < xl; i++) {
+        idx_t js = imax(1, i - mn - r + 1);
+        idx_t je = imin(yl, i + mx);
+        cost[0] = cost_y[i];
+        double min_cost = cost[0];
+        for (idx_t j = js; j < je; j++) {
+            double a = cost_prev[j - 1] + fabs(X[i] - Y[j]);
+            double b = cost_prev[j] + msm_cost((float)X[i], (float)X[i - 1], (float)Y[j], cf);
+            double d = cost[j - 1] + msm_cost((float)Y[j], (float)X[i], (float)Y[j - 1], cf);
+            double m = a;
+            if (b < m) m = b;
+            if (d < m) m = d;
+            cost[j] = m;
+            if (cost[j] < min_cost) min_cost = cost[j];
+        }
+        if (min_cost > min_dist) return INF;
+        if (je < yl) cost[je] = 0;
+        double *t = cost; cost = cost_prev; cost_prev = t;
+    }
+    return cost_prev[yl - 1];
+}
+
+/* twe_distance: distance/_elastic.pyx:1733-1829 */
+static double twe_rows(const double *X, idx_t xl, const double *Y, idx_t yl, idx_t r,
+                       double penalty, double stiffness, double *cost, double *cost_prev,
+                       double min_dist)
+{
+    idx_t mx = imax(0, yl - xl) + r;
+    idx_t mn = imax(0, xl - yl);
+    for (idx_t i = 0; i < imin(yl, mx); i++) cost_prev[i] = INF;
+    if (mx < yl) cost_prev[mx] = INF;
+    penalty = penalty + stiffness;
+    for (idx_t i = 0; i < xl; i++) {
+        idx_t js = imax(0, i - mn - r + 1);
+        idx_t je = imin(yl, i + mx);
+        if (js > 0) cost[js - 1] = 0;
+        double min_cost = INF;
+        for (idx_t j = js; j < je; j++) {
+            double up = cost_prev[j], left, up_left, x, y;
+            if (j == 0) { left = INF; up_left = (i == 0) ? 0 : INF; }
+            else { left = cost[j - 1]; up_left = cost_prev[j - 1]; }
+            x = (i == 0) ? 0 : X[i - 1];
+            y = X[i];
+            double del_x = up + fabs(x - y) + penalty;
+            x = (j == 0) ? 0 : Y[j - 1];
+            y = Y[j];
+            double del_y = left + fabs(x - y) + penalty;
+            x = (i == 0) ? 0 : X[i - 1];
+            y = (j == 0) ? 0 : Y[j - 1];
+            double match = up_left + fabs(X[i] - Y[j]) + fabs(x - y)
+                           + stiffness * 2.0 * (double)labs((long)(i - j));
+            double m = del_x;
+            if (del_y < m) m = del_y;
+            if (match < m) m = match;
+            cost[j] = m;
+            if (cost[j] < min_cost) min_cost = cost[j];
+        }
+        if (min_cost > min_dist) return INF;
+        if (je < yl) cost[je] = 0;
+        double *t = cost; cost = cost_prev; cost_prev = t;
+    }
+    return cost_prev[yl - 1];
+}
+
+/* euclidean_distance: distance/_metric.pyx:654-682 */
+static double euclid_scan(const double *S, idx_t sl, const double *T, idx_t tl,
+                          double min_dist, idx_t *index)
+{
+    for (idx_t i = 0; i < tl - sl + 1; i++) {
+        double dist = 0;
+        for (idx_t j = 0; j < sl; j++) {
+            if (dist >= min_dist) break;
+            double x = T[i + j];
+            x -= S[j];
+            dist += x * x;
+        }
+        if (dist < min_dist) {
+            min_dist = dist;
+            if (index) *index = i;
+        }
+    }
+    return sqrt(min_dist);
+}
+
+/* scaled_euclidean_distance + inner_scaled_euclidean_distance:
+ * distance/_metric.pyx:561-651 */
+static double scaled_euclid_scan(const double *S, idx_t sl, double s_mean, double s_std,
+                                 const double *T, idx_t tl, double *buf, idx_t *index)
+{
+    double mean = 0, std = 0, dist = 0, min_dist = INF, ex = 0, ex2 = 0;
+    for (idx_t i = 0; i < tl; i++) {
+        double cv = T[i];
+        ex += cv;
+        ex2 += cv * cv;
+        idx_t bp = i % sl;
+        buf[bp] = cv;
+        buf[bp + sl] = cv;
+        if (i >= sl - 1) {
+            idx_t j = (i + 1) % sl;
+            mean = ex / (double)sl;
+            double tmp = ex2 / (double)sl - mean * mean;
+            std = tmp > 0 ? sqrt(tmp) : 1.0;
+            dist = 0;
+            for (idx_t k = 0; k < sl; k++) {
+                if (dist >= min_dist) break;
+                double x = (S[k] - s_mean) / s_std;
+                x -= (buf[k + j] - mean) / std;
+                dist += x * x;
+            }
+            if (dist < min_dist) {
+                min_dist = dist;
+                if (index) *index = (i + 1) - sl;
+            }
+            cv = buf[j];
+            ex -= cv;
+            ex2 -= cv * cv;
+        }
+    }
+    return sqrt(min_dist);
+}
+
+/* ---------------------------------------------------------------------- */
+/* Metric objects: reset / distance / eadistance                          */
+/* ---------------------------------------------------------------------- */
+
+typedef struct {
+    int id;
+    wbo_params p;
+    double *weights;           /* WDTW / WDDTW / WLCSS */
+    double *std_x, *std_y;     /* EDR default epsilon tables */
+    idx_t xn, xd, xL, yn, yd, yL;
+} wbo_metric;
+
+typedef struct {
+    double *cost, *cost_prev, *gX, *gY, *cost_y, *d_x, *d_y;
+} wbo_scratch;
+
+static void scratch_init(wbo_scratch *s, idx_t L)
+{
+    idx_t n = L + 4;
+    s->cost = malloc(sizeof(double) * n);
+    s->cost_prev = malloc(sizeof(double) * n);
+    s->gX = malloc(sizeof(double) * n);
+    s->gY = malloc(sizeof(double) * n);
+    s->cost_y = malloc(sizeof(double) * n);
+    s->d_x = malloc(sizeof(double) * n);
+    s->d_y = malloc(sizeof(double) * n);
+}
+
+static void scratch_free(wbo_scratch *s)
+{
+    free(s->cost); free(s->cost_prev); free(s->gX); free(s->gY);
+    free(s->cost_y); free(s->d_x); free(s->d_y);
+}
+
+static double *logistic_weights(idx_t n, double g)
+{
+    /* WeightedDtwMetric.reset: distance/_elastic.pyx:3333-3341 */
+    double *w = malloc(sizeof(double) * (size_t)imax(n, 1));
+    for (idx_t i = 0; i < n; i++)
+        w[i] = 1.0 / (1.0 + exp(-g * ((double)i - (double)n / 2.0)));
+    return w;
+}
+
+/* Metric.reset for each metric class (X, Y are (n, d, L) C-contiguous) */
+static void metric_reset(wbo_metric *M, const double *X, idx_t xn, idx_t xd, idx_t xL,
+                         const double *Y, idx_t yn, idx_t yd, idx_t yL)
+{
+    M->xn = xn; M->xd = xd; M->xL = xL; M->yn = yn; M->yd = yd; M->yL = yL;
+    M->weights = NULL; M->std_x = NULL; M->std_y = NULL;
+    if (M->id == WBO_WDTW || M->id == WBO_WLCSS) {
+        M->weights = logistic_weights(imax(xL, yL), M->p.g);
+    } else if (M->id == WBO_WDDTW) {
+        /* WeightedDerivativeDtwMetric.reset: distance/_elastic.pyx:3415-3430 */
+        M->weights = logistic_weights(imax(xL - 2, yL - 2), M->p.g);
+    } else if (M->id == WBO_EDR && isnan(M->p.epsilon)) {
+        /* EdrMetric.reset: distance/_elastic.pyx:3731-3752 */
+        double mean, std;
+        M->std_x = malloc(sizeof(double) * (size_t)(xn * xd));
+        M->std_y = malloc(sizeof(double) * (size_t)(yn * yd));
+        for (idx_t i = 0; i < xn; i++)
+            for (idx_t d = 0; d < xd; d++) {
+                fast_mean_std(X + (i * xd + d) * xL, xL, &mean, &std);
+                M->std_x[d * xn + i] = std;
+            }
+        for (idx_t i = 0; i < yn; i++)
+            for (idx_t d = 0; d < yd; d++) {
+                fast_mean_std(Y + (i * yd + d) * yL, yL, &mean, &std);
+                M->std_y[d * yn + i] = std;
+            }
+    }
+}
+
+static void metric_free(wbo_metric *M)
+{
+    free(M->weights); free(M->std_x); free(M->std_y);
+    M->weights = M->std_x = M->std_y = NULL;
+}
+
+/*
+ * One call to the metric's distance (ea == 0) or eadistance (ea == 1).
+ * For eadistance, *min_dist is the in/out threshold and the return value is
+ * the bint result; for distance, the return value is the distance.
+ * x/y point at the row (already offset by index and dim).
+ */
+static double metric_call(const wbo_metric *M, wbo_scratch *s, const double *x, idx_t xl,
+                          idx_t x_index, const double *y, idx_t yl, idx_t y_index,
+                          idx_t dim, int ea, double *min_dist)
+{
+    const wbo_params *p = &M->p;
+    double dist, thr = 0;
+    switch (M->id) {
+    case WBO_EUCLIDEAN:
+        /* EuclideanMetric: distance/_metric.pyx:381-409 */
+        if (!ea) return euclid_scan(x, xl, y, yl, INF, NULL);
+        dist = euclid_scan(x, xl, y, yl, *min_dist * *min_dist, NULL);
+        break;
+    case WBO_DTW:
+    case WBO_WDTW:
+        /* DtwMetric: distance/_elastic.pyx:3167-3213 */
+        thr = ea ? *min_dist * *min_dist : INF;
+        dist = sqrt(dtw_rows(x, xl, y, yl, compute_r(imin(xl, yl), p->r), s->cost,
+                             s->cost_prev, M->weights, thr));
+        if (!ea) return dist;
+        break;
+    case WBO_DDTW:
+    case WBO_WDDTW:
+        /* DerivativeDtwMetric: distance/_elastic.pyx:3262-3320 */
+        if (imin(xl, yl) < 3) return 0;
+        average_slope(x, xl, s->d_x);
+        average_slope(y, yl, s->d_y);
+        if (!ea) {
+            return sqrt(dtw_rows(s->d_x, xl - 2, s->d_y, yl - 2,
+                                 compute_r(imin(xl, yl), p->r), s->cost, s->cost_prev,
+                                 M->weights, INF));
+        }
+        dist = sqrt(dtw_rows(s->d_x, xl - 2, s->d_y, yl - 2,
+                             compute_r(imin(xl - 2, yl - 2), p->r), s->cost, s->cost_prev,
+                             M->weights, *min_dist * *min_dist));
+        break;
+    case WBO_ADTW:
+        /* AmercingDtwMetric: distance/_elastic.pyx:3354-3401 */
+        thr = ea ? *min_dist * *min_dist : INF;
+        dist = sqrt(adtw_rows(x, xl, y, yl, compute_r(imin(xl, yl), p->r), s->cost,
+                              s->cost_prev, p->p, thr));
+        if (!ea) return dist;
+        break;
+    case WBO_LCSS:
+    case WBO_WLCSS: {
+        /* LcssMetric: distance/_elastic.pyx:3483-3535 */
+        if (ea) {
+            double ml = (double)imin(xl, yl);
+            thr = isinf(*min_dist) == 0 ? ml - *min_dist * ml : INF;
+        } else {
+            thr = INF;
+        }
+        dist = lcss_rows(x, xl, y, yl, compute_r(imin(xl, yl), p->r), p->epsilon, s->cost,
+                         s->cost_prev, M->weights, thr);
+        if (!ea) return dist;
+        break;
+    }
+    case WBO_EDR: {
+        /* EdrMetric.distance / eadistance (TSArray forms): _elastic.pyx:3754-3845 */
+        double eps;
+        if (isnan(p->epsilon))
+            eps = dmax(M->std_x[dim * M->xn + x_index], M->std_y[dim * M->yn + y_index]) / 4.0;
+        else
+            eps = p->epsilon;
+        if (!ea)
+            return edr_rows(x, xl, y, yl, compute_r(imin(xl, yl), p->r), eps, s->cost,
+                            s->cost_prev, INF);
+        /* the reference passes min(X.shape[2], X.shape[2]) here */
+        dist = edr_rows(x, xl, y, yl, compute_r(imin(xl, xl), p->r), eps, s->cost,
+                        s->cost_prev, *min_dist * (double)imax(xl, yl));
+        break;
+    }
+    case WBO_ERP:
+        /* ErpMetric: distance/_elastic.pyx:3612-3664 */
+        thr = ea ? *min_dist : INF;
+        dist = erp_rows(x, xl, y, yl, compute_r(imin(xl, yl), p->r), p->g, s->gX, s->gY,
+                        s->cost, s->cost_prev, thr);
+        if (!ea) return dist;
+        break;
+    case WBO_MSM:
+        /* MsmMetric: distance/_elastic.pyx:3933-3978 */
+        thr = ea ? *min_dist : INF;
+        dist = msm_rows(x, xl, y, yl, compute_r(imin(xl, yl), p->r), p->c, s->cost,
+                        s->cost_prev, s->cost_y, thr);
+        if (!ea) return dist;
+        break;
+    case WBO_TWE:
+        /* TweMetric: distance/_elastic.pyx:4038-4078 */
+        thr = ea ? *min_dist : INF;
+        dist = twe_rows(x, xl, y, yl, compute_r(imin(xl, yl), p->r), p->penalty,
+                        p->stiffness, s->cost, s->cost_prev, thr);
+        if (!ea) return dist;
+        break;
+    default:
+        return NAN;
+    }
+    if (dist < *min_dist) {
+        *min_dist = dist;
+        return 1;
+    }
+    return 0;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Heap keeping the k smallest: utils/_misc.pyx:18-107                     */
+/* ---------------------------------------------------------------------- */
+typedef struct { idx_t index; double value; } heap_el;
+
+static void heap_sift_toward_root(heap_el *h, idx_t start, idx_t pos)
+{
+    heap_el e = h[pos];
+    while (pos > start) {
+        idx_t parent = (pos - 1) >> 1;
+        if (e.value > h[parent].value) {
+            h[pos] = h[parent];
+            pos = parent;
+            continue;
+        }
+        break;
+    }
+    h[pos] = e;
+}
+
+static void heap_sift_to_leaf(heap_el *h, idx_t pos, idx_t end)
+{
+    idx_t start = pos;
+    heap_el e = h[pos];
+    idx_t child = 2 * pos + 1;
+    while (child < end) {
+        idx_t right = child + 1;
+        if (right < end && h[child].value < h[right].value) child = right;
+        h[pos] = h[child];
+        pos = child;
+        child = 2 * pos + 1;
+    }
+    h[pos] = e;
+    heap_sift_toward_root(h, start, pos);
+}
+
+static void heap_push(heap_el *h, idx_t *n, idx_t k, idx_t index, double value)
+{
+    heap_el e = {index, value};
+    if (*n == 0) {
+        h[0] = e;
+        *n = 1;
+    } else if (*n < k) {
+        h[*n] = e;
+        *n += 1;
+        heap_sift_toward_root(h, 0, *n - 1);
+    } else if (h[0].value > value) {
+        h[0] = e;
+        heap_sift_to_leaf(h, 0, k);
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+/* Drivers (run_in_parallel: contiguous batches over the outer axis,       */
+/* utils/_parallel.py:7-43)                                                */
+/* ---------------------------------------------------------------------- */
+
+typedef struct {
+    int kind;                 /* 0 pairwise, 1 singleton, 2 paired, 3 argmin, 4 subseq */
+    const wbo_metric *M;
+    const double *X, *Y;
+    idx_t xn, xd, xL, yn, yd, yL, dim;
+    double *out;
+    idx_t *out_idx;
+    idx_t k;
+    const double *lower_bound;
+    /* subsequence */
+    const double *shp;
+    const idx_t *shp_off, *shp_len;
+    const double *shp_mean, *shp_std;
+    idx_t m;
+    idx_t begin, end;
+} job_t;
+
+static void *run_job(void *arg)
+{
+    job_t *J = arg;
+    const wbo_metric *M = J->M;
+    wbo_scratch s;
+    idx_t L = imax(J->xL, J->yL);
+    scratch_init(&s, L);
+    double *sbuf = NULL;
+    heap_el *heap = NULL;
+    if (J->kind == 3) heap = malloc(sizeof(heap_el) * (size_t)imax(J->k, 1));
+    if (J->kind == 4) sbuf = malloc(sizeof(double) * (size_t)(2 * J->xL + 2));
+    for (idx_t i = J->begin; i < J->end; i++) {
+        const double *xr = J->X + (i * J->xd + J->dim) * J->xL;
+        if (J->kind == 0) {
+            for (idx_t j = 0; j < J->yn; j++) {
+                const double *yr = J->Y + (j * J->yd + J->dim) * J->yL;
+                J->out[i * J->yn + j] =
+                    metric_call(M, &s, xr, J->xL, i, yr, J->yL, j, J->dim, 0, NULL);
+            }
+        } else if (J->kind == 1) {
+            for (idx_t j = i + 1; j < J->xn; j++) {
+                const double *yr = J->X + (j * J->xd + J->dim) * J->xL;
+                double d = metric_call(M, &s, xr, J->xL, i, yr, J->xL, j, J->dim, 0, NULL);
+                J->out[i * J->xn + j] = d;
+                J->out[j * J->xn + i] = d;
+            }
+        } else if (J->kind == 2) {
+            const double *yr = J->Y + (i * J->yd + J->dim) * J->yL;
+            J->out[i] = metric_call(M, &s, xr, J->xL, i, yr, J->yL, i, J->dim, 0, NULL);
+        } else if (J->kind == 3) {
+            /* _ArgMinBatch.__call__: distance/_cdistance.pyx:1302-1345 */
+            double distance = INF;
+            idx_t hn = 0;
+            for (idx_t j = 0; j < J->yn; j++) {
+                if (J->lower_bound && J->lower_bound[i * J->yn + j] >= distance) continue;
+                const double *yr = J->Y + (j * J->yd + J->dim) * J->yL;
+                if (metric_call(M, &s, xr, J->xL, i, yr, J->yL, j, J->dim, 1, &distance)) {
+                    heap_push(heap, &hn, J->k, j, distance);
+                    distance = (hn == J->k) ? heap[0].value : INF;
+                }
+            }
+            /* the output array is zero-initialised; unfilled heap slots keep
+             * whatever the heap array held (never read when hn == k) */
+            for (idx_t j = 0; j < J->k; j++) {
+                if (j < hn) {
+                    J->out_idx[i * J->k + j] = heap[j].index;
+                    J->out[i * J->k + j] = heap[j].value;
+                }
+            }
+        } else if (J->kind == 4) {
+            /* _PairwiseSubsequenceDistance.__call__: distance/_cdistance.pyx:1001-1015 */
+            for (idx_t j = 0; j < J->m; j++) {
+                const double *S = J->shp + J->shp_off[j];
+                idx_t sl = J->shp_len[j];
+                idx_t mi = 0;
+                double d;
+                if (M->id == WBO_SCALED_EUCLIDEAN) {
+                    double sstd = J->shp_std[j] != 0 ? J->shp_std[j] : 1.0;
+                    d = scaled_euclid_scan(S, sl, J->shp_mean[j], sstd, xr, J->xL, sbuf, &mi);
+                } else {
+                    d = euclid_scan(S, sl, xr, J->xL, INF, &mi);
+                }
+                J->out[i * J->m + j] = d;
+                J->out_idx[i * J->m + j] = mi;
+            }
+        }
+    }
+    free(heap);
+    free(sbuf);
+    scratch_free(&s);
+    return NULL;
+}
+
+static void run_parallel(job_t *proto, idx_t n_work, int n_threads)
+{
+    if (n_threads < 1) n_threads = 1;
+    if (n_threads > n_work) n_threads = (int)(n_work > 0 ? n_work : 1);
+    pthread_t *th = malloc(sizeof(pthread_t) * (size_t)n_threads);
+    job_t *jobs = malloc(sizeof(job_t) * (size_t)n_threads);
+    idx_t base = n_work / n_threads, rem = n_work % n_threads, off = 0;
+    for (int t = 0; t < n_threads; t++) {
+        idx_t sz = base + (t < rem ? 1 : 0);
+        jobs[t] = *proto;
+        jobs[t].begin = off;
+        jobs[t].end = off + sz;
+        off += sz;
+        if (n_threads == 1) run_job(&jobs[t]);
+        else pthread_create(&th[t], NULL, run_job, &jobs[t]);
+    }
+    if (n_threads > 1)
+        for (int t = 0; t < n_threads; t++) pthread_join(th[t], NULL);
+    free(th);
+    free(jobs);
+}
+
+/* ---------------------------------------------------------------------- */
+/* Exported entry points (ctypes)                                          */
+/* ---------------------------------------------------------------------- */
+
+/* _pairwise_distance / _singleton_pairwise_distance: _cdistance.pyx:1184-1267.
+ * Y == NULL selects the singleton (x is y) path; out must be zero-filled. */
+int wbo_pairwise(const double *X, idx_t xn, idx_t xd, idx_t xL, const double *Y, idx_t yn,
+                 idx_t yd, idx_t yL, idx_t dim, int metric, const wbo_params *p,
+                 double *out, int n_threads)
+{
+    wbo_metric M = {0};
+    M.id = metric;
+    M.p = *p;
+    job_t J = {0};
+    J.M = &M;
+    J.X = X; J.xn = xn; J.xd = xd; J.xL = xL; J.dim = dim; J.out = out;
+    if (Y == NULL) {
+        metric_reset(&M, X, xn, xd, xL, X, xn, xd, xL);
+        J.kind = 1;
+        J.Y = X; J.yn = xn; J.yd = xd; J.yL = xL;
+    } else {
+        metric_reset(&M, X, xn, xd, xL, Y, yn, yd, yL);
+        J.kind = 0;
+        J.Y = Y; J.yn = yn; J.yd = yd; J.yL = yL;
+    }
+    run_parallel(&J, xn, n_threads);
+    metric_free(&M);
+    return 0;
+}
+
+/* _paired_distance: _cdistance.pyx:1597-1652.  A and B are the API's x and y;
+ * the metric sees (B, A): rows of the DP come from the second argument. */
+int wbo_paired(const double *A, const double *B, idx_t n, idx_t d, idx_t AL, idx_t BL,
+               idx_t dim, int metric, const wbo_params *p, double *out, int n_threads)
+{
+    wbo_metric M = {0};
+    M.id = metric;
+    M.p = *p;
+    metric_reset(&M, B, n, d, BL, A, n, d, AL);
+    job_t J = {0};
+    J.kind = 2; J.M = &M;
+    J.X = B; J.xn = n; J.xd = d; J.xL = BL;
+    J.Y = A; J.yn = n; J.yd = d; J.yL = AL;
+    J.dim = dim; J.out = out;
+    run_parallel(&J, n, n_threads);
+    metric_free(&M);
+    return 0;
+}
+
+/* _argmin_distance: _cdistance.pyx:1348-1378 (outputs zero-filled by caller) */
+int wbo_argmin(const double *X, idx_t xn, idx_t xd, idx_t xL, const double *Y, idx_t yn,
+               idx_t yd, idx_t yL, idx_t dim, int metric, const wbo_params *p, idx_t k,
+               const double *lower_bound, idx_t *out_idx, double *out_dist, int n_threads)
+{
+    wbo_metric M = {0};
+    M.id = metric;
+    M.p = *p;
+    metric_reset(&M, X, xn, xd, xL, Y, yn, yd, yL);
+    job_t J = {0};
+    J.kind = 3; J.M = &M;
+    J.X = X; J.xn = xn; J.xd = xd; J.xL = xL;
+    J.Y = Y; J.yn = yn; J.yd = yd; J.yL = yL;
+    J.dim = dim; J.k = k; J.lower_bound = lower_bound;
+    J.out = out_dist; J.out_idx = out_idx;
+    run_parallel(&J, xn, n_threads);
+    metric_free(&M);
+    return 0;
+}
+
+/* _pairwise_subsequence_distance (euclidean / scaled_euclidean):
+ * _cdistance.pyx:956-1037.  Shapelets are packed; mean/std come from
+ * np.mean/np.std on the caller side (ScaledSubsequenceMetric.from_array,
+ * _cdistance.pyx:453-467). */
+int wbo_subsequence(const double *shp, const idx_t *off, const idx_t *len,
+                    const double *smean, const double *sstd, idx_t m, const double *X,
+                    idx_t xn, idx_t xd, idx_t xL, idx_t dim, int metric, double *out_dist,
+                    idx_t *out_idx, int n_threads)
+{
+    wbo_metric M = {0};
+    M.id = metric;
+    job_t J = {0};
+    J.kind = 4; J.M = &M;
+    J.X = X; J.xn = xn; J.xd = xd; J.xL = xL; J.yL = xL; J.dim = dim;
+    J.shp = shp; J.shp_off = off; J.shp_len = len; J.shp_mean = smean; J.shp_std = sstd;
+    J.m = m; J.out = out_dist; J.out_idx = out_idx;
+    run_parallel(&J, xn, n_threads);
+    return 0;
+}
+
+/* single pair, full-matrix-free: distance of two 1-D rows (used by tests) */
+double wbo_distance_1d(const double *x, idx_t xl, const double *y, idx_t yl, int metric,
+                       const wbo_params *p)
+{
+    wbo_metric M = {0};
+    M.id = metric;
+    M.p = *p;
+    metric_reset(&M, x, 1, 1, xl, y, 1, 1, yl);
+    wbo_scratch s;
+    scratch_init(&s, imax(xl, yl));
+    double d = metric_call(&M, &s, x, xl, 0, y, yl, 0, 0, 0, NULL);
+    scratch_free(&s);
+    metric_free(&M);
+    return d;
+}
+
+/* fast_mean_std, exported for tests */
+void wbo_fast_mean_std(const double *x, idx_t n, double *mean, double *std)
+{
+    fast_mean_std(x, n, mean, std);
+}
+
+/* _dtw_alignment: distance/_elastic.pyx:1011-1073.  out is (n, m); cells
+ * outside the band are left as the caller filled them. */
+int wbo_dtw_alignment(const double *X, idx_t n, const double *Y, idx_t m, idx_t r,
+                      const double *weights, double *out)
+{
+    if (!(0 < r && r <= imax(n, m))) return -1;
+    double v, w = 1.0;
+#define OUT(i, j) out[(i) * m + (j)]
+    v = X[0] - Y[0];
+    if (weights) w = weights[0];
+    OUT(0, 0) = v * v * w;
+    for (idx_t i = 1; i < imin(n, r + 1); i++) {
+        v = X[i] - Y[0];
+        if (weights) w = weights[i];
+        OUT(i, 0) = OUT(i - 1, 0) + v * v * w;
+    }
+    for (idx_t i = 1; i < imin(m, imax(0, m - n) + r); i++) {
+        v = X[0] - Y[i];
+        if (weights) w = weights[i];
+        OUT(0, i) = OUT(0, i - 1) + v * v * w;
+    }
+    if (imax(0, m - n) + r < m) OUT(0, imax(0, m - n) + r) = INF;
+    for (idx_t i = 1; i < n; i++) {
+        idx_t js = imax(0, i - imax(0, n - m) - r + 1);
+        idx_t je = imin(m, i + imax(0, m - n) + r);
+        if (js > 0) OUT(i, js - 1) = INF;
+        for (idx_t j = js; j < je; j++) {
+            v = X[i] - Y[j];
+            double x = OUT(i - 1, j);
+            double y = j > 0 ? OUT(i, j - 1) : INF;
+            double z = j > 0 ? OUT(i - 1, j - 1) : INF;
+            if (weights) w = weights[labs((long)(i - j))];
+            OUT(i, j) = dmin(dmin(x, y), z) + v * v * w;
+        }
+        if (je < m) OUT(i, je) = INF;
+    }
+#undef OUT
+    return 0;
+}

@@ -1,0 +1,205 @@
+"""Generate the golden fixtures in this folder by running the reference itself.
+
+Usage (in a container where the reference wildboar is built and importable)::
+
+    WILDBOAR_REF_PATH=/path/to/built/wildboar/src python tests/golden/make_golden.py
+
+The reference is imported from ``WILDBOAR_REF_PATH`` and called through its
+public API (``wildboar.distance.pairwise_distance``, ``paired_distance``,
+``argmin_distance``, ``pairwise_subsequence_distance`` and
+``wildboar.distance.dtw.dtw_alignment``).  Inputs are seeded Gaussian random
+walks; every case stores its inputs, its call arguments and the reference's
+outputs in ``golden.npz`` with a JSON index in ``golden.json``.  The fixtures
+are read by tests/test_oracle_golden.py (oracle pinning) and by the GPU parity
+tests.  Nothing at test time imports the reference.
+"""
+
+import json
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _walk(rng, shape, scale=1.0):
+    return np.cumsum(rng.standard_normal(shape) * scale, axis=-1)
+
+
+ELASTIC = [
+    ("dtw", {"r": 0.0}),
+    ("dtw", {"r": 0.1}),
+    ("dtw", {"r": 0.3}),
+    ("dtw", {"r": 1.0}),
+    ("wdtw", {"r": 1.0, "g": 0.05}),
+    ("wdtw", {"r": 0.2, "g": 0.5}),
+    ("ddtw", {"r": 1.0}),
+    ("ddtw", {"r": 0.15}),
+    ("wddtw", {"r": 1.0, "g": 0.05}),
+    ("adtw", {"r": 1.0, "p": 1.0}),
+    ("adtw", {"r": 0.3, "p": 0.1}),
+    ("adtw", {"r": 1.0, "p": 10.0}),
+    ("lcss", {"r": 1.0, "epsilon": 0.5}),
+    ("lcss", {"r": 0.2, "epsilon": 1.0}),
+    ("wlcss", {"r": 1.0, "epsilon": 0.8, "g": 0.05}),
+    ("edr", {"r": 1.0}),
+    ("edr", {"r": 0.25, "epsilon": 0.4}),
+    ("erp", {"r": 1.0, "g": 0.0}),
+    ("erp", {"r": 0.2, "g": 0.5}),
+    ("msm", {"r": 1.0, "c": 1.0}),
+    ("msm", {"r": 0.1, "c": 0.5}),
+    ("msm", {"r": 0.3, "c": 0.1}),
+    ("twe", {"r": 1.0, "penalty": 1.0, "stiffness": 0.001}),
+    ("twe", {"r": 0.2, "penalty": 0.5, "stiffness": 0.1}),
+    ("euclidean", {}),
+]
+
+
+def main():
+    ref = os.environ.get("WILDBOAR_REF_PATH")
+    if ref:
+        sys.path.insert(0, ref)
+    import wildboar
+    from wildboar.distance import (
+        argmin_distance,
+        paired_distance,
+        pairwise_distance,
+        pairwise_subsequence_distance,
+    )
+    from wildboar.distance.dtw import dtw_alignment
+
+    rng = np.random.default_rng(20261203)
+    arrays = {}
+    cases = []
+
+    def add(name, kind, inputs, args, outputs):
+        entry = {"name": name, "kind": kind, "args": args, "inputs": {}, "outputs": {}}
+        for k, v in inputs.items():
+            key = f"{name}/in/{k}"
+            arrays[key] = np.asarray(v)
+            entry["inputs"][k] = key
+        for k, v in outputs.items():
+            key = f"{name}/out/{k}"
+            arrays[key] = np.asarray(v)
+            entry["outputs"][k] = key
+        cases.append(entry)
+
+    # equal-length pairwise, 6 x 5, L = 40
+    X = _walk(rng, (6, 40))
+    Y = _walk(rng, (5, 40))
+    # unequal lengths: Y shorter, and X shorter
+    Xs = _walk(rng, (4, 33))
+    Yl = _walk(rng, (5, 47))
+    for ci, (metric, params) in enumerate(ELASTIC):
+        tag = f"{metric}_{ci}"
+        d = pairwise_distance(X, Y, metric=metric, metric_params=params)
+        add(f"pairwise_eq_{tag}", "pairwise", {"x": X, "y": Y},
+            {"metric": metric, "metric_params": params}, {"d": d})
+        d = pairwise_distance(X, metric=metric, metric_params=params)
+        add(f"singleton_{tag}", "singleton", {"x": X},
+            {"metric": metric, "metric_params": params}, {"d": d})
+        if metric != "euclidean":
+            d = pairwise_distance(Xs, Yl, metric=metric, metric_params=params)
+            add(f"pairwise_uneq_{tag}", "pairwise", {"x": Xs, "y": Yl},
+                {"metric": metric, "metric_params": params}, {"d": d})
+            # WeightedDerivativeDtwMetric.reset sizes its x-derivative buffer by
+            # Y.shape[2] (distance/_elastic.pyx:3420), so a longer x overruns
+            # the heap in the reference; that case is not recorded.
+            if metric != "wddtw":
+                d = pairwise_distance(Yl, Xs, metric=metric, metric_params=params)
+                add(f"pairwise_uneq2_{tag}", "pairwise", {"x": Yl, "y": Xs},
+                    {"metric": metric, "metric_params": params}, {"d": d})
+        d = paired_distance(X[:5], Y, metric=metric, metric_params=params)
+        add(f"paired_eq_{tag}", "paired", {"x": X[:5], "y": Y},
+            {"metric": metric, "metric_params": params}, {"d": d})
+        for k in (1, 3):
+            Q = _walk(rng, (4, 30))
+            C = _walk(rng, (9, 30))
+            idx, dist = argmin_distance(Q, C, k=k, metric=metric, metric_params=params,
+                                        return_distance=True)
+            add(f"argmin_k{k}_{tag}", "argmin", {"x": Q, "y": C},
+                {"metric": metric, "metric_params": params, "k": k},
+                {"idx": idx, "dist": dist})
+            if metric not in ("euclidean", "wddtw"):
+                C2 = _walk(rng, (7, 26))
+                idx, dist = argmin_distance(Q, C2, k=k, metric=metric,
+                                            metric_params=params, return_distance=True)
+                add(f"argmin_uneq_k{k}_{tag}", "argmin", {"x": Q, "y": C2},
+                    {"metric": metric, "metric_params": params, "k": k},
+                    {"idx": idx, "dist": dist})
+
+    # lower bound pruning on dtw
+    Q = _walk(rng, (5, 32))
+    C = _walk(rng, (12, 32))
+    full = pairwise_distance(Q, C, metric="dtw", metric_params={"r": 0.2})
+    lb = full * rng.uniform(0.3, 1.0, size=full.shape)
+    idx, dist = argmin_distance(Q, C, k=3, metric="dtw", metric_params={"r": 0.2},
+                                lower_bound=lb, return_distance=True)
+    add("argmin_lb_dtw", "argmin", {"x": Q, "y": C, "lower_bound": lb},
+        {"metric": "dtw", "metric_params": {"r": 0.2}, "k": 3},
+        {"idx": idx, "dist": dist})
+
+    # multivariate, dim mean / full / int
+    XM = _walk(rng, (4, 3, 25))
+    YM = _walk(rng, (3, 3, 25))
+    for dim in ("mean", "full", 1):
+        for metric, params in (("dtw", {"r": 0.3}), ("msm", {"c": 1.0}),
+                               ("edr", {}), ("euclidean", {})):
+            d = pairwise_distance(XM, YM, dim=dim, metric=metric, metric_params=params)
+            add(f"pairwise_dim_{dim}_{metric}", "pairwise", {"x": XM, "y": YM},
+                {"metric": metric, "metric_params": params, "dim": dim}, {"d": d})
+            d = paired_distance(XM[:3], YM, dim=dim, metric=metric, metric_params=params)
+            add(f"paired_dim_{dim}_{metric}", "paired", {"x": XM[:3], "y": YM},
+                {"metric": metric, "metric_params": params, "dim": dim}, {"d": d})
+
+    # short series edge cases
+    for L in (1, 2, 3):
+        A = _walk(rng, (3, L))
+        B = _walk(rng, (2, L))
+        for metric, params in (("dtw", {}), ("ddtw", {}), ("msm", {}), ("twe", {}),
+                               ("lcss", {}), ("edr", {}), ("erp", {})):
+            d = pairwise_distance(A, B, metric=metric, metric_params=params)
+            add(f"short_L{L}_{metric}", "pairwise", {"x": A, "y": B},
+                {"metric": metric, "metric_params": params}, {"d": d})
+
+    # subsequence (euclidean / scaled_euclidean)
+    T = _walk(rng, (6, 120))
+    shp = [_walk(rng, (int(n),)) for n in rng.integers(5, 40, size=7)]
+    shp.append(T[2, 30:55].copy())  # exact match present
+    shp.append(np.full(9, 3.0))     # constant shapelet (std 0)
+    packed = np.concatenate(shp)
+    lens = np.array([s.shape[0] for s in shp])
+    for metric in ("euclidean", "scaled_euclidean"):
+        d, i = pairwise_subsequence_distance(shp, T, metric=metric, return_index=True)
+        add(f"subseq_{metric}", "subsequence",
+            {"x": T, "shapelets": packed, "lengths": lens},
+            {"metric": metric}, {"d": d, "idx": i})
+
+    # dtw_alignment (differentiation oracle)
+    a = _walk(rng, (30,))
+    b = _walk(rng, (24,))
+    for r in (0.2, 1.0):
+        al = dtw_alignment(a, b, r=r)
+        warp = max(math.floor(max(30, 24) * r), 1)
+        # only band cells and their +-1 INF sentinels are defined
+        mask = np.zeros(al.shape, dtype=bool)
+        for i in range(30):
+            js = max(0, i - max(0, 30 - 24) - warp + 1)
+            je = min(24, i + max(0, 24 - 30) + warp)
+            mask[i, js:je] = True
+        if True:
+            mask[0, : min(24, max(0, 24 - 30) + warp)] = True
+        add(f"alignment_r{r}", "alignment", {"x": a, "y": b, "mask": mask},
+            {"r": r}, {"a": np.where(mask, al, 0.0)})
+
+    np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
+    with open(os.path.join(HERE, "golden.json"), "w") as f:
+        json.dump({"reference_version": getattr(wildboar, "__version__", "?"),
+                   "numpy": np.__version__, "cases": cases}, f, indent=1)
+    print(len(cases), "cases")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,163 @@
+"""CPU-only checks: C ABI symbols, metric registry and validation, failure
+without a GPU (no silent CPU fallback)."""
+
+import ctypes
+import os
+import pickle
+import re
+
+import numpy as np
+import pytest
+
+from wildboar_gb300 import _build, _lib
+from wildboar_gb300.distance import (
+    _METRICS,
+    argmin_distance,
+    pairwise_distance,
+    pairwise_subsequence_distance,
+)
+from wildboar_gb300.distance._validation import is_end_of_series
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _header_symbols():
+    syms = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if f.endswith(".h"):
+            with open(os.path.join(inc, f)) as fh:
+                text = fh.read()
+            syms |= set(re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(wb_\w+)\s*\(", text, re.M))
+    return syms
+
+
+@pytest.fixture(scope="module")
+def libpath():
+    return _build.build()
+
+
+def test_library_exports_every_declared_symbol(libpath):
+    syms = _header_symbols()
+    assert {"wb_pairwise_distance", "wb_paired_distance", "wb_argmin_distance",
+            "wb_pairwise_subsequence_distance", "wb_last_error"} <= syms
+    L = ctypes.CDLL(libpath)
+    missing = [s for s in sorted(syms) if not hasattr(L, s)]
+    assert not missing, missing
+
+
+def test_no_gpu_raises_instead_of_falling_back():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(RuntimeError):
+        pairwise_distance(np.ones((2, 4)), np.zeros((2, 4)), metric="dtw")
+
+
+@pytest.mark.parametrize("metric", sorted(_METRICS))
+def test_pickle(metric):
+    m = _METRICS[metric]()
+    m2 = pickle.loads(pickle.dumps(m))
+    assert m == m2 and type(m2) is type(m)
+
+
+@pytest.mark.parametrize("metric", sorted(_METRICS))
+def test_metric_raises_bad_argument(metric):
+    # test_distance.py:809-813
+    with pytest.raises(TypeError):
+        _METRICS[metric](not_an_argument=10)
+
+
+@pytest.mark.parametrize("metric", ["dtw", "ddtw", "wdtw", "wddtw", "adtw", "lcss", "wlcss",
+                                    "erp", "edr", "msm", "twe"])
+@pytest.mark.parametrize("r", [-0.1, 1.1])
+def test_raises_bad_r_argument_value(metric, r):
+    # test_distance.py:816-826
+    with pytest.raises(ValueError, match="r =="):
+        _METRICS[metric](r=r)
+
+
+@pytest.mark.parametrize("metric,params,match", [
+    ("lcss", {"epsilon": 0}, "epsilon == 0.0, must be > 0"),
+    ("lcss", {"epsilon": -1}, "epsilon"),
+    ("edr", {"epsilon": 0}, "epsilon == 0.0, must be > 0"),
+    ("msm", {"c": -1}, "c == -1.0, must be >= 0"),
+    ("twe", {"penalty": -1}, "penalty == -1.0, must be >= 0.0"),
+    ("twe", {"stiffness": 0}, "stiffness == 0.0, must be > 0.0"),
+    ("erp", {"g": -1}, "g == -1.0, must be >= 0"),
+    ("wdtw", {"g": -1}, "g == -1.0, must be >= 0.0"),
+])
+def test_raises_bad_argument_value(metric, params, match):
+    # test_distance.py:829-848
+    with pytest.raises(ValueError, match=match):
+        _METRICS[metric](**params)
+
+
+def test_lcss_threshold_is_deprecated():
+    with pytest.warns(FutureWarning):
+        m = _METRICS["lcss"](threshold=0.5)
+    assert m.epsilon == 0.5
+
+
+def test_unknown_metric():
+    with pytest.raises(ValueError, match="unsupported metric"):
+        pairwise_distance(np.ones((2, 3)), metric="nope")
+
+
+def test_nan_and_eos_are_rejected():
+    x = np.ones((3, 5))
+    x[1, 2] = np.nan
+    with pytest.raises(ValueError, match="Input contains NaN."):
+        pairwise_distance(x, np.ones((2, 5)), metric="dtw")
+    eos = np.array(0x7F800009, dtype="I").view("f").item()
+    x = np.ones((3, 5))
+    x[0, 4] = eos
+    assert is_end_of_series(x).sum() == 1
+    with pytest.raises(ValueError, match="expected time series of equal length"):
+        pairwise_distance(x, np.ones((2, 5)), metric="dtw")
+    x = np.ones((3, 5))
+    x[0, 0] = np.inf
+    with pytest.raises(ValueError, match="infinity"):
+        pairwise_distance(x, np.ones((2, 5)), metric="dtw")
+
+
+def test_shape_errors():
+    with pytest.raises(ValueError, match="not compatible"):
+        pairwise_distance(np.ones((2, 3, 4)), np.ones((2, 4)), metric="dtw")
+    with pytest.raises(ValueError, match="same number of dimensions"):
+        pairwise_distance(np.ones((2, 3, 4)), np.ones((2, 2, 4)), metric="dtw")
+    with pytest.raises(ValueError, match="Illegal n_timestep"):
+        pairwise_distance(np.ones((2, 4)), np.ones((2, 5)), metric="euclidean")
+    with pytest.raises(ValueError, match="dim"):
+        pairwise_distance(np.ones((2, 3, 4)), np.ones((2, 3, 4)), dim=3, metric="dtw")
+
+
+def test_singleton_1d_is_zero():
+    assert pairwise_distance(np.ones(5), metric="dtw") == 0.0
+
+
+def test_argmin_parameter_validation():
+    with pytest.raises(ValueError, match="'k' parameter"):
+        argmin_distance(np.ones((2, 4)), np.ones((3, 4)), k=0)
+    with pytest.raises(TypeError, match="'metric' parameter"):
+        argmin_distance(np.ones((2, 4)), np.ones((3, 4)), metric="nope")
+    with pytest.raises(ValueError, match="lower bound must be of shape"):
+        argmin_distance(np.ones((2, 4)), np.ones((3, 4)), metric="dtw",
+                        lower_bound=np.ones((2, 2)))
+    with pytest.raises(ValueError, match="dim"):
+        argmin_distance(np.ones((2, 4)), np.ones((3, 4)), metric="dtw", dim=1)
+
+
+def test_subsequence_validation():
+    with pytest.raises(ValueError, match="cannot be empty"):
+        pairwise_subsequence_distance([], np.ones((2, 10)))
+    with pytest.raises(ValueError, match="Invalid subsequnce shape"):
+        pairwise_subsequence_distance(np.ones(11), np.ones((2, 10)))
+    with pytest.raises(ValueError, match="unsupported metric"):
+        pairwise_subsequence_distance(np.ones(3), np.ones((2, 10)), metric="dtw")
+
+
+def test_params_struct_matches_header():
+    # wb_params is seven doubles in declaration order
+    assert ctypes.sizeof(_lib.Params) == 7 * 8
+    assert ctypes.sizeof(_lib.Series) == 8 + 3 * 8 + 2 * 4

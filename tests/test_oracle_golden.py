@@ -1,0 +1,120 @@
+"""Pin the CPU oracle against the reference's own outputs (golden fixtures).
+
+The fixtures were produced by running the reference wildboar build through its
+public API (tests/golden/make_golden.py).  On x86-64 the oracle must reproduce
+them bit for bit; elsewhere a libm exp/pow that rounds differently may move
+WDTW weights or EDR epsilons by an ulp, hence the 1e-12 relative fallback.
+"""
+
+import platform
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import _golden
+
+EXACT = platform.machine() in ("x86_64", "AMD64")
+
+
+def _ts(x):
+    x = np.asarray(x, dtype=float)
+    if x.ndim == 1:
+        return x.reshape(1, 1, -1)
+    if x.ndim == 2:
+        return x.reshape(x.shape[0], 1, x.shape[1])
+    return x
+
+
+def _format_return(x, y_dims, x_dims):
+    # distance/_distance.py:514-540
+    if x_dims == 1 and y_dims == 1 and x.size == 1:
+        return x.item()
+    elif x_dims == 1 or y_dims == 1:
+        return np.squeeze(x)
+    return x
+
+
+def _dims(fn, n_dims, dim):
+    if n_dims == 1 and dim == "mean":
+        dim = 0
+    if dim in ("mean", "full"):
+        ds = [fn(d) for d in range(n_dims)]
+        return np.mean(ds, axis=0) if dim == "mean" else np.stack(ds, axis=0)
+    return fn(dim)
+
+
+def run_oracle(case):
+    a = case["args"]
+    metric, params = a.get("metric"), a.get("metric_params", {})
+    dim = a.get("dim", "mean")
+    kind = case["kind"]
+    inp = case["inputs"]
+    if kind == "pairwise":
+        x, y = inp["x"], inp["y"]
+        X, Y = _ts(x), _ts(y)
+        d = _dims(lambda k: O.pairwise(X, Y, dim=k, metric=metric, metric_params=params),
+                  X.shape[1], dim)
+        return {"d": _format_return(d, y.ndim, x.ndim)}
+    if kind == "singleton":
+        X = _ts(inp["x"])
+        d = _dims(lambda k: O.pairwise(X, None, dim=k, metric=metric,
+                                       metric_params=params), X.shape[1], dim)
+        return {"d": d}
+    if kind == "paired":
+        x, y = inp["x"], inp["y"]
+        X, Y = _ts(x), _ts(y)
+        d = _dims(lambda k: O.paired(X, Y, dim=k, metric=metric, metric_params=params),
+                  X.shape[1], dim)
+        return {"d": _format_return(d, y.ndim, x.ndim)}
+    if kind == "argmin":
+        idx, dist = O.argmin(inp["x"], inp["y"], k=a["k"], metric=metric,
+                             metric_params=params, lower_bound=inp.get("lower_bound"))
+        return {"idx": idx, "dist": dist}
+    if kind == "subsequence":
+        shp = _golden.unpack_shapelets(case)
+        d, i = O.subsequence(shp, inp["x"], metric=metric)
+        return {"d": d, "idx": i}
+    if kind == "alignment":
+        al = O.dtw_alignment(inp["x"], inp["y"], r=a["r"])
+        return {"a": np.where(inp["mask"], al, 0.0)}
+    raise AssertionError(kind)
+
+
+CASES = _golden.cases()
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_oracle_matches_reference(case):
+    got = run_oracle(case)
+    for key, want in case["outputs"].items():
+        g = np.asarray(got[key])
+        want = np.asarray(want)
+        assert g.shape == want.shape, (key, g.shape, want.shape)
+        if want.dtype.kind in "iu":
+            np.testing.assert_array_equal(g, want)
+        elif EXACT:
+            np.testing.assert_array_equal(g, want)
+        else:
+            np.testing.assert_allclose(g, want, rtol=1e-12, atol=0)
+
+
+def test_golden_covers_every_metric_and_kind():
+    kinds = {c["kind"] for c in CASES}
+    assert kinds >= {"pairwise", "singleton", "paired", "argmin", "subsequence",
+                     "alignment"}
+    metrics = {c["args"].get("metric") for c in CASES}
+    assert metrics >= {"dtw", "wdtw", "ddtw", "wddtw", "adtw", "lcss", "wlcss", "edr",
+                       "erp", "msm", "twe", "euclidean", "scaled_euclidean"}
+
+
+def test_alignment_endpoint_equals_dtw():
+    # sqrt of the last alignment cell is the dtw distance when the warp widths
+    # agree (equal lengths): distance/dtw.py:246-290 vs _elastic.pyx:3167-3186
+    rng = np.random.default_rng(5)
+    x = np.cumsum(rng.standard_normal(64))
+    y = np.cumsum(rng.standard_normal(64))
+    for r in (0.1, 0.2, 1.0):
+        al = O.dtw_alignment(x, y, r=r)
+        d = O.distance_1d(x, y, metric="dtw", metric_params={"r": r})
+        assert np.sqrt(al[-1, -1]) == d

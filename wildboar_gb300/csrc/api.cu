@@ -1,0 +1,694 @@
+// api.cu -- the extern "C" entry points declared in include/wbgpu.h.
+//
+// Each call: validates its arguments, stages host inputs into the stream's
+// device workspace (one 2-D copy per series set gathers the requested dim),
+// prepares per-metric tables on the device, launches the kernels and copies
+// host outputs back.  Host-side work is limited to argument checks and the
+// metric constructor's parameter tables (wdtw weights with libm exp, exactly
+// as WeightedDtwMetric.reset computes them, distance/_elastic.pyx:3333-3341).
+
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <vector>
+
+#include "elastic.cuh"
+#include "subseq.cuh"
+
+namespace wb {
+
+// --------------------------------------------------------------------------
+// errors
+
+static thread_local std::string g_last_error;
+static std::atomic<int64_t> g_launches{0};
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return WB_ENOMEM;
+    return WB_ECUDA;
+}
+
+void count_launch(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// --------------------------------------------------------------------------
+// device info
+
+const DeviceInfo &device_info() {
+    static thread_local DeviceInfo cache[64];
+    static thread_local bool have[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) dev = 0;
+    if (!have[dev]) {
+        DeviceInfo d;
+        d.device = dev;
+        cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&d.max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaDeviceGetAttribute(&d.smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        if (d.sm_count <= 0) d.sm_count = 1;
+        cache[dev] = d;
+        have[dev] = true;
+    }
+    return cache[dev];
+}
+
+// --------------------------------------------------------------------------
+// workspace
+
+static std::mutex g_arena_mu;
+static std::map<std::pair<int, cudaStream_t>, Arena *> g_arenas;
+
+static Arena *arena_for(cudaStream_t s) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> g(g_arena_mu);
+    auto key = std::make_pair(dev, s);
+    auto it = g_arenas.find(key);
+    if (it != g_arenas.end()) return it->second;
+    Arena *a = new Arena();
+    g_arenas[key] = a;
+    return a;
+}
+
+Workspace::Workspace(cudaStream_t stream)
+    : arena_(arena_for(stream)), stream_(stream), lock_(arena_->mu) {
+    arena_->used = 0;
+}
+
+Workspace::~Workspace() { arena_->used = 0; }
+
+int Workspace::reserve(size_t bytes) {
+    bytes = align256(bytes) + 4096;
+    if (bytes > arena_->cap) {
+        if (arena_->base) {
+            // cudaFree waits for the device, so earlier work on this stream
+            // that still reads the arena has finished
+            cudaError_t e = cudaFree(arena_->base);
+            arena_->base = nullptr;
+            arena_->cap = 0;
+            if (e != cudaSuccess) return cuda_fail(e, "cudaFree(workspace)");
+        }
+        size_t cap = bytes + bytes / 4;
+        cudaError_t e = cudaMalloc((void **)&arena_->base, cap);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            arena_->base = nullptr;
+            if (e != cudaErrorMemoryAllocation) return cuda_fail(e, "cudaMalloc(workspace)");
+            return fail(WB_ENOMEM, "cannot allocate " + std::to_string(cap) +
+                                       " bytes of device workspace");
+        }
+        arena_->cap = cap;
+    }
+    arena_->used = 0;
+    return WB_OK;
+}
+
+// --------------------------------------------------------------------------
+// argument handling
+
+static int check_series(const wb_series *s, const char *name, bool allow_f32 = false) {
+    if (!s) return fail(WB_EINVAL, std::string(name) + " is NULL");
+    if (s->n < 0 || s->n_dims < 1 || s->n_timestep < 1)
+        return fail(WB_EINVAL, std::string(name) + " has an invalid shape");
+    if (s->n > 0 && !s->data) return fail(WB_EINVAL, std::string(name) + " data is NULL");
+    if (s->dtype != WB_F64 && !(allow_f32 && s->dtype == WB_F32))
+        return fail(WB_EINVAL, std::string(name) + " must be float64");
+    if (s->n_timestep > (int64_t)1 << 28)
+        return fail(WB_EINVAL, std::string(name) + " has too many timesteps");
+    return WB_OK;
+}
+
+static bool is_elastic(int metric) {
+    return metric >= WB_DTW && metric <= WB_TWE;
+}
+
+static bool weighted(int metric) {
+    return metric == WB_WDTW || metric == WB_WDDTW || metric == WB_WLCSS;
+}
+
+static bool derivative(int metric) { return metric == WB_DDTW || metric == WB_WDDTW; }
+
+// Bytes needed to stage one dim of a series set on the device.
+static size_t stage_bytes(const wb_series *s) {
+    return s->on_device ? 0 : align256((size_t)s->n * s->n_timestep * sizeof(double));
+}
+
+// Series set of one dim: device data used in place, host data gathered into
+// the workspace with one strided copy.
+static int stage(const wb_series *s, int64_t dim, Workspace &ws, SeriesSet &out) {
+    out.count = s->n;
+    out.len = (int)s->n_timestep;
+    const double *base = static_cast<const double *>(s->data);
+    if (s->on_device) {
+        out.base = base + dim * s->n_timestep;
+        out.stride = s->n_dims * s->n_timestep;
+        return WB_OK;
+    }
+    WB_TAKE(d, double, ws, (size_t)s->n * s->n_timestep);
+    if (s->n > 0) {
+        WB_CUDA(cudaMemcpy2DAsync(d, s->n_timestep * sizeof(double),
+                                  base + dim * s->n_timestep,
+                                  s->n_dims * s->n_timestep * sizeof(double),
+                                  s->n_timestep * sizeof(double), s->n,
+                                  cudaMemcpyHostToDevice, ws.stream()));
+    }
+    out.base = d;
+    out.stride = s->n_timestep;
+    return WB_OK;
+}
+
+// logistic weights of WeightedDtwMetric.reset (distance/_elastic.pyx:3333-3341)
+static std::vector<double> logistic_weights(int64_t n, double g) {
+    std::vector<double> w((size_t)std::max<int64_t>(n, 1));
+    for (int64_t i = 0; i < n; i++)
+        w[i] = 1.0 / (1.0 + std::exp(-g * ((double)i - (double)n / 2.0)));
+    return w;
+}
+
+// Everything a recurrence job needs beyond the two series sets.
+struct MetricPrep {
+    ElasticJob job;
+    std::vector<double> weights;
+    size_t bytes = 0;  // workspace bytes needed by `build`
+};
+
+// Fill the metric fields of `job` (kind, result, band, parameters) for the
+// metric's distance (ea = false) or eadistance (ea = true) entry.
+static int metric_fields(int metric, const wb_params *p, int xl, int yl, bool ea,
+                         ElasticJob &J) {
+    J.len_norm_rows = xl;
+    J.len_norm_cols = yl;
+    int rl = std::min(xl, yl);
+    if (metric != WB_EUCLIDEAN && !(p->r >= 0.0 && p->r <= 1.0))
+        return fail(WB_EINVAL, "r must be in [0, 1]");
+    switch (metric) {
+        case WB_EUCLIDEAN:
+            J.kind = K_EUCLID;
+            J.result = R_SQRT;
+            J.band = 1;
+            return WB_OK;
+        case WB_DTW:
+        case WB_WDTW:
+            J.kind = metric == WB_DTW ? K_DTW : K_WDTW;
+            J.result = R_SQRT;
+            J.band = compute_r(rl, p->r);
+            return WB_OK;
+        case WB_DDTW:
+        case WB_WDDTW:
+            J.kind = metric == WB_DDTW ? K_DTW : K_WDTW;
+            J.result = R_SQRT;
+            // DerivativeDtwMetric: _distance uses the series lengths,
+            // _eadistance the slope lengths (distance/_elastic.pyx:3280, 3308)
+            J.band = compute_r(ea ? rl - 2 : rl, p->r);
+            return WB_OK;
+        case WB_ADTW:
+            J.kind = p->p >= 0.0 ? K_ADTW : K_ADTW_ANY;
+            J.result = R_SQRT;
+            J.p = p->p;
+            J.band = compute_r(rl, p->r);
+            return WB_OK;
+        case WB_LCSS:
+        case WB_WLCSS:
+            if (!(p->epsilon > 0.0)) return fail(WB_EINVAL, "epsilon must be > 0");
+            J.kind = metric == WB_LCSS ? K_LCSS : K_WLCSS;
+            J.result = R_LCSS;
+            J.eps = p->epsilon;
+            J.band = compute_r(rl, p->r);
+            return WB_OK;
+        case WB_EDR:
+            J.kind = K_EDR;
+            J.result = R_EDR;
+            J.eps = p->epsilon;
+            // EdrMetric.eadistance passes min(X.shape[2], X.shape[2])
+            // (distance/_elastic.pyx:3833)
+            J.band = compute_r(ea ? xl : rl, p->r);
+            return WB_OK;
+        case WB_ERP:
+            J.kind = K_ERP;
+            J.result = R_IDENT;
+            J.g = p->g;
+            J.band = compute_r(rl, p->r);
+            return WB_OK;
+        case WB_MSM:
+            J.kind = K_MSM;
+            J.result = R_IDENT;
+            J.c = p->c;
+            J.band = compute_r(rl, p->r);
+            return WB_OK;
+        case WB_TWE:
+            J.kind = K_TWE;
+            J.result = R_IDENT;
+            J.penalty = p->penalty;
+            J.stiffness = p->stiffness;
+            J.band = compute_r(rl, p->r);
+            return WB_OK;
+    }
+    return fail(WB_EUNSUPPORTED, "unsupported metric id " + std::to_string(metric));
+}
+
+// Workspace bytes of the per-metric tables for rows R and columns C.
+static size_t table_bytes(int metric, const wb_params *p, const SeriesSet &R,
+                          const SeriesSet &C, int64_t nR, int64_t nC, int lR, int lC) {
+    size_t b = 0;
+    if (derivative(metric))
+        b += align256((size_t)nR * std::max(lR - 2, 0) * 8) +
+             align256((size_t)nC * std::max(lC - 2, 0) * 8);
+    if (weighted(metric)) b += align256((size_t)std::max(lR, lC) * 8);
+    if (metric == WB_EDR && std::isnan(p->epsilon)) b += align256(nR * 8) + align256(nC * 8);
+    if (metric == WB_ERP) b += align256(nR * 8) + align256(nC * 8) + align256((size_t)nC * lC * 8);
+    if (metric == WB_TWE) b += align256((size_t)nC * lC * 8) + align256((size_t)std::max(lR, lC) * 8);
+    return b;
+}
+
+// Build the device tables of a recurrence job whose row/column sets are
+// already staged.  `same` marks the singleton path (rows and columns are the
+// same array, reset(x, x)).  wlen_* are the widths that size the weights.
+static int build_tables(int metric, const wb_params *p, ElasticJob &J, Workspace &ws,
+                        bool same, int wlen_rows, int wlen_cols) {
+    cudaStream_t s = ws.stream();
+    if (derivative(metric)) {
+        if (std::min(J.rows.len, J.cols.len) < 3) {
+            J.all_zero = 1;
+        } else {
+            SeriesSet dr = J.rows, dc = J.cols;
+            WB_TAKE(dR, double, ws, (size_t)J.rows.count * (J.rows.len - 2));
+            WB_TRY(launch_slopes(J.rows, dR, s));
+            dr.base = dR;
+            dr.stride = J.rows.len - 2;
+            dr.len = J.rows.len - 2;
+            if (same) {
+                dc = dr;
+            } else {
+                WB_TAKE(dC, double, ws, (size_t)J.cols.count * (J.cols.len - 2));
+                WB_TRY(launch_slopes(J.cols, dC, s));
+                dc.base = dC;
+                dc.stride = J.cols.len - 2;
+                dc.len = J.cols.len - 2;
+            }
+            J.rows = dr;
+            J.cols = dc;
+        }
+    }
+    if (weighted(metric)) {
+        int64_t nw = metric == WB_WDDTW ? std::max(wlen_rows - 2, wlen_cols - 2)
+                                        : std::max(wlen_rows, wlen_cols);
+        std::vector<double> w = logistic_weights(nw, p->g);
+        WB_TAKE(dw, double, ws, std::max<size_t>(w.size(), 1));
+        WB_CUDA(cudaMemcpyAsync(dw, w.data(), w.size() * sizeof(double),
+                                cudaMemcpyHostToDevice, s));
+        // the host vector must outlive the copy
+        WB_CUDA(cudaStreamSynchronize(s));
+        J.weights = dw;
+    }
+    if (metric == WB_EDR && std::isnan(p->epsilon)) {
+        WB_TAKE(sr, double, ws, J.rows.count);
+        WB_TRY(launch_mean_std(J.rows, sr, s));
+        double *sc = sr;
+        if (!same) {
+            sc = ws.take<double>(J.cols.count);
+            if (!sc) return fail(WB_ENOMEM, "workspace reservation exceeded");
+            WB_TRY(launch_mean_std(J.cols, sc, s));
+        }
+        J.std_rows = sr;
+        J.std_cols = sc;
+    }
+    if (metric == WB_ERP) {
+        WB_TAKE(gr, double, ws, J.rows.count);
+        WB_TAKE(gc, double, ws, J.cols.count);
+        WB_TAKE(gt, double, ws, (size_t)J.cols.count * J.cols.len);
+        WB_TRY(launch_erp_tables(J.rows, p->g, nullptr, gr, s));
+        WB_TRY(launch_erp_tables(J.cols, p->g, gt, gc, s));
+        J.gsum_rows = gr;
+        J.gsum_cols = gc;
+        J.gtab_cols = gt;
+    }
+    if (metric == WB_TWE) {
+        WB_TAKE(dt, double, ws, (size_t)J.cols.count * J.cols.len);
+        WB_TRY(launch_twe_tables(J.cols, dt, s));
+        int ns = std::max(J.rows.len, J.cols.len);
+        WB_TAKE(st, double, ws, ns);
+        WB_TRY(launch_fill_stab(p->stiffness * 2.0, ns, st, s));
+        J.dtab_cols = dt;
+        J.stab = st;
+    }
+    return WB_OK;
+}
+
+static int finish_host_copy(void *dst, const void *src, size_t bytes, bool out_on_device,
+                            cudaStream_t s) {
+    if (out_on_device) return WB_OK;
+    if (bytes) WB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+    WB_CUDA(cudaStreamSynchronize(s));
+    return WB_OK;
+}
+
+static int check_dim(const wb_series *x, int64_t dim) {
+    if (dim < 0 || dim >= x->n_dims) return fail(WB_EINVAL, "The parameter dim must be 0 <= dim < n_dims");
+    return WB_OK;
+}
+
+}  // namespace wb
+
+using namespace wb;
+
+// ==========================================================================
+
+extern "C" int wb_pairwise_distance(const wb_series *x, const wb_series *y, int64_t dim,
+                                    int32_t metric, const wb_params *params, double *out,
+                                    int32_t out_on_device, void *stream_) {
+    WB_TRY(check_series(x, "x"));
+    if (y) WB_TRY(check_series(y, "y"));
+    if (!params) return fail(WB_EINVAL, "params is NULL");
+    if (!out && x->n > 0) return fail(WB_EINVAL, "out is NULL");
+    WB_TRY(check_dim(x, dim));
+    if (y && y->n_dims != x->n_dims)
+        return fail(WB_EINVAL, "x and y must have the same number of dimensions.");
+    if (!is_elastic(metric) && metric != WB_EUCLIDEAN)
+        return fail(WB_EUNSUPPORTED, "unsupported metric id " + std::to_string(metric));
+    const bool same = (y == nullptr);
+    const wb_series *yy = same ? x : y;
+    if (metric == WB_EUCLIDEAN && x->n_timestep != yy->n_timestep)
+        return fail(WB_EINVAL, "Illegal n_timestep for non-elastic distance measure");
+    cudaStream_t s = (cudaStream_t)stream_;
+    const int xl = (int)x->n_timestep, yl = (int)yy->n_timestep;
+    ElasticJob J;
+    WB_TRY(metric_fields(metric, params, xl, yl, false, J));
+    if (x->n == 0 || yy->n == 0) return WB_OK;
+
+    Workspace ws(s);
+    const size_t out_elems = (size_t)x->n * yy->n;
+    SeriesSet probeR{nullptr, 0, x->n, xl}, probeC{nullptr, 0, yy->n, yl};
+    size_t need = stage_bytes(x) + (same ? 0 : stage_bytes(yy)) +
+                  table_bytes(metric, params, probeR, probeC, x->n, yy->n, xl, yl) +
+                  (out_on_device ? 0 : align256(out_elems * 8));
+    // ring workspace depends on the band of the (possibly derivative) job
+    ElasticJob probe = J;
+    probe.rows = probeR;
+    probe.cols = probeC;
+    probe.mode = same ? PM_UPPER : PM_ALL;
+    if (derivative(metric) && std::min(xl, yl) >= 3) {
+        probe.rows.len -= 2;
+        probe.cols.len -= 2;
+    }
+    need += elastic_workspace_bytes(probe);
+    WB_TRY(ws.reserve(need));
+
+    WB_TRY(stage(x, dim, ws, J.rows));
+    if (same) J.cols = J.rows;
+    else WB_TRY(stage(yy, dim, ws, J.cols));
+    WB_TRY(build_tables(metric, params, J, ws, same, xl, yl));
+    double *dout = out_on_device ? out : ws.take<double>(out_elems);
+    if (!dout) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    J.out = dout;
+    J.out_ld = yy->n;
+    J.mode = same ? PM_UPPER : PM_ALL;
+    if (same) {
+        WB_CUDA(cudaMemsetAsync(dout, 0, out_elems * sizeof(double), s));
+    }
+    WB_TRY(launch_elastic(J, ws, nullptr));
+    return finish_host_copy(out, dout, out_elems * sizeof(double), out_on_device, s);
+}
+
+extern "C" int wb_paired_distance(const wb_series *x, const wb_series *y, int64_t dim,
+                                  int32_t metric, const wb_params *params, double *out,
+                                  int32_t out_on_device, void *stream_) {
+    WB_TRY(check_series(x, "x"));
+    WB_TRY(check_series(y, "y"));
+    if (!params) return fail(WB_EINVAL, "params is NULL");
+    WB_TRY(check_dim(x, dim));
+    if (x->n != y->n) return fail(WB_EINVAL, "x and y must have the same number of samples.");
+    if (y->n_dims != x->n_dims)
+        return fail(WB_EINVAL, "x and y must have the same number of dimensions.");
+    if (!is_elastic(metric) && metric != WB_EUCLIDEAN)
+        return fail(WB_EUNSUPPORTED, "unsupported metric id " + std::to_string(metric));
+    if (metric == WB_EUCLIDEAN && x->n_timestep != y->n_timestep)
+        return fail(WB_EINVAL, "Illegal n_timestep for non-elastic distance measure");
+    if (x->n == 0) return WB_OK;
+    if (!out) return fail(WB_EINVAL, "out is NULL");
+    cudaStream_t s = (cudaStream_t)stream_;
+    // the metric sees (y, x): rows of the recurrence are y's series
+    const int rl = (int)y->n_timestep, cl = (int)x->n_timestep;
+    ElasticJob J;
+    WB_TRY(metric_fields(metric, params, rl, cl, false, J));
+    Workspace ws(s);
+    SeriesSet probeR{nullptr, 0, y->n, rl}, probeC{nullptr, 0, x->n, cl};
+    ElasticJob probe = J;
+    probe.rows = probeR;
+    probe.cols = probeC;
+    probe.mode = PM_PAIRED;
+    if (derivative(metric) && std::min(rl, cl) >= 3) {
+        probe.rows.len -= 2;
+        probe.cols.len -= 2;
+    }
+    size_t need = stage_bytes(x) + stage_bytes(y) +
+                  table_bytes(metric, params, probeR, probeC, y->n, x->n, rl, cl) +
+                  elastic_workspace_bytes(probe) +
+                  (out_on_device ? 0 : align256((size_t)x->n * 8));
+    WB_TRY(ws.reserve(need));
+    WB_TRY(stage(y, dim, ws, J.rows));
+    WB_TRY(stage(x, dim, ws, J.cols));
+    WB_TRY(build_tables(metric, params, J, ws, false, rl, cl));
+    double *dout = out_on_device ? out : ws.take<double>(x->n);
+    if (!dout) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    J.out = dout;
+    J.out_ld = 0;
+    J.mode = PM_PAIRED;
+    WB_TRY(launch_elastic(J, ws, nullptr));
+    return finish_host_copy(out, dout, (size_t)x->n * sizeof(double), out_on_device, s);
+}
+
+extern "C" int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_t dim,
+                                  int32_t metric, const wb_params *params, int64_t k,
+                                  const double *lower_bound, int64_t *indices,
+                                  double *distances, int32_t out_on_device, void *stream_) {
+    WB_TRY(check_series(x, "x"));
+    WB_TRY(check_series(y, "y"));
+    if (!params) return fail(WB_EINVAL, "params is NULL");
+    WB_TRY(check_dim(x, dim));
+    if (y->n_dims != x->n_dims)
+        return fail(WB_EINVAL, "x and y must have the same number of dimensions.");
+    if (!is_elastic(metric) && metric != WB_EUCLIDEAN)
+        return fail(WB_EUNSUPPORTED, "unsupported metric id " + std::to_string(metric));
+    if (metric == WB_EUCLIDEAN && x->n_timestep != y->n_timestep)
+        return fail(WB_EINVAL, "Illegal n_timestep for non-elastic distance measure.");
+    if (k < 1) return fail(WB_EINVAL, "k must be >= 1");
+    if (k > y->n) k = y->n;
+    if (x->n == 0 || y->n == 0) return WB_OK;
+    if (!indices || !distances) return fail(WB_EINVAL, "outputs are NULL");
+    cudaStream_t s = (cudaStream_t)stream_;
+    const int xl = (int)x->n_timestep, yl = (int)y->n_timestep;
+    ElasticJob J;
+    WB_TRY(metric_fields(metric, params, xl, yl, true, J));
+    Workspace ws(s);
+    const size_t pairs = (size_t)x->n * y->n;
+    SeriesSet probeR{nullptr, 0, x->n, xl}, probeC{nullptr, 0, y->n, yl};
+    ElasticJob probe = J;
+    probe.rows = probeR;
+    probe.cols = probeC;
+    probe.mode = PM_ALL;
+    if (derivative(metric) && std::min(xl, yl) >= 3) {
+        probe.rows.len -= 2;
+        probe.cols.len -= 2;
+    }
+    size_t need = stage_bytes(x) + stage_bytes(y) +
+                  table_bytes(metric, params, probeR, probeC, x->n, y->n, xl, yl) +
+                  elastic_workspace_bytes(probe) + 2 * align256(pairs * 8) +
+                  2 * align256((size_t)x->n * k * 8) +
+                  (lower_bound && !out_on_device ? align256(pairs * 8) : 0) +
+                  (out_on_device ? 0 : 2 * align256((size_t)x->n * k * 8));
+    WB_TRY(ws.reserve(need));
+    WB_TRY(stage(x, dim, ws, J.rows));
+    WB_TRY(stage(y, dim, ws, J.cols));
+    WB_TRY(build_tables(metric, params, J, ws, false, xl, yl));
+    WB_TAKE(D, double, ws, pairs);
+    WB_TAKE(K, double, ws, pairs);
+    J.out = D;
+    J.out_ld = y->n;
+    J.key = metric == WB_EUCLIDEAN ? nullptr : K;
+    J.mode = PM_ALL;
+    int never_push = 0;
+    if (derivative(metric) && std::min(xl, yl) < 3) never_push = 1;
+    if (!never_push) WB_TRY(launch_elastic(J, ws, nullptr));
+
+    const double *lb = lower_bound;
+    if (lower_bound && !out_on_device) {
+        WB_TAKE(dlb, double, ws, pairs);
+        WB_CUDA(cudaMemcpyAsync(dlb, lower_bound, pairs * 8, cudaMemcpyHostToDevice, s));
+        lb = dlb;
+    }
+    ArgminJob A;
+    A.metric = metric;
+    A.nx = x->n;
+    A.ny = y->n;
+    A.k = k;
+    A.dist = D;
+    A.key = J.key;
+    A.lower_bound = lb;
+    A.xl = xl;
+    A.yl = yl;
+    A.never_push = never_push;
+    A.heap_idx = ws.take<int64_t>((size_t)x->n * k);
+    A.heap_val = ws.take<double>((size_t)x->n * k);
+    A.out_idx = out_on_device ? indices : ws.take<int64_t>((size_t)x->n * k);
+    A.out_dist = out_on_device ? distances : ws.take<double>((size_t)x->n * k);
+    if (!A.heap_idx || !A.heap_val || !A.out_idx || !A.out_dist)
+        return fail(WB_ENOMEM, "workspace reservation exceeded");
+    WB_TRY(launch_argmin_replay(A, s));
+    if (!out_on_device) {
+        WB_CUDA(cudaMemcpyAsync(indices, A.out_idx, (size_t)x->n * k * 8,
+                                cudaMemcpyDeviceToHost, s));
+        WB_CUDA(cudaMemcpyAsync(distances, A.out_dist, (size_t)x->n * k * 8,
+                                cudaMemcpyDeviceToHost, s));
+        WB_CUDA(cudaStreamSynchronize(s));
+    }
+    return WB_OK;
+}
+
+extern "C" int wb_pairwise_subsequence_distance(
+    const double *shapelets, const int64_t *offsets, const int64_t *lengths,
+    const double *means, const double *stds, int64_t m, const wb_series *x, int64_t dim,
+    int32_t metric, double *out_dist, int64_t *out_idx, int32_t out_on_device,
+    void *stream_) {
+    WB_TRY(check_series(x, "x"));
+    WB_TRY(check_dim(x, dim));
+    if (metric != WB_EUCLIDEAN && metric != WB_SCALED_EUCLIDEAN)
+        return fail(WB_EUNSUPPORTED, "unsupported subsequence metric id " + std::to_string(metric));
+    if (m < 0) return fail(WB_EINVAL, "negative number of shapelets");
+    if (m == 0 || x->n == 0) return WB_OK;
+    if (!shapelets || !offsets || !lengths || !out_dist || !out_idx)
+        return fail(WB_EINVAL, "NULL shapelet or output array");
+    const bool scaled = metric == WB_SCALED_EUCLIDEAN;
+    if (scaled && (!means || !stds)) return fail(WB_EINVAL, "scaled metric needs means and stds");
+    cudaStream_t s = (cudaStream_t)stream_;
+    const bool dev_in = x->on_device != 0;
+
+    // Host copies of lengths/offsets drive the grouping by length.
+    std::vector<int64_t> hlen(m), hoff(m);
+    if (dev_in) {
+        WB_CUDA(cudaMemcpy(hlen.data(), lengths, m * 8, cudaMemcpyDeviceToHost));
+        WB_CUDA(cudaMemcpy(hoff.data(), offsets, m * 8, cudaMemcpyDeviceToHost));
+    } else {
+        std::memcpy(hlen.data(), lengths, m * 8);
+        std::memcpy(hoff.data(), offsets, m * 8);
+    }
+    int64_t total = 0;
+    for (int64_t i = 0; i < m; i++) {
+        if (hlen[i] < 1 || hlen[i] > x->n_timestep)
+            return fail(WB_EINVAL, "Invalid subsequnce shape (" + std::to_string(hlen[i]) +
+                                       " > " + std::to_string(x->n_timestep) + ")");
+        if (hoff[i] < 0) return fail(WB_EINVAL, "negative shapelet offset");
+        total = std::max(total, hoff[i] + hlen[i]);
+    }
+    std::vector<int64_t> order(m);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int64_t a, int64_t b) { return hlen[a] < hlen[b]; });
+    std::vector<int32_t> group_of(m), group_len;
+    for (int64_t t = 0; t < m; t++) {
+        int64_t i = order[t];
+        if (group_len.empty() || group_len.back() != hlen[i]) group_len.push_back((int32_t)hlen[i]);
+        group_of[i] = (int32_t)group_len.size() - 1;
+    }
+
+    SubseqJob J;
+    J.m = m;
+    J.n_groups = (int)group_len.size();
+    J.total_values = total;
+    J.win_stride = (int)x->n_timestep;
+    J.chunk = 64;
+    Workspace ws(s);
+    size_t need = stage_bytes(x) + align256(m * 8) * 3 + align256(m * 4) +
+                  align256(group_len.size() * 4) +
+                  (dev_in ? 0 : align256(total * 8) + 2 * align256(m * 8) + 2 * align256(m * 8)) +
+                  (out_on_device ? 0 : 2 * align256((size_t)x->n * m * 8));
+    J.x.count = x->n;
+    J.x.len = (int)x->n_timestep;
+    need += subseq_workspace_bytes(J, scaled);
+    WB_TRY(ws.reserve(need));
+    WB_TRY(stage(x, dim, ws, J.x));
+    if (dev_in) {
+        J.shapelets = shapelets;
+        J.offsets = offsets;
+        J.lengths = lengths;
+        J.means = means;
+        J.stds = stds;
+    } else {
+        WB_TAKE(dsh, double, ws, total);
+        WB_TAKE(doff, int64_t, ws, m);
+        WB_TAKE(dlen, int64_t, ws, m);
+        WB_CUDA(cudaMemcpyAsync(dsh, shapelets, total * 8, cudaMemcpyHostToDevice, s));
+        WB_CUDA(cudaMemcpyAsync(doff, offsets, m * 8, cudaMemcpyHostToDevice, s));
+        WB_CUDA(cudaMemcpyAsync(dlen, lengths, m * 8, cudaMemcpyHostToDevice, s));
+        J.shapelets = dsh;
+        J.offsets = doff;
+        J.lengths = dlen;
+        if (scaled) {
+            WB_TAKE(dm, double, ws, m);
+            WB_TAKE(ds, double, ws, m);
+            WB_CUDA(cudaMemcpyAsync(dm, means, m * 8, cudaMemcpyHostToDevice, s));
+            WB_CUDA(cudaMemcpyAsync(ds, stds, m * 8, cudaMemcpyHostToDevice, s));
+            J.means = dm;
+            J.stds = ds;
+        }
+    }
+    WB_TAKE(dorder, int64_t, ws, m);
+    WB_TAKE(dgroup, int32_t, ws, m);
+    WB_TAKE(dglen, int32_t, ws, group_len.size());
+    WB_CUDA(cudaMemcpyAsync(dorder, order.data(), m * 8, cudaMemcpyHostToDevice, s));
+    WB_CUDA(cudaMemcpyAsync(dgroup, group_of.data(), m * 4, cudaMemcpyHostToDevice, s));
+    WB_CUDA(cudaMemcpyAsync(dglen, group_len.data(), group_len.size() * 4,
+                            cudaMemcpyHostToDevice, s));
+    J.order = dorder;
+    J.group_of = dgroup;
+    J.group_len = dglen;
+    J.out_dist = out_on_device ? out_dist : ws.take<double>((size_t)x->n * m);
+    J.out_idx = out_on_device ? out_idx : ws.take<int64_t>((size_t)x->n * m);
+    if (!J.out_dist || !J.out_idx) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    WB_TRY(launch_subseq(J, scaled, ws));
+    if (!out_on_device) {
+        WB_CUDA(cudaMemcpyAsync(out_dist, J.out_dist, (size_t)x->n * m * 8,
+                                cudaMemcpyDeviceToHost, s));
+        WB_CUDA(cudaMemcpyAsync(out_idx, J.out_idx, (size_t)x->n * m * 8,
+                                cudaMemcpyDeviceToHost, s));
+    }
+    // the host vectors above feed asynchronous copies
+    WB_CUDA(cudaStreamSynchronize(s));
+    return WB_OK;
+}
+
+extern "C" const char *wb_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int32_t wb_version(void) { return 1; }
+
+extern "C" int64_t wb_launch_count(void) { return g_launches.load(); }
+
+extern "C" int wb_release_workspace(void *stream_) {
+    std::lock_guard<std::mutex> g(g_arena_mu);
+    for (auto it = g_arenas.begin(); it != g_arenas.end();) {
+        if (stream_ == nullptr || it->first.second == (cudaStream_t)stream_) {
+            Arena *a = it->second;
+            std::lock_guard<std::mutex> ga(a->mu);
+            if (a->base) cudaFree(a->base);
+            a->base = nullptr;
+            a->cap = 0;
+            it = g_arenas.erase(it);
+            // the arena object itself is kept alive: a concurrent Workspace
+            // may still hold a pointer to it
+        } else {
+            ++it;
+        }
+    }
+    return WB_OK;
+}

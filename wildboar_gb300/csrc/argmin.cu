@@ -1,0 +1,132 @@
+// argmin.cu -- k-nearest-neighbour selection with the reference's heap.
+//
+// The distance kernel has produced, for every (query i, candidate j), the
+// distance the metric's eadistance returns when it does not abandon, and the
+// abandon key K(i, j): the largest per-row minimum of the recurrence.  The
+// reference abandons a pair iff some checked row's minimum exceeds the
+// threshold, i.e. iff K(i, j) > threshold.  Replaying _ArgMinBatch.__call__
+// (distance/_cdistance.pyx:1302-1345) over j in order with those two numbers
+// reproduces its pushes, its heap (utils/_misc.pyx:18-107) and therefore its
+// output order exactly, including for metrics whose abandoning is not
+// monotone (negative adtw penalty, band-edge zeros of lcss/edr/erp/msm/twe).
+
+#include "elastic.cuh"
+
+namespace wb {
+
+__device__ __forceinline__ double abandon_threshold(int metric, double distance, int xl, int yl) {
+    switch (metric) {
+        case WB_DTW:
+        case WB_WDTW:
+        case WB_DDTW:
+        case WB_WDDTW:
+        case WB_ADTW:
+            return distance * distance;
+        case WB_LCSS:
+        case WB_WLCSS: {
+            if (isinf(distance)) return __longlong_as_double(0x7ff0000000000000LL);
+            double ml = (double)(xl < yl ? xl : yl);
+            return ml - distance * ml;
+        }
+        case WB_EDR:
+            return distance * (double)(xl > yl ? xl : yl);
+        default:
+            return distance;
+    }
+}
+
+// Heap.push and its sift helpers (utils/_misc.pyx:18-107)
+__device__ void heap_push(int64_t *hi, double *hv, int64_t &n, int64_t k, int64_t index,
+                          double value) {
+    if (n == 0) {
+        hi[0] = index;
+        hv[0] = value;
+        n = 1;
+        return;
+    }
+    if (n < k) {
+        // append, then move toward the root while larger than the parent
+        int64_t pos = n;
+        n += 1;
+        while (pos > 0) {
+            int64_t parent = (pos - 1) >> 1;
+            if (value > hv[parent]) {
+                hi[pos] = hi[parent];
+                hv[pos] = hv[parent];
+                pos = parent;
+                continue;
+            }
+            break;
+        }
+        hi[pos] = index;
+        hv[pos] = value;
+    } else if (hv[0] > value) {
+        // replace the root: move it to a leaf along larger children, then
+        // back toward the root (heapq's _siftup)
+        int64_t pos = 0, end = k;
+        int64_t child = 1;
+        while (child < end) {
+            int64_t right = child + 1;
+            if (right < end && hv[child] < hv[right]) child = right;
+            hi[pos] = hi[child];
+            hv[pos] = hv[child];
+            pos = child;
+            child = 2 * pos + 1;
+        }
+        while (pos > 0) {
+            int64_t parent = (pos - 1) >> 1;
+            if (value > hv[parent]) {
+                hi[pos] = hi[parent];
+                hv[pos] = hv[parent];
+                pos = parent;
+                continue;
+            }
+            break;
+        }
+        hi[pos] = index;
+        hv[pos] = value;
+    }
+}
+
+__global__ void argmin_replay_kernel(const ArgminJob J) {
+    const double INF = __longlong_as_double(0x7ff0000000000000LL);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < J.nx;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t *hi = J.heap_idx + i * J.k;
+        double *hv = J.heap_val + i * J.k;
+        const double *drow = J.dist + i * J.ny;
+        const double *krow = J.key ? J.key + i * J.ny : nullptr;
+        const double *lb = J.lower_bound ? J.lower_bound + i * J.ny : nullptr;
+        double distance = INF;
+        int64_t n = 0;
+        if (!J.never_push) {
+            for (int64_t j = 0; j < J.ny; j++) {
+                if (lb && lb[j] >= distance) continue;
+                if (krow) {
+                    double thr = abandon_threshold(J.metric, distance, J.xl, J.yl);
+                    if (krow[j] > thr) continue;  // abandoned: eadistance returns inf
+                }
+                double d = drow[j];
+                if (d < distance) {
+                    heap_push(hi, hv, n, J.k, j, d);
+                    distance = (n == J.k) ? hv[0] : INF;
+                }
+            }
+        }
+        for (int64_t t = 0; t < J.k; t++) {
+            J.out_idx[i * J.k + t] = t < n ? hi[t] : 0;
+            J.out_dist[i * J.k + t] = t < n ? hv[t] : 0.0;
+        }
+    }
+}
+
+int launch_argmin_replay(const ArgminJob &J, cudaStream_t s) {
+    if (J.nx == 0) return WB_OK;
+    int block = 128;
+    int64_t g = (J.nx + block - 1) / block;
+    argmin_replay_kernel<<<(int)g, block, 0, s>>>(J);
+    WB_LAUNCH_CHECK("argmin_replay_kernel");
+    return WB_OK;
+}
+
+}  // namespace wb

@@ -1,0 +1,105 @@
+// elastic.cuh -- job description of the FP64 elastic-distance kernels.
+#pragma once
+
+#include "common.cuh"
+
+namespace wb {
+
+// A set of equally long series: series s starts at base + s * stride.
+struct SeriesSet {
+    const double *base = nullptr;
+    int64_t stride = 0;
+    int64_t count = 0;
+    int len = 0;
+};
+
+enum PairMode {
+    PM_ALL = 0,     // every (row series, column series) pair
+    PM_UPPER = 1,   // rows == cols, pairs i < j, mirrored output
+    PM_PAIRED = 2,  // row series s with column series s
+};
+
+// kernel variants (one recurrence each)
+enum ElasticKind {
+    K_DTW = 0,      // dtw / ddtw (on slopes)
+    K_WDTW = 1,     // wdtw / wddtw
+    K_ADTW = 2,     // adtw, penalty >= 0
+    K_ADTW_ANY = 3, // adtw, negative penalty (IEEE min instead of integer min)
+    K_LCSS = 4,
+    K_WLCSS = 5,
+    K_EDR = 6,
+    K_ERP = 7,
+    K_MSM = 8,
+    K_TWE = 9,
+    K_EUCLID = 10,  // pairwise euclidean (EuclideanMetric), no recurrence
+};
+
+// final transform of the recurrence value
+enum ResultKind {
+    R_SQRT = 0,      // dtw family
+    R_LCSS = 1,      // 1 - v / min(n, m)
+    R_EDR = 2,       // v / max(n, m)
+    R_IDENT = 3,     // erp, msm, twe
+};
+
+struct ElasticJob {
+    int kind = K_DTW;
+    int result = R_SQRT;
+    int mode = PM_ALL;
+    SeriesSet rows;          // rows of the recurrence (the metric's X)
+    SeriesSet cols;          // columns of the recurrence (the metric's Y)
+    int band = 1;            // r of the recurrence
+    int len_norm_rows = 0;   // lengths used by the LCSS / EDR normalisation
+    int len_norm_cols = 0;
+    double eps = 0, p = 0, g = 0, c = 0, penalty = 0, stiffness = 0;
+    const double *weights = nullptr;    // wdtw / wlcss weights (device)
+    const double *std_rows = nullptr;   // edr default epsilon tables (device)
+    const double *std_cols = nullptr;
+    const double *gsum_rows = nullptr;  // erp: sum_i |x_i - g| per series
+    const double *gsum_cols = nullptr;
+    const double *gtab_cols = nullptr;  // erp: |y_j - g|, (cols.count, cols.len)
+    const double *dtab_cols = nullptr;  // twe: |y_{j-1} - y_j|, (cols.count, cols.len)
+    const double *stab = nullptr;       // twe: (2 * stiffness) * k
+    double *out = nullptr;              // distances
+    int64_t out_ld = 0;                 // row stride of out (PM_ALL / PM_UPPER)
+    double *key = nullptr;              // early-abandon keys (argmin), or null
+    int all_zero = 0;                   // ddtw on series shorter than 3
+};
+
+// Ring length (in elements) needed for a band recurrence of an (n x m)
+// problem with half-width r: the live window spans columns js-1 .. je.
+inline int ring_len(int n, int m, int r) {
+    int64_t w = (int64_t)(m > n ? m - n : n - m) + 2 * (int64_t)r + 2;
+    int64_t full = (int64_t)m + 1;
+    return (int)(w < full ? w : full);
+}
+
+int launch_elastic(const ElasticJob &job, Workspace &ws, size_t *ring_bytes_query);
+size_t elastic_workspace_bytes(const ElasticJob &job);
+
+// per-series preparation kernels
+int launch_slopes(const SeriesSet &in, double *out, cudaStream_t s);
+int launch_mean_std(const SeriesSet &in, double *std_out, cudaStream_t s);
+int launch_erp_tables(const SeriesSet &in, double g, double *tab, double *sums,
+                      cudaStream_t s);
+int launch_twe_tables(const SeriesSet &in, double *tab, cudaStream_t s);
+int launch_fill_stab(double s2, int n, double *stab, cudaStream_t s);
+int launch_fill(double *p, double v, int64_t n, cudaStream_t s);
+
+// argmin heap replay
+struct ArgminJob {
+    int metric = WB_DTW;
+    int64_t nx = 0, ny = 0, k = 1;
+    const double *dist = nullptr;   // (nx, ny)
+    const double *key = nullptr;    // (nx, ny) or null
+    const double *lower_bound = nullptr;
+    int xl = 0, yl = 0;             // series lengths (threshold transforms)
+    int never_push = 0;             // ddtw / wddtw with series shorter than 3
+    int64_t *out_idx = nullptr;
+    double *out_dist = nullptr;
+    int64_t *heap_idx = nullptr;    // (nx, k) scratch
+    double *heap_val = nullptr;     // (nx, k) scratch
+};
+int launch_argmin_replay(const ArgminJob &job, cudaStream_t s);
+
+}  // namespace wb

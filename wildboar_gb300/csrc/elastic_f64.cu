@@ -1,0 +1,733 @@
+// elastic_f64.cu -- FP64 elastic distances, one thread per pair.
+//
+// Layout.  A warp holds 32 pairs that share one column series (the metric's
+// Y, read with warp-uniform broadcast loads) and have 32 different row series
+// (the metric's X, one load per recurrence row).  Each thread keeps the live
+// band of the previous recurrence row in a ring of P doubles: in shared
+// memory, interleaved across the block ([k][thread], conflict-free), or for
+// wide bands in a global scratch ring interleaved across the grid
+// ([k][global thread], coalesced).  The cost matrix is never materialised.
+//
+// Arithmetic.  Every cell performs the reference's IEEE double operations in
+// the reference's order (the file is compiled with -fmad=false); only the
+// comparisons of non-negative costs run on the integer pipe (nn_min/nn_max),
+// which gives the same values.  GB300's FP64 pipe, not memory, bounds these
+// kernels.
+//
+// Band semantics restated from distance/_elastic.pyx (two-row recurrences):
+// row i covers columns [js, je) with js = max(0, i - max(0, n-m) - r + 1),
+// je = min(m, i + max(0, m-n) + r).  Out-of-band neighbours read the value
+// the reference writes next to the band: +inf for the dtw family, 0 for
+// lcss / edr / erp / twe and for msm's upper edge.  msm's left neighbour of
+// the first band cell is never written by the reference and holds the cell
+// two rows up (stale buffer content); the ring reproduces that value.
+
+#include "elastic.cuh"
+
+namespace wb {
+
+extern __shared__ double wb_smem[];
+
+struct RingS {
+    int off, s;
+    __device__ __forceinline__ double ld(int k) const { return wb_smem[off + k * s]; }
+    __device__ __forceinline__ void st(int k, double v) const { wb_smem[off + k * s] = v; }
+};
+
+struct RingG {
+    double *p;
+    int64_t s;
+    __device__ __forceinline__ double ld(int k) const { return p[(int64_t)k * s]; }
+    __device__ __forceinline__ void st(int k, double v) const { p[(int64_t)k * s] = v; }
+};
+
+#define WB_INF __longlong_as_double(0x7ff0000000000000LL)
+
+__device__ __forceinline__ int wrap_inc(int q, int P) { return (q + 1 == P) ? 0 : q + 1; }
+__device__ __forceinline__ int wrap_dec(int q, int P) { return (q == 0) ? P - 1 : q - 1; }
+__device__ __forceinline__ double ldg(const double *p) { return __ldg(p); }
+
+// --------------------------------------------------------------------------
+// dtw / wdtw / ddtw / wddtw: dtw_distance, distance/_elastic.pyx:869-940
+template <bool W, class R>
+__device__ double rec_dtw(R ring, int P, const double *__restrict__ X, int n,
+                          const double *__restrict__ Y, int m, int r,
+                          const double *__restrict__ w, double &key) {
+    const int mx = imax(0, m - n) + r;
+    const int mn = imax(0, n - m);
+    const double INF = WB_INF;
+    double x0 = X[0];
+    double v = x0 - ldg(Y);
+    double acc = W ? (v * v) * ldg(w) : v * v;
+    ring.st(0, acc);
+    const int lim = imin(m, mx);
+    int q = 1 % P;
+    for (int j = 1; j < lim; j++) {
+        v = x0 - ldg(Y + j);
+        double c = W ? (v * v) * ldg(w + j - 1) : v * v;
+        acc = acc + c;
+        ring.st(q, acc);
+        q = wrap_inc(q, P);
+    }
+    if (mx < m) ring.st(mx % P, INF);
+    double kmax = -INF;
+    for (int i = 1; i < n; i++) {
+        const int js = imax(0, i - mn - r + 1);
+        const int je = imin(m, i + mx);
+        const double xi = X[i];
+        q = js % P;
+        double diag = js > 0 ? ring.ld(wrap_dec(q, P)) : INF;
+        double left = INF;
+        double rmin = INF;
+        for (int j = js; j < je; j++) {
+            double up = ring.ld(q);
+            double d = xi - ldg(Y + j);
+            double c = W ? (d * d) * ldg(w + abs(i - j)) : d * d;
+            double nv = nn_min(nn_min(up, left), diag) + c;
+            ring.st(q, nv);
+            rmin = nn_min(rmin, nv);
+            diag = up;
+            left = nv;
+            q = wrap_inc(q, P);
+        }
+        if (je < m) ring.st(q, INF);
+        kmax = fmax(kmax, rmin);
+    }
+    key = kmax;
+    return ring.ld((m - 1) % P);
+}
+
+// adtw: adtw_distance, distance/_elastic.pyx:943-1008
+template <bool NONNEG, class R>
+__device__ double rec_adtw(R ring, int P, const double *__restrict__ X, int n,
+                           const double *__restrict__ Y, int m, int r, double pen,
+                           double &key) {
+    const int mx = imax(0, m - n) + r;
+    const int mn = imax(0, n - m);
+    const double INF = WB_INF;
+    double x0 = X[0];
+    double v = x0 - ldg(Y);
+    double acc = v * v;
+    ring.st(0, acc);
+    const int lim = imin(m, mx);
+    int q = 1 % P;
+    for (int j = 1; j < lim; j++) {
+        v = x0 - ldg(Y + j);
+        acc = acc + v * v;
+        ring.st(q, acc);
+        q = wrap_inc(q, P);
+    }
+    if (mx < m) ring.st(mx % P, INF);
+    double kmax = -INF;
+    for (int i = 1; i < n; i++) {
+        const int js = imax(0, i - mn - r + 1);
+        const int je = imin(m, i + mx);
+        const double xi = X[i];
+        q = js % P;
+        double diag = js > 0 ? ring.ld(wrap_dec(q, P)) : INF;
+        double left = INF;  // prev_cost + penalty with prev_cost = inf
+        double rmin = INF;
+        for (int j = js; j < je; j++) {
+            double up = ring.ld(q);
+            double a = up + pen;
+            double d = xi - ldg(Y + j);
+            double mv;
+            if (NONNEG) mv = nn_min(nn_min(a, left), diag);
+            else mv = cy_min(cy_min(a, left), diag);
+            double nv = mv + d * d;
+            ring.st(q, nv);
+            rmin = NONNEG ? nn_min(rmin, nv) : (nv < rmin ? nv : rmin);
+            diag = up;
+            left = nv + pen;
+            q = wrap_inc(q, P);
+        }
+        if (je < m) ring.st(q, INF);
+        kmax = fmax(kmax, rmin);
+    }
+    key = kmax;
+    return ring.ld((m - 1) % P);
+}
+
+// lcss / wlcss: lcss_distance, distance/_elastic.pyx:1118-1183
+template <bool W, class R>
+__device__ double rec_lcss(R ring, int P, const double *__restrict__ X, int n,
+                           const double *__restrict__ Y, int m, int r, double eps,
+                           const double *__restrict__ w, double &key) {
+    const int mx = imax(0, m - n) + r;
+    const int mn = imax(0, n - m);
+    const double INF = WB_INF;
+    const int lim = imin(m, mx);
+    int q = 0;
+    for (int j = 0; j < lim; j++) {
+        ring.st(q, 0.0);
+        q = wrap_inc(q, P);
+    }
+    if (mx < m) ring.st(mx % P, 0.0);
+    double kmax = -INF;
+    for (int i = 0; i < n; i++) {
+        const int js = imax(0, i - mn - r + 1);
+        const int je = imin(m, i + mx);
+        const double xi = X[i];
+        q = js % P;
+        double diag = js > 0 ? ring.ld(wrap_dec(q, P)) : 0.0;
+        double left = 0.0;
+        double rmin = INF;
+        for (int j = js; j < je; j++) {
+            double up = ring.ld(q);
+            double v = fabs(xi - ldg(Y + j));
+            double wt = W ? ldg(w + abs(i - j)) : 1.0;
+            double nv = (v <= eps) ? wt + diag : nn_max(left, up);
+            ring.st(q, nv);
+            rmin = nn_min(rmin, nv);
+            diag = up;
+            left = nv;
+            q = wrap_inc(q, P);
+        }
+        if (je < m) ring.st(q, 0.0);
+        kmax = fmax(kmax, rmin);
+    }
+    key = kmax;
+    return ring.ld((m - 1) % P);
+}
+
+// edr: edr_distance, distance/_elastic.pyx:1437-1497
+template <class R>
+__device__ double rec_edr(R ring, int P, const double *__restrict__ X, int n,
+                          const double *__restrict__ Y, int m, int r, double eps,
+                          double &key) {
+    const int mx = imax(0, m - n) + r;
+    const int mn = imax(0, n - m);
+    const double INF = WB_INF;
+    const int lim = imin(m, mx);
+    int q = 0;
+    for (int j = 0; j < lim; j++) {
+        ring.st(q, 0.0);
+        q = wrap_inc(q, P);
+    }
+    if (mx < m) ring.st(mx % P, 0.0);
+    double kmax = -INF;
+    for (int i = 0; i < n; i++) {
+        const int js = imax(0, i - mn - r + 1);
+        const int je = imin(m, i + mx);
+        const double xi = X[i];
+        q = js % P;
+        double diag = js > 0 ? ring.ld(wrap_dec(q, P)) : 0.0;
+        double left = 0.0;
+        double rmin = INF;
+        for (int j = js; j < je; j++) {
+            double up = ring.ld(q);
+            double v = fabs(xi - ldg(Y + j));
+            double a = diag + (v < eps ? 0.0 : 1.0);
+            double b = up + 1.0;
+            double c = left + 1.0;
+            double nv = nn_min(nn_min(a, b), c);
+            ring.st(q, nv);
+            rmin = nn_min(rmin, nv);
+            diag = up;
+            left = nv;
+            q = wrap_inc(q, P);
+        }
+        if (je < m) ring.st(q, 0.0);
+        kmax = fmax(kmax, rmin);
+    }
+    key = kmax;
+    return ring.ld((m - 1) % P);
+}
+
+// erp: erp_distance, distance/_elastic.pyx:1273-1347
+template <class R>
+__device__ double rec_erp(R ring, int P, const double *__restrict__ X, int n,
+                          const double *__restrict__ Y, int m, int r, double g,
+                          double gx_sum, double gy_sum, const double *__restrict__ gY,
+                          double &key) {
+    const int mx = imax(0, m - n) + r;
+    const int mn = imax(0, n - m);
+    const double INF = WB_INF;
+    const int lim = imin(m, mx);
+    int q = 0;
+    for (int j = 0; j < lim; j++) {
+        ring.st(q, gy_sum);
+        q = wrap_inc(q, P);
+    }
+    if (mx < m) ring.st(mx % P, gy_sum);
+    double kmax = -INF;
+    for (int i = 0; i < n; i++) {
+        const int js = imax(0, i - mn - r + 1);
+        const int je = imin(m, i + mx);
+        const double xi = X[i];
+        const double gxi = fabs(xi - g);
+        q = js % P;
+        double diag, left;
+        if (js > 0) {
+            diag = ring.ld(wrap_dec(q, P));
+            left = 0.0;
+        } else {
+            diag = (i == 0) ? 0.0 : gx_sum;
+            left = gx_sum;
+        }
+        double rmin = INF;
+        for (int j = js; j < je; j++) {
+            double up = ring.ld(q);
+            double v = fabs(xi - ldg(Y + j));
+            double a = diag + v;
+            double b = up + gxi;
+            double c = left + ldg(gY + j);
+            double nv = nn_min(a, nn_min(b, c));
+            ring.st(q, nv);
+            rmin = nn_min(rmin, nv);
+            diag = up;
+            left = nv;
+            q = wrap_inc(q, P);
+        }
+        if (je < m) ring.st(q, 0.0);
+        kmax = fmax(kmax, rmin);
+    }
+    key = kmax;
+    return ring.ld((m - 1) % P);
+}
+
+// _msm_cost, distance/_elastic.pyx:1583-1587: arguments narrowed to float,
+// comparisons and differences in float, the sum in double.
+__device__ __forceinline__ double msm_cost(float x, float y, float z, float c) {
+    if ((y <= x && x <= z) || (y >= x && x >= z)) return (double)c;
+    float a = fabsf(__fsub_rn(x, y));
+    float b = fabsf(__fsub_rn(x, z));
+    return (double)c + (double)(b < a ? b : a);
+}
+
+// msm: msm_distance, distance/_elastic.pyx:1592-1647
+template <class R>
+__device__ double rec_msm(R ring, int P, const double *__restrict__ X, int n,
+                          const double *__restrict__ Y, int m, int r, double cd,
+                          double &key) {
+    const int mx = imax(0, m - n) + r;
+    const int mn = imax(0, n - m);
+    const double INF = WB_INF;
+    const float c = (float)cd;
+    const float x0f = (float)X[0];
+    double acc = fabs(X[0] - ldg(Y));
+    ring.st(0, acc);
+    const int lim = imin(m, mx);
+    int q = 1 % P;
+    float yprev = (float)ldg(Y);
+    for (int j = 1; j < lim; j++) {
+        float yj = (float)ldg(Y + j);
+        acc = acc + msm_cost(yj, yprev, x0f, c);
+        ring.st(q, acc);
+        yprev = yj;
+        q = wrap_inc(q, P);
+    }
+    if (mx < m) {
+        acc = acc + msm_cost((float)ldg(Y + mx), (float)ldg(Y + mx - 1), x0f, c);
+        ring.st(mx % P, acc);
+    }
+    double cy = fabs(X[0] - ldg(Y));   // cost_y[0]
+    const float y0f = (float)ldg(Y);
+    double stale = 0.0;
+    double kmax = -INF;
+    float xprevf = x0f;
+    for (int i = 1; i < n; i++) {
+        const double xi = X[i];
+        const float xif = (float)xi;
+        const double cy_prev = cy;
+        cy = cy + msm_cost(xif, xprevf, y0f, c);
+        const int js = imax(1, i - mn - r + 1);
+        const int je = imin(m, i + mx);
+        q = js % P;
+        double diag, left;
+        if (js == 1) {
+            diag = cy_prev;
+            left = cy;
+        } else {
+            diag = ring.ld(wrap_dec(q, P));
+            left = stale;
+        }
+        double rmin = cy;
+        float ylf = (float)ldg(Y + js - 1);
+        for (int j = js; j < je; j++) {
+            double up = ring.ld(q);
+            if (j == js) stale = up;
+            const double yj = ldg(Y + j);
+            const float yjf = (float)yj;
+            double a = diag + fabs(xi - yj);
+            double b = up + msm_cost(xif, xprevf, yjf, c);
+            double d = left + msm_cost(yjf, xif, ylf, c);
+            double nv = nn_min(nn_min(a, b), d);
+            ring.st(q, nv);
+            rmin = nn_min(rmin, nv);
+            diag = up;
+            left = nv;
+            ylf = yjf;
+            q = wrap_inc(q, P);
+        }
+        if (je < m) ring.st(q, 0.0);
+        kmax = fmax(kmax, rmin);
+        xprevf = xif;
+    }
+    key = kmax;
+    if (m == 1) return n == 1 ? ring.ld(0) : cy;
+    return ring.ld((m - 1) % P);
+}
+
+// twe: twe_distance, distance/_elastic.pyx:1733-1829
+template <class R>
+__device__ double rec_twe(R ring, int P, const double *__restrict__ X, int n,
+                          const double *__restrict__ Y, int m, int r, double penalty,
+                          double stiffness, const double *__restrict__ dY,
+                          const double *__restrict__ stab, double &key) {
+    const int mx = imax(0, m - n) + r;
+    const int mn = imax(0, n - m);
+    const double INF = WB_INF;
+    const int lim = imin(m, mx);
+    int q = 0;
+    for (int j = 0; j < lim; j++) {
+        ring.st(q, INF);
+        q = wrap_inc(q, P);
+    }
+    if (mx < m) ring.st(mx % P, INF);
+    const double pen = penalty + stiffness;
+    double kmax = -INF;
+    double xp = 0.0;
+    for (int i = 0; i < n; i++) {
+        const int js = imax(0, i - mn - r + 1);
+        const int je = imin(m, i + mx);
+        const double xi = X[i];
+        const double dxi = fabs(xp - xi);
+        q = js % P;
+        double left, upleft, yp;
+        if (js > 0) {
+            left = 0.0;
+            upleft = ring.ld(wrap_dec(q, P));
+            yp = ldg(Y + js - 1);
+        } else {
+            left = INF;
+            upleft = (i == 0) ? 0.0 : INF;
+            yp = 0.0;
+        }
+        double rmin = INF;
+        for (int j = js; j < je; j++) {
+            double up = ring.ld(q);
+            const double yj = ldg(Y + j);
+            double del_x = (up + dxi) + pen;
+            double del_y = (left + ldg(dY + j)) + pen;
+            double match = ((upleft + fabs(xi - yj)) + fabs(xp - yp)) + ldg(stab + abs(i - j));
+            double nv = nn_min(nn_min(del_x, del_y), match);
+            ring.st(q, nv);
+            rmin = nn_min(rmin, nv);
+            upleft = up;
+            left = nv;
+            yp = yj;
+            q = wrap_inc(q, P);
+        }
+        if (je < m) ring.st(q, 0.0);
+        kmax = fmax(kmax, rmin);
+        xp = xi;
+    }
+    key = kmax;
+    return ring.ld((m - 1) % P);
+}
+
+// --------------------------------------------------------------------------
+
+template <int KIND, class R>
+__device__ __forceinline__ double run_pair(const ElasticJob &J, R ring, int P,
+                                           int64_t rs, int64_t cs, double &key) {
+    const double *X = J.rows.base + rs * J.rows.stride;
+    const double *Y = J.cols.base + cs * J.cols.stride;
+    const int n = J.rows.len, m = J.cols.len, r = J.band;
+    if constexpr (KIND == K_DTW) return rec_dtw<false>(ring, P, X, n, Y, m, r, nullptr, key);
+    if constexpr (KIND == K_WDTW) return rec_dtw<true>(ring, P, X, n, Y, m, r, J.weights, key);
+    if constexpr (KIND == K_ADTW) return rec_adtw<true>(ring, P, X, n, Y, m, r, J.p, key);
+    if constexpr (KIND == K_ADTW_ANY) return rec_adtw<false>(ring, P, X, n, Y, m, r, J.p, key);
+    if constexpr (KIND == K_LCSS) return rec_lcss<false>(ring, P, X, n, Y, m, r, J.eps, nullptr, key);
+    if constexpr (KIND == K_WLCSS) return rec_lcss<true>(ring, P, X, n, Y, m, r, J.eps, J.weights, key);
+    if constexpr (KIND == K_EDR) {
+        double eps = J.eps;
+        if (J.std_rows) eps = cy_max(J.std_rows[rs], J.std_cols[cs]) / 4.0;
+        return rec_edr(ring, P, X, n, Y, m, r, eps, key);
+    }
+    if constexpr (KIND == K_ERP)
+        return rec_erp(ring, P, X, n, Y, m, r, J.g, J.gsum_rows[rs], J.gsum_cols[cs],
+                       J.gtab_cols + cs * (int64_t)m, key);
+    if constexpr (KIND == K_MSM) return rec_msm(ring, P, X, n, Y, m, r, J.c, key);
+    if constexpr (KIND == K_EUCLID) {
+        // euclidean_distance with one window (equal lengths),
+        // distance/_metric.pyx:654-682: sum_j (y_j - x_j)^2 in order
+        double dist = 0.0;
+        for (int j = 0; j < m; j++) {
+            double v = ldg(Y + j);
+            v = v - X[j];
+            dist = dist + v * v;
+        }
+        key = -WB_INF;
+        return dist;
+    }
+    if constexpr (KIND == K_TWE)
+        return rec_twe(ring, P, X, n, Y, m, r, J.penalty, J.stiffness,
+                       J.dtab_cols + cs * (int64_t)m, J.stab, key);
+    return 0.0;
+}
+
+__device__ __forceinline__ double finish(const ElasticJob &J, double v) {
+    switch (J.result) {
+        case R_SQRT: return sqrt(v);
+        case R_LCSS: return 1.0 - v / (double)imin(J.len_norm_rows, J.len_norm_cols);
+        case R_EDR: return v / (double)imax(J.len_norm_rows, J.len_norm_cols);
+        default: return v;
+    }
+}
+
+constexpr int kThreads = 128;
+
+template <int KIND, bool GRING>
+__global__ void __launch_bounds__(kThreads)
+elastic_pairs_kernel(const ElasticJob J, double *gring, int P) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * kThreads + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * kThreads) >> 5;
+    const int64_t gtid = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    const int64_t gthreads = (int64_t)gridDim.x * kThreads;
+
+    auto body = [&](auto ring) {
+        if (J.mode == PM_PAIRED) {
+            for (int64_t s = gtid; s < J.rows.count; s += gthreads) {
+                double key, d;
+                d = J.all_zero ? 0.0 : finish(J, run_pair<KIND>(J, ring, P, s, s, key));
+                J.out[s] = d;
+            }
+            return;
+        }
+        const int64_t chunks = (J.rows.count + 31) >> 5;
+        const int64_t ntiles = chunks * J.cols.count;
+        for (int64_t t = warp; t < ntiles; t += nwarps) {
+            const int64_t cs = t / chunks;
+            const int64_t rs = (t - cs * chunks) * 32 + lane;
+            if (J.mode == PM_UPPER) {
+                if (rs >= cs) continue;
+            } else if (rs >= J.rows.count) {
+                continue;
+            }
+            double key = 0.0, d;
+            if (J.all_zero) d = 0.0;
+            else d = finish(J, run_pair<KIND>(J, ring, P, rs, cs, key));
+            J.out[rs * J.out_ld + cs] = d;
+            if (J.mode == PM_UPPER) J.out[cs * J.out_ld + rs] = d;
+            if (J.key) J.key[rs * J.out_ld + cs] = key;
+        }
+    };
+    if constexpr (GRING) {
+        body(RingG{gring + gtid, gthreads});
+    } else {
+        body(RingS{(int)threadIdx.x, kThreads});
+    }
+}
+
+template <int KIND>
+static int launch_kind(const ElasticJob &J, Workspace &ws, int P, bool gring_mode,
+                       double *gring, int grid) {
+    cudaStream_t s = ws.stream();
+    if (gring_mode) {
+        timer_begin("elastic_pairs_kernel", s);
+        elastic_pairs_kernel<KIND, true><<<grid, kThreads, 0, s>>>(J, gring, P);
+    } else {
+        size_t smem = (size_t)P * kThreads * sizeof(double);
+        auto kfn = elastic_pairs_kernel<KIND, false>;
+        WB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+        timer_begin("elastic_pairs_kernel", s);
+        kfn<<<grid, kThreads, smem, s>>>(J, nullptr, P);
+    }
+    timer_end(s);
+    WB_LAUNCH_CHECK("elastic_pairs_kernel");
+    return WB_OK;
+}
+
+// decide ring placement and grid size
+struct ElasticPlan {
+    int P;
+    bool gring;
+    int grid;
+    size_t gring_bytes;
+};
+
+static ElasticPlan plan_elastic(const ElasticJob &J) {
+    const DeviceInfo &dev = device_info();
+    ElasticPlan pl;
+    pl.P = imax(2, ring_len(J.rows.len, J.cols.len, J.band));
+    const size_t per_block = (size_t)pl.P * kThreads * sizeof(double);
+    int64_t work_threads;
+    if (J.mode == PM_PAIRED) work_threads = J.rows.count;
+    else work_threads = ((J.rows.count + 31) / 32) * 32 * J.cols.count;
+    int64_t want_blocks = (work_threads + kThreads - 1) / kThreads;
+    int blocks_per_sm = 0;
+    if (per_block <= (size_t)dev.smem_per_sm - 2048 && per_block <= (size_t)dev.max_smem_optin) {
+        blocks_per_sm = (int)(((size_t)dev.smem_per_sm - 1024) / (per_block + 1024));
+        if (blocks_per_sm > 4) blocks_per_sm = 4;
+    }
+    // a ring that leaves fewer than 4 warps per SM goes to global memory
+    if (blocks_per_sm >= 1) {
+        pl.gring = false;
+        int64_t cap = (int64_t)blocks_per_sm * dev.sm_count;
+        pl.grid = (int)(want_blocks < cap ? want_blocks : cap);
+        pl.gring_bytes = 0;
+    } else {
+        pl.gring = true;
+        int64_t cap = (int64_t)4 * dev.sm_count;
+        pl.grid = (int)(want_blocks < cap ? want_blocks : cap);
+        pl.gring_bytes = (size_t)pl.P * pl.grid * kThreads * sizeof(double);
+    }
+    if (pl.grid < 1) pl.grid = 1;
+    return pl;
+}
+
+size_t elastic_workspace_bytes(const ElasticJob &J) {
+    ElasticPlan pl = plan_elastic(J);
+    return align256(pl.gring_bytes);
+}
+
+int launch_elastic(const ElasticJob &J, Workspace &ws, size_t *) {
+    if (J.rows.count == 0 || J.cols.count == 0) return WB_OK;
+    ElasticPlan pl = plan_elastic(J);
+    double *gring = pl.gring ? ws.take<double>(pl.gring_bytes / sizeof(double)) : nullptr;
+    if (pl.gring && !gring) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    switch (J.kind) {
+        case K_DTW: return launch_kind<K_DTW>(J, ws, pl.P, pl.gring, gring, pl.grid);
+        case K_WDTW: return launch_kind<K_WDTW>(J, ws, pl.P, pl.gring, gring, pl.grid);
+        case K_ADTW: return launch_kind<K_ADTW>(J, ws, pl.P, pl.gring, gring, pl.grid);
+        case K_ADTW_ANY: return launch_kind<K_ADTW_ANY>(J, ws, pl.P, pl.gring, gring, pl.grid);
+        case K_LCSS: return launch_kind<K_LCSS>(J, ws, pl.P, pl.gring, gring, pl.grid);
+        case K_WLCSS: return launch_kind<K_WLCSS>(J, ws, pl.P, pl.gring, gring, pl.grid);
+        case K_EDR: return launch_kind<K_EDR>(J, ws, pl.P, pl.gring, gring, pl.grid);
+        case K_ERP: return launch_kind<K_ERP>(J, ws, pl.P, pl.gring, gring, pl.grid);
+        case K_MSM: return launch_kind<K_MSM>(J, ws, pl.P, pl.gring, gring, pl.grid);
+        case K_TWE: return launch_kind<K_TWE>(J, ws, pl.P, pl.gring, gring, pl.grid);
+        case K_EUCLID: return launch_kind<K_EUCLID>(J, ws, 2, false, nullptr, pl.grid);
+    }
+    return fail(WB_EINVAL, "unknown elastic kernel");
+}
+
+// --------------------------------------------------------------------------
+// per-series preparation
+
+// average_slope, distance/_elastic.pyx:3220-3225; out has stride len-2
+__global__ void slopes_kernel(const SeriesSet in, double *out) {
+    const int L = in.len;
+    const int64_t total = in.count * (int64_t)(L - 2);
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t s = t / (L - 2);
+        int i = (int)(t - s * (L - 2)) + 1;
+        const double *q = in.base + s * in.stride;
+        double a = q[i] - q[i - 1];
+        double b = (q[i + 1] - q[i - 1]) * 0.5;  // x / 2 == x * 0.5 exactly
+        out[t] = (a + b) * 0.5;
+    }
+}
+
+// fast_mean_std, utils/_stats.pyx:22-42 (one thread per series, sequential)
+__global__ void mean_std_kernel(const SeriesSet in, double *std_out) {
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < in.count;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const double *x = in.base + s * in.stride;
+        double ex = 0, ex2 = 0;
+        for (int i = 0; i < in.len; i++) {
+            double v = x[i];
+            ex = ex + v;
+            ex2 = ex2 + v * v;
+        }
+        double mean = ex / (double)in.len;
+        ex2 = ex2 / (double)in.len - mean * mean;
+        std_out[s] = ex2 > 1e-13 ? sqrt(ex2) : 0.0;
+    }
+}
+
+// erp gap tables: tab[s][j] = |y_j - g|, sums[s] = sequential sum
+__global__ void erp_tables_kernel(const SeriesSet in, double g, double *tab, double *sums) {
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < in.count;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const double *x = in.base + s * in.stride;
+        double acc = 0;
+        for (int i = 0; i < in.len; i++) {
+            double v = fabs(x[i] - g);
+            if (tab) tab[s * in.len + i] = v;
+            acc = acc + v;
+        }
+        sums[s] = acc;
+    }
+}
+
+// twe column table: tab[s][j] = |y_{j-1} - y_j| with y_{-1} = 0
+__global__ void twe_tables_kernel(const SeriesSet in, double *tab) {
+    const int L = in.len;
+    const int64_t total = in.count * (int64_t)L;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t s = t / L;
+        int j = (int)(t - s * L);
+        const double *y = in.base + s * in.stride;
+        double yp = j == 0 ? 0.0 : y[j - 1];
+        tab[t] = fabs(yp - y[j]);
+    }
+}
+
+__global__ void fill_stab_kernel(double s2, int n, double *stab) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        stab[k] = s2 * (double)k;
+}
+
+__global__ void fill_kernel(double *p, double v, int64_t n) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        p[k] = v;
+}
+
+static int grid_for(int64_t n, int block) {
+    int64_t g = (n + block - 1) / block;
+    int64_t cap = (int64_t)device_info().sm_count * 8;
+    if (g > cap) g = cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+int launch_slopes(const SeriesSet &in, double *out, cudaStream_t s) {
+    if (in.len < 3 || in.count == 0) return WB_OK;
+    slopes_kernel<<<grid_for(in.count * (in.len - 2), 256), 256, 0, s>>>(in, out);
+    WB_LAUNCH_CHECK("slopes_kernel");
+    return WB_OK;
+}
+
+int launch_mean_std(const SeriesSet &in, double *std_out, cudaStream_t s) {
+    if (in.count == 0) return WB_OK;
+    mean_std_kernel<<<grid_for(in.count, 128), 128, 0, s>>>(in, std_out);
+    WB_LAUNCH_CHECK("mean_std_kernel");
+    return WB_OK;
+}
+
+int launch_erp_tables(const SeriesSet &in, double g, double *tab, double *sums,
+                      cudaStream_t s) {
+    if (in.count == 0) return WB_OK;
+    erp_tables_kernel<<<grid_for(in.count, 128), 128, 0, s>>>(in, g, tab, sums);
+    WB_LAUNCH_CHECK("erp_tables_kernel");
+    return WB_OK;
+}
+
+int launch_twe_tables(const SeriesSet &in, double *tab, cudaStream_t s) {
+    if (in.count == 0) return WB_OK;
+    twe_tables_kernel<<<grid_for(in.count * in.len, 256), 256, 0, s>>>(in, tab);
+    WB_LAUNCH_CHECK("twe_tables_kernel");
+    return WB_OK;
+}
+
+int launch_fill_stab(double s2, int n, double *stab, cudaStream_t s) {
+    fill_stab_kernel<<<grid_for(n, 256), 256, 0, s>>>(s2, n, stab);
+    WB_LAUNCH_CHECK("fill_stab_kernel");
+    return WB_OK;
+}
+
+int launch_fill(double *p, double v, int64_t n, cudaStream_t s) {
+    if (n == 0) return WB_OK;
+    fill_kernel<<<grid_for(n, 256), 256, 0, s>>>(p, v, n);
+    WB_LAUNCH_CHECK("fill_kernel");
+    return WB_OK;
+}
+
+}  // namespace wb
