@@ -333,7 +333,13 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--nx", type=int, default=WORKLOAD["nx"],
+                    help="rows of X (smaller values for profiling captures)")
+    ap.add_argument("--ny", type=int, default=WORKLOAD["ny"])
     args = ap.parse_args()
+    if (args.nx, args.ny) != (WORKLOAD["nx"], WORKLOAD["ny"]):
+        WORKLOAD["nx"], WORKLOAD["ny"] = args.nx, args.ny
+        WORKLOAD["name"] = WORKLOAD["name"].replace("2000x2000", f"{args.nx}x{args.ny}")
     if args.impl == "reference":
         run_reference(args)
     else:
