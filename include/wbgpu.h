@@ -130,6 +130,27 @@ int wb_pairwise_subsequence_distance(const double *shapelets, const int64_t *off
                                      int64_t *out_idx, int32_t out_on_device,
                                      void *stream);
 
+/*
+ * wb_pairwise_distance_noalloc -- no counterpart in the reference.
+ * wb_pairwise_distance for callers that cannot have the library allocate
+ * device memory (memory budgeted up front, or no device-synchronising
+ * cudaMalloc/cudaFree allowed in their loop): x, y (or NULL for the singleton
+ * path) and out must be device memory; nothing is allocated.  The recurrence
+ * scratch lives in a static 64 MiB device array (wb_noalloc_scratch_bytes())
+ * that every GPU loading the library keeps until exit; a band ring that does
+ * not fit in it is rejected with WB_EINVAL.  Metrics: euclidean, dtw, wdtw,
+ * adtw, lcss, wlcss, edr (explicit epsilon), msm; others give
+ * WB_EUNSUPPORTED.  All calls share the array: calls that overlap on the GPU
+ * race.  The first call on a device looks the array up; make it before any
+ * stream capture.
+ */
+int wb_pairwise_distance_noalloc(const wb_series *x, const wb_series *y, int64_t dim,
+                                 int32_t metric, const wb_params *params, double *out,
+                                 void *stream);
+
+/* size in bytes of the static scratch of wb_pairwise_distance_noalloc */
+int64_t wb_noalloc_scratch_bytes(void);
+
 /* message of the last failed call on this thread ("" if none) */
 const char *wb_last_error(void);
 

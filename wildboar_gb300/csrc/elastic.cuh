@@ -75,6 +75,11 @@ inline int ring_len(int n, int m, int r) {
 }
 
 int launch_elastic(const ElasticJob &job, Workspace &ws, size_t *ring_bytes_query);
+// Same kernels with the per-thread rings in a caller-provided device buffer of
+// `ring_bytes` (always the global-ring variant); the grid is the largest that
+// fits.  WB_EINVAL when not even one block's rings fit.
+int launch_elastic_external_ring(const ElasticJob &job, double *ring, size_t ring_bytes,
+                                 cudaStream_t s);
 size_t elastic_workspace_bytes(const ElasticJob &job);
 
 // per-series preparation kernels

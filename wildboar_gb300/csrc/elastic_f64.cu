@@ -606,6 +606,49 @@ int launch_elastic(const ElasticJob &J, Workspace &ws, size_t *) {
     return fail(WB_EINVAL, "unknown elastic kernel");
 }
 
+int launch_elastic_external_ring(const ElasticJob &J, double *ring, size_t ring_bytes,
+                                 cudaStream_t s) {
+    if (J.rows.count == 0 || J.cols.count == 0) return WB_OK;
+    const DeviceInfo &dev = device_info();
+    const int P = imax(2, ring_len(J.rows.len, J.cols.len, J.band));
+    const size_t per_block = (size_t)P * kThreads * sizeof(double);
+    const int64_t fit = (int64_t)(ring_bytes / per_block);
+    if (fit < 1)
+        return fail(WB_EINVAL, "band ring of " + std::to_string(per_block) +
+                                   " bytes per block exceeds the static scratch of " +
+                                   std::to_string(ring_bytes) + " bytes");
+    int64_t work_threads;
+    if (J.mode == PM_PAIRED) work_threads = J.rows.count;
+    else work_threads = ((J.rows.count + 31) / 32) * 32 * J.cols.count;
+    int64_t grid = (work_threads + kThreads - 1) / kThreads;
+    const int64_t cap = (int64_t)4 * dev.sm_count;
+    if (grid > cap) grid = cap;
+    if (grid > fit) grid = fit;
+    if (grid < 1) grid = 1;
+    switch (J.kind) {
+#define WB_EXT_CASE(K)                                                              \
+    case K:                                                                         \
+        elastic_pairs_kernel<K, true><<<(int)grid, kThreads, 0, s>>>(J, ring, P);    \
+        break;
+        WB_EXT_CASE(K_DTW)
+        WB_EXT_CASE(K_WDTW)
+        WB_EXT_CASE(K_ADTW)
+        WB_EXT_CASE(K_ADTW_ANY)
+        WB_EXT_CASE(K_LCSS)
+        WB_EXT_CASE(K_WLCSS)
+        WB_EXT_CASE(K_EDR)
+        WB_EXT_CASE(K_ERP)
+        WB_EXT_CASE(K_MSM)
+        WB_EXT_CASE(K_TWE)
+        WB_EXT_CASE(K_EUCLID)
+#undef WB_EXT_CASE
+        default:
+            return fail(WB_EINVAL, "unknown elastic kernel");
+    }
+    WB_LAUNCH_CHECK("elastic_pairs_kernel (external ring)");
+    return WB_OK;
+}
+
 // --------------------------------------------------------------------------
 // per-series preparation
 
