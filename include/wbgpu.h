@@ -130,6 +130,51 @@ int wb_pairwise_subsequence_distance(const double *shapelets, const int64_t *off
                                      int64_t *out_idx, int32_t out_on_device,
                                      void *stream);
 
+/* ------------------------------------------------------------------------
+ * FP32 forms (batched, ragged, differentiable).  No counterpart in the
+ * reference, which computes every distance in FP64 on the CPU; they follow
+ * dtw_distance (distance/_elastic.pyx:869-940) with FP32 costs and
+ * compensated (TwoSum) accumulation, the final sqrt in FP64.  All pointers are
+ * device pointers; calls neither synchronise nor allocate once the stream's
+ * workspace has grown to the job, so they can be captured in CUDA graphs
+ * after a warm-up call.
+ * ------------------------------------------------------------------------ */
+typedef struct wb_dtw32 {
+    const float *x;            /* x series s starts at x + s * x_stride */
+    int64_t x_stride;
+    const int32_t *x_lengths;  /* valid length of each x series, or NULL (x_len) */
+    int32_t x_len;             /* padded (maximum) x length */
+    int64_t nx;
+    const float *y;
+    int64_t y_stride;
+    const int32_t *y_lengths;
+    int32_t y_len;
+    int64_t ny;
+    const int32_t *item_x;     /* item t pairs x series item_x[t] with y series */
+    const int32_t *item_y;     /* item_y[t]; both NULL: the nx*ny grid, t = j*nx + i */
+    int64_t n_items;
+    double r;                  /* band fraction in [0, 1] */
+    const float *weights;      /* wdtw weights (length >= max length) or NULL */
+    int32_t strip;             /* rows per register strip: 4, 8, 16, 24, 32 (0 = 16) */
+    int32_t block;             /* threads per block (0 = 128) */
+    int32_t grid;              /* persistent grid (0 = occupancy x SMs) */
+} wb_dtw32;
+
+/* dtw distance of every item: out[t] = sqrt(cost), out_cost[t] = cost (or NULL) */
+int wb_dtw32_distance(const wb_dtw32 *job, double *out, double *out_cost, void *stream);
+
+/* d distance[t] / d x and d distance[t] / d y of every item, scaled by
+ * grad_out[t] (NULL = 1): grad_x row t at grad_x + t * gx_stride (x_len
+ * floats), grad_y likewise.  Recomputes the forward with a direction bitmap
+ * and walks the optimal path back (dtw_mapping tie order: diag, up, left). */
+int wb_dtw32_backward(const wb_dtw32 *job, const double *grad_out, float *grad_x,
+                      int64_t gx_stride, float *grad_y, int64_t gy_stride, void *stream);
+
+/* valid length of each float32 series: index of its first NaN (padding or
+ * end-of-series marker, utils/variable_len.py:66-115), else L */
+int wb_series_lengths_f32(const float *x, int64_t n_series, int64_t stride, int32_t L,
+                          int32_t *lengths, void *stream);
+
 /*
  * wb_pairwise_distance_noalloc -- no counterpart in the reference.
  * wb_pairwise_distance for callers that cannot have the library allocate

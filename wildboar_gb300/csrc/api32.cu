@@ -1,0 +1,121 @@
+// api32.cu -- C ABI of the FP32 (compensated) dtw forms: batched / ragged
+// distances and the backward pass.  Device pointers only; no host
+// synchronisation and no allocation once the stream's workspace has grown to
+// the job's size, so a call can be captured in a CUDA graph after a warm-up.
+
+#include <algorithm>
+
+#include "dtw32.cuh"
+
+namespace wb {
+
+static int prepare32(const wb_dtw32 *q, bool backward, Workspace &ws, Dtw32Job &J,
+                     size_t extra_bytes) {
+    if (!q) return fail(WB_EINVAL, "job is NULL");
+    if (!q->x || !q->y) return fail(WB_EINVAL, "x and y must be device pointers");
+    if (q->x_len < 1 || q->y_len < 1) return fail(WB_EINVAL, "x_len and y_len must be >= 1");
+    if (!(q->r >= 0.0 && q->r <= 1.0)) return fail(WB_EINVAL, "r must be in [0, 1]");
+    if (q->n_items < 0) return fail(WB_EINVAL, "negative number of items");
+    const bool items = q->item_x != nullptr;
+    if (items != (q->item_y != nullptr)) return fail(WB_EINVAL, "item_x and item_y go together");
+    if (!items && q->n_items != q->nx * q->ny)
+        return fail(WB_EINVAL, "without item arrays n_items must be nx * ny");
+    const int strip = backward ? 16 : (q->strip ? q->strip : 16);
+    if (strip != 4 && strip != 8 && strip != 16 && strip != 24 && strip != 32)
+        return fail(WB_EINVAL, "strip must be one of 4, 8, 16, 24, 32");
+    const int block = q->block ? q->block : 128;
+    if (block % 32 || block < 32 || block > 256)
+        return fail(WB_EINVAL, "block must be a multiple of 32 in [32, 256]");
+    const DeviceInfo &dev = device_info();
+    int grid = q->grid;
+    if (grid <= 0) {
+        int nb = dtw32_blocks_per_sm(strip, q->weights != nullptr, backward, block);
+        if (nb < 1) nb = 1;
+        grid = nb * dev.sm_count;
+        int64_t need = (q->n_items + block - 1) / block;
+        if (need < grid) grid = (int)std::max<int64_t>(need, 1);
+    }
+    J.x = q->x;
+    J.x_stride = q->x_stride;
+    J.xlen = q->x_lengths;
+    J.x_len = q->x_len;
+    J.nx = q->nx;
+    J.y = q->y;
+    J.y_stride = q->y_stride;
+    J.ylen = q->y_lengths;
+    J.y_len = q->y_len;
+    J.ny = q->ny;
+    J.item_x = q->item_x;
+    J.item_y = q->item_y;
+    J.n_items = q->n_items;
+    J.r = q->r;
+    J.weights = q->weights;
+    J.grid = grid;
+    J.block = block;
+    J.ring_cols = q->y_len + 1;
+    const int64_t nth = (int64_t)grid * block;
+    size_t ring_bytes = align256((size_t)J.ring_cols * nth * sizeof(float2));
+    size_t dir_bytes = 0;
+    if (backward) {
+        int64_t words;
+        if (!q->x_lengths && !q->y_lengths) {
+            int r = compute_r(std::min(q->x_len, q->y_len), q->r);
+            words = dtw32_dir_words(q->x_len, q->y_len, r);
+        } else {
+            int64_t strips = q->x_len > 1 ? (q->x_len - 2) / 16 + 1 : 0;
+            words = strips * q->y_len + 1;
+        }
+        J.dir_words = words;
+        dir_bytes = align256((size_t)words * nth * sizeof(uint32_t));
+    }
+    WB_TRY(ws.reserve(ring_bytes + dir_bytes + 256 + extra_bytes));
+    J.ring = ws.take<float2>((size_t)J.ring_cols * nth);
+    J.queue = ws.take<unsigned long long>(1);
+    if (!J.ring || !J.queue) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    if (backward) {
+        J.dirs = ws.take<uint32_t>((size_t)J.dir_words * nth);
+        if (!J.dirs) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    }
+    return WB_OK;
+}
+
+}  // namespace wb
+
+using namespace wb;
+
+extern "C" int wb_dtw32_distance(const wb_dtw32 *q, double *out, double *out_cost,
+                                 void *stream_) {
+    if (!out) return fail(WB_EINVAL, "out is NULL");
+    cudaStream_t s = (cudaStream_t)stream_;
+    Workspace ws(s);
+    Dtw32Job J;
+    WB_TRY(prepare32(q, false, ws, J, 0));
+    J.out = out;
+    J.out_cost = out_cost;
+    return dtw32_forward(J, q->strip ? q->strip : 16, s);
+}
+
+extern "C" int wb_dtw32_backward(const wb_dtw32 *q, const double *grad_out, float *grad_x,
+                                 int64_t gx_stride, float *grad_y, int64_t gy_stride,
+                                 void *stream_) {
+    if (!grad_x || !grad_y) return fail(WB_EINVAL, "gradient outputs are NULL");
+    if (gx_stride < q->x_len || gy_stride < q->y_len)
+        return fail(WB_EINVAL, "gradient strides must cover x_len / y_len");
+    cudaStream_t s = (cudaStream_t)stream_;
+    Workspace ws(s);
+    Dtw32Job J;
+    WB_TRY(prepare32(q, true, ws, J, 0));
+    J.grad_out = grad_out;
+    J.grad_x = grad_x;
+    J.gx_stride = gx_stride;
+    J.grad_y = grad_y;
+    J.gy_stride = gy_stride;
+    return dtw32_backward(J, s);
+}
+
+extern "C" int wb_series_lengths_f32(const float *x, int64_t n_series, int64_t stride,
+                                     int32_t L, int32_t *lengths, void *stream_) {
+    if (n_series < 0 || L < 0) return fail(WB_EINVAL, "negative size");
+    if (n_series > 0 && (!x || !lengths)) return fail(WB_EINVAL, "NULL pointer");
+    return launch_series_lengths(x, n_series, stride, L, lengths, (cudaStream_t)stream_);
+}

@@ -1,0 +1,401 @@
+// dtw32.cu -- FP32 dtw / wdtw with compensated accumulation, forward and
+// backward, for batches of (possibly ragged) pairs.
+//
+// One thread per (x, y) problem, persistent: warps take 32 consecutive items
+// at a time from an atomic counter, so a batch sorted by cost keeps the 32
+// lanes of a warp on problems of similar size.  A thread sweeps its band in
+// strips of S rows: the S cells of one column live in registers as (hi, lo)
+// float pairs, the previous strip's bottom row is read from, and the strip's
+// own bottom row written to, a ring in global memory laid out
+// [column][thread] (coalesced when the lanes of a warp sweep the same column).
+//
+// Arithmetic: the cost (x_i - y_j)^2 (times the wdtw weight) is FP32; every
+// accumulation is a TwoSum, whose exact rounding error goes into the lo part,
+// so the cumulative cost carries ~48 bits.  The minimum picks the candidate
+// with the smallest hi in the dtw_mapping order (diag, up, left; distance/
+// dtw.py:362-426), which also gives the traceback direction.  The final
+// distance sqrt(hi + lo) is formed in FP64.  Band, row-0 weights and
+// out-of-band +inf follow dtw_distance (distance/_elastic.pyx:869-940).
+//
+// Backward: the same sweep stores a 2-bit direction per cell (one 32-bit word
+// per strip column for S = 16), then the thread walks the optimal path back
+// from (n-1, m-1) and writes d dist / d x_i and d dist / d y_j:
+// dD/dx_i = sum_{j:(i,j) on path} w_{|i-j|} (x_i - y_j) / D, dD/dy_j the
+// negative column sums (D = sqrt of the path cost).
+
+#include "dtw32.cuh"
+
+namespace wb {
+
+struct HL {
+    float h, l;
+};
+
+#define WB_FINF __int_as_float(0x7f800000)
+
+__device__ __forceinline__ HL hl_inf() { return HL{WB_FINF, 0.0f}; }
+
+// TwoSum (Knuth): s + err == a.h + b exactly; err joins the lo part.
+__device__ __forceinline__ HL add_c(HL a, float b) {
+    float s = __fadd_rn(a.h, b);
+    float bb = __fsub_rn(s, a.h);
+    float err = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return HL{s, __fadd_rn(a.l, err)};
+}
+
+__device__ __forceinline__ int band_of(int n, int m, double r) {
+    double v = floor((double)(n < m ? n : m) * r);
+    return (int)(v > 1.0 ? v : 1.0);
+}
+
+struct Item {
+    const float *X, *Y;
+    int n, m, r, mx, mn;
+};
+
+__device__ __forceinline__ Item load_item(const Dtw32Job &J, int64_t t) {
+    int64_t cx, cy;
+    if (J.item_x) {
+        cx = J.item_x[t];
+        cy = J.item_y[t];
+    } else {
+        cy = t / J.nx;
+        cx = t - cy * J.nx;
+    }
+    Item it;
+    it.X = J.x + cx * J.x_stride;
+    it.Y = J.y + cy * J.y_stride;
+    it.n = J.xlen ? J.xlen[cx] : J.x_len;
+    it.m = J.ylen ? J.ylen[cy] : J.y_len;
+    it.r = band_of(it.n, it.m, J.r);
+    it.mx = imax(0, it.m - it.n) + it.r;
+    it.mn = imax(0, it.n - it.m);
+    return it;
+}
+
+// One forward sweep; returns the (hi, lo) cost of cell (n-1, m-1).
+template <int S, bool W, bool DIRS>
+__device__ HL sweep(const Item &it, const float *__restrict__ w, float2 *ring, int64_t nth,
+                    uint32_t *dirs) {
+    const float *__restrict__ X = it.X;
+    const float *__restrict__ Y = it.Y;
+    const int n = it.n, m = it.m, r = it.r, mx = it.mx, mn = it.mn;
+    // row 0: cumulative, weight index j-1 for j >= 1
+    const float x0 = X[0];
+    float v = __fsub_rn(x0, Y[0]);
+    float c0 = __fmul_rn(v, v);
+    if (W) c0 = __fmul_rn(c0, w[0]);
+    HL acc{c0, 0.0f};
+    ring[0] = make_float2(acc.h, acc.l);
+    const int lim = imin(m, mx);
+    for (int c = 1; c < lim; c++) {
+        v = __fsub_rn(x0, Y[c]);
+        float cc = __fmul_rn(v, v);
+        if (W) cc = __fmul_rn(cc, w[c - 1]);
+        acc = add_c(acc, cc);
+        ring[(int64_t)c * nth] = make_float2(acc.h, acc.l);
+    }
+    HL result = acc;
+    int pstart = 0, pend = lim;
+    int64_t wofs = 0;
+    const int lo = -(mn + r - 1), hi = mx - 1;
+    for (int i0 = 1; i0 < n; i0 += S) {
+        const int rows = imin(S, n - i0);
+        float xr[S];
+#pragma unroll
+        for (int k = 0; k < S; k++) xr[k] = (k < rows) ? X[i0 + k] : 0.0f;
+        const int cstart = imax(0, i0 - mn - r + 1);
+        const int cend = imin(m, i0 + rows - 1 + mx);
+        HL prev[S];
+#pragma unroll
+        for (int k = 0; k < S; k++) prev[k] = hl_inf();
+        HL bdiag = hl_inf();
+        if (cstart - 1 >= pstart && cstart - 1 < pend) {
+            float2 t2 = ring[(int64_t)(cstart - 1) * nth];
+            bdiag = HL{t2.x, t2.y};
+        }
+        const bool last = (i0 + rows == n);
+        for (int c = cstart; c < cend; c++) {
+            HL bup = hl_inf();
+            if (c < pend) {
+                float2 t2 = ring[(int64_t)c * nth];
+                bup = HL{t2.x, t2.y};
+            }
+            const float yc = Y[c];
+            const int d0 = c - i0;
+            HL cur[S];
+            HL bottom = hl_inf();  // cell of row rows-1 in this column
+            uint32_t word = 0;
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+                HL up = (k == 0) ? bup : cur[k - 1];
+                HL dg = (k == 0) ? bdiag : prev[k - 1];
+                HL lf = prev[k];
+                HL best = dg;
+                int dir = 0;
+                if (up.h < best.h) {
+                    best = up;
+                    dir = 1;
+                }
+                if (lf.h < best.h) {
+                    best = lf;
+                    dir = 2;
+                }
+                float vv = __fsub_rn(xr[k], yc);
+                float cst = __fmul_rn(vv, vv);
+                if (W) cst = __fmul_rn(cst, w[abs(d0 - k)]);
+                HL nv = add_c(best, cst);
+                const int d = d0 - k;
+                const bool inb = (k < rows) && d >= lo && d <= hi;
+                cur[k] = inb ? nv : hl_inf();
+                if (k < rows) bottom = cur[k];
+                if (DIRS) word |= (uint32_t)dir << (2 * k);
+            }
+            if (DIRS) dirs[(wofs + (c - cstart)) * nth] = word;
+            if (last && c == m - 1) result = bottom;
+            ring[(int64_t)c * nth] = make_float2(cur[S - 1].h, cur[S - 1].l);
+            bdiag = bup;
+#pragma unroll
+            for (int k = 0; k < S; k++) prev[k] = cur[k];
+        }
+        pstart = cstart;
+        pend = cend;
+        wofs += cend - cstart;
+    }
+    return result;
+}
+
+__device__ __forceinline__ int64_t take_items(unsigned long long *q, int lane) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(q, 32ull);
+    return (int64_t)__shfl_sync(0xffffffffu, base, 0);
+}
+
+template <int S, bool W>
+__global__ void __launch_bounds__(256) dtw32_forward_kernel(const Dtw32Job J) {
+    const int lane = threadIdx.x & 31;
+    const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    float2 *ring = J.ring + gtid;
+    for (;;) {
+        const int64_t base = take_items(J.queue, lane);
+        if (base >= J.n_items) break;
+        const int64_t t = base + lane;
+        if (t < J.n_items) {
+            Item it = load_item(J, t);
+            double res;
+            if (it.n < 1 || it.m < 1 || it.m >= J.ring_cols) {
+                res = __longlong_as_double(0x7ff8000000000000LL);  // NaN: empty series
+                if (J.out_cost) J.out_cost[t] = res;
+            } else {
+                HL h = sweep<S, W, false>(it, J.weights, ring, nth, nullptr);
+                double cost = (double)h.h + (double)h.l;
+                if (J.out_cost) J.out_cost[t] = cost;
+                res = sqrt(cost);
+            }
+            J.out[t] = res;
+        }
+    }
+}
+
+constexpr int kGradStrip = 16;
+
+__host__ __device__ int64_t dtw32_dir_words(int n, int m, int band_r) {
+    // strips of 16 rows over rows 1..n-1, each covering at most
+    // (|m - n| + 2 r - 1) + 15 columns, clipped to m
+    int64_t strips = (n > 1) ? (n - 2) / kGradStrip + 1 : 0;
+    int64_t cols = (int64_t)(m > n ? m - n : n - m) + 2 * (int64_t)band_r - 1 + kGradStrip - 1;
+    if (cols > m) cols = m;
+    return strips * cols + 1;
+}
+
+template <bool W>
+__global__ void __launch_bounds__(256) dtw32_backward_kernel(const Dtw32Job J) {
+    constexpr int S = kGradStrip;
+    const int lane = threadIdx.x & 31;
+    const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    float2 *ring = J.ring + gtid;
+    uint32_t *dirs = J.dirs + gtid;
+    for (;;) {
+        const int64_t base = take_items(J.queue, lane);
+        if (base >= J.n_items) break;
+        const int64_t t = base + lane;
+        if (t >= J.n_items) continue;
+        Item it = load_item(J, t);
+        float *GX = J.grad_x + t * J.gx_stride;
+        float *GY = J.grad_y + t * J.gy_stride;
+        const double g = J.grad_out ? J.grad_out[t] : 1.0;
+        if (it.n < 1 || it.m < 1 || it.m >= J.ring_cols || g == 0.0 ||
+            dtw32_dir_words(it.n, it.m, it.r) > J.dir_words) {
+            for (int i = 0; i < J.x_len; i++) GX[i] = 0.0f;
+            for (int j = 0; j < J.y_len; j++) GY[j] = 0.0f;
+            continue;
+        }
+        HL h = sweep<S, W, true>(it, J.weights, ring, nth, dirs);
+        const double D = sqrt((double)h.h + (double)h.l);
+        const float sc = D > 0.0 ? (float)(g / D) : 0.0f;
+        const float *X = it.X;
+        const float *Y = it.Y;
+        const int n = it.n, m = it.m, r = it.r, mn = it.mn;
+        for (int i = n; i < J.x_len; i++) GX[i] = 0.0f;
+        for (int j = m; j < J.y_len; j++) GY[j] = 0.0f;
+        // strip bookkeeping for the walk (rows 1..n-1 in strips of S)
+        auto strip_cols = [&](int s) {
+            int i0 = 1 + s * S;
+            int rows = imin(S, n - i0);
+            int cs = imax(0, i0 - mn - r + 1);
+            int ce = imin(m, i0 + rows - 1 + it.mx);
+            return ce - cs;
+        };
+        int64_t total = 0;
+        const int nstrips = n > 1 ? (n - 2) / S + 1 : 0;
+        for (int s = 0; s < nstrips; s++) total += strip_cols(s);
+        int s = nstrips - 1;
+        int64_t wofs = s >= 0 ? total - strip_cols(s) : 0;
+        int i = n - 1, j = m - 1;
+        float gx = 0.0f, gy = 0.0f;
+        const int max_steps = n + m;
+        for (int step = 0; step < max_steps; step++) {
+            const float vv = __fsub_rn(X[i], Y[j]);
+            const float gc = W ? __fmul_rn(J.weights[abs(i - j)], vv) : vv;
+            gx = __fadd_rn(gx, gc);
+            gy = __fadd_rn(gy, gc);
+            if (i == 0 && j == 0) break;
+            int move;
+            if (i == 0) {
+                move = 2;
+            } else if (j == 0) {
+                move = 1;
+            } else {
+                const int i0 = 1 + s * S;
+                const int cs = imax(0, i0 - mn - r + 1);
+                const uint32_t word = dirs[(wofs + (j - cs)) * nth];
+                move = (word >> (2 * (i - i0))) & 3u;
+            }
+            if (move != 2) {  // leaving row i
+                GX[i] = sc * gx;
+                gx = 0.0f;
+            }
+            if (move != 1) {  // leaving column j
+                GY[j] = -(sc * gy);
+                gy = 0.0f;
+            }
+            if (move != 2) {
+                i -= 1;
+                if (i >= 1 && i < 1 + s * S) {
+                    s -= 1;
+                    wofs -= strip_cols(s);
+                }
+            }
+            if (move != 1) j -= 1;
+        }
+        GX[0] = sc * gx;
+        GY[0] = -(sc * gy);
+    }
+}
+
+template <int S>
+static int launch_fwd(const Dtw32Job &J, cudaStream_t s) {
+    if (J.weights) dtw32_forward_kernel<S, true><<<J.grid, J.block, 0, s>>>(J);
+    else dtw32_forward_kernel<S, false><<<J.grid, J.block, 0, s>>>(J);
+    WB_LAUNCH_CHECK("dtw32_forward_kernel");
+    return WB_OK;
+}
+
+int dtw32_forward(const Dtw32Job &J, int strip, cudaStream_t s) {
+    if (J.n_items == 0) return WB_OK;
+    WB_CUDA(cudaMemsetAsync(J.queue, 0, sizeof(unsigned long long), s));
+    timer_begin("dtw32_forward_kernel", s);
+    int st;
+    switch (strip) {
+        case 4: st = launch_fwd<4>(J, s); break;
+        case 8: st = launch_fwd<8>(J, s); break;
+        case 16: st = launch_fwd<16>(J, s); break;
+        case 24: st = launch_fwd<24>(J, s); break;
+        case 32: st = launch_fwd<32>(J, s); break;
+        default: return fail(WB_EINVAL, "strip must be one of 4, 8, 16, 24, 32");
+    }
+    timer_end(s);
+    return st;
+}
+
+int dtw32_backward(const Dtw32Job &J, cudaStream_t s) {
+    if (J.n_items == 0) return WB_OK;
+    WB_CUDA(cudaMemsetAsync(J.queue, 0, sizeof(unsigned long long), s));
+    timer_begin("dtw32_backward_kernel", s);
+    if (J.weights) dtw32_backward_kernel<true><<<J.grid, J.block, 0, s>>>(J);
+    else dtw32_backward_kernel<false><<<J.grid, J.block, 0, s>>>(J);
+    timer_end(s);
+    WB_LAUNCH_CHECK("dtw32_backward_kernel");
+    return WB_OK;
+}
+
+// resident blocks per SM of the kernel a job would launch (persistent grid)
+int dtw32_blocks_per_sm(int strip, bool weighted, bool backward, int block) {
+    int nb = 0;
+    cudaError_t e = cudaSuccess;
+    if (backward) {
+        e = weighted ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                           &nb, dtw32_backward_kernel<true>, block, 0)
+                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                           &nb, dtw32_backward_kernel<false>, block, 0);
+    } else {
+#define WB_OCC(SS)                                                                    \
+    case SS:                                                                          \
+        e = weighted ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(                 \
+                           &nb, dtw32_forward_kernel<SS, true>, block, 0)             \
+                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(                 \
+                           &nb, dtw32_forward_kernel<SS, false>, block, 0);           \
+        break;
+        switch (strip) {
+            WB_OCC(4)
+            WB_OCC(8)
+            WB_OCC(16)
+            WB_OCC(24)
+            WB_OCC(32)
+            default: return 0;
+        }
+#undef WB_OCC
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return nb;
+}
+
+// valid length of each series: index of the first NaN (EoS or NaN padding)
+__global__ void series_lengths_kernel(const float *x, int64_t n_series, int64_t stride, int L,
+                                      int32_t *lengths) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = warp; s < n_series; s += nwarps) {
+        const float *p = x + s * stride;
+        int first = L;
+        for (int b = 0; b < L; b += 32) {
+            int i = b + lane;
+            bool nan = (i < L) && isnan(p[i]);
+            unsigned mask = __ballot_sync(0xffffffffu, nan);
+            if (mask) {
+                first = b + __ffs(mask) - 1;
+                break;
+            }
+        }
+        if (lane == 0) lengths[s] = first;
+    }
+}
+
+int launch_series_lengths(const float *x, int64_t n_series, int64_t stride, int L,
+                          int32_t *lengths, cudaStream_t s) {
+    if (n_series == 0) return WB_OK;
+    int64_t blocks = (n_series * 32 + 255) / 256;
+    int64_t cap = (int64_t)device_info().sm_count * 16;
+    if (blocks > cap) blocks = cap;
+    series_lengths_kernel<<<(int)blocks, 256, 0, s>>>(x, n_series, stride, L, lengths);
+    WB_LAUNCH_CHECK("series_lengths_kernel");
+    return WB_OK;
+}
+
+}  // namespace wb

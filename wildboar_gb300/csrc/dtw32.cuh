@@ -1,0 +1,53 @@
+// dtw32.cuh -- job description of the FP32 (compensated) dtw / wdtw kernels.
+#pragma once
+
+#include "common.cuh"
+
+namespace wb {
+
+// A batch of (x series, y series) dtw problems in float32.  Series s of x
+// starts at x + s * x_stride; its valid length is xlen[s] (NaN padding cut
+// off) or x_len when xlen is null.  Item t pairs x series item_x[t] with y
+// series item_y[t]; without item arrays the items are the full grid
+// t = cy * nx + cx (32 consecutive items share one y series).
+struct Dtw32Job {
+    const float *x = nullptr;
+    int64_t x_stride = 0;
+    const int32_t *xlen = nullptr;
+    int x_len = 0;
+    int64_t nx = 0;
+    const float *y = nullptr;
+    int64_t y_stride = 0;
+    const int32_t *ylen = nullptr;
+    int y_len = 0;
+    int64_t ny = 0;
+    const int32_t *item_x = nullptr;
+    const int32_t *item_y = nullptr;
+    int64_t n_items = 0;
+    double r = 1.0;               // band fraction; per item band = max(floor(min(n,m) r), 1)
+    const float *weights = nullptr;  // wdtw weights (device) or null
+    double *out = nullptr;        // per item: sqrt(hi + lo) in double
+    double *out_cost = nullptr;   // optional per item: hi + lo (squared distance)
+    // backward
+    const double *grad_out = nullptr;  // per item upstream gradient of the distance
+    float *grad_x = nullptr;      // per item, x_len floats (row i of item t at t * gx_stride)
+    int64_t gx_stride = 0;
+    float *grad_y = nullptr;
+    int64_t gy_stride = 0;
+    // scratch
+    float2 *ring = nullptr;       // [column][thread] (hi, lo) boundary rows
+    int ring_cols = 0;            // columns per thread (max y length + 1)
+    uint32_t *dirs = nullptr;     // [word][thread] direction words (backward)
+    int64_t dir_words = 0;        // words per thread
+    unsigned long long *queue = nullptr;  // work counter (persistent kernel)
+    int grid = 0, block = 0;
+};
+
+int dtw32_forward(const Dtw32Job &J, int strip, cudaStream_t s);
+int dtw32_backward(const Dtw32Job &J, cudaStream_t s);
+__host__ __device__ int64_t dtw32_dir_words(int n, int m, int band_r);
+int dtw32_blocks_per_sm(int strip, bool weighted, bool backward, int block);
+int launch_series_lengths(const float *x, int64_t n_series, int64_t stride, int L,
+                          int32_t *lengths, cudaStream_t s);
+
+}  // namespace wb
