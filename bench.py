@@ -185,6 +185,149 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _timed(fn, steps, flush=None):
+    """Mean device time (ms) of `steps` calls, CUDA events on the current stream."""
+    import torch
+
+    ms = []
+    for _ in range(steps):
+        if flush is not None:
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return sum(ms) / len(ms)
+
+
+def bench_batched(args, dev, flush):
+    """Ragged batch: 65,536 pairs x 3 dims, lengths U{32..2048} NaN-padded to
+    2048, float32, r=0.1, one persistent launch replayed from a CUDA graph."""
+    import torch
+
+    from oracle import oracle as O
+    from wildboar_gb300.distance.batched import BatchedDTW
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(4)
+    N, d, L, r = args.c4_pairs, 3, 2048, 0.1
+    x = torch.randn((N, d, L), device=dev, generator=g).cumsum(-1)
+    y = torch.randn((N, d, L), device=dev, generator=g).cumsum(-1)
+    lx = torch.randint(32, L + 1, (N, d), device=dev, generator=g)
+    ly = torch.randint(32, L + 1, (N, d), device=dev, generator=g)
+    ar = torch.arange(L, device=dev)
+    x.masked_fill_(ar >= lx.unsqueeze(-1), float("nan"))
+    y.masked_fill_(ar >= ly.unsqueeze(-1), float("nan"))
+    t0 = time.perf_counter()
+    runner = BatchedDTW(x, y, r=r, tune=True, graph=True)
+    plan_s = time.perf_counter() - t0
+    cells = runner.cells
+    for _ in range(args.warmup):
+        runner.run()
+    torch.cuda.synchronize()
+    ms = _timed(runner.run, args.steps, flush)
+    out = runner.run().cpu().numpy()
+    # error against the FP64 oracle on a sample of pairs (same float32 inputs)
+    rng = np.random.default_rng(0)
+    idx = rng.choice(N, size=min(N, args.err_sample), replace=False)
+    xs, ys = x[idx].cpu().numpy(), y[idx].cpu().numpy()
+    lxs, lys = lx[idx].cpu().numpy(), ly[idx].cpu().numpy()
+    err = 0.0
+    for t, i in enumerate(idx):
+        acc = 0.0
+        for k in range(d):
+            acc += O.distance_1d(xs[t, k, : lxs[t, k]].astype(np.float64),
+                                 ys[t, k, : lys[t, k]].astype(np.float64), metric="dtw",
+                                 metric_params={"r": r})
+        err = max(err, abs(out[i] - acc / d) / (acc / d))
+    return {
+        "gcups": cells / (ms * 1e-3) / 1e9,
+        "ms_per_step": ms,
+        "cells_per_step": cells,
+        "config": f"{N} pairs x {d} dims, lengths U{{32..2048}} NaN-padded to 2048, "
+                  f"float32, r={r}, CUDA graph replay (lengths + kernel + dim mean)",
+        "tile": {"strip": runner.plan["strip"], "block": runner.plan["block"]},
+        "plan_and_autotune_s": plan_s,
+        "max_rel_err_vs_fp64": err,
+        "err_sample_pairs": int(len(idx)),
+    }
+
+
+def bench_fwd_bwd(args, dev, flush):
+    """Differentiable dtw: 4,096 float32 series of length 256 (32 sine / random
+    walk prototypes + N(0, 0.1)) against 32 learnable centroids, r=0.2;
+    a step is forward + backward of the soft-assignment barycenter loss and an
+    Adam update."""
+    import torch
+
+    from oracle import oracle as O
+    from wildboar_gb300.distance import autograd as AG
+    from wildboar_gb300.distance._band import band_cells
+
+    rng = np.random.default_rng(5)
+    L, K, N, r = 256, 32, args.c5_series, 0.2
+    t = np.linspace(0, 1, L)
+    protos = []
+    for k in range(K):
+        if k % 2 == 0:
+            protos.append(np.sin(2 * np.pi * (1 + k / 4) * t + rng.uniform(0, 6.28)) * 3)
+        else:
+            protos.append(np.cumsum(rng.standard_normal(L)) * 0.3)
+    protos = np.asarray(protos, dtype=np.float32)
+    labels = rng.integers(0, K, size=N)
+    X = protos[labels] + 0.1 * rng.standard_normal((N, L)).astype(np.float32)
+    x = torch.as_tensor(X, device=dev)
+    c = torch.as_tensor(X[rng.choice(N, K, replace=False)], device=dev).clone()
+    c.requires_grad_(True)
+    opt = torch.optim.Adam([c], lr=0.05)
+    cells_fwd = N * K * band_cells(L, L, r)
+
+    def step():
+        opt.zero_grad(set_to_none=True)
+        D = AG.dtw_matrix(x, c, r)
+        loss = AG.soft_assignment_loss(D, 1.0)
+        loss.backward()
+        opt.step()
+        return loss
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ms = _timed(step, args.steps, flush)
+    ms_fwd = _timed(lambda: AG.dtw_matrix(x, c.detach(), r), args.steps, flush)
+    # the configured 100 Adam barycenter steps
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = []
+    for _ in range(args.c5_adam_steps):
+        losses.append(step())
+    torch.cuda.synchronize()
+    adam_s = time.perf_counter() - t0
+    D = AG.dtw_matrix(x[:16], c.detach(), r).detach().cpu().numpy()
+    Cn = c.detach().cpu().numpy().astype(np.float64)
+    err = 0.0
+    for i in range(16):
+        for k in range(K):
+            want = O.distance_1d(X[i].astype(np.float64), Cn[k], metric="dtw",
+                                 metric_params={"r": r})
+            err = max(err, abs(D[i, k] - want) / want)
+    return {
+        "gcups": 2 * cells_fwd / (ms * 1e-3) / 1e9,
+        "ms_per_step": ms,
+        "forward_gcups": cells_fwd / (ms_fwd * 1e-3) / 1e9,
+        "cells_per_step": 2 * cells_fwd,
+        "config": f"{N} x {K} centroids, L={L}, r={r}, float32; step = forward + "
+                  "backward (recompute + path traceback, all pairs) + Adam",
+        "adam_steps": args.c5_adam_steps,
+        "adam_total_s": adam_s,
+        "loss_first_last": [float(losses[0].detach()), float(losses[-1].detach())],
+        "max_rel_err_vs_fp64": err,
+    }
+
+
 def run_gpu(args):
     import torch
 
@@ -298,6 +441,12 @@ def run_gpu(args):
     cpu = None
     if world == 1 and not args.no_cpu:
         cpu = cpu_reference(X, Y, wl, budget_s=args.cpu_budget)
+    forms = {}
+    if not args.no_forms:
+        forms["batched_fp32"] = bench_batched(args, dev, flush)
+        forms["fwd_bwd_fp32"] = bench_fwd_bwd(args, dev, flush)
+        forms["both_beat_fp64_drop_in"] = bool(
+            forms["batched_fp32"]["gcups"] > value and forms["fwd_bwd_fp32"]["gcups"] > value)
     line = {
         "metric": "DTW cell-updates/s (GCUPS), plain FP64 drop-in",
         "value": value,
@@ -319,6 +468,7 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
+        "forms": forms,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
@@ -336,6 +486,12 @@ def main():
     ap.add_argument("--nx", type=int, default=WORKLOAD["nx"],
                     help="rows of X (smaller values for profiling captures)")
     ap.add_argument("--ny", type=int, default=WORKLOAD["ny"])
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the batched FP32 and fwd+bwd measurements")
+    ap.add_argument("--c4-pairs", type=int, default=65536)
+    ap.add_argument("--c5-series", type=int, default=4096)
+    ap.add_argument("--c5-adam-steps", type=int, default=100)
+    ap.add_argument("--err-sample", type=int, default=64)
     args = ap.parse_args()
     if (args.nx, args.ny) != (WORKLOAD["nx"], WORKLOAD["ny"]):
         WORKLOAD["nx"], WORKLOAD["ny"] = args.nx, args.ny

@@ -216,12 +216,23 @@ AUTOTUNER = Autotuner()
 
 
 def band_cost(n, m, r):
-    """Band cell count of every (n, m) problem (torch int64), the sort key."""
+    """Exact band cell count of every (n, m) problem (torch int64).
+
+    Closed form of sum_i [min(m, i + mx) - max(0, i - mn - w + 1)], the cells
+    dtw_distance evaluates (distance/_elastic.pyx:869-940); zero for empty
+    series.  Used as the bucketing sort key and as the GCUPS numerator.
+    """
     torch = _torch()
-    lo = torch.minimum(n, m).double()
-    w = torch.clamp(torch.floor(lo * r), min=1).long()
-    width = torch.clamp((n - m).abs() + 2 * w - 1, max=m.long())
-    return n.long() * width
+    n = n.long()
+    m = m.long()
+    w = torch.clamp(torch.floor(torch.minimum(n, m).double() * r), min=1).long()
+    mx = torch.clamp(m - n, min=0) + w
+    mn = torch.clamp(n - m, min=0)
+    a = torch.minimum(torch.clamp(m - mx, min=0), n)
+    first = a * mx + a * (a - 1) // 2 + (n - a) * m
+    t = torch.clamp(n - (mn + w), min=0)
+    cells = first - t * (t + 1) // 2
+    return torch.where((n > 0) & (m > 0), cells, torch.zeros_like(cells))
 
 
 def plan_pairs(x, y, r, *, tune=True, weights=None):
