@@ -222,7 +222,8 @@ def bench_batched(args, dev, flush):
     x.masked_fill_(ar >= lx.unsqueeze(-1), float("nan"))
     y.masked_fill_(ar >= ly.unsqueeze(-1), float("nan"))
     t0 = time.perf_counter()
-    runner = BatchedDTW(x, y, r=r, tune=True, graph=True)
+    tile = tuple(int(v) for v in args.c4_tile.split(",")) if args.c4_tile else None
+    runner = BatchedDTW(x, y, r=r, tune=tile is None, graph=True, tile=tile)
     plan_s = time.perf_counter() - t0
     cells = runner.cells
     for _ in range(args.warmup):
@@ -349,10 +350,18 @@ def run_gpu(args):
             dist.barrier()
 
     wl = WORKLOAD
+    dev = torch.device("cuda", local)
+    if args.skip_fp64:
+        flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
+        forms = {"batched_fp32": bench_batched(args, dev, flush)}
+        if not args.no_fwd_bwd:
+            forms["fwd_bwd_fp32"] = bench_fwd_bwd(args, dev, flush)
+        if rank == 0:
+            print(json.dumps({"forms": forms}), flush=True)
+        return
     X, Y = make_data(rank, wl["nx"], wl["ny"], wl["L"])
     cells_pair = band_cells(wl["L"], wl["L"], wl["params"]["r"])
     cells = wl["nx"] * wl["ny"] * cells_pair
-    dev = torch.device("cuda", local)
     Xd = torch.as_tensor(X, device=dev)
     Yd = torch.as_tensor(Y, device=dev)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
@@ -492,6 +501,12 @@ def main():
     ap.add_argument("--c5-series", type=int, default=4096)
     ap.add_argument("--c5-adam-steps", type=int, default=100)
     ap.add_argument("--err-sample", type=int, default=64)
+    ap.add_argument("--c4-tile", default="",
+                    help="strip,block for the batched form instead of the autotuner")
+    ap.add_argument("--skip-fp64", action="store_true",
+                    help="only the FP32 forms (profiling captures)")
+    ap.add_argument("--no-fwd-bwd", action="store_true",
+                    help="with --skip-fp64: only the batched form")
     args = ap.parse_args()
     if (args.nx, args.ny) != (WORKLOAD["nx"], WORKLOAD["ny"]):
         WORKLOAD["nx"], WORKLOAD["ny"] = args.nx, args.ny

@@ -73,6 +73,45 @@ __device__ __forceinline__ Item load_item(const Dtw32Job &J, int64_t t) {
     return it;
 }
 
+// One column of a strip, updated in place: on entry P[k] holds cell
+// (i0 + k, c - 1), on exit cell (i0 + k, c).  With MASK, out-of-band cells get
+// an infinite cost (their hi is +inf and no in-band cell picks it); without,
+// every row of the strip is known to be in band for this column.  Rows past
+// the series end carry NaN x values: their cells are NaN and valid rows (which
+// only look upward) never read them.
+template <int S, bool W, bool DIRS, bool MASK>
+__device__ __forceinline__ void strip_column(HL (&P)[S], HL bup, HL bdiag, float yc,
+                                             const float (&xr)[S], int d0, int lo,
+                                             unsigned width, const float *__restrict__ w,
+                                             uint32_t &word) {
+    HL dg = bdiag;  // cell (i0 + k - 1, c - 1)
+    HL up = bup;    // cell (i0 + k - 1, c)
+#pragma unroll
+    for (int k = 0; k < S; k++) {
+        const HL lf = P[k];
+        HL best = dg;
+        int dir = 0;
+        if (up.h < best.h) {
+            best = up;
+            dir = 1;
+        }
+        if (lf.h < best.h) {
+            best = lf;
+            dir = 2;
+        }
+        const int d = d0 - k;  // c - i
+        float vv = __fsub_rn(xr[k], yc);
+        float cst = __fmul_rn(vv, vv);
+        if (W) cst = __fmul_rn(cst, w[abs(d)]);
+        if (MASK) cst = ((unsigned)(d - lo) < width) ? cst : WB_FINF;
+        const HL nv = add_c(best, cst);
+        if (DIRS) word |= (uint32_t)dir << (2 * k);
+        dg = lf;
+        up = nv;
+        P[k] = nv;
+    }
+}
+
 // One forward sweep; returns the (hi, lo) cost of cell (n-1, m-1).
 template <int S, bool W, bool DIRS>
 __device__ HL sweep(const Item &it, const float *__restrict__ w, float2 *ring, int64_t nth,
@@ -98,65 +137,69 @@ __device__ HL sweep(const Item &it, const float *__restrict__ w, float2 *ring, i
     HL result = acc;
     int pstart = 0, pend = lim;
     int64_t wofs = 0;
-    const int lo = -(mn + r - 1), hi = mx - 1;
+    // in band iff lo <= c - i <= hi
+    const int lo = -(mn + r - 1);
+    const int hi = mx - 1;
+    const unsigned width = (unsigned)(hi - lo + 1);
+    const float qnan = __int_as_float(0x7fc00000);
     for (int i0 = 1; i0 < n; i0 += S) {
         const int rows = imin(S, n - i0);
         float xr[S];
 #pragma unroll
-        for (int k = 0; k < S; k++) xr[k] = (k < rows) ? X[i0 + k] : 0.0f;
+        for (int k = 0; k < S; k++) xr[k] = (k < rows) ? X[i0 + k] : qnan;
         const int cstart = imax(0, i0 - mn - r + 1);
         const int cend = imin(m, i0 + rows - 1 + mx);
-        HL prev[S];
+        // columns where every row of a full strip is in band
+        int bstart = cend, bend = cend;
+        if (rows == S) {
+            bstart = imax(cstart, i0 + S - 1 + lo);
+            bend = imin(cend, i0 + hi + 1);
+            if (bstart >= bend) bstart = bend = cend;
+        }
+        HL P[S];
 #pragma unroll
-        for (int k = 0; k < S; k++) prev[k] = hl_inf();
+        for (int k = 0; k < S; k++) P[k] = hl_inf();
         HL bdiag = hl_inf();
         if (cstart - 1 >= pstart && cstart - 1 < pend) {
             float2 t2 = ring[(int64_t)(cstart - 1) * nth];
             bdiag = HL{t2.x, t2.y};
         }
-        const bool last = (i0 + rows == n);
-        for (int c = cstart; c < cend; c++) {
-            HL bup = hl_inf();
-            if (c < pend) {
+        // loads run two columns ahead of their use
+        auto load_up = [&](int c) {
+            HL b = hl_inf();
+            if (c < cend && c < pend) {
                 float2 t2 = ring[(int64_t)c * nth];
-                bup = HL{t2.x, t2.y};
+                b = HL{t2.x, t2.y};
             }
-            const float yc = Y[c];
-            const int d0 = c - i0;
-            HL cur[S];
-            HL bottom = hl_inf();  // cell of row rows-1 in this column
+            return b;
+        };
+        auto load_y = [&](int c) { return c < cend ? Y[c] : 0.0f; };
+        HL nb0 = load_up(cstart), nb1 = load_up(cstart + 1);
+        float ny0 = load_y(cstart), ny1 = load_y(cstart + 1);
+        const bool last = (i0 + rows == n);
+        const int krow = rows - 1;
+        for (int c = cstart; c < cend; c++) {
+            const HL bup = nb0;
+            const float yc = ny0;
+            nb0 = nb1;
+            ny0 = ny1;
+            nb1 = load_up(c + 2);
+            ny1 = load_y(c + 2);
             uint32_t word = 0;
-#pragma unroll
-            for (int k = 0; k < S; k++) {
-                HL up = (k == 0) ? bup : cur[k - 1];
-                HL dg = (k == 0) ? bdiag : prev[k - 1];
-                HL lf = prev[k];
-                HL best = dg;
-                int dir = 0;
-                if (up.h < best.h) {
-                    best = up;
-                    dir = 1;
-                }
-                if (lf.h < best.h) {
-                    best = lf;
-                    dir = 2;
-                }
-                float vv = __fsub_rn(xr[k], yc);
-                float cst = __fmul_rn(vv, vv);
-                if (W) cst = __fmul_rn(cst, w[abs(d0 - k)]);
-                HL nv = add_c(best, cst);
-                const int d = d0 - k;
-                const bool inb = (k < rows) && d >= lo && d <= hi;
-                cur[k] = inb ? nv : hl_inf();
-                if (k < rows) bottom = cur[k];
-                if (DIRS) word |= (uint32_t)dir << (2 * k);
-            }
+            if (c >= bstart && c < bend)
+                strip_column<S, W, DIRS, false>(P, bup, bdiag, yc, xr, c - i0, lo, width, w,
+                                                word);
+            else
+                strip_column<S, W, DIRS, true>(P, bup, bdiag, yc, xr, c - i0, lo, width, w,
+                                               word);
             if (DIRS) dirs[(wofs + (c - cstart)) * nth] = word;
-            if (last && c == m - 1) result = bottom;
-            ring[(int64_t)c * nth] = make_float2(cur[S - 1].h, cur[S - 1].l);
-            bdiag = bup;
+            if (last && c == m - 1) {
 #pragma unroll
-            for (int k = 0; k < S; k++) prev[k] = cur[k];
+                for (int k = 0; k < S; k++)
+                    if (k <= krow) result = P[k];
+            }
+            ring[(int64_t)c * nth] = make_float2(P[S - 1].h, P[S - 1].l);
+            bdiag = bup;
         }
         pstart = cstart;
         pend = cend;

@@ -235,7 +235,37 @@ def band_cost(n, m, r):
     return torch.where((n > 0) & (m > 0), cells, torch.zeros_like(cells))
 
 
-def plan_pairs(x, y, r, *, tune=True, weights=None):
+def bucket_order(n, m, r):
+    """Processing order of the items.
+
+    Items are grouped by (n in 32-wide buckets, m - n in 16-wide buckets): the
+    32 lanes of a warp then run nearly the same number of strips and of
+    columns per strip (band width |m - n| + 2r).  Buckets are ordered by
+    their mean band cell count, largest first, so the persistent queue ends on
+    small problems; within a bucket, larger problems first.
+    """
+    torch = _torch()
+    n = n.long()
+    m = m.long()
+    nb = (n // 32).clamp(0, 1023)
+    db = ((m - n + 4096) // 16).clamp(0, 1023)
+    bucket = nb * 1024 + db
+    cost = band_cost(n, m, r)
+    nbk = 1024 * 1024
+    tot = torch.zeros(nbk, dtype=torch.float64, device=n.device).index_add_(
+        0, bucket, cost.double())
+    cnt = torch.zeros(nbk, dtype=torch.float64, device=n.device).index_add_(
+        0, bucket, torch.ones_like(cost, dtype=torch.float64))
+    mean = tot / cnt.clamp(min=1)
+    # rank of every bucket by mean cost, largest first
+    brank = torch.empty(nbk, dtype=torch.long, device=n.device)
+    brank[torch.argsort(mean, descending=True, stable=True)] = torch.arange(
+        nbk, device=n.device)
+    key = brank[bucket] * (1 << 32) + (cost.max() - cost).clamp(0, (1 << 32) - 1)
+    return torch.argsort(key, stable=True)
+
+
+def plan_pairs(x, y, r, *, tune=True, weights=None, tile=None):
     """Items, lengths, order and kernel configuration of a paired batch.
 
     x, y: (N, d, L) float32 CUDA tensors (NaN padded).  Returns a dict with the
@@ -251,12 +281,14 @@ def plan_pairs(x, y, r, *, tune=True, weights=None):
     xl = series_lengths(xf)
     yl = series_lengths(yf)
     cost = band_cost(xl, yl, r)
-    order = torch.argsort(cost, descending=True, stable=True).to(torch.int32)
+    order = bucket_order(xl, yl, r).to(torch.int32)
     item = order.contiguous()
     plan = {"xf": xf, "yf": yf, "xl": xl, "yl": yl, "item_x": item, "item_y": item,
             "order": order.long(), "N": N, "d": d, "r": float(r), "weights": weights,
             "cells": int(cost.sum().item())}
-    if tune:
+    if tile is not None:
+        plan["strip"], plan["block"] = tile
+    elif tune:
         plan["strip"], plan["block"] = AUTOTUNER.pick(
             xf, yf, r=r, x_lengths=xl, y_lengths=yl, item_x=item, item_y=item,
             weights=weights)
@@ -309,13 +341,13 @@ class BatchedDTW:
     it on whatever the buffers ``x`` / ``y`` currently hold (same shapes).
     """
 
-    def __init__(self, x, y, r=1.0, *, tune=True, graph=True):
+    def __init__(self, x, y, r=1.0, *, tune=True, graph=True, tile=None):
         torch = _torch()
         if x.dim() == 2:
             x = x.unsqueeze(1)
             y = y.unsqueeze(1)
         self.x, self.y = x, y
-        self.plan = plan_pairs(x, y, r, tune=tune)
+        self.plan = plan_pairs(x, y, r, tune=tune, tile=tile)
         self.items = torch.empty(self.plan["item_x"].numel(), dtype=torch.float64,
                                  device=x.device)
         self.out = None
