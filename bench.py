@@ -329,6 +329,54 @@ def bench_fwd_bwd(args, dev, flush):
     }
 
 
+def c3_data(n_series, n_shapelets, T=1024, seed=6):
+    """Config 3 inputs: random-walk series and z-normalised random-walk
+    fragments of lengths U{16..128}."""
+    rng = np.random.default_rng(seed)
+    X = np.cumsum(rng.standard_normal((n_series, T)), axis=1)
+    lens = rng.integers(16, 129, size=n_shapelets)
+    shp = []
+    for L in lens:
+        f = np.cumsum(rng.standard_normal(L))
+        sd = f.std()
+        shp.append((f - f.mean()) / (sd if sd > 0 else 1.0))
+    return X, shp
+
+
+def bench_subsequence(args, dev, flush):
+    """pairwise_subsequence_distance of 10,000 shapelets against 1,000 series
+    of length 1,024 (float64, return_index), euclidean and scaled_euclidean."""
+    import torch
+
+    from oracle import oracle as O
+    from wildboar_gb300.distance import pairwise_subsequence_distance
+
+    X, shp = c3_data(args.c3_series, args.c3_shapelets)
+    T = X.shape[1]
+    elems = int(sum((T - len(s) + 1) * len(s) for s in shp)) * X.shape[0]
+    Xd = torch.as_tensor(X, device=dev)
+    res = {}
+    for metric in ("euclidean", "scaled_euclidean"):
+        def call():
+            return pairwise_subsequence_distance(shp, Xd, metric=metric, return_index=True)
+        call()
+        torch.cuda.synchronize()
+        ms = _timed(call, max(1, min(args.steps, 2)), flush)
+        d, i = call()
+        d = d.cpu().numpy()
+        i = i.cpu().numpy()
+        od, oi = O.subsequence(shp, X[:2], metric=metric, n_threads=os.cpu_count() or 1)
+        res[metric] = {
+            "ms": ms,
+            "g_window_elements_per_s": elems / (ms * 1e-3) / 1e9,
+            "argmin_exact_on_sample": bool(np.array_equal(i[:2], oi)),
+            "max_rel_err_on_sample": float(np.max(np.abs(d[:2] - od) / np.maximum(od, 1e-300))),
+        }
+    return {"config": f"{args.c3_shapelets} shapelets (L~U{{16..128}}, z-normalised "
+                      f"random-walk fragments) x {args.c3_series} series, T={T}, float64",
+            "algorithmic_window_elements": elems, **res}
+
+
 def run_gpu(args):
     import torch
 
@@ -353,9 +401,13 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     if args.skip_fp64:
         flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
-        forms = {"batched_fp32": bench_batched(args, dev, flush)}
-        if not args.no_fwd_bwd:
+        forms = {}
+        if args.only in ("", "batched"):
+            forms["batched_fp32"] = bench_batched(args, dev, flush)
+        if args.only in ("", "fwdbwd"):
             forms["fwd_bwd_fp32"] = bench_fwd_bwd(args, dev, flush)
+        if args.only in ("", "subseq"):
+            forms["subsequence"] = bench_subsequence(args, dev, flush)
         if rank == 0:
             print(json.dumps({"forms": forms}), flush=True)
         return
@@ -454,6 +506,7 @@ def run_gpu(args):
     if not args.no_forms:
         forms["batched_fp32"] = bench_batched(args, dev, flush)
         forms["fwd_bwd_fp32"] = bench_fwd_bwd(args, dev, flush)
+        forms["subsequence"] = bench_subsequence(args, dev, flush)
         forms["both_beat_fp64_drop_in"] = bool(
             forms["batched_fp32"]["gcups"] > value and forms["fwd_bwd_fp32"]["gcups"] > value)
     line = {
@@ -505,8 +558,10 @@ def main():
                     help="strip,block for the batched form instead of the autotuner")
     ap.add_argument("--skip-fp64", action="store_true",
                     help="only the FP32 forms (profiling captures)")
-    ap.add_argument("--no-fwd-bwd", action="store_true",
-                    help="with --skip-fp64: only the batched form")
+    ap.add_argument("--only", default="", choices=["", "batched", "fwdbwd", "subseq"],
+                    help="with --skip-fp64: run one form only")
+    ap.add_argument("--c3-series", type=int, default=1000)
+    ap.add_argument("--c3-shapelets", type=int, default=10000)
     args = ap.parse_args()
     if (args.nx, args.ny) != (WORKLOAD["nx"], WORKLOAD["ny"]):
         WORKLOAD["nx"], WORKLOAD["ny"] = args.nx, args.ny

@@ -117,18 +117,22 @@ int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_t dim,
  * minimum subsequence distance and first argmin window of every shapelet
  * against every x[i, dim]: out_dist / out_idx are (x.n, m).  Shapelets are
  * packed float64 values; offsets/lengths index them.  means/stds are the
- * np.mean / np.std of each shapelet (std <= 1e-13 given as 0), used by the
- * scaled metric only.  metric is WB_EUCLIDEAN or WB_SCALED_EUCLIDEAN.
- * Shapelet arrays live on the same side as x.  Replaces
+ * np.mean / np.std of each shapelet (std <= 1e-13 given as 0): the scaled
+ * metric uses both, edr with a NaN epsilon uses stds (epsilon = std / 4).
+ * metric is WB_EUCLIDEAN, WB_SCALED_EUCLIDEAN or an elastic id (dtw, wdtw,
+ * ddtw, wddtw, adtw, lcss, edr, erp, msm, twe) with `params` (NULL allowed for
+ * the euclidean ones).  Shapelet arrays live on the same side as x.  Replaces
  * _pairwise_subsequence_distance (distance/_cdistance.pyx:956-1037) with
- * euclidean_distance / scaled_euclidean_distance (distance/_metric.pyx:561-682).
+ * euclidean_distance / scaled_euclidean_distance (distance/_metric.pyx:561-682)
+ * and the elastic *_subsequence_distance functions (distance/_elastic.pyx:
+ * 622-1866), including their early abandoning at the running minimum.
  */
 int wb_pairwise_subsequence_distance(const double *shapelets, const int64_t *offsets,
                                      const int64_t *lengths, const double *means,
                                      const double *stds, int64_t m, const wb_series *x,
-                                     int64_t dim, int32_t metric, double *out_dist,
-                                     int64_t *out_idx, int32_t out_on_device,
-                                     void *stream);
+                                     int64_t dim, int32_t metric, const wb_params *params,
+                                     double *out_dist, int64_t *out_idx,
+                                     int32_t out_on_device, void *stream);
 
 /* ------------------------------------------------------------------------
  * FP32 forms (batched, ragged, differentiable).  No counterpart in the

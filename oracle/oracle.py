@@ -83,7 +83,7 @@ def lib():
         L.wbo_argmin.argtypes = [dp, i64, i64, i64, dp, i64, i64, i64, i64,
                                  ctypes.c_int, pp, i64, dp, ip, dp, ctypes.c_int]
         L.wbo_subsequence.argtypes = [dp, ip, ip, dp, dp, i64, dp, i64, i64, i64, i64,
-                                      ctypes.c_int, dp, ip, ctypes.c_int]
+                                      ctypes.c_int, pp, dp, ip, ctypes.c_int]
         L.wbo_distance_1d.argtypes = [dp, i64, dp, i64, ctypes.c_int, pp]
         L.wbo_distance_1d.restype = ctypes.c_double
         L.wbo_fast_mean_std.argtypes = [dp, i64, dp, dp]
@@ -171,7 +171,24 @@ def argmin(x, y, *, k=1, dim=0, metric="dtw", metric_params=None, lower_bound=No
     return idx, dist
 
 
-def subsequence(shapelets, x, *, dim=0, metric="euclidean", n_threads=1):
+# Constructor defaults of the elastic subsequence metric classes
+# (distance/_elastic.pyx:2206-3124)
+SUBSEQ_DEFAULTS = {
+    "dtw": {"r": 1.0},
+    "wdtw": {"r": 1.0, "g": 0.05},
+    "ddtw": {"r": 1.0},
+    "wddtw": {"r": 1.0, "g": 0.05},
+    "adtw": {"r": 1.0, "p": 1.0},
+    "lcss": {"r": 1.0, "epsilon": 1.0},
+    "edr": {"r": 1.0, "epsilon": math.nan},
+    "erp": {"r": 1.0, "g": 0.0},
+    "msm": {"r": 1.0, "c": 1.0},
+    "twe": {"r": 1.0, "penalty": 1.0, "stiffness": 0.001},
+}
+
+
+def subsequence(shapelets, x, *, dim=0, metric="euclidean", metric_params=None,
+                n_threads=1):
     """(n_samples, n_shapelets) min distance and first argmin index."""
     X = _ts(x)
     shp = [np.asarray(s, dtype=np.float64).ravel() for s in shapelets]
@@ -184,10 +201,21 @@ def subsequence(shapelets, x, *, dim=0, metric="euclidean", n_threads=1):
     sstd = np.array([np.std(s) for s in shp])
     sstd[sstd <= 1e-13] = 0.0
     dist = np.empty((X.shape[0], len(shp)))
-    idx = np.empty((X.shape[0], len(shp)), dtype=np.int64)
+    idx = np.zeros((X.shape[0], len(shp)), dtype=np.int64)
+    pd = dict(SUBSEQ_DEFAULTS.get(metric, {}))
+    pd.update(metric_params or {})
+    p = Params()
+    p.r = pd.get("r", 1.0)
+    p.g = pd.get("g", 0.0)
+    p.p = pd.get("p", 1.0)
+    p.epsilon = pd.get("epsilon", math.nan)
+    p.c = pd.get("c", 1.0)
+    p.penalty = pd.get("penalty", 1.0)
+    p.stiffness = pd.get("stiffness", 0.001)
     lib().wbo_subsequence(_dp(packed), _ip(offs), _ip(lens), _dp(smean), _dp(sstd),
                           len(shp), _dp(X), X.shape[0], X.shape[1], X.shape[2], dim,
-                          METRIC_IDS[metric], _dp(dist), _ip(idx), n_threads)
+                          METRIC_IDS[metric], ctypes.byref(p), _dp(dist), _ip(idx),
+                          n_threads)
     return dist, idx
 
 

@@ -585,6 +585,82 @@ static double metric_call(const wbo_metric *M, wbo_scratch *s, const double *x, 
     return 0;
 }
 
+/* Elastic subsequence distance: the *_subsequence_distance functions of
+ * distance/_elastic.pyx (dtw :622-655, adtw :701-731, ddtw :769-806, lcss
+ * :1186-1217, erp :1350-1382, edr :1500-1534, msm :1650-1681, twe :1832-1866)
+ * with the metric classes' parameters (:2206-3124).  Every window T[i:i+L] is
+ * compared with S, early abandoning at the running minimum (transformed as the
+ * reference does), keeping the first strictly smaller window. */
+static double subseq_elastic(int metric, const wbo_params *p, const double *S, idx_t sl,
+                             double s_std, const double *T, idx_t tl, wbo_scratch *s,
+                             const double *weights, double *sbuf, double *tbuf,
+                             idx_t *index)
+{
+    idx_t r = compute_r(sl, p->r);
+    idx_t length = tl - sl + 1;
+    double min_dist = INF, dist = 0;
+    if ((metric == WBO_DDTW || metric == WBO_WDDTW) && sl < 3) return 0;
+    if (metric == WBO_DDTW || metric == WBO_WDDTW) average_slope(S, sl, sbuf);
+    for (idx_t i = 0; i < length; i++) {
+        switch (metric) {
+        case WBO_DTW:
+        case WBO_WDTW:
+            dist = dtw_rows(S, sl, T + i, sl, r, s->cost, s->cost_prev, weights, min_dist);
+            break;
+        case WBO_ADTW:
+            dist = adtw_rows(S, sl, T + i, sl, r, s->cost, s->cost_prev, p->p, min_dist);
+            break;
+        case WBO_DDTW:
+        case WBO_WDDTW:
+            average_slope(T + i, sl, tbuf);
+            dist = dtw_rows(sbuf, sl - 2, tbuf, sl - 2, r, s->cost, s->cost_prev, weights,
+                            min_dist);
+            break;
+        case WBO_LCSS: {
+            double ml = (double)imin(sl, tl);
+            double thr = isinf(min_dist) == 0 ? ml - min_dist * ml : min_dist;
+            dist = lcss_rows(S, sl, T + i, sl, r, p->epsilon, s->cost, s->cost_prev, NULL,
+                             thr);
+            break;
+        }
+        case WBO_EDR: {
+            double eps = isnan(p->epsilon) ? s_std / 4.0 : p->epsilon;
+            dist = edr_rows(S, sl, T + i, sl, r, eps, s->cost, s->cost_prev,
+                            min_dist * (double)imax(sl, tl));
+            break;
+        }
+        case WBO_ERP:
+            dist = erp_rows(S, sl, T + i, sl, r, p->g, s->gX, s->gY, s->cost, s->cost_prev,
+                            min_dist);
+            break;
+        case WBO_MSM:
+            dist = msm_rows(S, sl, T + i, sl, r, p->c, s->cost, s->cost_prev, s->cost_y,
+                            min_dist);
+            break;
+        case WBO_TWE:
+            dist = twe_rows(S, sl, T + i, sl, r, p->penalty, p->stiffness, s->cost,
+                            s->cost_prev, min_dist);
+            break;
+        default:
+            return NAN;
+        }
+        if (dist < min_dist) {
+            if (index) *index = i;
+            min_dist = dist;
+        }
+    }
+    switch (metric) {
+    case WBO_DTW:
+    case WBO_WDTW:
+    case WBO_ADTW:
+    case WBO_DDTW:
+    case WBO_WDDTW:
+        return sqrt(min_dist);
+    default:
+        return min_dist;
+    }
+}
+
 /* ---------------------------------------------------------------------- */
 /* Heap keeping the k smallest: utils/_misc.pyx:18-107                     */
 /* ---------------------------------------------------------------------- */
@@ -655,6 +731,8 @@ typedef struct {
     const double *shp;
     const idx_t *shp_off, *shp_len;
     const double *shp_mean, *shp_std;
+    const double *sub_weights;
+    wbo_params sub_params;
     idx_t m;
     idx_t begin, end;
 } job_t;
@@ -669,7 +747,11 @@ static void *run_job(void *arg)
     double *sbuf = NULL;
     heap_el *heap = NULL;
     if (J->kind == 3) heap = malloc(sizeof(heap_el) * (size_t)imax(J->k, 1));
-    if (J->kind == 4) sbuf = malloc(sizeof(double) * (size_t)(2 * J->xL + 2));
+    double *tbuf = NULL;
+    if (J->kind == 4) {
+        sbuf = malloc(sizeof(double) * (size_t)(2 * J->xL + 2));
+        tbuf = malloc(sizeof(double) * (size_t)(2 * J->xL + 2));
+    }
     for (idx_t i = J->begin; i < J->end; i++) {
         const double *xr = J->X + (i * J->xd + J->dim) * J->xL;
         if (J->kind == 0) {
@@ -718,8 +800,12 @@ static void *run_job(void *arg)
                 if (M->id == WBO_SCALED_EUCLIDEAN) {
                     double sstd = J->shp_std[j] != 0 ? J->shp_std[j] : 1.0;
                     d = scaled_euclid_scan(S, sl, J->shp_mean[j], sstd, xr, J->xL, sbuf, &mi);
-                } else {
+                } else if (M->id == WBO_EUCLIDEAN) {
                     d = euclid_scan(S, sl, xr, J->xL, INF, &mi);
+                } else {
+                    double sstd = J->shp_std && J->shp_std[j] != 0 ? J->shp_std[j] : 1.0;
+                    d = subseq_elastic(M->id, &J->sub_params, S, sl, sstd, xr, J->xL, &s,
+                                       J->sub_weights, sbuf, tbuf, &mi);
                 }
                 J->out[i * J->m + j] = d;
                 J->out_idx[i * J->m + j] = mi;
@@ -728,6 +814,7 @@ static void *run_job(void *arg)
     }
     free(heap);
     free(sbuf);
+    free(tbuf);
     scratch_free(&s);
     return NULL;
 }
@@ -829,8 +916,8 @@ int wbo_argmin(const double *X, idx_t xn, idx_t xd, idx_t xL, const double *Y, i
  * _cdistance.pyx:453-467). */
 int wbo_subsequence(const double *shp, const idx_t *off, const idx_t *len,
                     const double *smean, const double *sstd, idx_t m, const double *X,
-                    idx_t xn, idx_t xd, idx_t xL, idx_t dim, int metric, double *out_dist,
-                    idx_t *out_idx, int n_threads)
+                    idx_t xn, idx_t xd, idx_t xL, idx_t dim, int metric,
+                    const wbo_params *p, double *out_dist, idx_t *out_idx, int n_threads)
 {
     wbo_metric M = {0};
     M.id = metric;
@@ -839,7 +926,15 @@ int wbo_subsequence(const double *shp, const idx_t *off, const idx_t *len,
     J.X = X; J.xn = xn; J.xd = xd; J.xL = xL; J.yL = xL; J.dim = dim;
     J.shp = shp; J.shp_off = off; J.shp_len = len; J.shp_mean = smean; J.shp_std = sstd;
     J.m = m; J.out = out_dist; J.out_idx = out_idx;
+    double *w = NULL;
+    if (p) J.sub_params = *p;
+    /* WeightedDtwSubsequenceMetric.reset (_elastic.pyx:2364-2376): n = X.shape[2];
+     * WeightedDerivativeDtwSubsequenceMetric.reset (:2533-2546): n = X.shape[2] - 2 */
+    if (metric == WBO_WDTW) w = logistic_weights(xL, p->g);
+    if (metric == WBO_WDDTW) w = logistic_weights(xL - 2 > 0 ? xL - 2 : 0, p->g);
+    J.sub_weights = w;
     run_parallel(&J, xn, n_threads);
+    free(w);
     return 0;
 }
 

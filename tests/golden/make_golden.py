@@ -194,6 +194,27 @@ def main():
         add(f"alignment_r{r}", "alignment", {"x": a, "y": b, "mask": mask},
             {"r": r}, {"a": np.where(mask, al, 0.0)})
 
+    # elastic subsequence metrics (distance/_elastic.pyx:2206-3124)
+    T2 = _walk(rng, (5, 80))
+    shp2 = [_walk(rng, (int(n),)) for n in (2, 3, 9, 17, 33)]
+    shp2.append(T2[1, 10:30].copy())
+    packed2 = np.concatenate(shp2)
+    lens2 = np.array([s.shape[0] for s in shp2])
+    for metric, params in (("dtw", {"r": 0.2}), ("dtw", {}), ("wdtw", {"r": 0.5, "g": 0.1}),
+                           ("ddtw", {"r": 0.3}), ("wddtw", {}), ("adtw", {"p": 0.3}),
+                           ("lcss", {"r": 0.3, "epsilon": 0.7}), ("edr", {}),
+                           ("edr", {"r": 0.4, "epsilon": 0.3}), ("erp", {"g": 0.2}),
+                           ("msm", {"r": 0.2}), ("twe", {"r": 0.4})):
+        d, i = pairwise_subsequence_distance(shp2, T2, metric=metric,
+                                             metric_params=params, return_index=True)
+        if metric in ("ddtw", "wddtw"):
+            # series shorter than 3 return 0 without setting the index
+            i = np.where(lens2[None, :] < 3, -1, i)
+        tag = "_".join(f"{k}{v}" for k, v in params.items())
+        add(f"subseq_{metric}_{tag}", "subsequence",
+            {"x": T2, "shapelets": packed2, "lengths": lens2},
+            {"metric": metric, "metric_params": params}, {"d": d, "idx": i})
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"reference_version": getattr(wildboar, "__version__", "?"),

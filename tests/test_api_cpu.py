@@ -154,7 +154,7 @@ def test_subsequence_validation():
     with pytest.raises(ValueError, match="Invalid subsequnce shape"):
         pairwise_subsequence_distance(np.ones(11), np.ones((2, 10)))
     with pytest.raises(ValueError, match="unsupported metric"):
-        pairwise_subsequence_distance(np.ones(3), np.ones((2, 10)), metric="dtw")
+        pairwise_subsequence_distance(np.ones(3), np.ones((2, 10)), metric="manhattan")
 
 
 def test_params_struct_matches_header():

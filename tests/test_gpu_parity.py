@@ -59,7 +59,7 @@ def run_api(case):
     if kind == "subsequence":
         shp = _golden.unpack_shapelets(case)
         d, i = pairwise_subsequence_distance(shp, inp["x"], metric=metric,
-                                             return_index=True)
+                                             metric_params=params, return_index=True)
         return {"d": d, "idx": i}
     return None
 
@@ -75,7 +75,8 @@ def test_golden(case):
         want = np.asarray(want)
         assert g.shape == want.shape
         if want.dtype.kind in "iu":
-            np.testing.assert_array_equal(g, want)
+            keep = want >= 0  # -1: the reference leaves the index unset
+            np.testing.assert_array_equal(g[keep], want[keep])
         else:
             np.testing.assert_allclose(g, want, rtol=RTOL, atol=0)
 
@@ -177,6 +178,31 @@ def test_subsequence_vs_oracle(metric):
     od, oi = O.subsequence(shp, T, metric=metric)
     np.testing.assert_array_equal(i, oi)
     np.testing.assert_allclose(d, od, rtol=RTOL, atol=0)
+
+
+SUBSEQ_ELASTIC = [
+    ("dtw", {"r": 0.2}), ("dtw", {"r": 1.0}), ("wdtw", {"r": 0.5, "g": 0.1}),
+    ("ddtw", {"r": 0.3}), ("wddtw", {}), ("adtw", {"p": 0.3}), ("adtw", {"p": -0.1}),
+    ("lcss", {"r": 0.3, "epsilon": 0.7}), ("edr", {}), ("edr", {"epsilon": 0.3}),
+    ("erp", {"g": 0.2}), ("msm", {"r": 0.2}), ("twe", {"r": 0.4}),
+]
+
+
+@pytest.mark.parametrize("metric,params", SUBSEQ_ELASTIC)
+def test_elastic_subsequence_vs_oracle(metric, params):
+    rng = np.random.default_rng(zlib.crc32(repr((metric, params)).encode()))
+    T = _walk(rng, (6, 120))
+    shp = [_walk(rng, (int(n),)) for n in (2, 3, 5, 11, 24, 47, 64)]
+    shp.append(T[3, 40:70].copy())
+    d, i = pairwise_subsequence_distance(shp, T, metric=metric, metric_params=params,
+                                         return_index=True)
+    od, oi = O.subsequence(shp, T, metric=metric, metric_params=params)
+    lens = np.array([len(s) for s in shp])
+    keep = np.ones_like(oi, dtype=bool)
+    if metric in ("ddtw", "wddtw"):
+        keep[:, lens < 3] = False  # the reference leaves the index unset
+    np.testing.assert_array_equal(i[keep], oi[keep])
+    np.testing.assert_allclose(d, od, rtol=RTOL, atol=0, equal_nan=True)
 
 
 def test_subsequence_full_length_equals_pairwise():

@@ -63,7 +63,7 @@ def _declare(L):
     L.wb_argmin_distance.argtypes = [P(Series), P(Series), i64, i32, P(Params), i64, vp, vp,
                                      vp, i32, vp]
     L.wb_pairwise_subsequence_distance.argtypes = [vp, vp, vp, vp, vp, i64, P(Series), i64,
-                                                   i32, vp, vp, i32, vp]
+                                                   i32, P(Params), vp, vp, i32, vp]
     L.wb_last_error.restype = ctypes.c_char_p
     L.wb_version.restype = i32
     L.wb_release_workspace.argtypes = [vp]

@@ -556,15 +556,163 @@ extern "C" int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_
     return WB_OK;
 }
 
+// elastic subsequence metrics: the *_subsequence_distance functions of
+// distance/_elastic.pyx:622-1866 with the metric classes of :2206-3124
+static int subseq_elastic(const double *shapelets, const int64_t *offsets,
+                          const int64_t *lengths, const double *stds, int64_t m,
+                          const wb_series *x, int64_t dim, int32_t metric,
+                          const wb_params *p, double *out_dist, int64_t *out_idx,
+                          int32_t out_on_device, cudaStream_t s,
+                          const std::vector<int64_t> &hlen, int64_t total) {
+    if (!(p->r >= 0.0 && p->r <= 1.0)) return fail(WB_EINVAL, "r must be in [0, 1]");
+    const bool dev_in = x->on_device != 0;
+    const bool slopes = derivative(metric);
+    const int T = (int)x->n_timestep;
+    SubseqElasticJob J;
+    J.m = m;
+    J.metric = metric;
+    J.slopes = slopes ? 1 : 0;
+    J.t_len_thr = T;
+    J.eps = p->epsilon;
+    J.p = p->p;
+    J.g = p->g;
+    J.c = p->c;
+    J.penalty = p->penalty;
+    J.stiffness = p->stiffness;
+    int kind;
+    switch (metric) {
+        case WB_DTW: case WB_DDTW: kind = K_DTW; break;
+        case WB_WDTW: case WB_WDDTW: kind = K_WDTW; break;
+        case WB_ADTW: kind = p->p >= 0.0 ? K_ADTW : K_ADTW_ANY; break;
+        case WB_LCSS:
+            if (!(p->epsilon > 0.0)) return fail(WB_EINVAL, "epsilon must be > 0");
+            kind = K_LCSS;
+            break;
+        case WB_EDR:
+            if (std::isnan(p->epsilon) && !stds)
+                return fail(WB_EINVAL, "edr with the default epsilon needs shapelet stds");
+            kind = K_EDR;
+            break;
+        case WB_ERP: kind = K_ERP; break;
+        case WB_MSM: kind = K_MSM; break;
+        case WB_TWE: kind = K_TWE; break;
+        default:
+            return fail(WB_EUNSUPPORTED, "unsupported subsequence metric id " +
+                                             std::to_string(metric));
+    }
+    // per-shapelet bands: _compute_r(s_len, r)
+    std::vector<int32_t> band(m);
+    int max_len = 1, max_band = 1, max_orig = 1;
+    for (int64_t i = 0; i < m; i++) {
+        band[i] = compute_r(hlen[i], p->r);
+        int cl = (int)(slopes ? std::max<int64_t>(hlen[i] - 2, 1) : hlen[i]);
+        max_len = std::max(max_len, cl);
+        max_band = std::max(max_band, (int)band[i]);
+        max_orig = std::max(max_orig, (int)hlen[i]);
+    }
+    const int xs_len = slopes ? std::max(T - 2, 1) : T;
+    J.x.count = x->n;
+    J.x.len = xs_len;
+    J.t_len = xs_len;
+    int P = 0, grid = 0;
+    size_t ring = elastic_subseq_ring_bytes(J, max_len, max_band, &P, &grid);
+    std::vector<double> w;
+    if (metric == WB_WDTW) w = logistic_weights(T, p->g);
+    if (metric == WB_WDDTW) w = logistic_weights(std::max(T - 2, 0), p->g);
+    Workspace ws(s);
+    size_t need = ring + stage_bytes(x) + align256(m * 4) + align256(w.size() * 8 + 8) +
+                  (dev_in ? 0 : align256(total * 8) + 3 * align256(m * 8)) +
+                  (slopes ? align256((size_t)x->n * xs_len * 8) + align256(total * 8) : 0) +
+                  (metric == WB_ERP ? align256((size_t)x->n * T * 8) + align256(x->n * 8) : 0) +
+                  (metric == WB_TWE ? align256((size_t)max_orig * 8 + 8) : 0) +
+                  (out_on_device ? 0 : 2 * align256((size_t)x->n * m * 8));
+    WB_TRY(ws.reserve(need));
+    WB_TAKE(gring, double, ws, ring / sizeof(double));
+    SeriesSet X;
+    WB_TRY(stage(x, dim, ws, X));
+    const double *dshp = shapelets;
+    const int64_t *doff = offsets, *dlen = lengths;
+    const double *dstd = stds;
+    if (!dev_in) {
+        WB_TAKE(hs, double, ws, total);
+        WB_TAKE(ho, int64_t, ws, m);
+        WB_TAKE(hl, int64_t, ws, m);
+        WB_CUDA(cudaMemcpyAsync(hs, shapelets, total * 8, cudaMemcpyHostToDevice, s));
+        WB_CUDA(cudaMemcpyAsync(ho, offsets, m * 8, cudaMemcpyHostToDevice, s));
+        WB_CUDA(cudaMemcpyAsync(hl, lengths, m * 8, cudaMemcpyHostToDevice, s));
+        dshp = hs;
+        doff = ho;
+        dlen = hl;
+        if (stds) {
+            WB_TAKE(hd, double, ws, m);
+            WB_CUDA(cudaMemcpyAsync(hd, stds, m * 8, cudaMemcpyHostToDevice, s));
+            dstd = hd;
+        }
+    }
+    WB_TAKE(dband, int32_t, ws, m);
+    WB_CUDA(cudaMemcpyAsync(dband, band.data(), m * 4, cudaMemcpyHostToDevice, s));
+    if (!w.empty()) {
+        WB_TAKE(dw, double, ws, w.size());
+        WB_CUDA(cudaMemcpyAsync(dw, w.data(), w.size() * 8, cudaMemcpyHostToDevice, s));
+        J.weights = dw;
+    }
+    J.x = X;
+    J.x.len = xs_len;
+    if (slopes) {
+        WB_TAKE(xsl, double, ws, (size_t)x->n * xs_len);
+        WB_TRY(launch_slopes(X, xsl, s));
+        J.x.base = xsl;
+        J.x.stride = xs_len;
+        WB_TAKE(ssl, double, ws, total);
+        WB_TRY(launch_shapelet_slopes(dshp, doff, dlen, m, ssl, s));
+        dshp = ssl;
+    }
+    if (metric == WB_ERP) {
+        WB_TAKE(gt, double, ws, (size_t)x->n * T);
+        WB_TAKE(gs, double, ws, x->n);
+        WB_TRY(launch_erp_tables(X, p->g, gt, gs, s));
+        J.gtab = gt;
+    }
+    if (metric == WB_TWE) {
+        WB_TAKE(st, double, ws, max_orig);
+        WB_TRY(launch_fill_stab(p->stiffness * 2.0, max_orig, st, s));
+        J.stab = st;
+    }
+    J.shp = dshp;
+    J.off = doff;
+    J.len = dlen;
+    J.band_of_len = dband;
+    J.shp_std = (metric == WB_EDR && std::isnan(p->epsilon)) ? dstd : nullptr;
+    double *od = out_dist;
+    int64_t *oi = out_idx;
+    if (!out_on_device) {
+        od = ws.take<double>((size_t)x->n * m);
+        oi = ws.take<int64_t>((size_t)x->n * m);
+        if (!od || !oi) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    }
+    J.out_dist = od;
+    J.out_idx = oi;
+    WB_TRY(launch_elastic_subseq(J, kind, gring, P, grid, s));
+    if (!out_on_device) {
+        WB_CUDA(cudaMemcpyAsync(out_dist, od, (size_t)x->n * m * 8, cudaMemcpyDeviceToHost, s));
+        WB_CUDA(cudaMemcpyAsync(out_idx, oi, (size_t)x->n * m * 8, cudaMemcpyDeviceToHost, s));
+    }
+    // host vectors above feed asynchronous copies
+    WB_CUDA(cudaStreamSynchronize(s));
+    return WB_OK;
+}
+
 extern "C" int wb_pairwise_subsequence_distance(
     const double *shapelets, const int64_t *offsets, const int64_t *lengths,
     const double *means, const double *stds, int64_t m, const wb_series *x, int64_t dim,
-    int32_t metric, double *out_dist, int64_t *out_idx, int32_t out_on_device,
-    void *stream_) {
+    int32_t metric, const wb_params *params, double *out_dist, int64_t *out_idx,
+    int32_t out_on_device, void *stream_) {
     WB_TRY(check_series(x, "x"));
     WB_TRY(check_dim(x, dim));
-    if (metric != WB_EUCLIDEAN && metric != WB_SCALED_EUCLIDEAN)
+    const bool elastic = is_elastic(metric) && metric != WB_WLCSS;
+    if (metric != WB_EUCLIDEAN && metric != WB_SCALED_EUCLIDEAN && !elastic)
         return fail(WB_EUNSUPPORTED, "unsupported subsequence metric id " + std::to_string(metric));
+    if (elastic && !params) return fail(WB_EINVAL, "params is NULL");
     if (m < 0) return fail(WB_EINVAL, "negative number of shapelets");
     if (m == 0 || x->n == 0) return WB_OK;
     if (!shapelets || !offsets || !lengths || !out_dist || !out_idx)
@@ -591,6 +739,9 @@ extern "C" int wb_pairwise_subsequence_distance(
         if (hoff[i] < 0) return fail(WB_EINVAL, "negative shapelet offset");
         total = std::max(total, hoff[i] + hlen[i]);
     }
+    if (elastic)
+        return subseq_elastic(shapelets, offsets, lengths, stds, m, x, dim, metric, params,
+                              out_dist, out_idx, out_on_device, s, hlen, total);
     std::vector<int64_t> order(m);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(),

@@ -82,6 +82,34 @@ int launch_elastic_external_ring(const ElasticJob &job, double *ring, size_t rin
                                  cudaStream_t s);
 size_t elastic_workspace_bytes(const ElasticJob &job);
 
+// elastic subsequence distance (one warp per (series, shapelet), one lane per
+// window); rows are the shapelet (or its slopes), columns the window.
+struct SubseqElasticJob {
+    SeriesSet x;                  // series scanned (slopes for ddtw / wddtw)
+    int t_len = 0;                // row stride of gtab (erp) = x.len
+    int t_len_thr = 0;            // the series length the reference's thresholds use
+    const double *shp = nullptr;  // packed shapelets (slopes for ddtw / wddtw)
+    const int64_t *off = nullptr;
+    const int64_t *len = nullptr; // original shapelet lengths
+    const int32_t *band_of_len = nullptr;  // band of each shapelet
+    const double *shp_std = nullptr;       // edr default epsilon (NaN epsilon)
+    int64_t m = 0;
+    int metric = WB_DTW;
+    int slopes = 0;
+    double eps = 0, p = 0, g = 0, c = 0, penalty = 0, stiffness = 0;
+    const double *weights = nullptr;
+    const double *gtab = nullptr;  // erp: |x - g| per series, (x.count, t_len)
+    const double *stab = nullptr;  // twe: (2 stiffness) k
+    double *out_dist = nullptr;
+    int64_t *out_idx = nullptr;
+};
+size_t elastic_subseq_ring_bytes(const SubseqElasticJob &J, int max_len, int max_band,
+                                 int *P_out, int *grid_out);
+int launch_elastic_subseq(const SubseqElasticJob &J, int kind, double *gring, int P, int grid,
+                          cudaStream_t s);
+int launch_shapelet_slopes(const double *shp, const int64_t *off, const int64_t *len,
+                           int64_t m, double *out, cudaStream_t s);
+
 // per-series preparation kernels
 int launch_slopes(const SeriesSet &in, double *out, cudaStream_t s);
 int launch_mean_std(const SeriesSet &in, double *std_out, cudaStream_t s);

@@ -369,8 +369,10 @@ __device__ double rec_msm(R ring, int P, const double *__restrict__ X, int n,
     return ring.ld((m - 1) % P);
 }
 
-// twe: twe_distance, distance/_elastic.pyx:1733-1829
-template <class R>
+// twe: twe_distance, distance/_elastic.pyx:1733-1829.  DYTAB: |y_{j-1} - y_j|
+// from a per-series table; otherwise computed (windows of a longer series
+// start with y_{-1} = 0, which no whole-series table holds).
+template <class R, bool DYTAB = true>
 __device__ double rec_twe(R ring, int P, const double *__restrict__ X, int n,
                           const double *__restrict__ Y, int m, int r, double penalty,
                           double stiffness, const double *__restrict__ dY,
@@ -409,7 +411,8 @@ __device__ double rec_twe(R ring, int P, const double *__restrict__ X, int n,
             double up = ring.ld(q);
             const double yj = ldg(Y + j);
             double del_x = (up + dxi) + pen;
-            double del_y = (left + ldg(dY + j)) + pen;
+            const double dyj = DYTAB ? ldg(dY + j) : fabs(yp - yj);
+            double del_y = (left + dyj) + pen;
             double match = ((upleft + fabs(xi - yj)) + fabs(xp - yp)) + ldg(stab + abs(i - j));
             double nv = nn_min(nn_min(del_x, del_y), match);
             ring.st(q, nv);
@@ -604,6 +607,174 @@ int launch_elastic(const ElasticJob &J, Workspace &ws, size_t *) {
         case K_EUCLID: return launch_kind<K_EUCLID>(J, ws, 2, false, nullptr, pl.grid);
     }
     return fail(WB_EINVAL, "unknown elastic kernel");
+}
+
+// --------------------------------------------------------------------------
+// elastic subsequence distance: one warp per (series, shapelet), one lane per
+// window, the reference's sequential early-abandoning replayed per round.
+
+__device__ __forceinline__ double subseq_threshold(int metric, double min_dist, int L, int T) {
+    switch (metric) {
+        case WB_LCSS: return isinf(min_dist) ? min_dist : (double)L - min_dist * (double)L;
+        case WB_EDR: return min_dist * (double)(L > T ? L : T);
+        default: return min_dist;
+    }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kThreads)
+elastic_subseq_kernel(const SubseqElasticJob J, double *gring, int P) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * kThreads + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * kThreads) >> 5;
+    const int64_t gtid = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    const int64_t gthreads = (int64_t)gridDim.x * kThreads;
+    RingG ring{gring + gtid, gthreads};
+    const double INF = WB_INF;
+    const int64_t ntask = J.x.count * J.m;
+    for (int64_t task = warp; task < ntask; task += nwarps) {
+        const int64_t si = task / J.m;
+        const int64_t sh = task - si * J.m;
+        const int Lorig = (int)J.len[sh];
+        const int L = J.slopes ? Lorig - 2 : Lorig;  // length of the compared rows
+        if (J.slopes && Lorig < 3) {
+            // ddtw_subsequence_distance returns 0 for shapelets shorter than 3
+            if (lane == 0) {
+                J.out_dist[si * J.m + sh] = 0.0;
+                J.out_idx[si * J.m + sh] = 0;
+            }
+            continue;
+        }
+        const double *S = J.shp + J.off[sh];
+        const double *T = J.x.base + si * J.x.stride;
+        const int nwin = J.x.len - L + 1;  // = series length - shapelet length + 1
+        const int band = J.band_of_len[sh];
+        double eps = J.eps;
+        if (KIND == K_EDR && J.shp_std) {
+            const double sd = J.shp_std[sh] != 0.0 ? J.shp_std[sh] : 1.0;
+            eps = sd / 4.0;
+        }
+        double gx_sum = 0.0;
+        if (KIND == K_ERP)
+            for (int k = 0; k < L; k++) gx_sum = gx_sum + fabs(S[k] - J.g);
+        double min_dist = INF;
+        int best = 0;
+        for (int base = 0; base < nwin; base += 32) {
+            const int w = base + lane;
+            double d = INF, key = INF;
+            if (w < nwin) {
+                const double *Y = T + w;
+                double raw;
+                if constexpr (KIND == K_DTW)
+                    raw = rec_dtw<false>(ring, P, S, L, Y, L, band, nullptr, key);
+                else if constexpr (KIND == K_WDTW)
+                    raw = rec_dtw<true>(ring, P, S, L, Y, L, band, J.weights, key);
+                else if constexpr (KIND == K_ADTW)
+                    raw = rec_adtw<true>(ring, P, S, L, Y, L, band, J.p, key);
+                else if constexpr (KIND == K_ADTW_ANY)
+                    raw = rec_adtw<false>(ring, P, S, L, Y, L, band, J.p, key);
+                else if constexpr (KIND == K_LCSS)
+                    raw = rec_lcss<false>(ring, P, S, L, Y, L, band, eps, nullptr, key);
+                else if constexpr (KIND == K_EDR)
+                    raw = rec_edr(ring, P, S, L, Y, L, band, eps, key);
+                else if constexpr (KIND == K_ERP) {
+                    double gy_sum = 0.0;
+                    for (int k = 0; k < L; k++) gy_sum = gy_sum + ldg(J.gtab + si * J.t_len + w + k);
+                    raw = rec_erp(ring, P, S, L, Y, L, band, J.g, gx_sum, gy_sum,
+                                  J.gtab + si * J.t_len + w, key);
+                } else if constexpr (KIND == K_MSM)
+                    raw = rec_msm(ring, P, S, L, Y, L, band, J.c, key);
+                else
+                    raw = rec_twe<RingG, false>(ring, P, S, L, Y, L, band, J.penalty,
+                                                J.stiffness, nullptr, J.stab, key);
+                if (KIND == K_LCSS) d = 1.0 - raw / (double)L;
+                else if (KIND == K_EDR) d = raw / (double)L;
+                else d = raw;
+            }
+            // replay windows base..base+31 in order, as the reference scans them
+            for (int t = 0; t < 32; t++) {
+                const double dt = __shfl_sync(0xffffffffu, d, t);
+                const double kt = __shfl_sync(0xffffffffu, key, t);
+                if (base + t >= nwin) break;
+                const double thr = subseq_threshold(J.metric, min_dist, L, J.t_len_thr);
+                if (!(kt > thr) && dt < min_dist) {
+                    min_dist = dt;
+                    best = base + t;
+                }
+            }
+        }
+        if (lane == 0) {
+            const bool sq = KIND == K_DTW || KIND == K_WDTW || KIND == K_ADTW ||
+                            KIND == K_ADTW_ANY;
+            J.out_dist[si * J.m + sh] = sq ? sqrt(min_dist) : min_dist;
+            J.out_idx[si * J.m + sh] = best;
+        }
+    }
+}
+
+size_t elastic_subseq_ring_bytes(const SubseqElasticJob &J, int max_len, int max_band,
+                                 int *P_out, int *grid_out) {
+    const DeviceInfo &dev = device_info();
+    int P = imax(2, ring_len(max_len, max_len, max_band));
+    int64_t warps = J.x.count * J.m;
+    int64_t grid = (warps * 32 + kThreads - 1) / kThreads;
+    int64_t cap = (int64_t)4 * dev.sm_count;
+    if (grid > cap) grid = cap;
+    if (grid < 1) grid = 1;
+    *P_out = P;
+    *grid_out = (int)grid;
+    return align256((size_t)P * grid * kThreads * sizeof(double));
+}
+
+int launch_elastic_subseq(const SubseqElasticJob &J, int kind, double *gring, int P, int grid,
+                          cudaStream_t s) {
+    if (J.x.count == 0 || J.m == 0) return WB_OK;
+    timer_begin("elastic_subseq_kernel", s);
+    switch (kind) {
+#define WB_SUB_CASE(K)                                                           \
+    case K:                                                                      \
+        elastic_subseq_kernel<K><<<grid, kThreads, 0, s>>>(J, gring, P);         \
+        break;
+        WB_SUB_CASE(K_DTW)
+        WB_SUB_CASE(K_WDTW)
+        WB_SUB_CASE(K_ADTW)
+        WB_SUB_CASE(K_ADTW_ANY)
+        WB_SUB_CASE(K_LCSS)
+        WB_SUB_CASE(K_EDR)
+        WB_SUB_CASE(K_ERP)
+        WB_SUB_CASE(K_MSM)
+        WB_SUB_CASE(K_TWE)
+#undef WB_SUB_CASE
+        default:
+            return fail(WB_EINVAL, "unsupported elastic subsequence kernel");
+    }
+    timer_end(s);
+    WB_LAUNCH_CHECK("elastic_subseq_kernel");
+    return WB_OK;
+}
+
+// slopes of packed shapelets, in place of each shapelet's first len-2 slots
+__global__ void shapelet_slopes_kernel(const double *shp, const int64_t *off,
+                                       const int64_t *len, int64_t m, double *out) {
+    for (int64_t s = blockIdx.x; s < m; s += gridDim.x) {
+        const double *q = shp + off[s];
+        double *d = out + off[s];
+        const int L = (int)len[s];
+        for (int i = 1 + threadIdx.x; i < L - 1; i += blockDim.x) {
+            double a = q[i] - q[i - 1];
+            double b = (q[i + 1] - q[i - 1]) * 0.5;
+            d[i - 1] = (a + b) * 0.5;
+        }
+    }
+}
+
+int launch_shapelet_slopes(const double *shp, const int64_t *off, const int64_t *len,
+                           int64_t m, double *out, cudaStream_t s) {
+    if (m == 0) return WB_OK;
+    int grid = (int)(m < 65535 ? m : 65535);
+    shapelet_slopes_kernel<<<grid, 64, 0, s>>>(shp, off, len, m, out);
+    WB_LAUNCH_CHECK("shapelet_slopes_kernel");
+    return WB_OK;
 }
 
 int launch_elastic_external_ring(const ElasticJob &J, double *ring, size_t ring_bytes,

@@ -468,7 +468,8 @@ def pairwise_subsequence_distance(y, x, *, dim=0, metric="euclidean", metric_par
     metric = Metric_(**metric_params)
     if not (0 <= dim < X.shape[1]):
         raise ValueError("The parameter dim must be 0 <= dim < n_dims")
-    packed, offs, lens, means, stds = _pack_shapelets(y, metric.scaled)
+    packed, offs, lens, means, stds = _pack_shapelets(
+        y, metric.scaled or getattr(metric, "needs_std", False))
     dev = _device_of(X)
     m = len(y)
     if dev is not None:
@@ -484,10 +485,11 @@ def pairwise_subsequence_distance(y, x, *, dim=0, metric="euclidean", metric_par
     dist = _empty(dev, (X.shape[0], m))
     idx = _empty(dev, (X.shape[0], m), dtype=np.int64)
     sx = X.series()
+    p = metric.params() if hasattr(metric, "params") else _lib.Params()
     st = _lib.lib().wb_pairwise_subsequence_distance(
         _lib.ptr(packed), _lib.ptr(offs), _lib.ptr(lens), _lib.ptr(means), _lib.ptr(stds),
-        m, ctypes.byref(sx), dim, metric.metric_id, _lib.ptr(dist), _lib.ptr(idx),
-        1 if dev else 0, _stream(X))
+        m, ctypes.byref(sx), dim, metric.metric_id, ctypes.byref(p), _lib.ptr(dist),
+        _lib.ptr(idx), 1 if dev else 0, _stream(X))
     _lib.check(st)
     if dev is None:
         idx = idx.astype(np.intp, copy=False)

@@ -302,6 +302,158 @@ class ScaledEuclideanSubsequenceMetric(SubsequenceMetric):
     scaled = True
 
 
+class _ElasticSubsequence(SubsequenceMetric):
+    """Base of the elastic subsequence metrics (distance/_elastic.pyx:2206-3124)."""
+
+    scaled = False
+
+    def __reduce__(self):
+        return self.__class__, tuple(getattr(self, a) for a in self._args)
+
+    def __eq__(self, other):
+        return type(self) is type(other) and all(
+            _same(getattr(self, a), getattr(other, a)) for a in self._args)
+
+    def __hash__(self):
+        return hash((type(self).__name__,) + tuple(getattr(self, a) for a in self._args))
+
+    params = Metric.params
+
+
+class DtwSubsequenceMetric(_ElasticSubsequence):
+    """DtwSubsequenceMetric, distance/_elastic.pyx:2206-2290."""
+
+    metric_id = 1
+    _args = ("r",)
+
+    def __init__(self, r=1.0):
+        r = _double(r, "r")
+        check_scalar(r, "r", float, min_val=0.0, max_val=1.0)
+        self.r = r
+
+
+class AmercingDtwSubsequenceMetric(DtwSubsequenceMetric):
+    """AmercingDtwSubsequenceMetric, distance/_elastic.pyx:2293-2351 (p unchecked)."""
+
+    metric_id = 5
+    _args = ("r", "p")
+
+    def __init__(self, r=1.0, p=1.0):
+        super().__init__(r=r)
+        self.p = _double(p, "p")
+
+
+class WeightedDtwSubsequenceMetric(DtwSubsequenceMetric):
+    """WeightedDtwSubsequenceMetric, distance/_elastic.pyx:2354-2440."""
+
+    metric_id = 2
+    _args = ("r", "g")
+
+    def __init__(self, r=1.0, g=0.05):
+        super().__init__(r=r)
+        check_scalar(g, "g", float, min_val=0.0)
+        self.g = float(g)
+
+
+class DerivativeDtwSubsequenceMetric(DtwSubsequenceMetric):
+    """DerivativeDtwSubsequenceMetric, distance/_elastic.pyx:2443-2519."""
+
+    metric_id = 3
+
+
+class WeightedDerivativeDtwSubsequenceMetric(DerivativeDtwSubsequenceMetric):
+    """WeightedDerivativeDtwSubsequenceMetric, distance/_elastic.pyx:2522-2613."""
+
+    metric_id = 4
+    _args = ("r", "g")
+
+    def __init__(self, r=1.0, g=0.05):
+        super().__init__(r=r)
+        check_scalar(g, "g", float, min_val=0.0)
+        self.g = float(g)
+
+
+class LcssSubsequenceMetric(_ElasticSubsequence):
+    """LcssSubsequenceMetric, distance/_elastic.pyx:2616-2705."""
+
+    metric_id = 6
+    _args = ("r", "epsilon")
+
+    def __init__(self, r=1.0, epsilon=1.0):
+        r = _double(r, "r")
+        epsilon = _double(epsilon, "epsilon")
+        check_scalar(r, "r", float, min_val=0.0, max_val=1.0)
+        check_scalar(epsilon, "epsilon", float, min_val=0, include_boundaries="neither")
+        self.r = r
+        self.epsilon = epsilon
+
+
+class EdrSubsequenceMetric(_ElasticSubsequence):
+    """EdrSubsequenceMetric, distance/_elastic.pyx:2708-2812 (epsilon=NaN: std/4)."""
+
+    metric_id = 8
+    _args = ("r", "epsilon")
+    needs_std = True
+
+    def __init__(self, r=1.0, epsilon=math.nan):
+        r = _double(r, "r")
+        epsilon = _double(epsilon, "epsilon")
+        check_scalar(r, "r", float, min_val=0.0, max_val=1.0)
+        if not math.isnan(epsilon):
+            check_scalar(epsilon, "epsilon", float, min_val=0, include_boundaries="neither")
+        self.r = r
+        self.epsilon = epsilon
+
+
+class TweSubsequenceMetric(_ElasticSubsequence):
+    """TweSubsequenceMetric, distance/_elastic.pyx:2815-2911."""
+
+    metric_id = 11
+    _args = ("r", "penalty", "stiffness")
+
+    def __init__(self, r=1.0, penalty=1.0, stiffness=0.001):
+        r = _double(r, "r")
+        penalty = _double(penalty, "penalty")
+        stiffness = _double(stiffness, "stiffness")
+        check_scalar(r, "r", float, min_val=0.0, max_val=1.0)
+        check_scalar(penalty, "penalty", float, min_val=0.0)
+        check_scalar(stiffness, "stiffness", float, min_val=0.0,
+                     include_boundaries="neither")
+        self.r = r
+        self.penalty = penalty
+        self.stiffness = stiffness
+
+
+class MsmSubsequenceMetric(_ElasticSubsequence):
+    """MsmSubsequenceMetric, distance/_elastic.pyx:2914-3010."""
+
+    metric_id = 10
+    _args = ("r", "c")
+
+    def __init__(self, r=1.0, c=1.0):
+        r = _double(r, "r")
+        c = _double(c, "c")
+        check_scalar(r, "r", float, min_val=0.0, max_val=1.0)
+        check_scalar(c, "c", float, min_val=0)
+        self.r = r
+        self.c = c
+
+
+class ErpSubsequenceMetric(_ElasticSubsequence):
+    """ErpSubsequenceMetric, distance/_elastic.pyx:3013-3124."""
+
+    metric_id = 9
+    _args = ("r", "g")
+
+    def __init__(self, r=1.0, g=0.0):
+        r = _double(r, "r")
+        g = _double(g, "g")
+        check_scalar(r, "r", float, min_val=0.0, max_val=1.0)
+        check_scalar(g, "g", float, min_val=0)
+        self.r = r
+        self.g = g
+
+
 # distance/_distance.py:186-205 (the metrics this implementation provides)
 _METRICS = {
     "euclidean": EuclideanMetric,
@@ -322,4 +474,14 @@ _METRICS = {
 _SUBSEQUENCE_METRICS = {
     "euclidean": EuclideanSubsequenceMetric,
     "scaled_euclidean": ScaledEuclideanSubsequenceMetric,
+    "dtw": DtwSubsequenceMetric,
+    "wdtw": WeightedDtwSubsequenceMetric,
+    "ddtw": DerivativeDtwSubsequenceMetric,
+    "wddtw": WeightedDerivativeDtwSubsequenceMetric,
+    "adtw": AmercingDtwSubsequenceMetric,
+    "lcss": LcssSubsequenceMetric,
+    "edr": EdrSubsequenceMetric,
+    "twe": TweSubsequenceMetric,
+    "msm": MsmSubsequenceMetric,
+    "erp": ErpSubsequenceMetric,
 }
