@@ -377,6 +377,46 @@ def bench_subsequence(args, dev, flush):
             "algorithmic_window_elements": elems, **res}
 
 
+def bench_euclid_tc(args, dev, flush):
+    """Full-series euclidean 8192 x 8192 at length 1024: tensor-core 3xTF32
+    GEMM form against the FP64 drop-in kernel on the same device data."""
+    import torch
+
+    from wildboar_gb300.distance import pairwise_distance
+    from wildboar_gb300.distance.precision import pairwise_euclidean_tc
+
+    n, L = args.c3_full, 1024
+    rng = np.random.default_rng(9)
+    X = np.cumsum(rng.standard_normal((n, L)), axis=1)
+    Y = np.cumsum(rng.standard_normal((n, L)), axis=1)
+    Xd = torch.as_tensor(X, device=dev)
+    Yd = torch.as_tensor(Y, device=dev)
+    pairwise_euclidean_tc(Xd, Yd)
+    torch.cuda.synchronize()
+    ms_tc = _timed(lambda: pairwise_euclidean_tc(Xd, Yd), max(1, args.steps), flush)
+    D = pairwise_euclidean_tc(Xd, Yd)
+    # FP64 drop-in on the same data (sequential per-pair sums, the reference's order)
+    ms_64 = _timed(lambda: pairwise_distance(Xd, Yd, metric="euclidean"), 1, flush)
+    D64 = pairwise_distance(Xd, Yd, metric="euclidean")
+    err = (D - D64).abs().max().item()
+    rel = ((D - D64).abs() / D64.clamp(min=1e-300)).max().item()
+    nx = (Xd * Xd).sum(1, keepdim=True)
+    ny = (Yd * Yd).sum(1, keepdim=True).t()
+    norm_err = ((D * D - D64 * D64).abs() / (nx + ny)).max().item()
+    flops = 2.0 * n * n * L
+    return {
+        "config": f"{n} x {n} series, L={L}, float64 in, float64 out",
+        "tc_ms": ms_tc,
+        "tc_tflops_useful": flops / (ms_tc * 1e-3) / 1e12,
+        "tc_tflops_issued_3xtf32": 3 * flops / (ms_tc * 1e-3) / 1e12,
+        "fp64_dropin_ms": ms_64,
+        "speedup_vs_fp64_dropin": ms_64 / ms_tc,
+        "max_abs_err_vs_fp64": err,
+        "max_rel_err_vs_fp64": rel,
+        "max_d2_err_over_norms": norm_err,
+    }
+
+
 def run_gpu(args):
     import torch
 
@@ -408,6 +448,8 @@ def run_gpu(args):
             forms["fwd_bwd_fp32"] = bench_fwd_bwd(args, dev, flush)
         if args.only in ("", "subseq"):
             forms["subsequence"] = bench_subsequence(args, dev, flush)
+        if args.only in ("", "euclid"):
+            forms["euclidean_full_tc"] = bench_euclid_tc(args, dev, flush)
         if rank == 0:
             print(json.dumps({"forms": forms}), flush=True)
         return
@@ -507,6 +549,7 @@ def run_gpu(args):
         forms["batched_fp32"] = bench_batched(args, dev, flush)
         forms["fwd_bwd_fp32"] = bench_fwd_bwd(args, dev, flush)
         forms["subsequence"] = bench_subsequence(args, dev, flush)
+        forms["euclidean_full_tc"] = bench_euclid_tc(args, dev, flush)
         forms["both_beat_fp64_drop_in"] = bool(
             forms["batched_fp32"]["gcups"] > value and forms["fwd_bwd_fp32"]["gcups"] > value)
     line = {
@@ -558,10 +601,11 @@ def main():
                     help="strip,block for the batched form instead of the autotuner")
     ap.add_argument("--skip-fp64", action="store_true",
                     help="only the FP32 forms (profiling captures)")
-    ap.add_argument("--only", default="", choices=["", "batched", "fwdbwd", "subseq"],
+    ap.add_argument("--only", default="", choices=["", "batched", "fwdbwd", "subseq", "euclid"],
                     help="with --skip-fp64: run one form only")
     ap.add_argument("--c3-series", type=int, default=1000)
     ap.add_argument("--c3-shapelets", type=int, default=10000)
+    ap.add_argument("--c3-full", type=int, default=8192)
     args = ap.parse_args()
     if (args.nx, args.ny) != (WORKLOAD["nx"], WORKLOAD["ny"]):
         WORKLOAD["nx"], WORKLOAD["ny"] = args.nx, args.ny

@@ -174,6 +174,16 @@ int wb_dtw32_distance(const wb_dtw32 *job, double *out, double *out_cost, void *
 int wb_dtw32_backward(const wb_dtw32 *job, const double *grad_out, float *grad_x,
                       int64_t gx_stride, float *grad_y, int64_t gy_stride, void *stream);
 
+/* Full-series euclidean distance matrix on the tensor cores (precision form,
+ * no counterpart in the reference, whose EuclideanMetric sums in FP64 on the
+ * CPU, distance/_metric.pyx:381-409): out[i, j] = sqrt(|x_i|^2 + |y_j|^2 -
+ * 2 x_i . y_j) with the dot products from a tcgen05 kind::tf32 GEMM over the
+ * 3xTF32 split of the float32-rounded series (FP32 accumulation), norms and
+ * the combination in FP64.  x, y: device float64 series of equal length;
+ * out (x.n, y.n) float64 on the device or host. */
+int wb_euclidean_tc(const wb_series *x, const wb_series *y, int64_t dim, double *out,
+                    int32_t out_on_device, void *stream);
+
 /* valid length of each float32 series: index of its first NaN (padding or
  * end-of-series marker, utils/variable_len.py:66-115), else L */
 int wb_series_lengths_f32(const float *x, int64_t n_series, int64_t stride, int32_t L,

@@ -1,0 +1,413 @@
+// euclid_gemm.cu -- full-series euclidean distance matrix on the tensor cores.
+//
+// d(x_i, y_j)^2 = |x_i|^2 + |y_j|^2 - 2 x_i . y_j.  The dot products come
+// from a tcgen05 GEMM of kind::tf32 with the 3xTF32 split: every float32 value
+// v = hi + lo with hi = tf32(v) and lo = v - hi, and
+// x . y ~ hi_x.hi_y + hi_x.lo_y + lo_x.hi_y (the lo.lo term is below FP32
+// resolution), accumulated in FP32 in tensor memory.  Norms and the final
+// combination are FP64; the inputs of the euclidean metric are float64 and
+// are rounded once to float32.
+//
+// Kernel: one CTA per 128 x 128 output tile, 128 threads.  Thread 0 issues
+// the TMA loads (128-byte swizzled K-major tiles of 32 floats) into a
+// 3-stage ring and the MMAs (M=128, N=128, K=8, 12 per stage); tcgen05.commit
+// frees a stage; the accumulator (128 lanes x 128 columns of TMEM) is read
+// back by the four warps with tcgen05.ld.  Every mbarrier wait is bounded: a
+// wait that runs out sets an error flag, the CTA still releases its TMEM.
+
+#include <cuda.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace wb {
+
+constexpr int kBM = 128, kBN = 128, kBK = 32;  // kBK floats = 128 bytes (one swizzle row)
+constexpr int kStages = 3;
+constexpr int kTileBytes = kBM * kBK * 4;      // 16 KB per operand tile
+constexpr int kStageBytes = 4 * kTileBytes;    // A hi, A lo, B hi, B lo
+constexpr int kGemmThreads = 128;
+// four accumulators of 128 columns: consecutive quarters of K accumulate
+// separately in FP32 and are added in FP64 by the epilogue, which cuts the
+// accumulation error of long K by ~4x
+constexpr int kNumAcc = 4;
+constexpr int kTmemCols = kBN * kNumAcc;
+constexpr long long kWaitLimit = 1ll << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// bounded wait on the phase `parity` of an mbarrier; false when it gave up
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (long long i = 0; i < kWaitLimit; i++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int c0,
+                                            int c1, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+        : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (SBO), descriptor version 1
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFF) >> 4);
+    d |= (uint64_t)1 << 16;             // leading byte offset (unused for SW128 K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+    d |= (uint64_t)1 << 46;             // version
+    d |= (uint64_t)2 << 61;             // layout: SWIZZLE_128B
+    return d;
+}
+
+// instruction descriptor: D = F32, A = B = TF32, both K-major, N = 128, M = 128
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kBN >> 3) << 17) |
+                            ((uint32_t)(kBM >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            bar)
+        : "memory");
+}
+
+__global__ void __launch_bounds__(kGemmThreads, 1)
+euclid_tc_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
+                 const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
+                 const double *__restrict__ nx, const double *__restrict__ ny, int M, int N,
+                 int Kp, double *out, int64_t ld_out, int *err) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte aligned stage ring
+    unsigned char *smem =
+        (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    __shared__ __align__(8) uint64_t full_bar[kStages];
+    __shared__ __align__(8) uint64_t empty_bar[kStages];
+    __shared__ __align__(8) uint64_t done_bar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int abort_flag;
+
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5;
+    const int m0 = blockIdx.y * kBM;
+    const int n0 = blockIdx.x * kBN;
+    const int KT = Kp / kBK;
+
+    if (tid == 0) {
+        for (int s = 0; s < kStages; s++) {
+            mbar_init(smem_u32(&full_bar[s]), 1);
+            mbar_init(smem_u32(&empty_bar[s]), 1);
+        }
+        mbar_init(smem_u32(&done_bar), 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&tmem_slot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+
+    if (tid == 0) {
+        auto stage_ptr = [&](int s, int which) { return smem + s * kStageBytes + which * kTileBytes; };
+        auto issue_loads = [&](int kt, int s) {
+            const uint32_t bar = smem_u32(&full_bar[s]);
+            mbar_expect_tx(bar, kStageBytes);
+            const int kc = kt * kBK;
+            tma_load_2d(smem_u32(stage_ptr(s, 0)), &mAhi, kc, m0, bar);
+            tma_load_2d(smem_u32(stage_ptr(s, 1)), &mAlo, kc, m0, bar);
+            tma_load_2d(smem_u32(stage_ptr(s, 2)), &mBhi, kc, n0, bar);
+            tma_load_2d(smem_u32(stage_ptr(s, 3)), &mBlo, kc, n0, bar);
+        };
+        uint32_t full_phase = 0, empty_phase = 0;  // one parity bit per stage
+        const int pre = KT < kStages ? KT : kStages;
+        const int per_acc = (KT + kNumAcc - 1) / kNumAcc;  // k tiles per accumulator
+        for (int kt = 0; kt < pre; kt++) issue_loads(kt, kt);
+        bool ok = true;
+        for (int kt = 0; kt < KT && ok; kt++) {
+            const int s = kt % kStages;
+            ok = mbar_wait(smem_u32(&full_bar[s]), (full_phase >> s) & 1u);
+            full_phase ^= 1u << s;
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t ahi = smem_u32(stage_ptr(s, 0)), alo = smem_u32(stage_ptr(s, 1));
+            const uint32_t bhi = smem_u32(stage_ptr(s, 2)), blo = smem_u32(stage_ptr(s, 3));
+            const int acc = kt / per_acc;
+            const uint32_t dtm = tmem + (uint32_t)(acc * kBN);
+            const bool first = (kt % per_acc) == 0;
+#pragma unroll
+            for (int kk = 0; kk < kBK / 8; kk++) {
+                const uint32_t off = kk * 32;  // 8 tf32 = 32 bytes along K
+                const uint64_t dAh = smem_desc_sw128(ahi + off), dAl = smem_desc_sw128(alo + off);
+                const uint64_t dBh = smem_desc_sw128(bhi + off), dBl = smem_desc_sw128(blo + off);
+                mma_tf32(dtm, dAh, dBh, (!first || kk > 0) ? 1u : 0u);
+                mma_tf32(dtm, dAh, dBl, 1u);
+                mma_tf32(dtm, dAl, dBh, 1u);
+            }
+            mma_commit(smem_u32(&empty_bar[s]));
+            // refill the stage used one iteration ago once its MMAs are done
+            if (kt >= 1) {
+                const int sp = (kt - 1) % kStages;
+                const int knext = kt - 1 + kStages;
+                if (knext < KT) {
+                    ok = mbar_wait(smem_u32(&empty_bar[sp]), (empty_phase >> sp) & 1u);
+                    empty_phase ^= 1u << sp;
+                    if (ok) issue_loads(knext, sp);
+                }
+            }
+        }
+        if (!ok) {
+            abort_flag = 1;
+            atomicExch(err, 1);
+        }
+        // tracks every MMA issued so far, also after an abort, so that no MMA
+        // is in flight when the TMEM is released
+        mma_commit(smem_u32(&done_bar));
+    }
+    __syncthreads();
+    bool ok = mbar_wait(smem_u32(&done_bar), 0);
+    if (abort_flag) ok = false;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+        const int row = warp * 32 + (tid & 31);  // TMEM lane = accumulator row
+        const int gi = m0 + row;
+        const double nxi = gi < M ? nx[gi] : 0.0;
+        const int KTn = Kp / kBK;
+        const int used = (KTn + ((KTn + kNumAcc - 1) / kNumAcc) - 1) / ((KTn + kNumAcc - 1) / kNumAcc);
+#pragma unroll 1
+        for (int c0 = 0; c0 < kBN; c0 += 32) {
+          double dot[32];
+#pragma unroll
+          for (int j = 0; j < 32; j++) dot[j] = 0.0;
+#pragma unroll 1
+          for (int a = 0; a < used; a++) {
+            uint32_t v[32];
+            const uint32_t taddr =
+                tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * kBN + c0);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                  "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+                  "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]),
+                  "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+                  "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+                  "=r"(v[30]), "=r"(v[31])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int j = 0; j < 32; j++) dot[j] += (double)__uint_as_float(v[j]);
+          }
+          if (gi < M) {
+              double *o = out + (int64_t)gi * ld_out;
+#pragma unroll
+              for (int j = 0; j < 32; j++) {
+                  const int gj = n0 + c0 + j;
+                  if (gj < N) {
+                      const double d2 = (nxi + ny[gj]) - 2.0 * dot[j];
+                      o[gj] = sqrt(d2 > 0.0 ? d2 : 0.0);
+                  }
+              }
+          }
+        }
+    } else if (tid == 0) {
+        atomicExch(err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(kTmemCols)
+                     : "memory");
+    }
+}
+
+// float64 rows -> float32 hi/lo tf32 split (zero padded to (rows_p, Kp)) and
+// FP64 squared norms of the float32-rounded rows
+__global__ void tf32_split_kernel(const double *__restrict__ x, int64_t stride, int rows, int K,
+                                  int rows_p, int Kp, float *hi, float *lo, double *norm) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = warp; r < rows_p; r += nwarps) {
+        double acc = 0.0;
+        for (int k = lane; k < Kp; k += 32) {
+            float v = 0.0f;
+            if (r < rows && k < K) v = (float)x[r * stride + k];
+            uint32_t hb;
+            asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hb) : "f"(v));
+            const float h = __uint_as_float(hb);
+            const float l = v - h;
+            hi[r * (int64_t)Kp + k] = h;
+            lo[r * (int64_t)Kp + k] = l;
+            acc += (double)v * (double)v;
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0 && r < rows) norm[r] = acc;
+    }
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+static int make_map(CUtensorMap *map, float *base, int rows_p, int Kp) {
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return fail(WB_ECUDA, "cuTensorMapEncodeTiled is unavailable");
+    cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows_p};
+    cuuint64_t strides[1] = {(cuuint64_t)Kp * sizeof(float)};
+    cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kBM};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(WB_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return WB_OK;
+}
+
+static int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+// x: (M, K) float64 rows with row stride sx; y: (N, K); out (M, N) float64
+int euclid_tc(const double *x, int64_t sx, int M, const double *y, int64_t sy, int N, int K,
+              double *out, int64_t ld_out, Workspace &ws, bool reserve_only, size_t *bytes) {
+    const int Mp = round_up(std::max(M, 1), kBM), Np = round_up(std::max(N, 1), kBN);
+    const int Kp = round_up(std::max(K, 1), kBK);
+    const size_t need = 2 * align256((size_t)Mp * Kp * 4) + 2 * align256((size_t)Np * Kp * 4) +
+                        align256((size_t)M * 8) + align256((size_t)N * 8) + 256;
+    if (reserve_only) {
+        *bytes = need;
+        return WB_OK;
+    }
+    cudaStream_t s = ws.stream();
+    WB_TAKE(ahi, float, ws, (size_t)Mp * Kp);
+    WB_TAKE(alo, float, ws, (size_t)Mp * Kp);
+    WB_TAKE(bhi, float, ws, (size_t)Np * Kp);
+    WB_TAKE(blo, float, ws, (size_t)Np * Kp);
+    WB_TAKE(nxv, double, ws, M);
+    WB_TAKE(nyv, double, ws, N);
+    WB_TAKE(err, int, ws, 1);
+    WB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+    const int sgrid = std::min<int64_t>((int64_t)device_info().sm_count * 8, (Mp + 7) / 8 + 1);
+    tf32_split_kernel<<<sgrid, 256, 0, s>>>(x, sx, M, K, Mp, Kp, ahi, alo, nxv);
+    WB_LAUNCH_CHECK("tf32_split_kernel");
+    tf32_split_kernel<<<sgrid, 256, 0, s>>>(y, sy, N, K, Np, Kp, bhi, blo, nyv);
+    WB_LAUNCH_CHECK("tf32_split_kernel");
+    CUtensorMap mAh, mAl, mBh, mBl;
+    WB_TRY(make_map(&mAh, ahi, Mp, Kp));
+    WB_TRY(make_map(&mAl, alo, Mp, Kp));
+    WB_TRY(make_map(&mBh, bhi, Np, Kp));
+    WB_TRY(make_map(&mBl, blo, Np, Kp));
+    const int smem = kStages * kStageBytes + 1024;
+    WB_CUDA(cudaFuncSetAttribute(euclid_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem));
+    dim3 grid(Np / kBN, Mp / kBM);
+    timer_begin("euclid_tc_kernel", s);
+    euclid_tc_kernel<<<grid, kGemmThreads, smem, s>>>(mAh, mAl, mBh, mBl, nxv, nyv, M, N, Kp,
+                                                      out, ld_out, err);
+    timer_end(s);
+    WB_LAUNCH_CHECK("euclid_tc_kernel");
+    int herr = 0;
+    WB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    WB_CUDA(cudaStreamSynchronize(s));
+    if (herr) return fail(WB_ETIMEOUT, "euclid_tc_kernel: a pipeline wait gave up");
+    return WB_OK;
+}
+
+}  // namespace wb
+
+using namespace wb;
+
+extern "C" int wb_euclidean_tc(const wb_series *x, const wb_series *y, int64_t dim, double *out,
+                               int32_t out_on_device, void *stream_) {
+    if (!x || !y) return fail(WB_EINVAL, "x and y are required");
+    if (x->dtype != WB_F64 || y->dtype != WB_F64) return fail(WB_EINVAL, "float64 series expected");
+    if (!x->on_device || !y->on_device)
+        return fail(WB_EINVAL, "the tensor-core euclidean path takes device series");
+    if (x->n_timestep != y->n_timestep)
+        return fail(WB_EINVAL, "Illegal n_timestep for non-elastic distance measure");
+    if (dim < 0 || dim >= x->n_dims || y->n_dims != x->n_dims)
+        return fail(WB_EINVAL, "The parameter dim must be 0 <= dim < n_dims");
+    if (x->n > (1 << 30) || y->n > (1 << 30) || x->n_timestep > (1 << 28))
+        return fail(WB_EINVAL, "problem too large");
+    if (x->n == 0 || y->n == 0) return WB_OK;
+    if (!out) return fail(WB_EINVAL, "out is NULL");
+    cudaStream_t s = (cudaStream_t)stream_;
+    const int M = (int)x->n, N = (int)y->n, K = (int)x->n_timestep;
+    Workspace ws(s);
+    size_t need = 0;
+    euclid_tc(nullptr, 0, M, nullptr, 0, N, K, nullptr, 0, ws, true, &need);
+    size_t out_bytes = out_on_device ? 0 : align256((size_t)M * N * 8);
+    WB_TRY(ws.reserve(need + out_bytes));
+    double *dout = out;
+    if (!out_on_device) {
+        dout = ws.take<double>((size_t)M * N);
+        if (!dout) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    }
+    const double *xb = static_cast<const double *>(x->data) + dim * x->n_timestep;
+    const double *yb = static_cast<const double *>(y->data) + dim * y->n_timestep;
+    WB_TRY(euclid_tc(xb, x->n_dims * x->n_timestep, M, yb, y->n_dims * y->n_timestep, N, K,
+                     dout, N, ws, false, nullptr));
+    if (!out_on_device) {
+        WB_CUDA(cudaMemcpyAsync(out, dout, (size_t)M * N * 8, cudaMemcpyDeviceToHost, s));
+        WB_CUDA(cudaStreamSynchronize(s));
+    }
+    return WB_OK;
+}
