@@ -417,6 +417,67 @@ def bench_euclid_tc(args, dev, flush):
     }
 
 
+def _cells_w(n, m, w):
+    mx = max(0, m - n) + w
+    mn = max(0, n - m)
+    return sum(min(m, i + mx) - max(0, i - mn - w + 1) for i in range(n))
+
+
+def bench_precision(args, dev, flush):
+    """Every elastic metric on n x n univariate random walks of length 512:
+    the FP64 drop-in against the FP32-compensated form on the same device
+    data; error of the FP32 form against the FP64 drop-in over the whole
+    matrix and against the CPU oracle on a 16 x 16 corner."""
+    import torch
+
+    from oracle import oracle as O
+    from wildboar_gb300.distance import pairwise_distance
+    from wildboar_gb300.distance._band import compute_r
+    from wildboar_gb300.distance.precision import pairwise_distance_fp32
+
+    n, L = args.c2_series, 512
+    rng = np.random.default_rng(12)
+    X = np.cumsum(rng.standard_normal((n, L)), axis=1)
+    Y = np.cumsum(rng.standard_normal((n, L)), axis=1)
+    eps = 0.1 * float(np.concatenate([X, Y]).std())
+    Xd = torch.as_tensor(X, device=dev)
+    Yd = torch.as_tensor(Y, device=dev)
+    sweep = [("dtw", {"r": 0.1}), ("dtw", {"r": 1.0}), ("wdtw", {"g": 0.05}), ("ddtw", {}),
+             ("adtw", {}), ("lcss", {"epsilon": eps}), ("edr", {"epsilon": eps}),
+             ("erp", {"g": 0.0}), ("msm", {"c": 1.0}),
+             ("twe", {"stiffness": 0.001, "penalty": 1.0})]
+    out = []
+    for metric, params in sweep:
+        r = params.get("r", 1.0)
+        w = compute_r(L, r)
+        lc = L - 2 if metric == "ddtw" else L
+        cells = n * n * _cells_w(lc, lc, w)
+        res = {"metric": metric, "params": params}
+        for tag, fn in (("fp64", pairwise_distance), ("fp32", pairwise_distance_fp32)):
+            fn(Xd[:64], Yd[:64], metric=metric, metric_params=params)
+            torch.cuda.synchronize()
+            ms = _timed(lambda: fn(Xd, Yd, metric=metric, metric_params=params), 1, flush)
+            res[tag + "_ms"] = ms
+            res[tag + "_gcups"] = cells / (ms * 1e-3) / 1e9
+        D64 = pairwise_distance(Xd, Yd, metric=metric, metric_params=params)
+        D32 = pairwise_distance_fp32(Xd, Yd, metric=metric, metric_params=params)
+        diff = (D32 - D64).abs()
+        rel = diff / D64.abs().clamp(min=1e-300)
+        res["max_abs_err_vs_fp64"] = diff.max().item()
+        res["max_rel_err_vs_fp64"] = rel[D64 != 0].max().item() if bool((D64 != 0).any()) else 0.0
+        res["frac_entries_differing"] = (diff > 0).double().mean().item()
+        ref = O.pairwise(X[:16, None, :], Y[:16, None, :], dim=0, metric=metric,
+                         metric_params=params)
+        corner = D32[:16, :16].cpu().numpy()
+        res["max_rel_err_vs_oracle_16x16"] = float(
+            np.max(np.abs(corner - ref) / np.maximum(np.abs(ref), 1e-300)))
+        res["speedup"] = res["fp64_ms"] / res["fp32_ms"]
+        out.append(res)
+    return {"config": f"{n} x {n} univariate random walks, L={L}, float64 in/out; "
+                      f"lcss/edr epsilon = 0.1 std = {eps:.6g}",
+            "cells": "evaluated band cells (ddtw on the L-2 slopes)", "metrics": out}
+
+
 def run_gpu(args):
     import torch
 
@@ -450,6 +511,8 @@ def run_gpu(args):
             forms["subsequence"] = bench_subsequence(args, dev, flush)
         if args.only in ("", "euclid"):
             forms["euclidean_full_tc"] = bench_euclid_tc(args, dev, flush)
+        if args.only in ("", "precision"):
+            forms["precision_sweep"] = bench_precision(args, dev, flush)
         if rank == 0:
             print(json.dumps({"forms": forms}), flush=True)
         return
@@ -550,6 +613,7 @@ def run_gpu(args):
         forms["fwd_bwd_fp32"] = bench_fwd_bwd(args, dev, flush)
         forms["subsequence"] = bench_subsequence(args, dev, flush)
         forms["euclidean_full_tc"] = bench_euclid_tc(args, dev, flush)
+        forms["precision_sweep"] = bench_precision(args, dev, flush)
         forms["both_beat_fp64_drop_in"] = bool(
             forms["batched_fp32"]["gcups"] > value and forms["fwd_bwd_fp32"]["gcups"] > value)
     line = {
@@ -601,11 +665,14 @@ def main():
                     help="strip,block for the batched form instead of the autotuner")
     ap.add_argument("--skip-fp64", action="store_true",
                     help="only the FP32 forms (profiling captures)")
-    ap.add_argument("--only", default="", choices=["", "batched", "fwdbwd", "subseq", "euclid"],
+    ap.add_argument("--only", default="", choices=["", "batched", "fwdbwd", "subseq", "euclid",
+                                                     "precision"],
                     help="with --skip-fp64: run one form only")
     ap.add_argument("--c3-series", type=int, default=1000)
     ap.add_argument("--c3-shapelets", type=int, default=10000)
     ap.add_argument("--c3-full", type=int, default=8192)
+    ap.add_argument("--c2-series", type=int, default=1000,
+                    help="n for the per-metric FP64 vs FP32 sweep (n x n, L=512)")
     args = ap.parse_args()
     if (args.nx, args.ny) != (WORKLOAD["nx"], WORKLOAD["ny"]):
         WORKLOAD["nx"], WORKLOAD["ny"] = args.nx, args.ny

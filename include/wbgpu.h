@@ -184,6 +184,19 @@ int wb_dtw32_backward(const wb_dtw32 *job, const double *grad_out, float *grad_x
 int wb_euclidean_tc(const wb_series *x, const wb_series *y, int64_t dim, double *out,
                     int32_t out_on_device, void *stream);
 
+/* Pairwise distance of the elastic metrics in FP32 (precision form, no
+ * counterpart in the reference, which computes in FP64: the arguments and
+ * the output are those of wb_pairwise_distance, ref distance/_distance.py:
+ * 644-748).  Series are rounded to float32; every cumulative cost is a
+ * compensated (hi, lo) float pair (TwoSum on each addition, minima on hi);
+ * the final normalisation and sqrt are FP64.  dtw, wdtw, ddtw and wddtw run
+ * on the dtw strip kernel (slopes and weights formed in FP64 first), the
+ * other elastic metrics on a thread-per-pair kernel.  euclidean is not
+ * accepted here (wb_euclidean_tc is its precision form). */
+int wb_pairwise_distance_fp32(const wb_series *x, const wb_series *y, int64_t dim,
+                              int32_t metric, const wb_params *params, double *out,
+                              int32_t out_on_device, void *stream);
+
 /* valid length of each float32 series: index of its first NaN (padding or
  * end-of-series marker, utils/variable_len.py:66-115), else L */
 int wb_series_lengths_f32(const float *x, int64_t n_series, int64_t stride, int32_t L,

@@ -14,6 +14,7 @@
 #include <numeric>
 #include <vector>
 
+#include "dtw32.cuh"
 #include "elastic.cuh"
 #include "subseq.cuh"
 
@@ -418,6 +419,125 @@ extern "C" int wb_pairwise_distance(const wb_series *x, const wb_series *y, int6
         WB_CUDA(cudaMemsetAsync(dout, 0, out_elems * sizeof(double), s));
     }
     WB_TRY(launch_elastic(J, ws, nullptr));
+    return finish_host_copy(out, dout, out_elems * sizeof(double), out_on_device, s);
+}
+
+extern "C" int wb_pairwise_distance_fp32(const wb_series *x, const wb_series *y, int64_t dim,
+                                         int32_t metric, const wb_params *params, double *out,
+                                         int32_t out_on_device, void *stream_) {
+    WB_TRY(check_series(x, "x"));
+    if (y) WB_TRY(check_series(y, "y"));
+    if (!params) return fail(WB_EINVAL, "params is NULL");
+    if (!out && x->n > 0) return fail(WB_EINVAL, "out is NULL");
+    WB_TRY(check_dim(x, dim));
+    if (y && y->n_dims != x->n_dims)
+        return fail(WB_EINVAL, "x and y must have the same number of dimensions.");
+    if (!is_elastic(metric))
+        return fail(WB_EUNSUPPORTED, "no FP32 form of metric id " + std::to_string(metric));
+    const bool same = (y == nullptr);
+    const wb_series *yy = same ? x : y;
+    cudaStream_t s = (cudaStream_t)stream_;
+    const int xl = (int)x->n_timestep, yl = (int)yy->n_timestep;
+    ElasticJob J;
+    WB_TRY(metric_fields(metric, params, xl, yl, false, J));
+    if (x->n == 0 || yy->n == 0) return WB_OK;
+    if (same && x->n > ((int64_t)1 << 31) - 1) return fail(WB_EINVAL, "too many series");
+
+    const size_t out_elems = (size_t)x->n * yy->n;
+    const bool all_zero = derivative(metric) && std::min(xl, yl) < 3;
+    const bool strips = (J.kind == K_DTW || J.kind == K_WDTW) && !all_zero;
+    const int lr = derivative(metric) && !all_zero ? xl - 2 : xl;
+    const int lc = derivative(metric) && !all_zero ? yl - 2 : yl;
+    const int64_t nw = metric == WB_WDDTW ? std::max(xl - 2, yl - 2) : std::max(xl, yl);
+    SeriesSet probeR{nullptr, 0, x->n, xl}, probeC{nullptr, 0, yy->n, yl};
+    size_t need = stage_bytes(x) + (same ? 0 : stage_bytes(yy)) +
+                  table_bytes(metric, params, probeR, probeC, x->n, yy->n, xl, yl) +
+                  (out_on_device ? 0 : align256(out_elems * 8)) +
+                  align256((size_t)std::max<int64_t>(nw, 1) * 4);
+    Dtw32Job D;
+    int strip = 16;
+    const int64_t n_items = same ? x->n * (x->n - 1) / 2 : (int64_t)out_elems;
+    if (strips) {
+        // planning reads only whether the item and weight pointers are set;
+        // the real ones are filled in below
+        static const int32_t plan_mark = 0;
+        wb_dtw32 q{};
+        q.x_len = lr;
+        q.y_len = lc;
+        q.nx = x->n;
+        q.ny = yy->n;
+        q.item_x = same ? &plan_mark : nullptr;
+        q.item_y = same ? &plan_mark : nullptr;
+        q.n_items = n_items;
+        q.r = params->r;
+        q.weights = J.kind == K_WDTW ? reinterpret_cast<const float *>(&plan_mark) : nullptr;
+        strip = lr >= 512 ? 32 : (lr >= 128 ? 16 : 8);
+        q.strip = strip;
+        size_t dbytes = 0;
+        WB_TRY(dtw32_plan(&q, false, D, dbytes));
+        need += dbytes + align256((size_t)x->n * lr * 4) + (same ? 0 : align256((size_t)yy->n * lc * 4)) +
+                align256((size_t)std::max<int64_t>(n_items, 1) * 8) +
+                (same ? 2 * align256((size_t)std::max<int64_t>(n_items, 1) * 4) : 0);
+    } else {
+        ElasticJob probe = J;
+        probe.rows = probeR;
+        probe.cols = probeC;
+        probe.mode = same ? PM_UPPER : PM_ALL;
+        need += elastic_workspace_bytes(probe);
+    }
+    Workspace ws(s);
+    WB_TRY(ws.reserve(need));
+    WB_TRY(stage(x, dim, ws, J.rows));
+    if (same) J.cols = J.rows;
+    else WB_TRY(stage(yy, dim, ws, J.cols));
+    WB_TRY(build_tables(metric, params, J, ws, same, xl, yl));
+    double *dout = out_on_device ? out : ws.take<double>(out_elems);
+    if (!dout) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    float *w32 = nullptr;
+    if (weighted(metric)) {
+        w32 = ws.take<float>((size_t)std::max<int64_t>(nw, 1));
+        if (!w32) return fail(WB_ENOMEM, "workspace reservation exceeded");
+        WB_TRY(launch_weights_f32(J.weights, (int)nw, w32, s));
+    }
+    if (strips) {
+        WB_TRY(dtw32_take(ws, D, false));
+        WB_TAKE(fr, float, ws, (size_t)x->n * lr);
+        WB_TRY(launch_to_f32(J.rows, fr, s));
+        float *fc = fr;
+        if (!same) {
+            fc = ws.take<float>((size_t)yy->n * lc);
+            if (!fc) return fail(WB_ENOMEM, "workspace reservation exceeded");
+            WB_TRY(launch_to_f32(J.cols, fc, s));
+        }
+        WB_TAKE(item_out, double, ws, (size_t)std::max<int64_t>(n_items, 1));
+        D.x = fr;
+        D.x_stride = lr;
+        D.y = fc;
+        D.y_stride = lc;
+        D.band_fixed = J.band;
+        D.weights = w32;
+        D.out = item_out;
+        D.out_cost = nullptr;
+        D.item_x = D.item_y = nullptr;
+        if (same) {
+            WB_TAKE(ix, int32_t, ws, (size_t)std::max<int64_t>(n_items, 1));
+            WB_TAKE(iy, int32_t, ws, (size_t)std::max<int64_t>(n_items, 1));
+            WB_TRY(launch_upper_items(x->n, ix, iy, s));
+            D.item_x = ix;
+            D.item_y = iy;
+        }
+        D.n_items = n_items;
+        if (n_items > 0) WB_TRY(dtw32_forward(D, strip, s));
+        WB_TRY(launch_grid_to_matrix(item_out, x->n, yy->n, same ? 1 : 0, dout, s));
+    } else {
+        J.weights32 = w32;
+        J.out = dout;
+        J.out_ld = yy->n;
+        J.mode = same ? PM_UPPER : PM_ALL;
+        if (same) WB_CUDA(cudaMemsetAsync(dout, 0, out_elems * sizeof(double), s));
+        if (all_zero) WB_TRY(launch_elastic(J, ws, nullptr));
+        else WB_TRY(launch_elastic32(J, ws));
+    }
     return finish_host_copy(out, dout, out_elems * sizeof(double), out_on_device, s);
 }
 

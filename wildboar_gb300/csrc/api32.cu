@@ -9,10 +9,10 @@
 
 namespace wb {
 
-static int prepare32(const wb_dtw32 *q, bool backward, Workspace &ws, Dtw32Job &J,
-                     size_t extra_bytes) {
+// Validate a job and fill `J` (everything but the scratch pointers); `bytes`
+// is the workspace the scratch needs.
+int dtw32_plan(const wb_dtw32 *q, bool backward, Dtw32Job &J, size_t &bytes) {
     if (!q) return fail(WB_EINVAL, "job is NULL");
-    if (!q->x || !q->y) return fail(WB_EINVAL, "x and y must be device pointers");
     if (q->x_len < 1 || q->y_len < 1) return fail(WB_EINVAL, "x_len and y_len must be >= 1");
     if (!(q->r >= 0.0 && q->r <= 1.0)) return fail(WB_EINVAL, "r must be in [0, 1]");
     if (q->n_items < 0) return fail(WB_EINVAL, "negative number of items");
@@ -68,7 +68,13 @@ static int prepare32(const wb_dtw32 *q, bool backward, Workspace &ws, Dtw32Job &
         J.dir_words = words;
         dir_bytes = align256((size_t)words * nth * sizeof(uint32_t));
     }
-    WB_TRY(ws.reserve(ring_bytes + dir_bytes + 256 + extra_bytes));
+    bytes = ring_bytes + dir_bytes + 256;
+    return WB_OK;
+}
+
+// Take the scratch of a planned job from a reserved workspace.
+int dtw32_take(Workspace &ws, Dtw32Job &J, bool backward) {
+    const int64_t nth = (int64_t)J.grid * J.block;
     J.ring = ws.take<float2>((size_t)J.ring_cols * nth);
     J.queue = ws.take<unsigned long long>(1);
     if (!J.ring || !J.queue) return fail(WB_ENOMEM, "workspace reservation exceeded");
@@ -77,6 +83,14 @@ static int prepare32(const wb_dtw32 *q, bool backward, Workspace &ws, Dtw32Job &
         if (!J.dirs) return fail(WB_ENOMEM, "workspace reservation exceeded");
     }
     return WB_OK;
+}
+
+static int prepare32(const wb_dtw32 *q, bool backward, Workspace &ws, Dtw32Job &J) {
+    if (q && (!q->x || !q->y)) return fail(WB_EINVAL, "x and y must be device pointers");
+    size_t bytes = 0;
+    WB_TRY(dtw32_plan(q, backward, J, bytes));
+    WB_TRY(ws.reserve(bytes));
+    return dtw32_take(ws, J, backward);
 }
 
 }  // namespace wb
@@ -89,7 +103,7 @@ extern "C" int wb_dtw32_distance(const wb_dtw32 *q, double *out, double *out_cos
     cudaStream_t s = (cudaStream_t)stream_;
     Workspace ws(s);
     Dtw32Job J;
-    WB_TRY(prepare32(q, false, ws, J, 0));
+    WB_TRY(prepare32(q, false, ws, J));
     J.out = out;
     J.out_cost = out_cost;
     return dtw32_forward(J, q->strip ? q->strip : 16, s);
@@ -98,13 +112,14 @@ extern "C" int wb_dtw32_distance(const wb_dtw32 *q, double *out, double *out_cos
 extern "C" int wb_dtw32_backward(const wb_dtw32 *q, const double *grad_out, float *grad_x,
                                  int64_t gx_stride, float *grad_y, int64_t gy_stride,
                                  void *stream_) {
+    if (!q) return fail(WB_EINVAL, "job is NULL");
     if (!grad_x || !grad_y) return fail(WB_EINVAL, "gradient outputs are NULL");
     if (gx_stride < q->x_len || gy_stride < q->y_len)
         return fail(WB_EINVAL, "gradient strides must cover x_len / y_len");
     cudaStream_t s = (cudaStream_t)stream_;
     Workspace ws(s);
     Dtw32Job J;
-    WB_TRY(prepare32(q, true, ws, J, 0));
+    WB_TRY(prepare32(q, true, ws, J));
     J.grad_out = grad_out;
     J.grad_x = grad_x;
     J.gx_stride = gx_stride;

@@ -67,7 +67,7 @@ __device__ __forceinline__ Item load_item(const Dtw32Job &J, int64_t t) {
     it.Y = J.y + cy * J.y_stride;
     it.n = J.xlen ? J.xlen[cx] : J.x_len;
     it.m = J.ylen ? J.ylen[cy] : J.y_len;
-    it.r = band_of(it.n, it.m, J.r);
+    it.r = J.band_fixed > 0 ? J.band_fixed : band_of(it.n, it.m, J.r);
     it.mx = imax(0, it.m - it.n) + it.r;
     it.mn = imax(0, it.n - it.m);
     return it;
@@ -406,6 +406,61 @@ int dtw32_blocks_per_sm(int strip, bool weighted, bool backward, int block) {
         return 0;
     }
     return nb;
+}
+
+// Item-order distances -> (nx, ny) row-major matrix.  Full grid: item
+// t = j * nx + i holds (x_i, y_j).  Upper (singleton, nx == ny): item
+// t = j (j - 1) / 2 + i holds the pair i < j; it is mirrored, the diagonal is 0.
+__global__ void grid_to_matrix_kernel(const double *in, int64_t nx, int64_t ny, int upper,
+                                      double *out) {
+    const int64_t total = nx * ny;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / ny, j = t - (t / ny) * ny;
+        double v;
+        if (!upper) {
+            v = in[j * nx + i];
+        } else if (i == j) {
+            v = 0.0;
+        } else {
+            const int64_t a = i < j ? i : j, b = i < j ? j : i;
+            v = in[b * (b - 1) / 2 + a];
+        }
+        out[t] = v;
+    }
+}
+
+int launch_grid_to_matrix(const double *in, int64_t nx, int64_t ny, int upper, double *out,
+                          cudaStream_t s) {
+    if (nx == 0 || ny == 0) return WB_OK;
+    int64_t g = (nx * ny + 255) / 256;
+    int64_t cap = (int64_t)device_info().sm_count * 16;
+    grid_to_matrix_kernel<<<(int)(g < cap ? g : cap), 256, 0, s>>>(in, nx, ny, upper, out);
+    WB_LAUNCH_CHECK("grid_to_matrix_kernel");
+    return WB_OK;
+}
+
+// items of the pairs i < j of n series, ordered by j then i
+__global__ void upper_items_kernel(int64_t n, int32_t *ix, int32_t *iy) {
+    const int64_t total = n * (n - 1) / 2;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t j = (int64_t)((1.0 + sqrt(1.0 + 8.0 * (double)t)) * 0.5);
+        while (j * (j - 1) / 2 > t) j--;
+        while ((j + 1) * j / 2 <= t) j++;
+        ix[t] = (int32_t)(t - j * (j - 1) / 2);
+        iy[t] = (int32_t)j;
+    }
+}
+
+int launch_upper_items(int64_t n, int32_t *item_x, int32_t *item_y, cudaStream_t s) {
+    const int64_t total = n * (n - 1) / 2;
+    if (total <= 0) return WB_OK;
+    int64_t g = (total + 255) / 256;
+    int64_t cap = (int64_t)device_info().sm_count * 16;
+    upper_items_kernel<<<(int)(g < cap ? g : cap), 256, 0, s>>>(n, item_x, item_y);
+    WB_LAUNCH_CHECK("upper_items_kernel");
+    return WB_OK;
 }
 
 // valid length of each series: index of the first NaN (EoS or NaN padding)

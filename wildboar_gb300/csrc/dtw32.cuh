@@ -25,6 +25,7 @@ struct Dtw32Job {
     const int32_t *item_y = nullptr;
     int64_t n_items = 0;
     double r = 1.0;               // band fraction; per item band = max(floor(min(n,m) r), 1)
+    int band_fixed = 0;           // > 0: this band for every item (ddtw: band of the series)
     const float *weights = nullptr;  // wdtw weights (device) or null
     double *out = nullptr;        // per item: sqrt(hi + lo) in double
     double *out_cost = nullptr;   // optional per item: hi + lo (squared distance)
@@ -47,6 +48,11 @@ int dtw32_forward(const Dtw32Job &J, int strip, cudaStream_t s);
 int dtw32_backward(const Dtw32Job &J, cudaStream_t s);
 __host__ __device__ int64_t dtw32_dir_words(int n, int m, int band_r);
 int dtw32_blocks_per_sm(int strip, bool weighted, bool backward, int block);
+int launch_grid_to_matrix(const double *in, int64_t nx, int64_t ny, int upper, double *out,
+                          cudaStream_t s);
+int dtw32_plan(const wb_dtw32 *q, bool backward, Dtw32Job &J, size_t &bytes);
+int dtw32_take(Workspace &ws, Dtw32Job &J, bool backward);
+int launch_upper_items(int64_t n, int32_t *item_x, int32_t *item_y, cudaStream_t s);
 int launch_series_lengths(const float *x, int64_t n_series, int64_t stride, int L,
                           int32_t *lengths, cudaStream_t s);
 

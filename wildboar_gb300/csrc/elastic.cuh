@@ -53,6 +53,7 @@ struct ElasticJob {
     int len_norm_cols = 0;
     double eps = 0, p = 0, g = 0, c = 0, penalty = 0, stiffness = 0;
     const double *weights = nullptr;    // wdtw / wlcss weights (device)
+    const float *weights32 = nullptr;   // the same weights in float32 (FP32 kernels)
     const double *std_rows = nullptr;   // edr default epsilon tables (device)
     const double *std_cols = nullptr;
     const double *gsum_rows = nullptr;  // erp: sum_i |x_i - g| per series
@@ -109,6 +110,11 @@ int launch_elastic_subseq(const SubseqElasticJob &J, int kind, double *gring, in
                           cudaStream_t s);
 int launch_shapelet_slopes(const double *shp, const int64_t *off, const int64_t *len,
                            int64_t m, double *out, cudaStream_t s);
+
+// FP32 (compensated) kernels of the non-dtw elastic metrics (elastic_f32.cu)
+int launch_elastic32(const ElasticJob &J, Workspace &ws);
+int launch_to_f32(const SeriesSet &in, float *out, cudaStream_t s);
+int launch_weights_f32(const double *w, int n, float *out, cudaStream_t s);
 
 // per-series preparation kernels
 int launch_slopes(const SeriesSet &in, double *out, cudaStream_t s);

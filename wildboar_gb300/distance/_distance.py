@@ -192,14 +192,14 @@ def _device_of(*inputs):
     return None
 
 
-def _pairwise_one(X, Y, dim, metric):
+def _pairwise_one(X, Y, dim, metric, entry="wb_pairwise_distance"):
     dev = _device_of(X, Y)
     ny = X.shape[0] if Y is None else Y.shape[0]
     out = _zeros(dev, (X.shape[0], ny)) if Y is None else _empty(dev, (X.shape[0], ny))
     sx = X.series()
     sy = None if Y is None else Y.series()
     p = metric.params()
-    st = _lib.lib().wb_pairwise_distance(
+    st = getattr(_lib.lib(), entry)(
         ctypes.byref(sx), None if sy is None else ctypes.byref(sy), dim,
         metric.metric_id, ctypes.byref(p), _lib.ptr(out), 1 if dev else 0, _stream(X, Y))
     _lib.check(st)
@@ -230,6 +230,10 @@ def pairwise_distance(x, y=None, *, dim="mean", metric="euclidean", metric_param
     the singleton path (upper triangle, mirrored, zero diagonal, no squeeze);
     otherwise the result is squeezed like the reference's ``_format_return``.
     """
+    return _pairwise(x, y, dim, metric, metric_params, "wb_pairwise_distance")
+
+
+def _pairwise(x, y, dim, metric, metric_params, entry):
     Metric_ = check_metric(metric)
     metric_params = metric_params if metric_params is not None else {}
     metric = Metric_(**metric_params)
@@ -240,7 +244,7 @@ def pairwise_distance(x, y=None, *, dim="mean", metric="euclidean", metric_param
         if X.ndim == 1:
             return 0.0
         n_dims = X.shape[1]
-        return _dims(lambda d: _pairwise_one(X, None, d, metric), n_dims, dim)
+        return _dims(lambda d: _pairwise_one(X, None, d, metric, entry), n_dims, dim)
     X = _as_input(x)
     Y = _as_input(y)
     if X.ndim != 1 and Y.ndim != 1 and X.ndim != Y.ndim:
@@ -257,7 +261,7 @@ def pairwise_distance(x, y=None, *, dim="mean", metric="euclidean", metric_param
     n_dims = X.shape[1]
     if Y.shape[1] != n_dims:
         raise ValueError("x and y must have the same number of dimensions.")
-    d = _dims(lambda k: _pairwise_one(X, Y, k, metric), n_dims, dim)
+    d = _dims(lambda k: _pairwise_one(X, Y, k, metric, entry), n_dims, dim)
     return _format_return(d, Y.ndim, X.ndim)
 
 

@@ -6,8 +6,13 @@
 * ``pairwise_dtw_fp32(x, y, r)`` -- dtw / wdtw with FP32 costs and compensated
   (TwoSum) accumulation, FP64 only for the final square root
   (``wb_dtw32_distance``).
+* ``pairwise_distance_fp32(x, y, metric=..., metric_params=...)`` -- every
+  elastic metric in FP32 with compensated accumulation, with the arguments,
+  validation and output layout of ``pairwise_distance``
+  (``wb_pairwise_distance_fp32``).
 
-Both take and return CUDA torch tensors.
+The first two take and return CUDA torch tensors; the third takes what
+``pairwise_distance`` takes.
 """
 
 import ctypes
@@ -15,11 +20,37 @@ import ctypes
 import torch
 
 from .. import _lib
+from . import _distance
 from . import batched as _b
 
 _lib.declare("wb_euclidean_tc", [ctypes.POINTER(_lib.Series), ctypes.POINTER(_lib.Series),
                                  ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32,
                                  ctypes.c_void_p])
+
+
+_lib.declare("wb_pairwise_distance_fp32",
+             [ctypes.POINTER(_lib.Series), ctypes.POINTER(_lib.Series), ctypes.c_int64,
+              ctypes.c_int32, ctypes.POINTER(_lib.Params), ctypes.c_void_p, ctypes.c_int32,
+              ctypes.c_void_p])
+
+ELASTIC = ("dtw", "wdtw", "ddtw", "wddtw", "adtw", "lcss", "wlcss", "edr", "erp", "msm",
+           "twe")
+
+
+def pairwise_distance_fp32(x, y=None, *, dim="mean", metric="dtw", metric_params=None):
+    """``pairwise_distance`` of an elastic metric in FP32.
+
+    Same arguments, validation and output (float64 values, shapes, squeezing)
+    as ``pairwise_distance``; the recurrence runs on float32-rounded series
+    with compensated (hi, lo) accumulation.  Relative error against the FP64
+    distance is a few float32 ulps of the inputs' rounding (about 1e-7 to
+    1e-6 for dtw-like metrics; lcss / edr counts are exact unless rounding
+    moves a difference across epsilon).
+    """
+    if not isinstance(metric, str) or metric not in ELASTIC:
+        raise ValueError("pairwise_distance_fp32 supports the elastic metrics %s, got %r"
+                         % (", ".join(ELASTIC), metric))
+    return _distance._pairwise(x, y, dim, metric, metric_params, "wb_pairwise_distance_fp32")
 
 
 def _as3(t):
