@@ -77,13 +77,14 @@ __device__ __forceinline__ Item load_item(const Dtw32Job &J, int64_t t) {
 // (i0 + k, c - 1), on exit cell (i0 + k, c).  With MASK, out-of-band cells get
 // an infinite cost (their hi is +inf and no in-band cell picks it); without,
 // every row of the strip is known to be in band for this column.  Rows past
-// the series end carry NaN x values: their cells are NaN and valid rows (which
-// only look upward) never read them.
+// the series end (k >= valid) carry NaN x values: their cells are NaN, valid
+// rows (which only look upward) never read them, and they read weight 0 so
+// that |c - i| never runs past the weight table.
 template <int S, bool W, bool DIRS, bool MASK>
 __device__ __forceinline__ void strip_column(HL (&P)[S], HL bup, HL bdiag, float yc,
                                              const float (&xr)[S], int d0, int lo,
                                              unsigned width, const float *__restrict__ w,
-                                             uint32_t &word) {
+                                             int valid, uint32_t &word) {
     HL dg = bdiag;  // cell (i0 + k - 1, c - 1)
     HL up = bup;    // cell (i0 + k - 1, c)
 #pragma unroll
@@ -102,7 +103,7 @@ __device__ __forceinline__ void strip_column(HL (&P)[S], HL bup, HL bdiag, float
         const int d = d0 - k;  // c - i
         float vv = __fsub_rn(xr[k], yc);
         float cst = __fmul_rn(vv, vv);
-        if (W) cst = __fmul_rn(cst, w[abs(d)]);
+        if (W) cst = __fmul_rn(cst, w[(!MASK || k < valid) ? abs(d) : 0]);
         if (MASK) cst = ((unsigned)(d - lo) < width) ? cst : WB_FINF;
         const HL nv = add_c(best, cst);
         if (DIRS) word |= (uint32_t)dir << (2 * k);
@@ -188,10 +189,10 @@ __device__ HL sweep(const Item &it, const float *__restrict__ w, float2 *ring, i
             uint32_t word = 0;
             if (c >= bstart && c < bend)
                 strip_column<S, W, DIRS, false>(P, bup, bdiag, yc, xr, c - i0, lo, width, w,
-                                                word);
+                                                rows, word);
             else
                 strip_column<S, W, DIRS, true>(P, bup, bdiag, yc, xr, c - i0, lo, width, w,
-                                               word);
+                                               rows, word);
             if (DIRS) dirs[(wofs + (c - cstart)) * nth] = word;
             if (last && c == m - 1) {
 #pragma unroll

@@ -4,9 +4,14 @@
 // from a tcgen05 GEMM of kind::tf32 with the 3xTF32 split: every float32 value
 // v = hi + lo with hi = tf32(v) and lo = v - hi, and
 // x . y ~ hi_x.hi_y + hi_x.lo_y + lo_x.hi_y (the lo.lo term is below FP32
-// resolution), accumulated in FP32 in tensor memory.  Norms and the final
-// combination are FP64; the inputs of the euclidean metric are float64 and
-// are rounded once to float32.
+// resolution), accumulated in FP32 in tensor memory.  The inputs of the
+// euclidean metric are float64 and are rounded once to float32; their squared
+// norms are summed in FP64 and kept as (hi, lo) float pairs.  The epilogue
+// adds the partial accumulators and forms |x|^2 + |y|^2 - 2 x.y with
+// compensated FP32 arithmetic (TwoSum, error terms carried in a lo part), so
+// the combination loses nothing against FP64; the square root is FP32 (the
+// products' own error, ~1e-7 of the norms, dominates) and the result is
+// stored as float64 through a shared-memory transpose (coalesced rows).
 //
 // Kernel: one CTA per 128 x 128 output tile, 128 threads.  Thread 0 issues
 // the TMA loads (128-byte swizzled K-major tiles of 32 floats) into a
@@ -30,11 +35,19 @@ constexpr int kTileBytes = kBM * kBK * 4;      // 16 KB per operand tile
 constexpr int kStageBytes = 4 * kTileBytes;    // A hi, A lo, B hi, B lo
 constexpr int kGemmThreads = 128;
 // four accumulators of 128 columns: consecutive quarters of K accumulate
-// separately in FP32 and are added in FP64 by the epilogue, which cuts the
-// accumulation error of long K by ~4x
+// separately in FP32 and are added with TwoSum by the epilogue, which cuts
+// the accumulation error of long K by ~4x
 constexpr int kNumAcc = 4;
 constexpr int kTmemCols = kBN * kNumAcc;
 constexpr long long kWaitLimit = 1ll << 26;
+
+// TwoSum (Knuth): returns s = fl(a + b) and sets e so that s + e == a + b exactly
+__device__ __forceinline__ float two_sum(float a, float b, float &e) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -110,7 +123,7 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 __global__ void __launch_bounds__(kGemmThreads, 1)
 euclid_tc_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
                  const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
-                 const double *__restrict__ nx, const double *__restrict__ ny, int M, int N,
+                 const float2 *__restrict__ nx, const float2 *__restrict__ ny, int M, int N,
                  int Kp, double *out, int64_t ld_out, int *err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // 1024-byte aligned stage ring
@@ -210,16 +223,19 @@ euclid_tc_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant
     if (abort_flag) ok = false;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (ok) {
-        const int row = warp * 32 + (tid & 31);  // TMEM lane = accumulator row
+        const int lane = tid & 31;
+        const int row = warp * 32 + lane;  // TMEM lane = accumulator row
         const int gi = m0 + row;
-        const double nxi = gi < M ? nx[gi] : 0.0;
+        const float2 nxi = gi < M ? nx[gi] : make_float2(0.0f, 0.0f);
         const int KTn = Kp / kBK;
         const int used = (KTn + ((KTn + kNumAcc - 1) / kNumAcc) - 1) / ((KTn + kNumAcc - 1) / kNumAcc);
+        // the stage ring is idle once done_bar has fired: 32 x 33 doubles per warp
+        double *tile = reinterpret_cast<double *>(smem) + warp * (32 * 33);
 #pragma unroll 1
         for (int c0 = 0; c0 < kBN; c0 += 32) {
-          double dot[32];
+          float sh[32], sl[32];
 #pragma unroll
-          for (int j = 0; j < 32; j++) dot[j] = 0.0;
+          for (int j = 0; j < 32; j++) sh[j] = sl[j] = 0.0f;
 #pragma unroll 1
           for (int a = 0; a < used; a++) {
             uint32_t v[32];
@@ -238,19 +254,33 @@ euclid_tc_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant
                 : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-            for (int j = 0; j < 32; j++) dot[j] += (double)__uint_as_float(v[j]);
+            for (int j = 0; j < 32; j++) {
+                float e;
+                sh[j] = two_sum(sh[j], __uint_as_float(v[j]), e);
+                sl[j] = __fadd_rn(sl[j], e);
+            }
           }
-          if (gi < M) {
-              double *o = out + (int64_t)gi * ld_out;
 #pragma unroll
-              for (int j = 0; j < 32; j++) {
-                  const int gj = n0 + c0 + j;
-                  if (gj < N) {
-                      const double d2 = (nxi + ny[gj]) - 2.0 * dot[j];
-                      o[gj] = sqrt(d2 > 0.0 ? d2 : 0.0);
-                  }
-              }
+          for (int j = 0; j < 32; j++) {
+              const int gj = n0 + c0 + j;
+              const float2 nyj = gj < N ? ny[gj] : make_float2(0.0f, 0.0f);
+              // d2 = (nx + ny) - 2 dot with every rounding error carried
+              float e1, e2;
+              const float s1 = two_sum(nxi.x, nyj.x, e1);
+              const float t = two_sum(s1, __fmul_rn(-2.0f, sh[j]), e2);
+              const float corr = __fsub_rn(__fadd_rn(__fadd_rn(e1, e2), __fadd_rn(nxi.y, nyj.y)),
+                                           __fmul_rn(2.0f, sl[j]));
+              const float d2 = __fadd_rn(t, corr);
+              tile[lane * 33 + j] = (double)sqrtf(d2 > 0.0f ? d2 : 0.0f);
           }
+          __syncwarp();
+          const int gj = n0 + c0 + lane;
+#pragma unroll 4
+          for (int r = 0; r < 32; r++) {
+              const int gr = m0 + warp * 32 + r;
+              if (gr < M && gj < N) out[(int64_t)gr * ld_out + gj] = tile[r * 33 + lane];
+          }
+          __syncwarp();
         }
     } else if (tid == 0) {
         atomicExch(err, 1);
@@ -265,9 +295,10 @@ euclid_tc_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant
 }
 
 // float64 rows -> float32 hi/lo tf32 split (zero padded to (rows_p, Kp)) and
-// FP64 squared norms of the float32-rounded rows
+// the squared norms of the float32-rounded rows (summed in FP64, stored as a
+// (hi, lo) float pair)
 __global__ void tf32_split_kernel(const double *__restrict__ x, int64_t stride, int rows, int K,
-                                  int rows_p, int Kp, float *hi, float *lo, double *norm) {
+                                  int rows_p, int Kp, float *hi, float *lo, float2 *norm) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -285,7 +316,10 @@ __global__ void tf32_split_kernel(const double *__restrict__ x, int64_t stride, 
             acc += (double)v * (double)v;
         }
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0 && r < rows) norm[r] = acc;
+        if (lane == 0 && r < rows) {
+            const float h = (float)acc;
+            norm[r] = make_float2(h, (float)(acc - (double)h));
+        }
     }
 }
 
@@ -331,7 +365,7 @@ int euclid_tc(const double *x, int64_t sx, int M, const double *y, int64_t sy, i
     const int Mp = round_up(std::max(M, 1), kBM), Np = round_up(std::max(N, 1), kBN);
     const int Kp = round_up(std::max(K, 1), kBK);
     const size_t need = 2 * align256((size_t)Mp * Kp * 4) + 2 * align256((size_t)Np * Kp * 4) +
-                        align256((size_t)M * 8) + align256((size_t)N * 8) + 256;
+                        align256((size_t)M * 8) + align256((size_t)N * 8) + 256;  // float2 norms
     if (reserve_only) {
         *bytes = need;
         return WB_OK;
@@ -341,8 +375,8 @@ int euclid_tc(const double *x, int64_t sx, int M, const double *y, int64_t sy, i
     WB_TAKE(alo, float, ws, (size_t)Mp * Kp);
     WB_TAKE(bhi, float, ws, (size_t)Np * Kp);
     WB_TAKE(blo, float, ws, (size_t)Np * Kp);
-    WB_TAKE(nxv, double, ws, M);
-    WB_TAKE(nyv, double, ws, N);
+    WB_TAKE(nxv, float2, ws, M);
+    WB_TAKE(nyv, float2, ws, N);
     WB_TAKE(err, int, ws, 1);
     WB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
     const int sgrid = std::min<int64_t>((int64_t)device_info().sm_count * 8, (Mp + 7) / 8 + 1);
