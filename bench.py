@@ -453,14 +453,21 @@ def bench_precision(args, dev, flush):
         lc = L - 2 if metric == "ddtw" else L
         cells = n * n * _cells_w(lc, lc, w)
         res = {"metric": metric, "params": params}
+        outs = {}
         for tag, fn in (("fp64", pairwise_distance), ("fp32", pairwise_distance_fp32)):
             fn(Xd[:64], Yd[:64], metric=metric, metric_params=params)
             torch.cuda.synchronize()
-            ms = _timed(lambda: fn(Xd, Yd, metric=metric, metric_params=params), 1, flush)
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            outs[tag] = fn(Xd, Yd, metric=metric, metric_params=params)
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
             res[tag + "_ms"] = ms
             res[tag + "_gcups"] = cells / (ms * 1e-3) / 1e9
-        D64 = pairwise_distance(Xd, Yd, metric=metric, metric_params=params)
-        D32 = pairwise_distance_fp32(Xd, Yd, metric=metric, metric_params=params)
+        D64, D32 = outs["fp64"], outs["fp32"]
         diff = (D32 - D64).abs()
         rel = diff / D64.abs().clamp(min=1e-300)
         res["max_abs_err_vs_fp64"] = diff.max().item()
@@ -483,6 +490,7 @@ def run_gpu(args):
 
     from wildboar_gb300 import _build, _lib
     from wildboar_gb300.distance import pairwise_distance
+    from wildboar_gb300.distance.sharded import max_over_ranks
 
     rank, world = _rank()
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -553,9 +561,7 @@ def run_gpu(args):
     _lib.profile_enable(False)
     t_step = sum(step_ms) / len(step_ms)
     if dist is not None:
-        tt = torch.tensor([t_step], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+        t_step = max_over_ranks(t_step)
     value = world * cells / (t_step * 1e-3) / 1e9
 
     # end to end through the public API with pinned host buffers
@@ -576,9 +582,7 @@ def run_gpu(args):
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     t_e2e = sum(e2e_ms) / len(e2e_ms)
     if dist is not None:
-        tt = torch.tensor([t_e2e], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+        t_e2e = max_over_ranks(t_e2e)
     e2e = {"value": world * cells / (t_e2e * 1e-3) / 1e9, "unit": "GCUPS",
            "h2d_bytes_per_step": int(Xh.nbytes + Yh.nbytes),
            "d2h_bytes_per_step": int(np.asarray(out).nbytes)}

@@ -483,7 +483,7 @@ extern "C" int wb_pairwise_distance_fp32(const wb_series *x, const wb_series *y,
         probe.rows = probeR;
         probe.cols = probeC;
         probe.mode = same ? PM_UPPER : PM_ALL;
-        need += elastic_workspace_bytes(probe);
+        need += std::max(strip_workspace_bytes(probe, true), elastic_workspace_bytes(probe));
     }
     Workspace ws(s);
     WB_TRY(ws.reserve(need));
@@ -536,7 +536,7 @@ extern "C" int wb_pairwise_distance_fp32(const wb_series *x, const wb_series *y,
         J.mode = same ? PM_UPPER : PM_ALL;
         if (same) WB_CUDA(cudaMemsetAsync(dout, 0, out_elems * sizeof(double), s));
         if (all_zero) WB_TRY(launch_elastic(J, ws, nullptr));
-        else WB_TRY(launch_elastic32(J, ws));
+        else WB_TRY(launch_strip(J, ws, true));
     }
     return finish_host_copy(out, dout, out_elems * sizeof(double), out_on_device, s);
 }

@@ -111,8 +111,14 @@ int launch_elastic_subseq(const SubseqElasticJob &J, int kind, double *gring, in
 int launch_shapelet_slopes(const double *shp, const int64_t *off, const int64_t *len,
                            int64_t m, double *out, cudaStream_t s);
 
-// FP32 (compensated) kernels of the non-dtw elastic metrics (elastic_f32.cu)
-int launch_elastic32(const ElasticJob &J, Workspace &ws);
+// register-strip kernels of every elastic metric, FP64 (exact) or FP32
+// (compensated) (elastic_strip.cu)
+bool strip_supported(const ElasticJob &J);
+bool strip_forced();
+size_t strip_workspace_bytes(const ElasticJob &J, bool fp32);
+int launch_strip(const ElasticJob &J, Workspace &ws, bool fp32);
+
+// float64 -> float32 conversions for the FP32 dtw strip kernel (elastic_strip.cu)
 int launch_to_f32(const SeriesSet &in, float *out, cudaStream_t s);
 int launch_weights_f32(const double *w, int n, float *out, cudaStream_t s);
 

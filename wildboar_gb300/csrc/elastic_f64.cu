@@ -583,13 +583,27 @@ static ElasticPlan plan_elastic(const ElasticJob &J) {
     return pl;
 }
 
+// FP64: the ring kernel keeps a band that fits in shared memory at no extra
+// cost per cell, while the strip kernel also evaluates (and discards) the
+// cells of each strip's ragged band edges; measured on GB300 (dtw, L = 512)
+// the ring kernel wins for shared-memory rings (r = 0.1: 171 vs 152 GCUPS)
+// and the strip kernel for global rings (r = 1: 167 vs 128 GCUPS; lcss 168 vs
+// 134, erp 127 vs 115, msm 64 vs 58), except twe (53 vs 57).
+static bool use_strip_f64(const ElasticJob &J) {
+    if (!strip_supported(J)) return false;
+    if (strip_forced()) return true;
+    return J.kind != K_TWE && plan_elastic(J).gring;
+}
+
 size_t elastic_workspace_bytes(const ElasticJob &J) {
+    if (use_strip_f64(J)) return strip_workspace_bytes(J, false);
     ElasticPlan pl = plan_elastic(J);
     return align256(pl.gring_bytes);
 }
 
 int launch_elastic(const ElasticJob &J, Workspace &ws, size_t *) {
     if (J.rows.count == 0 || J.cols.count == 0) return WB_OK;
+    if (use_strip_f64(J)) return launch_strip(J, ws, false);
     ElasticPlan pl = plan_elastic(J);
     double *gring = pl.gring ? ws.take<double>(pl.gring_bytes / sizeof(double)) : nullptr;
     if (pl.gring && !gring) return fail(WB_ENOMEM, "workspace reservation exceeded");
