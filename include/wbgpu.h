@@ -134,6 +134,61 @@ int wb_pairwise_subsequence_distance(const double *shapelets, const int64_t *off
                                      double *out_dist, int64_t *out_idx,
                                      int32_t out_on_device, void *stream);
 
+/*
+ * shapelet i against x[i, dim] only (m == x.n): out_dist / out_idx are (m,).
+ * Arguments as wb_pairwise_subsequence_distance.  Replaces
+ * _paired_subsequence_distance (distance/_cdistance.pyx:1040-1062).
+ */
+int wb_paired_subsequence_distance(const double *shapelets, const int64_t *offsets,
+                                   const int64_t *lengths, const double *means,
+                                   const double *stds, int64_t m, const wb_series *x,
+                                   int64_t dim, int32_t metric, const wb_params *params,
+                                   double *out_dist, int64_t *out_idx,
+                                   int32_t out_on_device, void *stream);
+
+/*
+ * every window of shapelet i against x[i, dim] (m == x.n), no minimum:
+ * out_raw[i * ld + w] is the final value of the metric's recurrence for
+ * window w (squared sum for euclidean / scaled_euclidean, squared cost for
+ * the dtw family, match count for lcss, edit count for edr, the cost for
+ * erp / msm / twe; NaN past the pair's last window) and out_key[i * ld + w]
+ * the largest per-row minimum of the recurrence (the value the reference's
+ * early abandoning compares with its threshold; -inf for the euclidean
+ * metrics, whose key may be NULL).  ld >= x.n_timestep - min length + 1.
+ * Shapelets may share storage (equal offsets).  stds of 0 are taken as 1
+ * (persistent subsequences, _cdistance.pyx:283-343) unless std_as_given
+ * (the distance profile's transient statistics, _cdistance.pyx:1680-1699,
+ * divide by them as they are).  With these two numbers the
+ * caller reproduces the distances and the match sets of
+ * SubsequenceMetric._matches (distance/_cdistance.pyx:301-432) for any
+ * threshold: distance_profile, subsequence_match and paired_subsequence_match
+ * (distance/_distance.py:732-1080, 1477-1620).
+ */
+int wb_subsequence_profile(const double *shapelets, const int64_t *offsets,
+                           const int64_t *lengths, const double *means, const double *stds,
+                           int64_t m, const wb_series *x, int64_t dim, int32_t metric,
+                           const wb_params *params, double *out_raw, double *out_key,
+                           int64_t ld, int32_t std_as_given, int32_t out_on_device,
+                           void *stream);
+
+/*
+ * the k closest windows of subsequence i in x[i, dim] (argmin_subsequence_
+ * distance, distance/_distance.py:1636-1761): s is (n, s_stride) float64
+ * on the host (row i holds s_len[i] values), x.n == n.  metric is a pairwise
+ * metric id (euclidean or elastic) evaluated through its eadistance with the
+ * reference's early abandoning; scaled z-normalises the subsequence with
+ * s_mean / s_std (fast_mean_std of the row; host arrays) and every window
+ * with the IncStats sequence of its series.  indices / distances are (n, k)
+ * in the reference's heap order.  Replaces _argmin_subsequence_distance
+ * (distance/_cdistance.pyx:1381-1594).
+ */
+int wb_argmin_subsequence_distance(const double *s, const int64_t *s_len, int64_t s_stride,
+                                   int64_t n, const double *s_mean, const double *s_std,
+                                   const wb_series *x, int64_t dim, int32_t metric,
+                                   const wb_params *params, int32_t scaled, int64_t k,
+                                   int64_t *indices, double *distances, int32_t out_on_device,
+                                   void *stream);
+
 /* ------------------------------------------------------------------------
  * FP32 forms (batched, ragged, differentiable).  No counterpart in the
  * reference, which computes every distance in FP64 on the CPU; they follow

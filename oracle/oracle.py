@@ -88,6 +88,12 @@ def lib():
         L.wbo_distance_1d.restype = ctypes.c_double
         L.wbo_fast_mean_std.argtypes = [dp, i64, dp, dp]
         L.wbo_dtw_alignment.argtypes = [dp, i64, dp, i64, i64, dp, dp]
+        L.wbo_subsequence_matches.argtypes = [dp, ip, ip, dp, dp, i64, dp, i64, i64, i64,
+                                              ctypes.c_int, pp, ctypes.c_double, dp, dp, i64,
+                                              ctypes.c_int, ctypes.c_int]
+        L.wbo_argmin_subsequence.argtypes = [dp, ip, i64, i64, dp, i64, i64, i64,
+                                             ctypes.c_int, pp, ctypes.c_int, i64, ip, dp,
+                                             ctypes.c_int]
         _lib = L
     return _lib
 
@@ -217,6 +223,85 @@ def subsequence(shapelets, x, *, dim=0, metric="euclidean", metric_params=None,
                           METRIC_IDS[metric], ctypes.byref(p), _dp(dist), _ip(idx),
                           n_threads)
     return dist, idx
+
+
+def _subseq_params(metric, metric_params):
+    pd = dict(SUBSEQ_DEFAULTS.get(metric, {}))
+    pd.update(metric_params or {})
+    p = Params()
+    p.r = pd.get("r", 1.0)
+    p.g = pd.get("g", 0.0)
+    p.p = pd.get("p", 1.0)
+    p.epsilon = pd.get("epsilon", math.nan)
+    p.c = pd.get("c", 1.0)
+    p.penalty = pd.get("penalty", 1.0)
+    p.stiffness = pd.get("stiffness", 0.001)
+    return p
+
+
+def subsequence_matches(shapelets, x, threshold, *, dim=0, metric="euclidean",
+                        metric_params=None, transient=False, n_threads=1):
+    """SubsequenceMetric._matches for pairs (shapelets[i], x[i]).
+
+    Returns (dist, keep), each (n, ld) with ld = n_timestep - min length + 1:
+    every window's distance as the reference computes it and 1.0 where the
+    reference keeps the window for `threshold` (NaN / 0 past a pair's last
+    window).  threshold=inf gives the distance profile.  transient: the
+    shapelet statistics of _DistanceProfile (fast_mean_std, a zero std kept,
+    distance/_cdistance.pyx:1680-1699) instead of from_array's np.mean/np.std.
+    """
+    X = _ts(x)
+    shp = [np.asarray(s, dtype=np.float64).ravel() for s in shapelets]
+    lens = np.array([s.shape[0] for s in shp], dtype=np.int64)
+    offs = np.zeros(len(shp), dtype=np.int64)
+    offs[1:] = np.cumsum(lens)[:-1]
+    packed = np.ascontiguousarray(np.concatenate(shp))
+    smean = np.array([np.mean(s) for s in shp])
+    sstd = np.array([np.std(s) for s in shp])
+    sstd[sstd <= 1e-13] = 0.0
+    if transient:
+        st = [fast_mean_std(s) for s in shp]
+        smean = np.array([a for a, _ in st])
+        sstd = np.array([b for _, b in st])
+    ld = int(X.shape[2] - lens.min() + 1)
+    dist = np.full((len(shp), ld), np.nan)
+    keep = np.zeros((len(shp), ld))
+    p = _subseq_params(metric, metric_params)
+    lib().wbo_subsequence_matches(_dp(packed), _ip(offs), _ip(lens), _dp(smean), _dp(sstd),
+                                  len(shp), _dp(X), X.shape[1], X.shape[2], dim,
+                                  METRIC_IDS[metric], ctypes.byref(p), float(threshold),
+                                  _dp(dist), _dp(keep), ld, 1 if transient else 0,
+                                  n_threads)
+    return dist, keep
+
+
+def argmin_subsequence(y, x, *, k=1, dim=0, metric="euclidean", metric_params=None,
+                       scale=False, n_threads=1):
+    """_argmin_subsequence_distance: (n, k) indices and distances in heap order.
+
+    y: (n, L) array or a list of n 1-D arrays (zero padded to the longest, as
+    argmin_subsequence_distance does); pair i = (y[i], x[i]).
+    """
+    X = _ts(x)
+    if isinstance(y, np.ndarray) and y.ndim == 2:
+        S = np.ascontiguousarray(y, dtype=np.float64)
+        lens = np.full(S.shape[0], S.shape[1], dtype=np.int64)
+    else:
+        lens = np.array([len(s) for s in y], dtype=np.int64)
+        S = np.zeros((len(y), int(lens.max())))
+        for i, s in enumerate(y):
+            S[i, :len(s)] = s
+    if metric.startswith("scaled_"):
+        metric = metric[7:]
+        scale = True
+    idx = np.zeros((S.shape[0], k), dtype=np.int64)
+    dist = np.zeros((S.shape[0], k))
+    p = make_params(metric, metric_params)
+    lib().wbo_argmin_subsequence(_dp(S), _ip(lens), S.shape[1], S.shape[0], _dp(X),
+                                 X.shape[1], X.shape[2], dim, METRIC_IDS[metric],
+                                 ctypes.byref(p), 1 if scale else 0, k, _ip(idx),
+                                 _dp(dist), n_threads)
+    return idx, dist
 
 
 def distance_1d(x, y, *, metric="dtw", metric_params=None):

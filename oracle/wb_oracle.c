@@ -399,6 +399,45 @@ static double scaled_euclid_scan(const double *S, idx_t sl, double s_mean, doubl
     return sqrt(min_dist);
 }
 
+/* IncStats (Welford updates with unit weights): utils/_stats.pyx:45-93 */
+typedef struct { double mean, n_samples, sum_square, sum; } incstats;
+
+static void inc_init(incstats *s) { s->mean = s->n_samples = s->sum_square = s->sum = 0.0; }
+
+static void inc_add(incstats *s, double w, double v)
+{
+    double next_m;
+    s->n_samples += w;
+    next_m = s->mean + (v - s->mean) / s->n_samples;
+    s->sum_square += (v - s->mean) * (v - next_m);
+    s->mean = next_m;
+    s->sum += w * v;
+}
+
+static void inc_remove(incstats *s, double w, double v)
+{
+    if (s->n_samples == 1.0) {
+        s->n_samples = 0.0;
+        s->mean = 0.0;
+        s->sum_square = 0.0;
+    } else {
+        double old_m = (s->n_samples * s->mean - v) / (s->n_samples - w);
+        s->sum_square -= (v - s->mean) * (v - old_m);
+        s->mean = old_m;
+        s->n_samples -= w;
+    }
+    s->sum -= w * v;
+}
+
+static double inc_variance(const incstats *s)
+{
+    double n = s->n_samples;
+    if (n <= 1) return 0;
+    double var = s->sum_square / n;
+    if (var < 1e-13) var = 0.0;
+    return var;
+}
+
 /* ---------------------------------------------------------------------- */
 /* Metric objects: reset / distance / eadistance                          */
 /* ---------------------------------------------------------------------- */
@@ -540,8 +579,26 @@ static double metric_call(const wbo_metric *M, wbo_scratch *s, const double *x, 
         break;
     }
     case WBO_EDR: {
-        /* EdrMetric.distance / eadistance (TSArray forms): _elastic.pyx:3754-3845 */
         double eps;
+        if (x_index < 0) {
+            /* EdrMetric._distance / _eadistance (pointer forms, x_index < 0):
+             * _elastic.pyx:3785-3880 -- epsilon from the two inputs themselves */
+            if (isnan(p->epsilon)) {
+                double mean, sx, sy;
+                fast_mean_std(x, xl, &mean, &sx);
+                fast_mean_std(y, yl, &mean, &sy);
+                eps = dmax(sx, sy) / 4.0;
+            } else {
+                eps = p->epsilon;
+            }
+            if (!ea)
+                return edr_rows(x, xl, y, yl, compute_r(imin(xl, yl), p->r), eps, s->cost,
+                                s->cost_prev, INF);
+            dist = edr_rows(x, xl, y, yl, compute_r(imin(xl, yl), p->r), eps, s->cost,
+                            s->cost_prev, *min_dist * (double)imax(xl, yl));
+            break;
+        }
+        /* EdrMetric.distance / eadistance (TSArray forms): _elastic.pyx:3754-3845 */
         if (isnan(p->epsilon))
             eps = dmax(M->std_x[dim * M->xn + x_index], M->std_y[dim * M->yn + y_index]) / 4.0;
         else
@@ -661,6 +718,126 @@ static double subseq_elastic(int metric, const wbo_params *p, const double *S, i
     }
 }
 
+/* SubsequenceMetric._matches for one (S, T) pair: every window's distance
+ * and whether the reference keeps it for `threshold` --
+ * euclidean_distance_matches / scaled_euclidean_distance_matches
+ * (distance/_metric.pyx:762-870) and the elastic *_subsequence_matches
+ * (distance/_elastic.pyx:658-1910), each called with the threshold the
+ * metric class passes.  dist[i] is the value the reference computes for
+ * window i (its stored distance when kept); keep[i] is 1 when kept. */
+static void subseq_matches(int metric, const wbo_params *p, const double *S, idx_t sl,
+                           double s_mean, double s_std, const double *T, idx_t tl,
+                           wbo_scratch *s, const double *weights, double *sbuf,
+                           double *tbuf, double threshold, double *dist_out,
+                           double *keep_out)
+{
+    idx_t length = tl - sl + 1;
+    if (metric == WBO_EUCLIDEAN) {
+        double thr = threshold * threshold;
+        for (idx_t i = 0; i < length; i++) {
+            double dist = 0;
+            for (idx_t j = 0; j < sl; j++) {
+                if (dist > thr) break;
+                double x = T[i + j];
+                x -= S[j];
+                dist += x * x;
+            }
+            dist_out[i] = sqrt(dist);
+            keep_out[i] = dist <= thr;
+        }
+        return;
+    }
+    if (metric == WBO_SCALED_EUCLIDEAN) {
+        double thr = threshold * threshold, ex = 0, ex2 = 0;
+        for (idx_t i = 0; i < tl; i++) {
+            double cv = T[i];
+            ex += cv;
+            ex2 += cv * cv;
+            idx_t bp = i % sl;
+            sbuf[bp] = cv;
+            sbuf[bp + sl] = cv;
+            if (i >= sl - 1) {
+                idx_t j = (i + 1) % sl;
+                double mean = ex / (double)sl;
+                double tmp = ex2 / (double)sl - mean * mean;
+                double std = tmp > 0 ? sqrt(tmp) : 1.0;
+                double dist = 0;
+                for (idx_t k = 0; k < sl; k++) {
+                    if (dist >= thr) break;
+                    double x = (S[k] - s_mean) / s_std;
+                    x -= (sbuf[k + j] - mean) / std;
+                    dist += x * x;
+                }
+                dist_out[i + 1 - sl] = sqrt(dist);
+                keep_out[i + 1 - sl] = dist <= thr;
+                cv = sbuf[j];
+                ex -= cv;
+                ex2 -= cv * cv;
+            }
+        }
+        return;
+    }
+    idx_t r = compute_r(sl, p->r);
+    int sq = metric == WBO_DTW || metric == WBO_WDTW || metric == WBO_ADTW ||
+             metric == WBO_DDTW || metric == WBO_WDDTW;
+    if ((metric == WBO_DDTW || metric == WBO_WDDTW) && sl < 3) {
+        for (idx_t i = 0; i < length; i++) {
+            dist_out[i] = NAN;
+            keep_out[i] = 0;
+        }
+        return;
+    }
+    if (metric == WBO_DDTW || metric == WBO_WDDTW) average_slope(S, sl, sbuf);
+    double thr = sq ? threshold * threshold : threshold;
+    for (idx_t i = 0; i < length; i++) {
+        double dist;
+        switch (metric) {
+        case WBO_DTW:
+        case WBO_WDTW:
+            dist = dtw_rows(S, sl, T + i, sl, r, s->cost, s->cost_prev, weights, thr);
+            break;
+        case WBO_ADTW:
+            dist = adtw_rows(S, sl, T + i, sl, r, s->cost, s->cost_prev, p->p, thr);
+            break;
+        case WBO_DDTW:
+        case WBO_WDDTW:
+            average_slope(T + i, sl, tbuf);
+            dist = dtw_rows(sbuf, sl - 2, tbuf, sl - 2, r, s->cost, s->cost_prev, weights,
+                            thr);
+            break;
+        case WBO_LCSS: {
+            double ml = (double)imin(sl, tl);
+            double t2 = isinf(threshold) == 0 ? ml - threshold * ml : threshold;
+            dist = lcss_rows(S, sl, T + i, sl, r, p->epsilon, s->cost, s->cost_prev, NULL,
+                             t2);
+            break;
+        }
+        case WBO_EDR: {
+            double eps = isnan(p->epsilon) ? s_std / 4.0 : p->epsilon;
+            dist = edr_rows(S, sl, T + i, sl, r, eps, s->cost, s->cost_prev,
+                            threshold * (double)imax(sl, tl));
+            break;
+        }
+        case WBO_ERP:
+            dist = erp_rows(S, sl, T + i, sl, r, p->g, s->gX, s->gY, s->cost, s->cost_prev,
+                            thr);
+            break;
+        case WBO_MSM:
+            dist = msm_rows(S, sl, T + i, sl, r, p->c, s->cost, s->cost_prev, s->cost_y, thr);
+            break;
+        case WBO_TWE:
+            dist = twe_rows(S, sl, T + i, sl, r, p->penalty, p->stiffness, s->cost,
+                            s->cost_prev, thr);
+            break;
+        default:
+            dist = NAN;
+        }
+        keep_out[i] = dist <= thr;
+        if (metric == WBO_LCSS || metric == WBO_EDR) keep_out[i] = dist <= threshold;
+        dist_out[i] = sq ? sqrt(dist) : dist;
+    }
+}
+
 /* ---------------------------------------------------------------------- */
 /* Heap keeping the k smallest: utils/_misc.pyx:18-107                     */
 /* ---------------------------------------------------------------------- */
@@ -734,6 +911,11 @@ typedef struct {
     const double *sub_weights;
     wbo_params sub_params;
     idx_t m;
+    double threshold;          /* matches */
+    double *out_keep;          /* matches: (n, ld) */
+    idx_t ld;
+    idx_t s_stride;            /* argmin subsequence: row stride of the subsequences */
+    int scaled;
     idx_t begin, end;
 } job_t;
 
@@ -748,10 +930,11 @@ static void *run_job(void *arg)
     heap_el *heap = NULL;
     if (J->kind == 3) heap = malloc(sizeof(heap_el) * (size_t)imax(J->k, 1));
     double *tbuf = NULL;
-    if (J->kind == 4) {
+    if (J->kind >= 4) {
         sbuf = malloc(sizeof(double) * (size_t)(2 * J->xL + 2));
         tbuf = malloc(sizeof(double) * (size_t)(2 * J->xL + 2));
     }
+    if (J->kind == 5) heap = malloc(sizeof(heap_el) * (size_t)imax(J->k, 1));
     for (idx_t i = J->begin; i < J->end; i++) {
         const double *xr = J->X + (i * J->xd + J->dim) * J->xL;
         if (J->kind == 0) {
@@ -809,6 +992,58 @@ static void *run_job(void *arg)
                 }
                 J->out[i * J->m + j] = d;
                 J->out_idx[i * J->m + j] = mi;
+            }
+        } else if (J->kind == 6) {
+            /* _subsequence_match / _paired_subsequence_match / _distance_profile:
+             * _cdistance.pyx:1065-1141, :345-403; pair i = (shapelet i, series i) */
+            const double *S = J->shp + J->shp_off[i];
+            idx_t sl = J->shp_len[i];
+            double smean = J->shp_mean ? J->shp_mean[i] : 0.0;
+            double sstd = J->shp_std && (J->shp_std[i] != 0 || J->scaled) ? J->shp_std[i] : 1.0;
+            subseq_matches(M->id, &J->sub_params, S, sl, smean, sstd, xr, J->xL, &s,
+                           J->sub_weights, sbuf, tbuf, J->threshold, J->out + i * J->ld,
+                           J->out_keep + i * J->ld);
+        } else if (J->kind == 5) {
+            /* _ArgminSubsequenceDistance / _ScaledArgminSubsequenceDistance:
+             * _cdistance.pyx:1381-1557 */
+            idx_t sl = J->shp_len[i];
+            const double *S = J->shp + i * J->s_stride;
+            const double *sv = S;
+            idx_t nwin = J->xL - sl + 1;
+            incstats st;
+            if (J->scaled) {
+                double mean, std;
+                fast_mean_std(S, sl, &mean, &std);
+                if (std == 0.0) std = 1.0;
+                inc_init(&st);
+                for (idx_t n = 0; n < sl - 1; n++) {
+                    sbuf[n] = (S[n] - mean) / std;
+                    inc_add(&st, 1.0, xr[n]);
+                }
+                sbuf[sl - 1] = (S[sl - 1] - mean) / std;
+                sv = sbuf;
+            }
+            double distance = INF;
+            idx_t hn = 0;
+            for (idx_t j = 0; j < nwin; j++) {
+                const double *wv = xr + j;
+                if (J->scaled) {
+                    inc_add(&st, 1.0, xr[j + sl - 1]);
+                    double sd = inc_variance(&st);
+                    if (sd == 0.0) sd = 1.0;
+                    else sd = sqrt(sd);
+                    double mu = st.mean;
+                    for (idx_t n = 0; n < sl; n++) tbuf[n] = (xr[j + n] - mu) / sd;
+                    inc_remove(&st, 1.0, xr[j]);
+                    wv = tbuf;
+                }
+                if (metric_call(M, &s, sv, sl, -1, wv, sl, -1, 0, 1, &distance))
+                    heap_push(heap, &hn, J->k, j, distance);
+                distance = (hn == J->k) ? heap[0].value : INF;
+            }
+            for (idx_t j = 0; j < J->k && j < hn; j++) {
+                J->out_idx[i * J->k + j] = heap[j].index;
+                J->out[i * J->k + j] = heap[j].value;
             }
         }
     }
@@ -935,6 +1170,57 @@ int wbo_subsequence(const double *shp, const idx_t *off, const idx_t *len,
     J.sub_weights = w;
     run_parallel(&J, xn, n_threads);
     free(w);
+    return 0;
+}
+
+/* SubsequenceMetric._matches for pairs (shapelet i, x[i, dim]):
+ * out_dist / out_keep are (n, ld), windows past a pair's last untouched.
+ * std_as_given: a zero shapelet std is not replaced by 1 (the distance
+ * profile passes its transient statistics as they are). */
+int wbo_subsequence_matches(const double *shp, const idx_t *off, const idx_t *len,
+                            const double *smean, const double *sstd, idx_t n,
+                            const double *X, idx_t xd, idx_t xL, idx_t dim, int metric,
+                            const wbo_params *p, double threshold, double *out_dist,
+                            double *out_keep, idx_t ld, int std_as_given, int n_threads)
+{
+    wbo_metric M = {0};
+    M.id = metric;
+    job_t J = {0};
+    J.kind = 6; J.M = &M;
+    J.X = X; J.xn = n; J.xd = xd; J.xL = xL; J.yL = xL; J.dim = dim;
+    J.shp = shp; J.shp_off = off; J.shp_len = len; J.shp_mean = smean; J.shp_std = sstd;
+    J.m = n; J.out = out_dist; J.out_keep = out_keep; J.ld = ld; J.threshold = threshold;
+    J.scaled = std_as_given;  /* kind 6: a zero std is used as is */
+    double *w = NULL;
+    if (p) J.sub_params = *p;
+    if (metric == WBO_WDTW) w = logistic_weights(xL, p->g);
+    if (metric == WBO_WDDTW) w = logistic_weights(xL - 2 > 0 ? xL - 2 : 0, p->g);
+    J.sub_weights = w;
+    run_parallel(&J, n, n_threads);
+    free(w);
+    return 0;
+}
+
+/* _argmin_subsequence_distance: _cdistance.pyx:1559-1594.  S is (n, s_stride)
+ * (the reference's (n, 1, max_len) subsequence array), s_len the lengths;
+ * metric reset with (x, S) as the reference does.  Outputs zero-filled by the
+ * caller; (n, k) in heap order. */
+int wbo_argmin_subsequence(const double *S, const idx_t *s_len, idx_t s_stride, idx_t n,
+                           const double *X, idx_t xd, idx_t xL, idx_t dim, int metric,
+                           const wbo_params *p, int scaled, idx_t k, idx_t *out_idx,
+                           double *out_dist, int n_threads)
+{
+    wbo_metric M = {0};
+    M.id = metric;
+    M.p = *p;
+    metric_reset(&M, X, n, xd, xL, S, n, 1, s_stride);
+    job_t J = {0};
+    J.kind = 5; J.M = &M;
+    J.X = X; J.xn = n; J.xd = xd; J.xL = xL; J.yL = s_stride; J.dim = dim;
+    J.shp = S; J.shp_len = s_len; J.s_stride = s_stride; J.scaled = scaled; J.k = k;
+    J.out = out_dist; J.out_idx = out_idx;
+    run_parallel(&J, n, n_threads);
+    metric_free(&M);
     return 0;
 }
 

@@ -6,7 +6,9 @@ Usage (in a container where the reference wildboar is built and importable)::
 
 The reference is imported from ``WILDBOAR_REF_PATH`` and called through its
 public API (``wildboar.distance.pairwise_distance``, ``paired_distance``,
-``argmin_distance``, ``pairwise_subsequence_distance`` and
+``argmin_distance``, ``pairwise_subsequence_distance``,
+``paired_subsequence_distance``, ``argmin_subsequence_distance``,
+``distance_profile``, ``subsequence_match``, ``paired_subsequence_match`` and
 ``wildboar.distance.dtw.dtw_alignment``).  Inputs are seeded Gaussian random
 walks; every case stores its inputs, its call arguments and the reference's
 outputs in ``golden.npz`` with a JSON index in ``golden.json``.  The fixtures
@@ -64,9 +66,14 @@ def main():
     import wildboar
     from wildboar.distance import (
         argmin_distance,
+        argmin_subsequence_distance,
+        distance_profile,
         paired_distance,
+        paired_subsequence_distance,
+        paired_subsequence_match,
         pairwise_distance,
         pairwise_subsequence_distance,
+        subsequence_match,
     )
     from wildboar.distance.dtw import dtw_alignment
 
@@ -214,6 +221,93 @@ def main():
         add(f"subseq_{metric}_{tag}", "subsequence",
             {"x": T2, "shapelets": packed2, "lengths": lens2},
             {"metric": metric, "metric_params": params}, {"d": d, "idx": i})
+
+    def tagof(params, scale=False):
+        t = "_".join(f"{k}{v}" for k, v in params.items())
+        return t + ("_scaled" if scale else "")
+
+    # paired subsequence distance (distance/_distance.py:639-729)
+    T3 = _walk(rng, (6, 70))
+    shp3 = [_walk(rng, (int(n),)) for n in (4, 9, 17, 25, 3, 40)]
+    shp3[2] = T3[2, 5:22].copy()
+    packed3 = np.concatenate(shp3)
+    lens3 = np.array([s.shape[0] for s in shp3])
+    for metric, params in (("euclidean", {}), ("scaled_euclidean", {}), ("dtw", {"r": 0.3}),
+                           ("msm", {}), ("lcss", {"epsilon": 0.8}), ("edr", {}),
+                           ("twe", {"r": 0.5}), ("erp", {"g": 0.1})):
+        d, i = paired_subsequence_distance(shp3, T3, metric=metric, metric_params=params,
+                                           return_index=True)
+        add(f"paired_subseq_{metric}_{tagof(params)}", "paired_subsequence",
+            {"x": T3, "shapelets": packed3, "lengths": lens3},
+            {"metric": metric, "metric_params": params}, {"d": d, "idx": i})
+
+    # argmin subsequence distance (distance/_distance.py:1636-1761): heap order
+    T4 = _walk(rng, (5, 60))
+    S4 = _walk(rng, (5, 12))
+    S4[3] = T4[3, 20:32]
+    for metric, params, scale in (("euclidean", {}, False), ("euclidean", {}, True),
+                                  ("dtw", {"r": 0.3}, False), ("dtw", {}, True),
+                                  ("msm", {}, False), ("adtw", {"p": -0.2}, False),
+                                  ("lcss", {"epsilon": 0.5}, False), ("erp", {}, False),
+                                  ("twe", {}, True)):
+        for k in (1, 4):
+            idx, dist = argmin_subsequence_distance(S4, T4, k=k, metric=metric,
+                                                    metric_params=params, scale=scale,
+                                                    return_distance=True)
+            add(f"argmin_subseq_{metric}_{tagof(params, scale)}_k{k}", "argmin_subsequence",
+                {"x": T4, "y": S4},
+                {"metric": metric, "metric_params": params, "scale": scale, "k": k},
+                {"idx": idx, "dist": dist})
+
+    # distance profile (dilation 1, no padding: distance/_distance.py:1477-1620)
+    T5 = _walk(rng, (4, 50))
+    q5 = _walk(rng, (10,))
+    q5b = T5[2, 7:17].copy()
+    for metric, params in (("euclidean", {}), ("scaled_euclidean", {}), ("dtw", {"r": 0.3}),
+                           ("msm", {}), ("lcss", {"epsilon": 0.6}), ("twe", {}),
+                           ("adtw", {"p": -0.3})):
+        for qi, q in enumerate((q5, q5b)):
+            dp = distance_profile(q, T5, metric=metric, metric_params=params)
+            add(f"profile_{metric}_{tagof(params)}_q{qi}", "distance_profile",
+                {"x": T5, "y": q}, {"metric": metric, "metric_params": params},
+                {"d": dp})
+
+    # subsequence matches (distance/_distance.py:732-1080), stored flat
+    def flat(res):
+        idx, dist = res
+        counts = np.array([0 if a is None else len(a) for a in idx], dtype=np.int64)
+        fi = [np.asarray(a, dtype=np.int64) for a in idx if a is not None]
+        fd = [np.asarray(a, dtype=float) for a in dist if a is not None]
+        return {"counts": counts,
+                "idx": np.concatenate(fi) if fi else np.zeros(0, np.int64),
+                "dist": np.concatenate(fd) if fd else np.zeros(0)}
+
+    for metric, params, kw in (
+            ("euclidean", {}, {"threshold": 4.0}),
+            ("euclidean", {}, {}),
+            ("euclidean", {}, {"threshold": 6.0, "max_matches": 3}),
+            ("euclidean", {}, {"threshold": 6.0, "exclude": 2}),
+            ("euclidean", {}, {"exclude": 0.5}),
+            ("scaled_euclidean", {}, {"threshold": 2.0}),
+            ("dtw", {"r": 0.3}, {"threshold": 3.0}),
+            ("msm", {}, {"max_matches": 5}),
+            ("adtw", {"p": -0.3}, {"threshold": 3.0})):
+        res = subsequence_match(q5b, T5, metric=metric, metric_params=params,
+                                return_distance=True, **kw)
+        tag = tagof(params) + "_" + "_".join(f"{k}{v}" for k, v in kw.items())
+        add(f"match_{metric}_{tag}", "subsequence_match", {"x": T5, "y": q5b},
+            {"metric": metric, "metric_params": params, "kw": kw}, flat(res))
+    shp6 = [T5[i, 3 + i:13 + i].copy() for i in range(4)]
+    for metric, params, kw in (("euclidean", {}, {"threshold": 5.0}),
+                               ("euclidean", {}, {"max_matches": 2}),
+                               ("dtw", {}, {"threshold": 4.0})):
+        res = paired_subsequence_match(shp6, T5, metric=metric, metric_params=params,
+                                       return_distance=True, **kw)
+        tag = tagof(params) + "_" + "_".join(f"{k}{v}" for k, v in kw.items())
+        add(f"paired_match_{metric}_{tag}", "paired_subsequence_match",
+            {"x": T5, "shapelets": np.concatenate(shp6),
+             "lengths": np.array([10, 10, 10, 10])},
+            {"metric": metric, "metric_params": params, "kw": kw}, flat(res))
 
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:

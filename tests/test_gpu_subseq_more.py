@@ -1,0 +1,163 @@
+"""paired_subsequence_distance, argmin_subsequence_distance, distance_profile,
+subsequence_match and paired_subsequence_match on the GPU.
+
+Parity: the reference's own outputs (golden fixtures made by running it,
+tests/golden/make_golden.py) through the public API, and the CPU oracle on
+larger seeded cases.  Distances within 1e-12 relative (the kernels perform
+the reference's operations; 1e-12 absorbs libm differences between
+machines), indices and match sets exact.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():  # pragma: no cover
+    pytest.skip("needs a CUDA device", allow_module_level=True)
+
+from oracle import oracle as O  # noqa: E402
+from tests import _golden  # noqa: E402
+from wildboar_gb300.distance import (  # noqa: E402
+    argmin_subsequence_distance,
+    distance_profile,
+    paired_subsequence_distance,
+    paired_subsequence_match,
+    subsequence_match,
+)
+
+RTOL = 1e-12
+
+
+def _flat(res):
+    idx, dist = res
+    idx = np.atleast_1d(np.asarray(idx, dtype=object)) if not isinstance(idx, np.ndarray) \
+        else idx
+    if idx.dtype != object:  # a single sample's matches come back as one array
+        idx, dist = [idx], [dist]
+    counts = np.array([0 if a is None else len(a) for a in idx], dtype=np.int64)
+    fi = [np.asarray(a, dtype=np.int64) for a in idx if a is not None]
+    fd = [np.asarray(a, dtype=float) for a in dist if a is not None]
+    return (counts, np.concatenate(fi) if fi else np.zeros(0, np.int64),
+            np.concatenate(fd) if fd else np.zeros(0))
+
+
+def _cases(kind):
+    cs = _golden.cases(kind)
+    return pytest.mark.parametrize("case", cs, ids=[c["name"] for c in cs])
+
+
+@_cases("paired_subsequence")
+def test_paired_subsequence_golden(case):
+    a = case["args"]
+    shp = _golden.unpack_shapelets(case)
+    d, i = paired_subsequence_distance(shp, case["inputs"]["x"], metric=a["metric"],
+                                       metric_params=a.get("metric_params"),
+                                       return_index=True)
+    np.testing.assert_allclose(d, case["outputs"]["d"], rtol=RTOL, atol=0)
+    np.testing.assert_array_equal(i, case["outputs"]["idx"])
+
+
+@_cases("argmin_subsequence")
+def test_argmin_subsequence_golden(case):
+    a = case["args"]
+    inp = case["inputs"]
+    idx, dist = argmin_subsequence_distance(inp["y"], inp["x"], k=a["k"], metric=a["metric"],
+                                            metric_params=a.get("metric_params"),
+                                            scale=a["scale"], return_distance=True)
+    np.testing.assert_array_equal(idx, case["outputs"]["idx"])
+    np.testing.assert_allclose(dist, case["outputs"]["dist"], rtol=RTOL, atol=0)
+
+
+@_cases("distance_profile")
+def test_distance_profile_golden(case):
+    a = case["args"]
+    inp = case["inputs"]
+    dp = distance_profile(inp["y"], inp["x"], metric=a["metric"],
+                          metric_params=a.get("metric_params"))
+    np.testing.assert_allclose(dp, case["outputs"]["d"], rtol=RTOL, atol=0)
+
+
+@_cases("subsequence_match")
+def test_subsequence_match_golden(case):
+    a = case["args"]
+    inp = case["inputs"]
+    res = subsequence_match(inp["y"], inp["x"], metric=a["metric"],
+                            metric_params=a.get("metric_params"), return_distance=True,
+                            **a["kw"])
+    counts, idx, dist = _flat(res)
+    np.testing.assert_array_equal(counts, case["outputs"]["counts"])
+    np.testing.assert_array_equal(idx, case["outputs"]["idx"])
+    np.testing.assert_allclose(dist, case["outputs"]["dist"], rtol=RTOL, atol=0)
+
+
+@_cases("paired_subsequence_match")
+def test_paired_subsequence_match_golden(case):
+    a = case["args"]
+    shp = _golden.unpack_shapelets(case)
+    res = paired_subsequence_match(shp, case["inputs"]["x"], metric=a["metric"],
+                                   metric_params=a.get("metric_params"),
+                                   return_distance=True, **a["kw"])
+    counts, idx, dist = _flat(res)
+    np.testing.assert_array_equal(counts, case["outputs"]["counts"])
+    np.testing.assert_array_equal(idx, case["outputs"]["idx"])
+    np.testing.assert_allclose(dist, case["outputs"]["dist"], rtol=RTOL, atol=0)
+
+
+ARGMIN_METRICS = [
+    ("euclidean", {}, False), ("euclidean", {}, True), ("dtw", {"r": 0.2}, False),
+    ("dtw", {"r": 0.5}, True), ("wdtw", {"g": 0.1}, False), ("ddtw", {"r": 0.3}, False),
+    ("ddtw", {}, True), ("adtw", {"p": 0.4}, False), ("adtw", {"p": -0.1}, True),
+    ("lcss", {"epsilon": 0.4}, False), ("edr", {"epsilon": 0.3}, True),
+    ("erp", {"g": 0.1}, False), ("erp", {}, True), ("msm", {"c": 0.7}, False),
+    ("twe", {"penalty": 0.5}, True),
+]
+
+
+@pytest.mark.parametrize("metric,params,scale", ARGMIN_METRICS,
+                         ids=[f"{m}-{s}-{i}" for i, (m, _, s) in enumerate(ARGMIN_METRICS)])
+def test_argmin_subsequence_vs_oracle(metric, params, scale):
+    rng = np.random.default_rng(41)
+    X = np.cumsum(rng.standard_normal((17, 150)), axis=1)
+    lens = rng.integers(8, 40, size=17)
+    Y = [np.cumsum(rng.standard_normal(int(L))) for L in lens]
+    Y[3] = X[3, 50:50 + len(Y[3])].copy()
+    k = 5
+    idx, dist = argmin_subsequence_distance(Y, X, k=k, metric=metric, metric_params=params,
+                                            scale=scale, return_distance=True)
+    oi, od = O.argmin_subsequence(Y, X, k=k, metric=metric, metric_params=params,
+                                  scale=scale)
+    np.testing.assert_array_equal(idx, oi)
+    np.testing.assert_allclose(dist, od, rtol=RTOL, atol=0)
+
+
+PROFILE_METRICS = [("euclidean", {}), ("scaled_euclidean", {}), ("dtw", {"r": 0.3}),
+                   ("wdtw", {"g": 0.2}), ("ddtw", {}), ("adtw", {"p": -0.2}),
+                   ("lcss", {"epsilon": 0.5}), ("edr", {}), ("erp", {"g": 0.3}),
+                   ("msm", {}), ("twe", {"stiffness": 0.01})]
+
+
+@pytest.mark.parametrize("metric,params", PROFILE_METRICS, ids=[m for m, _ in PROFILE_METRICS])
+def test_profile_and_matches_vs_oracle(metric, params):
+    rng = np.random.default_rng(43)
+    X = np.cumsum(rng.standard_normal((9, 120)), axis=1)
+    q = X[4, 30:52].copy() + rng.standard_normal(22) * 0.05
+    dp = distance_profile(q, X, metric=metric, metric_params=params)
+    od, _ = O.subsequence_matches([q] * 9, X, math.inf, metric=metric, metric_params=params,
+                                  transient=True)
+    np.testing.assert_allclose(dp, od, rtol=RTOL, atol=0)
+    # matches at a threshold near the 20th percentile of the profile
+    thr = float(np.nanpercentile(dp, 20))
+    res = subsequence_match(q, X, thr, metric=metric, metric_params=params,
+                            return_distance=True)
+    counts, idx, dist = _flat(res)
+    d2, keep = O.subsequence_matches([q] * 9, X, thr, metric=metric, metric_params=params)
+    want_counts = (keep > 0).sum(axis=1)
+    np.testing.assert_array_equal(counts, want_counts)
+    np.testing.assert_array_equal(idx, np.concatenate(
+        [np.flatnonzero(keep[i] > 0) for i in range(9)]))
+    np.testing.assert_allclose(dist, d2[keep > 0], rtol=RTOL, atol=0)

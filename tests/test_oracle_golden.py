@@ -6,6 +6,7 @@ them bit for bit; elsewhere a libm exp/pow that rounds differently may move
 WDTW weights or EDR epsilons by an ulp, hence the 1e-12 relative fallback.
 """
 
+import math
 import platform
 
 import numpy as np
@@ -75,13 +76,76 @@ def run_oracle(case):
         shp = _golden.unpack_shapelets(case)
         d, i = O.subsequence(shp, inp["x"], metric=metric, metric_params=params)
         return {"d": d, "idx": i}
+    if kind == "paired_subsequence":
+        # _paired_subsequence_distance (distance/_cdistance.pyx:1040-1062) is the
+        # pairwise scan of shapelet i against series i
+        shp = _golden.unpack_shapelets(case)
+        d, i = O.subsequence(shp, inp["x"], metric=metric, metric_params=params)
+        n = len(shp)
+        return {"d": d[np.arange(n), np.arange(n)], "idx": i[np.arange(n), np.arange(n)]}
+    if kind == "argmin_subsequence":
+        idx, dist = O.argmin_subsequence(inp["y"], inp["x"], k=a["k"], metric=metric,
+                                         metric_params=params, scale=a["scale"])
+        return {"idx": idx, "dist": dist}
+    if kind == "distance_profile":
+        X = _ts(inp["x"])
+        q = inp["y"]
+        d, _ = O.subsequence_matches([q] * X.shape[0], X, math.inf, metric=metric,
+                                     metric_params=params, transient=True)
+        return {"d": np.squeeze(d[:, : X.shape[2] - q.shape[0] + 1])}
+    if kind in ("subsequence_match", "paired_subsequence_match"):
+        X = _ts(inp["x"])
+        if kind == "subsequence_match":
+            shp = [inp["y"]] * X.shape[0]
+        else:
+            shp = _golden.unpack_shapelets(case)
+        return oracle_matches(shp, X, metric, params, dict(a["kw"]), kind)
     if kind == "alignment":
         al = O.dtw_alignment(inp["x"], inp["y"], r=a["r"])
         return {"a": np.where(inp["mask"], al, 0.0)}
     raise AssertionError(kind)
 
 
-CASES = _golden.cases()
+ORACLE_KINDS = {"pairwise", "singleton", "paired", "argmin", "subsequence", "alignment",
+                "paired_subsequence"}
+ORACLE_KINDS |= {"argmin_subsequence", "distance_profile", "subsequence_match",
+                 "paired_subsequence_match"}
+CASES = [c for c in _golden.cases() if c["kind"] in ORACLE_KINDS]
+
+
+def oracle_matches(shp, X, metric, params, kw, kind):
+    """The oracle's per-window distances and keep flags, then the reference's
+    host-side filters (distance/_distance.py:400-512, 732-1080)."""
+    from wildboar_gb300.distance import _subsequence as SS
+
+    threshold = kw.get("threshold")
+    max_matches = kw.get("max_matches")
+    exclude = kw.get("exclude")
+    if threshold is None:
+        threshold = math.inf
+        if max_matches is None:
+            max_matches = 10
+    dist, keep = O.subsequence_matches(shp, X, threshold, metric=metric,
+                                       metric_params=params)
+    ind, dis = [], []
+    for i, s in enumerate(shp):
+        nwin = X.shape[2] - len(s) + 1
+        sel = np.flatnonzero(keep[i, :nwin] > 0)
+        ind.append(sel.astype(np.intp) if sel.size else None)
+        dis.append(dist[i, sel] if sel.size else None)
+    if kind == "subsequence_match" and exclude is not None:
+        if isinstance(exclude, float):
+            exclude = math.ceil(len(shp[0]) * exclude)
+        if exclude:
+            ind, dis = SS._exclude_trivial_matches(ind, dis, exclude)
+    if max_matches:
+        ind, dis = SS._filter_by_max_matches(ind, dis, max_matches)
+    counts = np.array([0 if a is None else len(a) for a in ind], dtype=np.int64)
+    fi = [np.asarray(a, dtype=np.int64) for a in ind if a is not None]
+    fd = [np.asarray(a, dtype=float) for a in dis if a is not None]
+    return {"counts": counts,
+            "idx": np.concatenate(fi) if fi else np.zeros(0, np.int64),
+            "dist": np.concatenate(fd) if fd else np.zeros(0)}
 
 
 @pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])

@@ -64,6 +64,12 @@ def _declare(L):
                                      vp, i32, vp]
     L.wb_pairwise_subsequence_distance.argtypes = [vp, vp, vp, vp, vp, i64, P(Series), i64,
                                                    i32, P(Params), vp, vp, i32, vp]
+    L.wb_paired_subsequence_distance.argtypes = [vp, vp, vp, vp, vp, i64, P(Series), i64,
+                                                 i32, P(Params), vp, vp, i32, vp]
+    L.wb_argmin_subsequence_distance.argtypes = [vp, vp, i64, i64, vp, vp, P(Series), i64,
+                                                 i32, P(Params), i32, i64, vp, vp, i32, vp]
+    L.wb_subsequence_profile.argtypes = [vp, vp, vp, vp, vp, i64, P(Series), i64, i32,
+                                         P(Params), vp, vp, i64, i32, i32, vp]
     L.wb_last_error.restype = ctypes.c_char_p
     L.wb_version.restype = i32
     L.wb_release_workspace.argtypes = [vp]

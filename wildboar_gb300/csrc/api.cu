@@ -683,13 +683,19 @@ static int subseq_elastic(const double *shapelets, const int64_t *offsets,
                           const wb_series *x, int64_t dim, int32_t metric,
                           const wb_params *p, double *out_dist, int64_t *out_idx,
                           int32_t out_on_device, cudaStream_t s,
-                          const std::vector<int64_t> &hlen, int64_t total) {
+                          const std::vector<int64_t> &hlen, int64_t total, bool paired,
+                          double *prof_raw = nullptr, double *prof_key = nullptr,
+                          int64_t prof_ld = 0, int std_as_given = 0) {
     if (!(p->r >= 0.0 && p->r <= 1.0)) return fail(WB_EINVAL, "r must be in [0, 1]");
     const bool dev_in = x->on_device != 0;
     const bool slopes = derivative(metric);
     const int T = (int)x->n_timestep;
+    const bool profile = prof_raw != nullptr;
+    const size_t n_out = profile ? (size_t)m * prof_ld * 2 : (paired ? (size_t)m : (size_t)x->n * m);
     SubseqElasticJob J;
     J.m = m;
+    J.paired = paired ? 1 : 0;
+    J.std_as_given = std_as_given;
     J.metric = metric;
     J.slopes = slopes ? 1 : 0;
     J.t_len_thr = T;
@@ -745,7 +751,7 @@ static int subseq_elastic(const double *shapelets, const int64_t *offsets,
                   (slopes ? align256((size_t)x->n * xs_len * 8) + align256(total * 8) : 0) +
                   (metric == WB_ERP ? align256((size_t)x->n * T * 8) + align256(x->n * 8) : 0) +
                   (metric == WB_TWE ? align256((size_t)max_orig * 8 + 8) : 0) +
-                  (out_on_device ? 0 : 2 * align256((size_t)x->n * m * 8));
+                  (out_on_device ? 0 : 2 * align256(n_out * 8));
     WB_TRY(ws.reserve(need));
     WB_TAKE(gring, double, ws, ring / sizeof(double));
     SeriesSet X;
@@ -803,31 +809,58 @@ static int subseq_elastic(const double *shapelets, const int64_t *offsets,
     J.len = dlen;
     J.band_of_len = dband;
     J.shp_std = (metric == WB_EDR && std::isnan(p->epsilon)) ? dstd : nullptr;
+    if (profile) {
+        const size_t np = (size_t)m * prof_ld;
+        double *rr = prof_raw, *kk = prof_key;
+        if (!out_on_device) {
+            rr = ws.take<double>(np);
+            kk = ws.take<double>(np);
+            if (!rr || !kk) return fail(WB_ENOMEM, "workspace reservation exceeded");
+        }
+        J.prof_raw = rr;
+        J.prof_key = kk;
+        J.prof_ld = prof_ld;
+        WB_TRY(launch_elastic_subseq(J, kind, gring, P, grid, s));
+        if (!out_on_device) {
+            WB_CUDA(cudaMemcpyAsync(prof_raw, rr, np * 8, cudaMemcpyDeviceToHost, s));
+            WB_CUDA(cudaMemcpyAsync(prof_key, kk, np * 8, cudaMemcpyDeviceToHost, s));
+        }
+        WB_CUDA(cudaStreamSynchronize(s));
+        return WB_OK;
+    }
     double *od = out_dist;
     int64_t *oi = out_idx;
     if (!out_on_device) {
-        od = ws.take<double>((size_t)x->n * m);
-        oi = ws.take<int64_t>((size_t)x->n * m);
+        od = ws.take<double>(n_out);
+        oi = ws.take<int64_t>(n_out);
         if (!od || !oi) return fail(WB_ENOMEM, "workspace reservation exceeded");
     }
     J.out_dist = od;
     J.out_idx = oi;
     WB_TRY(launch_elastic_subseq(J, kind, gring, P, grid, s));
     if (!out_on_device) {
-        WB_CUDA(cudaMemcpyAsync(out_dist, od, (size_t)x->n * m * 8, cudaMemcpyDeviceToHost, s));
-        WB_CUDA(cudaMemcpyAsync(out_idx, oi, (size_t)x->n * m * 8, cudaMemcpyDeviceToHost, s));
+        WB_CUDA(cudaMemcpyAsync(out_dist, od, n_out * 8, cudaMemcpyDeviceToHost, s));
+        WB_CUDA(cudaMemcpyAsync(out_idx, oi, n_out * 8, cudaMemcpyDeviceToHost, s));
     }
     // host vectors above feed asynchronous copies
     WB_CUDA(cudaStreamSynchronize(s));
     return WB_OK;
 }
 
-extern "C" int wb_pairwise_subsequence_distance(
-    const double *shapelets, const int64_t *offsets, const int64_t *lengths,
-    const double *means, const double *stds, int64_t m, const wb_series *x, int64_t dim,
-    int32_t metric, const wb_params *params, double *out_dist, int64_t *out_idx,
-    int32_t out_on_device, void *stream_) {
+// Shared by the pairwise (every series against every shapelet) and paired
+// (series i against shapelet i) subsequence entries.
+static int subseq_entry(const double *shapelets, const int64_t *offsets, const int64_t *lengths,
+                        const double *means, const double *stds, int64_t m, const wb_series *x,
+                        int64_t dim, int32_t metric, const wb_params *params, double *out_dist,
+                        int64_t *out_idx, int32_t out_on_device, void *stream_, bool paired,
+                        double *prof_raw = nullptr, double *prof_key = nullptr,
+                        int64_t prof_ld = 0, int std_as_given = 0) {
     WB_TRY(check_series(x, "x"));
+    const bool profile = prof_raw != nullptr;
+    if (paired && m != x->n)
+        return fail(WB_EINVAL, "The number of subsequences and samples must be the same, got " +
+                                   std::to_string(m) + " subsequences and " +
+                                   std::to_string(x->n) + " samples.");
     WB_TRY(check_dim(x, dim));
     const bool elastic = is_elastic(metric) && metric != WB_WLCSS;
     if (metric != WB_EUCLIDEAN && metric != WB_SCALED_EUCLIDEAN && !elastic)
@@ -835,7 +868,7 @@ extern "C" int wb_pairwise_subsequence_distance(
     if (elastic && !params) return fail(WB_EINVAL, "params is NULL");
     if (m < 0) return fail(WB_EINVAL, "negative number of shapelets");
     if (m == 0 || x->n == 0) return WB_OK;
-    if (!shapelets || !offsets || !lengths || !out_dist || !out_idx)
+    if (!shapelets || !offsets || !lengths || (!profile && (!out_dist || !out_idx)))
         return fail(WB_EINVAL, "NULL shapelet or output array");
     const bool scaled = metric == WB_SCALED_EUCLIDEAN;
     if (scaled && (!means || !stds)) return fail(WB_EINVAL, "scaled metric needs means and stds");
@@ -858,10 +891,14 @@ extern "C" int wb_pairwise_subsequence_distance(
                                        " > " + std::to_string(x->n_timestep) + ")");
         if (hoff[i] < 0) return fail(WB_EINVAL, "negative shapelet offset");
         total = std::max(total, hoff[i] + hlen[i]);
+        if (profile && x->n_timestep - hlen[i] + 1 > prof_ld)
+            return fail(WB_EINVAL, "ld is smaller than the number of windows");
     }
     if (elastic)
         return subseq_elastic(shapelets, offsets, lengths, stds, m, x, dim, metric, params,
-                              out_dist, out_idx, out_on_device, s, hlen, total);
+                              out_dist, out_idx, out_on_device, s, hlen, total, paired,
+                              prof_raw, prof_key, prof_ld, std_as_given);
+    const size_t n_out = profile ? (size_t)m * prof_ld : (paired ? (size_t)m : (size_t)x->n * m);
     std::vector<int64_t> order(m);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(),
@@ -873,9 +910,29 @@ extern "C" int wb_pairwise_subsequence_distance(
         group_of[i] = (int32_t)group_len.size() - 1;
     }
 
+    // scaled metric: chunks of <= 64 shapelets of one length for the tiled kernel
+    std::vector<int64_t> ch_first;
+    std::vector<int32_t> ch_count, ch_group;
+    int max_len = 0;
+    for (int64_t i = 0; i < m; i++) max_len = std::max<int>(max_len, (int)hlen[i]);
+    const bool tiled = scaled && !paired && max_len <= kScaledTileMaxLen;
+    if (tiled) {
+        for (int64_t t = 0; t < m;) {
+            int64_t u = t;
+            while (u < m && u - t < 64 && group_of[order[u]] == group_of[order[t]]) u++;
+            ch_first.push_back(t);
+            ch_count.push_back((int32_t)(u - t));
+            ch_group.push_back(group_of[order[t]]);
+            t = u;
+        }
+    }
+
     SubseqJob J;
     J.m = m;
     J.n_groups = (int)group_len.size();
+    J.max_len = max_len;
+    J.paired = paired ? 1 : 0;
+    J.std_as_given = std_as_given;
     J.total_values = total;
     J.win_stride = (int)x->n_timestep;
     J.chunk = 64;
@@ -883,7 +940,8 @@ extern "C" int wb_pairwise_subsequence_distance(
     size_t need = stage_bytes(x) + align256(m * 8) * 3 + align256(m * 4) +
                   align256(group_len.size() * 4) +
                   (dev_in ? 0 : align256(total * 8) + 2 * align256(m * 8) + 2 * align256(m * 8)) +
-                  (out_on_device ? 0 : 2 * align256((size_t)x->n * m * 8));
+                  (out_on_device ? 0 : 2 * align256(n_out * 8)) +
+                  align256(ch_first.size() * 8) + 2 * align256(ch_first.size() * 4);
     J.x.count = x->n;
     J.x.len = (int)x->n_timestep;
     need += subseq_workspace_bytes(J, scaled);
@@ -924,19 +982,81 @@ extern "C" int wb_pairwise_subsequence_distance(
     J.order = dorder;
     J.group_of = dgroup;
     J.group_len = dglen;
-    J.out_dist = out_on_device ? out_dist : ws.take<double>((size_t)x->n * m);
-    J.out_idx = out_on_device ? out_idx : ws.take<int64_t>((size_t)x->n * m);
+    if (tiled) {
+        const size_t nc = ch_first.size();
+        WB_TAKE(dcf, int64_t, ws, nc);
+        WB_TAKE(dcc, int32_t, ws, nc);
+        WB_TAKE(dcg, int32_t, ws, nc);
+        WB_CUDA(cudaMemcpyAsync(dcf, ch_first.data(), nc * 8, cudaMemcpyHostToDevice, s));
+        WB_CUDA(cudaMemcpyAsync(dcc, ch_count.data(), nc * 4, cudaMemcpyHostToDevice, s));
+        WB_CUDA(cudaMemcpyAsync(dcg, ch_group.data(), nc * 4, cudaMemcpyHostToDevice, s));
+        J.chunk_first = dcf;
+        J.chunk_count = dcc;
+        J.chunk_group = dcg;
+        J.n_chunks = (int64_t)nc;
+    }
+    if (profile) {
+        double *rr = out_on_device ? prof_raw : ws.take<double>(n_out);
+        if (!rr) return fail(WB_ENOMEM, "workspace reservation exceeded");
+        WB_TRY(launch_subseq_profile(J, scaled, ws, rr, prof_ld));
+        if (prof_key) {
+            // the euclidean sums have no abandoning rows: key -inf
+            if (out_on_device) {
+                WB_TRY(launch_fill(prof_key, -HUGE_VAL, (int64_t)n_out, s));
+            } else {
+                std::vector<double> kk(n_out, -HUGE_VAL);
+                std::memcpy(prof_key, kk.data(), n_out * 8);
+            }
+        }
+        if (!out_on_device)
+            WB_CUDA(cudaMemcpyAsync(prof_raw, rr, n_out * 8, cudaMemcpyDeviceToHost, s));
+        WB_CUDA(cudaStreamSynchronize(s));
+        return WB_OK;
+    }
+    J.out_dist = out_on_device ? out_dist : ws.take<double>(n_out);
+    J.out_idx = out_on_device ? out_idx : ws.take<int64_t>(n_out);
     if (!J.out_dist || !J.out_idx) return fail(WB_ENOMEM, "workspace reservation exceeded");
     WB_TRY(launch_subseq(J, scaled, ws));
     if (!out_on_device) {
-        WB_CUDA(cudaMemcpyAsync(out_dist, J.out_dist, (size_t)x->n * m * 8,
-                                cudaMemcpyDeviceToHost, s));
-        WB_CUDA(cudaMemcpyAsync(out_idx, J.out_idx, (size_t)x->n * m * 8,
-                                cudaMemcpyDeviceToHost, s));
+        WB_CUDA(cudaMemcpyAsync(out_dist, J.out_dist, n_out * 8, cudaMemcpyDeviceToHost, s));
+        WB_CUDA(cudaMemcpyAsync(out_idx, J.out_idx, n_out * 8, cudaMemcpyDeviceToHost, s));
     }
     // the host vectors above feed asynchronous copies
     WB_CUDA(cudaStreamSynchronize(s));
     return WB_OK;
+}
+
+extern "C" int wb_pairwise_subsequence_distance(
+    const double *shapelets, const int64_t *offsets, const int64_t *lengths,
+    const double *means, const double *stds, int64_t m, const wb_series *x, int64_t dim,
+    int32_t metric, const wb_params *params, double *out_dist, int64_t *out_idx,
+    int32_t out_on_device, void *stream_) {
+    return subseq_entry(shapelets, offsets, lengths, means, stds, m, x, dim, metric, params,
+                        out_dist, out_idx, out_on_device, stream_, false);
+}
+
+extern "C" int wb_subsequence_profile(const double *shapelets, const int64_t *offsets,
+                                      const int64_t *lengths, const double *means,
+                                      const double *stds, int64_t m, const wb_series *x,
+                                      int64_t dim, int32_t metric, const wb_params *params,
+                                      double *out_raw, double *out_key, int64_t ld,
+                                      int32_t std_as_given, int32_t out_on_device,
+                                      void *stream_) {
+    if (!out_raw) return fail(WB_EINVAL, "out_raw is NULL");
+    if (!out_key && metric != WB_EUCLIDEAN && metric != WB_SCALED_EUCLIDEAN)
+        return fail(WB_EINVAL, "out_key is NULL");
+    return subseq_entry(shapelets, offsets, lengths, means, stds, m, x, dim, metric, params,
+                        nullptr, nullptr, out_on_device, stream_, true, out_raw, out_key, ld,
+                        std_as_given ? 1 : 0);
+}
+
+extern "C" int wb_paired_subsequence_distance(
+    const double *shapelets, const int64_t *offsets, const int64_t *lengths,
+    const double *means, const double *stds, int64_t m, const wb_series *x, int64_t dim,
+    int32_t metric, const wb_params *params, double *out_dist, int64_t *out_idx,
+    int32_t out_on_device, void *stream_) {
+    return subseq_entry(shapelets, offsets, lengths, means, stds, m, x, dim, metric, params,
+                        out_dist, out_idx, out_on_device, stream_, true);
 }
 
 extern "C" const char *wb_last_error(void) { return g_last_error.c_str(); }

@@ -103,6 +103,13 @@ struct SubseqElasticJob {
     const double *stab = nullptr;  // twe: (2 stiffness) k
     double *out_dist = nullptr;
     int64_t *out_idx = nullptr;
+    int paired = 0;  // series i against shapelet i only (x.count == m), outputs (m,)
+    // profile (paired only): every window's final recurrence value and abandon
+    // key at [pair * prof_ld + window] instead of the minimum
+    double *prof_raw = nullptr;
+    double *prof_key = nullptr;
+    int64_t prof_ld = 0;
+    int std_as_given = 0;  // a zero shapelet std gives epsilon 0 (distance profile)
 };
 size_t elastic_subseq_ring_bytes(const SubseqElasticJob &J, int max_len, int max_band,
                                  int *P_out, int *grid_out);
@@ -110,6 +117,15 @@ int launch_elastic_subseq(const SubseqElasticJob &J, int kind, double *gring, in
                           cudaStream_t s);
 int launch_shapelet_slopes(const double *shp, const int64_t *off, const int64_t *len,
                            int64_t m, double *out, cudaStream_t s);
+
+// argmin_subsequence_distance (argmin_subseq.cu)
+struct ArgminSubseqJob;
+int wb_argmin_subsequence_impl(const double *s, const int64_t *s_len, int64_t s_stride,
+                               int64_t n, const double *s_mean, const double *s_std,
+                               const wb_series *x, int64_t dim, int32_t metric,
+                               const wb_params *params, int32_t scaled, int64_t k,
+                               int64_t *indices, double *distances, int32_t out_on_device,
+                               cudaStream_t stream);
 
 // register-strip kernels of every elastic metric, FP64 (exact) or FP32
 // (compensated) (elastic_strip.cu)

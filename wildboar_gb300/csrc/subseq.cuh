@@ -20,11 +20,28 @@ struct SubseqJob {
     int64_t total_values = 0;
     int win_stride = 0;                  // row stride of the window-stat tables
     int chunk = 64;                      // shapelets per block
+    // scaled metric, tiled kernel: chunks of <= chunk shapelets of one length
+    // (positions [chunk_first, chunk_first + chunk_count) of `order`)
+    const int64_t *chunk_first = nullptr;
+    const int32_t *chunk_count = nullptr;
+    const int32_t *chunk_group = nullptr;
+    int64_t n_chunks = 0;
+    int max_len = 0;
+    // paired: series i against shapelet i only (x.count == m); outputs (m,),
+    // window-stat tables one row per series at its shapelet's length
+    int paired = 0;
+    int std_as_given = 0;  // a zero std divides as is (distance profile's transient stats)
     double *out_dist = nullptr;          // (x.count, m)
     int64_t *out_idx = nullptr;          // (x.count, m)
 };
 
 size_t subseq_workspace_bytes(const SubseqJob &J, bool scaled);
+// longest shapelet the tiled scaled kernel takes (its z-normalised window
+// tile is L x 32 doubles of shared memory)
+constexpr int kScaledTileMaxLen = 384;
 int launch_subseq(const SubseqJob &J, bool scaled, Workspace &ws);
+// paired jobs: every window's full sum at raw[pair * ld + window]
+int launch_subseq_profile(const SubseqJob &J, bool scaled, Workspace &ws, double *raw,
+                          int64_t ld);
 
 }  // namespace wb

@@ -6,16 +6,28 @@ from ._distance import (
     check_metric,
     check_subsequence_metric,
     paired_distance,
+    paired_subsequence_distance,
     pairwise_distance,
     pairwise_subsequence_distance,
 )
 from ._metrics import _METRICS, _SUBSEQUENCE_METRICS
+from ._subsequence import (
+    argmin_subsequence_distance,
+    distance_profile,
+    paired_subsequence_match,
+    subsequence_match,
+)
 
 __all__ = [
     "pairwise_distance",
     "paired_distance",
     "argmin_distance",
     "pairwise_subsequence_distance",
+    "paired_subsequence_distance",
+    "distance_profile",
+    "argmin_subsequence_distance",
+    "subsequence_match",
+    "paired_subsequence_match",
     "check_metric",
     "check_subsequence_metric",
     "InvalidParameterError",

@@ -453,25 +453,9 @@ def _pack_shapelets(shapelets, scaled):
     return packed, offs, lens, means, stds
 
 
-def pairwise_subsequence_distance(y, x, *, dim=0, metric="euclidean", metric_params=None,
-                                  scale=False, return_index=False, n_jobs=None):
-    """Minimum subsequence distance between subsequences and time series.
-
-    Mirrors distance/_distance.py:543-636 for the euclidean and
-    scaled_euclidean subsequence metrics.
-    """
-    y = _validate_subsequence(y)
-    X = _as_input(x)
-    for s in y:
-        if s.shape[0] > X.shape[-1]:
-            raise ValueError(
-                "Invalid subsequnce shape (%d > %d)" % (s.shape[0], X.shape[-1])
-            )
-    Metric_ = check_subsequence_metric(metric, scale=scale)
-    metric_params = metric_params or {}
-    metric = Metric_(**metric_params)
-    if not (0 <= dim < X.shape[1]):
-        raise ValueError("The parameter dim must be 0 <= dim < n_dims")
+def _subsequence_call(y, X, dim, metric, paired):
+    """Run the pairwise ((n_x, m) outputs) or paired ((m,) outputs) subsequence
+    entry for validated shapelets y and input X."""
     packed, offs, lens, means, stds = _pack_shapelets(
         y, metric.scaled or getattr(metric, "needs_std", False))
     dev = _device_of(X)
@@ -486,17 +470,76 @@ def pairwise_subsequence_distance(y, x, *, dim=0, metric="euclidean", metric_par
         if means is not None:
             means = torch.as_tensor(means, device=devc)
             stds = torch.as_tensor(stds, device=devc)
-    dist = _empty(dev, (X.shape[0], m))
-    idx = _empty(dev, (X.shape[0], m), dtype=np.int64)
+    shape = (m,) if paired else (X.shape[0], m)
+    dist = _empty(dev, shape)
+    idx = _empty(dev, shape, dtype=np.int64)
     sx = X.series()
     p = metric.params() if hasattr(metric, "params") else _lib.Params()
-    st = _lib.lib().wb_pairwise_subsequence_distance(
+    entry = (_lib.lib().wb_paired_subsequence_distance if paired
+             else _lib.lib().wb_pairwise_subsequence_distance)
+    st = entry(
         _lib.ptr(packed), _lib.ptr(offs), _lib.ptr(lens), _lib.ptr(means), _lib.ptr(stds),
         m, ctypes.byref(sx), dim, metric.metric_id, ctypes.byref(p), _lib.ptr(dist),
         _lib.ptr(idx), 1 if dev else 0, _stream(X))
     _lib.check(st)
     if dev is None:
         idx = idx.astype(np.intp, copy=False)
+    return dist, idx
+
+
+def pairwise_subsequence_distance(y, x, *, dim=0, metric="euclidean", metric_params=None,
+                                  scale=False, return_index=False, n_jobs=None):
+    """Minimum subsequence distance between subsequences and time series.
+
+    Mirrors distance/_distance.py:543-636: every subsequence in y against
+    every series in x, (n_samples, n_subsequences) outputs.
+    """
+    y = _validate_subsequence(y)
+    X = _as_input(x)
+    for s in y:
+        if s.shape[0] > X.shape[-1]:
+            raise ValueError(
+                "Invalid subsequnce shape (%d > %d)" % (s.shape[0], X.shape[-1])
+            )
+    Metric_ = check_subsequence_metric(metric, scale=scale)
+    metric_params = metric_params or {}
+    metric = Metric_(**metric_params)
+    if not (0 <= dim < X.shape[1]):
+        raise ValueError("The parameter dim must be 0 <= dim < n_dims")
+    dist, idx = _subsequence_call(y, X, dim, metric, paired=False)
+    if return_index:
+        return _format_return(dist, len(y), X.ndim), _format_return(idx, len(y), X.ndim)
+    return _format_return(dist, len(y), X.ndim)
+
+
+def paired_subsequence_distance(y, x, *, dim=0, metric="euclidean", metric_params=None,
+                                scale=False, return_index=False, n_jobs=None):
+    """Minimum subsequence distance between the i:th subsequence and the i:th
+    time series.
+
+    Mirrors distance/_distance.py:639-729 (including its dim check, which
+    accepts dim 0 only, and its messages); outputs have shape (n_samples,).
+    """
+    y = _validate_subsequence(y)
+    X = _as_input(x)
+    n_dims = X.shape[1]
+    if not 0 >= dim < n_dims:
+        raise ValueError("The parameter dim must be 0 <= dim < n_dims")
+    for s in y:
+        if s.shape[0] > X.shape[-1]:
+            raise ValueError(
+                "Invalid subsequnce shape (%d > %d)" % (s.shape[0], X.shape[-1])
+            )
+    Metric_ = check_subsequence_metric(metric, scale=scale)
+    n_samples = X.shape[0] if X.ndim > 1 else 1
+    if len(y) != n_samples:
+        raise ValueError(
+            "The number of subsequences and samples must be the same, got %d "
+            "subsequences and %d samples." % (len(y), n_samples)
+        )
+    metric_params = metric_params if metric_params is not None else {}
+    metric = Metric_(**metric_params)
+    dist, idx = _subsequence_call(y, X, dim, metric, paired=True)
     if return_index:
         return _format_return(dist, len(y), X.ndim), _format_return(idx, len(y), X.ndim)
     return _format_return(dist, len(y), X.ndim)
