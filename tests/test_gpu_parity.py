@@ -64,7 +64,10 @@ def run_api(case):
     return None
 
 
-GOLDEN = [c for c in _golden.cases() if c["kind"] != "alignment"]
+# the subsequence search kinds (paired, argmin, profile, matches) are run by
+# tests/test_gpu_subseq_more.py
+GOLDEN = [c for c in _golden.cases()
+          if c["kind"] in ("pairwise", "singleton", "paired", "argmin", "subsequence")]
 
 
 @pytest.mark.parametrize("case", GOLDEN, ids=[c["name"] for c in GOLDEN])
