@@ -161,3 +161,21 @@ def test_profile_and_matches_vs_oracle(metric, params):
     np.testing.assert_array_equal(idx, np.concatenate(
         [np.flatnonzero(keep[i] > 0) for i in range(9)]))
     np.testing.assert_allclose(dist, d2[keep > 0], rtol=RTOL, atol=0)
+
+
+@pytest.mark.parametrize("metric", ["euclidean", "scaled_euclidean"])
+def test_min_scan_near_ties_vs_oracle(metric):
+    # periodic series: many windows tie or nearly tie with the best one, so the
+    # FP32 pre-filter must keep every window that can still be the first minimum
+    from wildboar_gb300.distance import pairwise_subsequence_distance
+
+    rng = np.random.default_rng(44)
+    t = np.arange(600)
+    base = np.sin(t * 2 * np.pi / 37.0) * 3.0 + 50.0
+    X = np.stack([base + rng.standard_normal(600) * s for s in (0.0, 1e-9, 1e-6, 1e-3, 0.1)])
+    shp = [base[k:k + L].copy() for k, L in ((0, 37), (5, 74), (11, 20), (3, 111))]
+    shp += [base[0:50] + 1e-7, np.full(16, 50.0), rng.standard_normal(40)]
+    d, i = pairwise_subsequence_distance(shp, X, metric=metric, return_index=True)
+    od, oi = O.subsequence(shp, X, metric=metric)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(d, od)

@@ -14,6 +14,20 @@
 // reference keeps (scaled_euclidean_distance, distance/_metric.pyx:561-622);
 // those sums depend only on (series, length), so one thread per (series,
 // length) reproduces their exact sequence into a table first.
+//
+// FP32 pre-filter.  Once a scan has a best sum b, a window is first summed in
+// FP32 on float copies t', s' of its values; it is evaluated in FP64 only if
+// that cannot prove its FP64 sum d64 > b.  With u = 2^-24, e = u (max|t| +
+// max|s|) bounding |(t - s) - (t' - s')| per element, and d32 the FP32 sum
+// (one rounding per subtraction and per fused multiply-add):
+//   sqrt(d64) >= (sqrt(d32 / F) - e sqrt(L)) (1 - g),
+//   F = 1 + (L + 4) u 1.01,  g = (L + 4) 2^-53 1.01
+// (sums of non-negative terms; the triangle inequality in the 2-norm for the
+// input rounding).  So d32 > F (sqrt(b)(1 + g) + e sqrt(L))^2, rounded up to
+// float, implies d64 > b: such a window can be neither the minimum nor the
+// first window attaining it, exactly as if the FP64 sum had been abandoned.
+// Partial FP32 sums only grow, so the filter abandons early too.  Results are
+// unchanged; only the number of FP64 evaluations drops.
 
 #include "subseq.cuh"
 
@@ -66,6 +80,40 @@ __global__ void shapelet_norm_kernel(const SubseqJob J, double *norm) {
     }
 }
 
+// float threshold of the FP32 pre-filter for best FP64 sum `best`
+__device__ __forceinline__ float filter_threshold(double best, double e, int L) {
+    if (!(best < __longlong_as_double(0x7ff0000000000000LL)))
+        return __int_as_float(0x7f800000);
+    const double F = 1.0 + (double)(L + 4) * 5.9604644775390625e-08 * 1.01;
+    const double g = (double)(L + 4) * 1.1102230246251565e-16 * 1.01;
+    const double root = sqrt(best) * (1.0 + g) + e * sqrt((double)L);
+    return __double2float_ru(F * root * root * (1.0 + 1e-12));
+}
+
+// float copies of packed shapelet values and the max |value| of each
+__global__ void shapelet_f32_kernel(const double *src, const int64_t *off, const int64_t *len,
+                                    int64_t m, float *dst, double *absmax) {
+    __shared__ double red[32];
+    for (int64_t s = blockIdx.x; s < m; s += gridDim.x) {
+        const int L = (int)len[s];
+        double mx = 0.0;
+        for (int k = threadIdx.x; k < L; k += blockDim.x) {
+            const double v = src[off[s] + k];
+            dst[off[s] + k] = (float)v;
+            mx = fmax(mx, fabs(v));
+        }
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double a = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) a = fmax(a, red[w]);
+            absmax[s] = a;
+        }
+    }
+}
+
 constexpr int kSubThreads = 128;
 constexpr int kSubWarps = kSubThreads / 32;
 
@@ -79,14 +127,28 @@ subseq_scan_kernel(const SubseqJob J, const double *norm, const double *mean_tab
     const int64_t chunks = (J.m + J.chunk - 1) / J.chunk;
     const int nt = J.x.len;
     double *T = wb_smem_sub;
+    float *Tf = reinterpret_cast<float *>(T + nt);          // nt floats (unscaled filter)
+    unsigned int *tmax = reinterpret_cast<unsigned int *>(Tf + nt + (nt & 1));
+    const bool filt = !SCALED && J.shp_f32 != nullptr;
     for (int64_t b = blockIdx.x; b < J.x.count * chunks; b += gridDim.x) {
         const int64_t si = b / chunks;
         const int64_t c0 = (b - si * chunks) * J.chunk;
         const int64_t c1 = c0 + J.chunk < J.m ? c0 + J.chunk : J.m;
         __syncthreads();
-        const double *Tg = J.x.base + si * J.x.stride;
-        for (int i = threadIdx.x; i < nt; i += kSubThreads) T[i] = Tg[i];
+        if (filt && threadIdx.x == 0) *tmax = 0u;
         __syncthreads();
+        const double *Tg = J.x.base + si * J.x.stride;
+        for (int i = threadIdx.x; i < nt; i += kSubThreads) {
+            const double v = Tg[i];
+            T[i] = v;
+            if (filt) {
+                Tf[i] = (float)v;
+                // max |t| as a float rounded up (non-negative: integer order)
+                atomicMax(tmax, __float_as_uint(__double2float_ru(fabs(v))));
+            }
+        }
+        __syncthreads();
+        const double MT = filt ? (double)__uint_as_float(*tmax) : 0.0;
         for (int64_t sh = c0 + wid; sh < c1; sh += kSubWarps) {
             const int64_t idx = J.order ? J.order[sh] : sh;
             const int L = (int)J.lengths[idx];
@@ -100,10 +162,26 @@ subseq_scan_kernel(const SubseqJob J, const double *norm, const double *mean_tab
             }
             double best = INF;
             int bidx = 0;
+            const float *Sf = filt ? J.shp_f32 + J.offsets[idx] : nullptr;
+            const double e = filt ? 5.9604644775390625e-08 * (MT + J.shp_absmax[idx]) + 1e-37
+                                  : 0.0;
+            float thr32 = __int_as_float(0x7f800000);
             for (int base = 0; base < nwin; base += 32) {
                 const int w = base + lane;
                 double dist = INF;
-                if (w < nwin) {
+                bool cand = w < nwin;
+                if (filt && cand && best < INF) {
+                    float d32 = 0.0f;
+                    for (int k = 0; k < L; k++) {
+                        const float y = __fsub_rn(Tf[w + k], __ldg(Sf + k));
+                        d32 = __fmaf_rn(y, y, d32);
+                        if (d32 > thr32) {
+                            cand = false;
+                            break;
+                        }
+                    }
+                }
+                if (cand) {
                     dist = 0.0;
                     if (SCALED) {
                         const double mean = mt[w];
@@ -138,6 +216,7 @@ subseq_scan_kernel(const SubseqJob J, const double *norm, const double *mean_tab
                 if (v < best) {
                     best = v;
                     bidx = vi;
+                    if (filt) thr32 = filter_threshold(best, e, L);
                 }
             }
             if (lane == 0) {
@@ -168,6 +247,9 @@ subseq_scaled_tiled_kernel(const SubseqJob J, const double *norm, const double *
     double *best = T + nt;                        // chunk
     int *bidx = reinterpret_cast<int *>(best + J.chunk);  // chunk
     double *Z = best + J.chunk + (J.chunk + 1) / 2;      // [max_len][32]
+    float *Zf = reinterpret_cast<float *>(Z + (size_t)J.max_len * 32);  // [max_len][32]
+    unsigned int *zmax = reinterpret_cast<unsigned int *>(Zf + (size_t)J.max_len * 32);
+    const bool filt = J.shp_f32 != nullptr;
     for (int64_t b = blockIdx.x; b < J.x.count * J.n_chunks; b += gridDim.x) {
         const int64_t si = b / J.n_chunks;
         const int64_t ch = b - si * J.n_chunks;
@@ -188,20 +270,44 @@ subseq_scaled_tiled_kernel(const SubseqJob J, const double *norm, const double *
         }
         for (int base = 0; base < nwin; base += 32) {
             __syncthreads();
+            if (threadIdx.x == 0) *zmax = 0u;
+            __syncthreads();
             for (int e = threadIdx.x; e < L * 32; e += kSubThreads) {
                 const int k = e >> 5, w = e & 31;
                 double z = 0.0;
                 if (base + w < nwin) z = (T[base + w + k] - mt[base + w]) / st[base + w];
                 Z[e] = z;
+                if (filt) {
+                    Zf[e] = (float)z;
+                    atomicMax(zmax, __float_as_uint(__double2float_ru(fabs(z))));
+                }
             }
             __syncthreads();
+            const double MZ = filt ? (double)__uint_as_float(*zmax) : 0.0;
             const int w = base + lane;
             for (int q = wid; q < cnt; q += kSubWarps) {
                 const int64_t idx = J.order[first + q];
                 const double *S = norm + J.offsets[idx];
                 const double bq = best[q];
                 double dist = INF;
-                if (w < nwin) {
+                bool cand = w < nwin;
+                if (filt && cand && bq < INF) {
+                    // FP32 pre-filter (see the file header); e bounds the
+                    // rounding of z and of the normalised shapelet to float
+                    const double e = 5.9604644775390625e-08 * (MZ + J.shp_absmax[idx]) + 1e-37;
+                    const float thr32 = filter_threshold(bq, e, L);
+                    const float *Sf = J.shp_f32 + J.offsets[idx];
+                    float d32 = 0.0f;
+                    for (int k = 0; k < L; k++) {
+                        const float y = __fsub_rn(__ldg(Sf + k), Zf[k * 32 + lane]);
+                        d32 = __fmaf_rn(y, y, d32);
+                        if (d32 > thr32) {
+                            cand = false;
+                            break;
+                        }
+                    }
+                }
+                if (cand) {
                     dist = 0.0;
                     for (int k = 0; k < L; k++) {
                         if (dist >= bq) break;
@@ -375,7 +481,7 @@ int launch_subseq_profile(const SubseqJob &J, bool scaled, Workspace &ws, double
 
 static size_t scaled_tiled_smem(const SubseqJob &J) {
     return (size_t)J.x.len * 8 + (size_t)J.chunk * 8 + (size_t)((J.chunk + 1) / 2) * 8 +
-           (size_t)J.max_len * 32 * 8;
+           (size_t)J.max_len * 32 * 8 + (size_t)J.max_len * 32 * 4 + 16;
 }
 
 static int sub_grid(int64_t n, int block) {
@@ -386,10 +492,26 @@ static int sub_grid(int64_t n, int block) {
 }
 
 size_t subseq_workspace_bytes(const SubseqJob &J, bool scaled) {
-    if (!scaled) return 0;
+    // FP32 copies of the (normalised) shapelets and their max |value|
+    const size_t filt = align256((size_t)J.total_values * sizeof(float)) +
+                        align256((size_t)J.m * sizeof(double));
+    if (!scaled) return filt;
     const size_t rows = J.paired ? (size_t)J.x.count : (size_t)J.n_groups * J.x.count;
     size_t tab = rows * J.win_stride * sizeof(double);
-    return 2 * align256(tab) + align256((size_t)J.total_values * sizeof(double));
+    return 2 * align256(tab) + align256((size_t)J.total_values * sizeof(double)) + filt;
+}
+
+static int make_f32_copies(const SubseqJob &J, const double *src, Workspace &ws,
+                           SubseqJob &out) {
+    float *f = ws.take<float>((size_t)J.total_values);
+    double *mx = ws.take<double>((size_t)J.m);
+    if (!f || !mx) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    shapelet_f32_kernel<<<(int)(J.m < 65535 ? J.m : 65535), 128, 0, ws.stream()>>>(
+        src, J.offsets, J.lengths, J.m, f, mx);
+    WB_LAUNCH_CHECK("shapelet_f32_kernel");
+    out.shp_f32 = f;
+    out.shp_absmax = mx;
+    return WB_OK;
 }
 
 int launch_subseq(const SubseqJob &J, bool scaled, Workspace &ws) {
@@ -422,13 +544,15 @@ int launch_subseq(const SubseqJob &J, bool scaled, Workspace &ws) {
         }
         const size_t tsm = scaled_tiled_smem(J);
         if (J.n_chunks > 0 && tsm <= (size_t)device_info().max_smem_optin) {
+            SubseqJob Jf = J;
+            WB_TRY(make_f32_copies(J, norm, ws, Jf));
             auto kt = subseq_scaled_tiled_kernel;
             WB_CUDA(cudaFuncSetAttribute(kt, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)tsm));
             const int64_t tb = J.x.count * J.n_chunks;
             const int tgrid = (int)(tb < cap ? tb : cap);
             timer_begin("subseq_scaled_tiled_kernel", s);
-            kt<<<tgrid, kSubThreads, tsm, s>>>(J, norm, mean_tab, std_tab);
+            kt<<<tgrid, kSubThreads, tsm, s>>>(Jf, norm, mean_tab, std_tab);
             timer_end(s);
             WB_LAUNCH_CHECK("subseq_scaled_tiled_kernel");
             return WB_OK;
@@ -446,10 +570,14 @@ int launch_subseq(const SubseqJob &J, bool scaled, Workspace &ws) {
         timer_end(s);
         WB_LAUNCH_CHECK("subseq_paired_kernel");
     } else {
+        SubseqJob Jf = J;
+        WB_TRY(make_f32_copies(J, J.shapelets, ws, Jf));
+        // T (doubles), its float copy and the max |t| word
+        const size_t fsmem = (size_t)J.x.len * 12 + 16;
         auto k = subseq_scan_kernel<false>;
-        WB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        WB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
         timer_begin("subseq_scan_kernel", s);
-        k<<<grid, kSubThreads, smem, s>>>(J, nullptr, nullptr, nullptr);
+        k<<<grid, kSubThreads, fsmem, s>>>(Jf, nullptr, nullptr, nullptr);
         timer_end(s);
         WB_LAUNCH_CHECK("subseq_scan_kernel");
     }

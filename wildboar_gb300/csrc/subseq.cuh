@@ -31,6 +31,9 @@ struct SubseqJob {
     // window-stat tables one row per series at its shapelet's length
     int paired = 0;
     int std_as_given = 0;  // a zero std divides as is (distance profile's transient stats)
+    // FP32 pre-filter of the minimum scans (set by launch_subseq)
+    const float *shp_f32 = nullptr;      // packed shapelets (z-normalised when scaled)
+    const double *shp_absmax = nullptr;  // (m,) max |value| of each packed shapelet
     double *out_dist = nullptr;          // (x.count, m)
     int64_t *out_idx = nullptr;          // (x.count, m)
 };
