@@ -13,12 +13,13 @@
 // products' own error, ~1e-7 of the norms, dominates) and the result is
 // stored as float64 through a shared-memory transpose (coalesced rows).
 //
-// Kernel: one CTA per 128 x 128 output tile, 128 threads.  Thread 0 issues
-// the TMA loads (128-byte swizzled K-major tiles of 32 floats) into a
-// 3-stage ring and the MMAs (M=128, N=128, K=8, 12 per stage); tcgen05.commit
-// frees a stage; the accumulator (128 lanes x 128 columns of TMEM) is read
-// back by the four warps with tcgen05.ld.  Every mbarrier wait is bounded: a
-// wait that runs out sets an error flag, the CTA still releases its TMEM.
+// Kernel: persistent, one CTA per SM over 128 x 128 output tiles, 192
+// threads: a TMA producer warp (128-byte swizzled K-major tiles of 32 floats
+// into a 3-stage ring), an MMA warp (M=128, N=128, K=8, 12 MMAs per stage,
+// tcgen05.commit frees a stage) and four epilogue warps that read the
+// accumulators back with tcgen05.ld while the next tile accumulates into the
+// second TMEM buffer.  Every mbarrier wait is bounded: a wait that runs out
+// sets an error flag, the CTA still releases its TMEM.
 
 #include <cuda.h>
 
@@ -33,12 +34,12 @@ constexpr int kBM = 128, kBN = 128, kBK = 32;  // kBK floats = 128 bytes (one sw
 constexpr int kStages = 3;
 constexpr int kTileBytes = kBM * kBK * 4;      // 16 KB per operand tile
 constexpr int kStageBytes = 4 * kTileBytes;    // A hi, A lo, B hi, B lo
-constexpr int kGemmThreads = 128;
-// four accumulators of 128 columns: consecutive quarters of K accumulate
-// separately in FP32 and are added with TwoSum by the epilogue, which cuts
-// the accumulation error of long K by ~4x
-constexpr int kNumAcc = 4;
-constexpr int kTmemCols = kBN * kNumAcc;
+constexpr int kGemmThreads = 192;  // producer warp, MMA warp, 4 epilogue warps
+// per output tile kNumAcc accumulators of 128 columns: consecutive halves of
+// K accumulate separately in FP32 and are added with TwoSum by the epilogue;
+// two such buffers fill the 512 TMEM columns
+constexpr int kNumAcc = 2;
+constexpr int kTmemCols = kBN * kNumAcc * 2;
 constexpr long long kWaitLimit = 1ll << 26;
 
 // TwoSum (Knuth): returns s = fl(a + b) and sets e so that s + e == a + b exactly
@@ -120,37 +121,79 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
         : "memory");
 }
 
+// Persistent, warp-specialised: one CTA per SM walks the output tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ...  Warp 0 (one lane) streams the
+// operand tiles with TMA into a kStages-deep ring; warp 1 owns the tensor
+// memory and (one lane) issues the MMAs; warps 2-5 run the epilogue, warp w
+// reading TMEM lanes 32 (w % 4) .. +31.  Two accumulator buffers let the
+// epilogue of tile t overlap the MMAs of tile t + 1: each buffer holds
+// kNumAcc accumulators of 128 columns (consecutive parts of K).
+//   full[s]  : TMA bytes of stage s landed        (producer -> MMA)
+//   empty[s] : MMAs reading stage s completed     (MMA -> producer)
+//   accf[b]  : all MMAs of buffer b's tile done   (MMA -> epilogue)
+//   acce[b]  : epilogue finished reading buffer b (epilogue -> MMA, 4 arrivals)
+// Every wait is bounded; one that runs out raises a shared abort flag that
+// the other roles poll, the error word is set, and the CTA still waits for its
+// issued MMAs before releasing the tensor memory.
+__device__ __forceinline__ bool bwait(uint32_t bar, uint32_t parity, volatile int *abort_flag) {
+    for (long long i = 0; i < kWaitLimit; i++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if ((i & 1023) == 1023 && *abort_flag) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 __global__ void __launch_bounds__(kGemmThreads, 1)
 euclid_tc_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
                  const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
                  const float2 *__restrict__ nx, const float2 *__restrict__ ny, int M, int N,
                  int Kp, double *out, int64_t ld_out, int *err) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    // 1024-byte aligned stage ring
     unsigned char *smem =
         (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    double *stage_out = reinterpret_cast<double *>(smem + kStages * kStageBytes);
     __shared__ __align__(8) uint64_t full_bar[kStages];
     __shared__ __align__(8) uint64_t empty_bar[kStages];
+    __shared__ __align__(8) uint64_t accf_bar[2];
+    __shared__ __align__(8) uint64_t acce_bar[2];
     __shared__ __align__(8) uint64_t done_bar;
     __shared__ uint32_t tmem_slot;
-    __shared__ int abort_flag;
+    __shared__ volatile int abort_flag;
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5;
-    const int m0 = blockIdx.y * kBM;
-    const int n0 = blockIdx.x * kBN;
+    const int lane = tid & 31;
     const int KT = Kp / kBK;
+    const int tiles_n = (N + kBN - 1) / kBN;
+    const int ntiles = ((M + kBM - 1) / kBM) * tiles_n;
+    const int per_acc = (KT + kNumAcc - 1) / kNumAcc;  // k tiles per accumulator
 
     if (tid == 0) {
         for (int s = 0; s < kStages; s++) {
             mbar_init(smem_u32(&full_bar[s]), 1);
             mbar_init(smem_u32(&empty_bar[s]), 1);
         }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(smem_u32(&accf_bar[b]), 1);
+            mbar_init(smem_u32(&acce_bar[b]), 4);
+        }
         mbar_init(smem_u32(&done_bar), 1);
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) {
+    if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(&tmem_slot)),
                      "r"(kTmemCols)
@@ -161,133 +204,164 @@ euclid_tc_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_slot;
+    auto stage_ptr = [&](int st, int which) { return smem + st * kStageBytes + which * kTileBytes; };
 
-    if (tid == 0) {
-        auto stage_ptr = [&](int s, int which) { return smem + s * kStageBytes + which * kTileBytes; };
-        auto issue_loads = [&](int kt, int s) {
-            const uint32_t bar = smem_u32(&full_bar[s]);
-            mbar_expect_tx(bar, kStageBytes);
-            const int kc = kt * kBK;
-            tma_load_2d(smem_u32(stage_ptr(s, 0)), &mAhi, kc, m0, bar);
-            tma_load_2d(smem_u32(stage_ptr(s, 1)), &mAlo, kc, m0, bar);
-            tma_load_2d(smem_u32(stage_ptr(s, 2)), &mBhi, kc, n0, bar);
-            tma_load_2d(smem_u32(stage_ptr(s, 3)), &mBlo, kc, n0, bar);
-        };
-        uint32_t full_phase = 0, empty_phase = 0;  // one parity bit per stage
-        const int pre = KT < kStages ? KT : kStages;
-        const int per_acc = (KT + kNumAcc - 1) / kNumAcc;  // k tiles per accumulator
-        for (int kt = 0; kt < pre; kt++) issue_loads(kt, kt);
-        bool ok = true;
-        for (int kt = 0; kt < KT && ok; kt++) {
-            const int s = kt % kStages;
-            ok = mbar_wait(smem_u32(&full_bar[s]), (full_phase >> s) & 1u);
-            full_phase ^= 1u << s;
-            if (!ok) break;
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t ahi = smem_u32(stage_ptr(s, 0)), alo = smem_u32(stage_ptr(s, 1));
-            const uint32_t bhi = smem_u32(stage_ptr(s, 2)), blo = smem_u32(stage_ptr(s, 3));
-            const int acc = kt / per_acc;
-            const uint32_t dtm = tmem + (uint32_t)(acc * kBN);
-            const bool first = (kt % per_acc) == 0;
-#pragma unroll
-            for (int kk = 0; kk < kBK / 8; kk++) {
-                const uint32_t off = kk * 32;  // 8 tf32 = 32 bytes along K
-                const uint64_t dAh = smem_desc_sw128(ahi + off), dAl = smem_desc_sw128(alo + off);
-                const uint64_t dBh = smem_desc_sw128(bhi + off), dBl = smem_desc_sw128(blo + off);
-                mma_tf32(dtm, dAh, dBh, (!first || kk > 0) ? 1u : 0u);
-                mma_tf32(dtm, dAh, dBl, 1u);
-                mma_tf32(dtm, dAl, dBh, 1u);
-            }
-            mma_commit(smem_u32(&empty_bar[s]));
-            // refill the stage used one iteration ago once its MMAs are done
-            if (kt >= 1) {
-                const int sp = (kt - 1) % kStages;
-                const int knext = kt - 1 + kStages;
-                if (knext < KT) {
-                    ok = mbar_wait(smem_u32(&empty_bar[sp]), (empty_phase >> sp) & 1u);
-                    empty_phase ^= 1u << sp;
-                    if (ok) issue_loads(knext, sp);
+    if (warp == 0) {
+        // ---------------- producer
+        if (lane == 0) {
+            int st = 0;
+            uint32_t ph = 0;
+            bool ok = true;
+            for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+                const int m0 = (tile / tiles_n) * kBM, n0 = (tile % tiles_n) * kBN;
+                for (int kt = 0; kt < KT; kt++) {
+                    ok = bwait(smem_u32(&empty_bar[st]), ph ^ 1u, &abort_flag);
+                    if (!ok) break;
+                    const uint32_t bar = smem_u32(&full_bar[st]);
+                    mbar_expect_tx(bar, kStageBytes);
+                    const int kc = kt * kBK;
+                    tma_load_2d(smem_u32(stage_ptr(st, 0)), &mAhi, kc, m0, bar);
+                    tma_load_2d(smem_u32(stage_ptr(st, 1)), &mAlo, kc, m0, bar);
+                    tma_load_2d(smem_u32(stage_ptr(st, 2)), &mBhi, kc, n0, bar);
+                    tma_load_2d(smem_u32(stage_ptr(st, 3)), &mBlo, kc, n0, bar);
+                    if (++st == kStages) {
+                        st = 0;
+                        ph ^= 1u;
+                    }
                 }
             }
+            if (!ok) {
+                abort_flag = 1;
+                atomicExch(err, 1);
+            }
         }
-        if (!ok) {
+    } else if (warp == 1) {
+        // ---------------- MMA issuer
+        if (lane == 0) {
+            int st = 0;
+            uint32_t ph = 0;
+            bool ok = true;
+            int it = 0;
+            for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, it++) {
+                const int b = it & 1;
+                const uint32_t bph = (uint32_t)(it >> 1) & 1u;
+                ok = bwait(smem_u32(&acce_bar[b]), bph ^ 1u, &abort_flag);
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                for (int kt = 0; kt < KT; kt++) {
+                    ok = bwait(smem_u32(&full_bar[st]), ph, &abort_flag);
+                    if (!ok) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t ahi = smem_u32(stage_ptr(st, 0)), alo = smem_u32(stage_ptr(st, 1));
+                    const uint32_t bhi = smem_u32(stage_ptr(st, 2)), blo = smem_u32(stage_ptr(st, 3));
+                    const int acc = kt / per_acc;
+                    const uint32_t dtm = tmem + (uint32_t)((b * kNumAcc + acc) * kBN);
+                    const bool first = (kt % per_acc) == 0;
+#pragma unroll
+                    for (int kk = 0; kk < kBK / 8; kk++) {
+                        const uint32_t off = kk * 32;  // 8 tf32 = 32 bytes along K
+                        const uint64_t dAh = smem_desc_sw128(ahi + off), dAl = smem_desc_sw128(alo + off);
+                        const uint64_t dBh = smem_desc_sw128(bhi + off), dBl = smem_desc_sw128(blo + off);
+                        mma_tf32(dtm, dAh, dBh, (!first || kk > 0) ? 1u : 0u);
+                        mma_tf32(dtm, dAh, dBl, 1u);
+                        mma_tf32(dtm, dAl, dBh, 1u);
+                    }
+                    mma_commit(smem_u32(&empty_bar[st]));
+                    if (++st == kStages) {
+                        st = 0;
+                        ph ^= 1u;
+                    }
+                }
+                if (!ok) break;
+                mma_commit(smem_u32(&accf_bar[b]));
+            }
+            if (!ok) {
+                abort_flag = 1;
+                atomicExch(err, 1);
+            }
+            // no MMA may still be running when the tensor memory is released
+            mma_commit(smem_u32(&done_bar));
+            if (!mbar_wait(smem_u32(&done_bar), 0u)) atomicExch(err, 1);
+        }
+    } else {
+        // ---------------- epilogue (warps 2..5)
+        const int q = warp & 3;  // TMEM lane quarter this warp may read
+        double *tile_s = stage_out + (warp - 2) * (32 * 17);
+        int it = 0;
+        bool ok = true;
+        for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, it++) {
+            const int m0 = (tile / tiles_n) * kBM, n0 = (tile % tiles_n) * kBN;
+            const int b = it & 1;
+            const uint32_t bph = (uint32_t)(it >> 1) & 1u;
+            ok = bwait(smem_u32(&accf_bar[b]), bph, &abort_flag);
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int row = q * 32 + lane;
+            const int gi = m0 + row;
+            const float2 nxi = gi < M ? nx[gi] : make_float2(0.0f, 0.0f);
+            const int used = (KT + per_acc - 1) / per_acc;
+#pragma unroll 1
+            for (int c0 = 0; c0 < kBN; c0 += 16) {
+                float sh[16], sl[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) sh[j] = sl[j] = 0.0f;
+#pragma unroll 1
+                for (int a = 0; a < used; a++) {
+                    uint32_t v[16];
+                    const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) +
+                                           (uint32_t)((b * kNumAcc + a) * kBN + c0);
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                          "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]),
+                          "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                        : "r"(taddr));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        float e;
+                        sh[j] = two_sum(sh[j], __uint_as_float(v[j]), e);
+                        sl[j] = __fadd_rn(sl[j], e);
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int gj = n0 + c0 + j;
+                    const float2 nyj = gj < N ? ny[gj] : make_float2(0.0f, 0.0f);
+                    // d2 = (nx + ny) - 2 dot with every rounding error carried
+                    float e1, e2;
+                    const float s1 = two_sum(nxi.x, nyj.x, e1);
+                    const float t = two_sum(s1, __fmul_rn(-2.0f, sh[j]), e2);
+                    const float corr = __fsub_rn(__fadd_rn(__fadd_rn(e1, e2), __fadd_rn(nxi.y, nyj.y)),
+                                                 __fmul_rn(2.0f, sl[j]));
+                    const float d2 = __fadd_rn(t, corr);
+                    tile_s[lane * 17 + j] = (double)sqrtf(d2 > 0.0f ? d2 : 0.0f);
+                }
+                __syncwarp();
+                // 32 rows x 16 columns: each half-warp writes one row's 16 values
+#pragma unroll 4
+                for (int r2 = 0; r2 < 32; r2 += 2) {
+                    const int r = r2 + (lane >> 4);
+                    const int gr = m0 + q * 32 + r;
+                    const int gj = n0 + c0 + (lane & 15);
+                    if (gr < M && gj < N) out[(int64_t)gr * ld_out + gj] = tile_s[r * 17 + (lane & 15)];
+                }
+                __syncwarp();
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&acce_bar[b]));
+        }
+        if (!ok && lane == 0) {
             abort_flag = 1;
             atomicExch(err, 1);
         }
-        // tracks every MMA issued so far, also after an abort, so that no MMA
-        // is in flight when the TMEM is released
-        mma_commit(smem_u32(&done_bar));
-    }
-    __syncthreads();
-    bool ok = mbar_wait(smem_u32(&done_bar), 0);
-    if (abort_flag) ok = false;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (ok) {
-        const int lane = tid & 31;
-        const int row = warp * 32 + lane;  // TMEM lane = accumulator row
-        const int gi = m0 + row;
-        const float2 nxi = gi < M ? nx[gi] : make_float2(0.0f, 0.0f);
-        const int KTn = Kp / kBK;
-        const int used = (KTn + ((KTn + kNumAcc - 1) / kNumAcc) - 1) / ((KTn + kNumAcc - 1) / kNumAcc);
-        // the stage ring is idle once done_bar has fired: 32 x 33 doubles per warp
-        double *tile = reinterpret_cast<double *>(smem) + warp * (32 * 33);
-#pragma unroll 1
-        for (int c0 = 0; c0 < kBN; c0 += 32) {
-          float sh[32], sl[32];
-#pragma unroll
-          for (int j = 0; j < 32; j++) sh[j] = sl[j] = 0.0f;
-#pragma unroll 1
-          for (int a = 0; a < used; a++) {
-            uint32_t v[32];
-            const uint32_t taddr =
-                tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * kBN + c0);
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-                "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-                  "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
-                  "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]),
-                  "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-                  "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
-                  "=r"(v[30]), "=r"(v[31])
-                : "r"(taddr));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-            for (int j = 0; j < 32; j++) {
-                float e;
-                sh[j] = two_sum(sh[j], __uint_as_float(v[j]), e);
-                sl[j] = __fadd_rn(sl[j], e);
-            }
-          }
-#pragma unroll
-          for (int j = 0; j < 32; j++) {
-              const int gj = n0 + c0 + j;
-              const float2 nyj = gj < N ? ny[gj] : make_float2(0.0f, 0.0f);
-              // d2 = (nx + ny) - 2 dot with every rounding error carried
-              float e1, e2;
-              const float s1 = two_sum(nxi.x, nyj.x, e1);
-              const float t = two_sum(s1, __fmul_rn(-2.0f, sh[j]), e2);
-              const float corr = __fsub_rn(__fadd_rn(__fadd_rn(e1, e2), __fadd_rn(nxi.y, nyj.y)),
-                                           __fmul_rn(2.0f, sl[j]));
-              const float d2 = __fadd_rn(t, corr);
-              tile[lane * 33 + j] = (double)sqrtf(d2 > 0.0f ? d2 : 0.0f);
-          }
-          __syncwarp();
-          const int gj = n0 + c0 + lane;
-#pragma unroll 4
-          for (int r = 0; r < 32; r++) {
-              const int gr = m0 + warp * 32 + r;
-              if (gr < M && gj < N) out[(int64_t)gr * ld_out + gj] = tile[r * 33 + lane];
-          }
-          __syncwarp();
-        }
-    } else if (tid == 0) {
-        atomicExch(err, 1);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0) {
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                      "r"(kTmemCols)
                      : "memory");
@@ -389,10 +463,12 @@ int euclid_tc(const double *x, int64_t sx, int M, const double *y, int64_t sy, i
     WB_TRY(make_map(&mAl, alo, Mp, Kp));
     WB_TRY(make_map(&mBh, bhi, Np, Kp));
     WB_TRY(make_map(&mBl, blo, Np, Kp));
-    const int smem = kStages * kStageBytes + 1024;
+    // stage ring + 4 epilogue staging blocks of 32 x 17 doubles + alignment slack
+    const int smem = kStages * kStageBytes + 4 * 32 * 17 * 8 + 1024;
     WB_CUDA(cudaFuncSetAttribute(euclid_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  smem));
-    dim3 grid(Np / kBN, Mp / kBM);
+    const int ntiles = (Mp / kBM) * (Np / kBN);
+    const int grid = std::min(ntiles, device_info().sm_count);
     timer_begin("euclid_tc_kernel", s);
     euclid_tc_kernel<<<grid, kGemmThreads, smem, s>>>(mAh, mAl, mBh, mBl, nxv, nyv, M, N, Kp,
                                                       out, ld_out, err);
