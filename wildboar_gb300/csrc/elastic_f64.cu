@@ -197,6 +197,96 @@ size_t elastic_workspace_bytes(const ElasticJob &J) {
     return align256(pl.gring_bytes);
 }
 
+// --------------------------------------------------------------------------
+// Euclidean pairwise distance, tiled: a block computes a 64 x 64 tile of
+// (row series i, column series j) pairs, 4 x 4 per thread, staging 32 values
+// of each of the 64 + 64 series in shared memory per step.  Every pair's sum
+// still runs k = 0 .. L-1 in order with the reference's operations (v = y_k -
+// x_k, dist = dist + v * v; euclidean_distance with one window,
+// distance/_metric.pyx:654-682), so results are bit-identical; the tiling
+// only replaces the per-lane strided row reads of the thread-per-pair kernel
+// (whose speed depended on the L1 carve-out) by shared-memory reuse.
+constexpr int kEuT = 64, kEuK = 32;
+
+__global__ void __launch_bounds__(256) euclid_tiled_kernel(const ElasticJob J) {
+    __shared__ double xs[kEuK][kEuT + 1];
+    __shared__ double ys[kEuK][kEuT + 1];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int L = J.rows.len;
+    const int64_t tiles_c = (J.cols.count + kEuT - 1) / kEuT;
+    const int64_t tiles_r = (J.rows.count + kEuT - 1) / kEuT;
+    for (int64_t t = blockIdx.x; t < tiles_r * tiles_c; t += gridDim.x) {
+        const int64_t tr = t / tiles_c, tc = t - (t / tiles_c) * tiles_c;
+        if (J.mode == PM_UPPER && tr > tc) continue;  // the mirror tile fills it
+        const int64_t r0 = tr * kEuT, c0 = tc * kEuT;
+        double acc[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) acc[a][b] = 0.0;
+        for (int k0 = 0; k0 < L; k0 += kEuK) {
+            __syncthreads();
+            for (int e = threadIdx.x; e < kEuK * kEuT; e += 256) {
+                const int s = e / kEuK, k = e - (e / kEuK) * kEuK;
+                const int64_t ri = r0 + s, ci = c0 + s;
+                double xv = 0.0, yv = 0.0;
+                if (k0 + k < L) {
+                    if (ri < J.rows.count) xv = J.rows.base[ri * J.rows.stride + k0 + k];
+                    if (ci < J.cols.count) yv = J.cols.base[ci * J.cols.stride + k0 + k];
+                }
+                xs[k][s] = xv;
+                ys[k][s] = yv;
+            }
+            __syncthreads();
+            const int kn = L - k0 < kEuK ? L - k0 : kEuK;
+            for (int k = 0; k < kn; k++) {
+                double xv[4], yv[4];
+#pragma unroll
+                for (int a = 0; a < 4; a++) xv[a] = xs[k][ty + 16 * a];
+#pragma unroll
+                for (int b = 0; b < 4; b++) yv[b] = ys[k][tx + 16 * b];
+#pragma unroll
+                for (int a = 0; a < 4; a++)
+#pragma unroll
+                    for (int b = 0; b < 4; b++) {
+                        double v = yv[b];
+                        v = v - xv[a];
+                        acc[a][b] = acc[a][b] + v * v;
+                    }
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            const int64_t i = r0 + ty + 16 * a;
+            if (i >= J.rows.count) continue;
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                const int64_t j = c0 + tx + 16 * b;
+                if (j >= J.cols.count) continue;
+                if (J.mode == PM_UPPER) {
+                    if (i >= j) continue;
+                    const double d = J.all_zero ? 0.0 : sqrt(acc[a][b]);
+                    J.out[i * J.out_ld + j] = d;
+                    J.out[j * J.out_ld + i] = d;
+                } else {
+                    J.out[i * J.out_ld + j] = J.all_zero ? 0.0 : sqrt(acc[a][b]);
+                }
+            }
+        }
+    }
+}
+
+static int launch_euclid_tiled(const ElasticJob &J, cudaStream_t s) {
+    const int64_t tiles = ((J.rows.count + kEuT - 1) / kEuT) * ((J.cols.count + kEuT - 1) / kEuT);
+    const int64_t cap = (int64_t)device_info().sm_count * 8;
+    const int grid = (int)(tiles < cap ? tiles : cap);
+    timer_begin("euclid_tiled_kernel", s);
+    euclid_tiled_kernel<<<grid, 256, 0, s>>>(J);
+    timer_end(s);
+    WB_LAUNCH_CHECK("euclid_tiled_kernel");
+    return WB_OK;
+}
+
 int launch_elastic(const ElasticJob &J, Workspace &ws, size_t *) {
     if (J.rows.count == 0 || J.cols.count == 0) return WB_OK;
     if (use_strip_f64(J)) return launch_strip(J, ws, false);
@@ -214,7 +304,10 @@ int launch_elastic(const ElasticJob &J, Workspace &ws, size_t *) {
         case K_ERP: return launch_kind<K_ERP>(J, ws, pl.P, pl.gring, gring, pl.grid);
         case K_MSM: return launch_kind<K_MSM>(J, ws, pl.P, pl.gring, gring, pl.grid);
         case K_TWE: return launch_kind<K_TWE>(J, ws, pl.P, pl.gring, gring, pl.grid);
-        case K_EUCLID: return launch_kind<K_EUCLID>(J, ws, 2, false, nullptr, pl.grid);
+        case K_EUCLID:
+            if (J.mode != PM_PAIRED && J.key == nullptr && J.rows.len == J.cols.len)
+                return launch_euclid_tiled(J, ws.stream());
+            return launch_kind<K_EUCLID>(J, ws, 2, false, nullptr, pl.grid);
     }
     return fail(WB_EINVAL, "unknown elastic kernel");
 }
