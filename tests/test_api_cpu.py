@@ -161,3 +161,53 @@ def test_params_struct_matches_header():
     # wb_params is seven doubles in declaration order
     assert ctypes.sizeof(_lib.Params) == 7 * 8
     assert ctypes.sizeof(_lib.Series) == 8 + 3 * 8 + 2 * 4
+
+
+def test_subsequence_search_validation():
+    # the checks of distance/_distance.py:639-1761 run before any device call
+    from wildboar_gb300.distance import (
+        argmin_subsequence_distance,
+        distance_profile,
+        paired_subsequence_distance,
+        paired_subsequence_match,
+        subsequence_match,
+    )
+
+    X = np.cumsum(np.random.default_rng(0).standard_normal((4, 30)), axis=1)
+    with pytest.raises(ValueError, match="same"):
+        paired_subsequence_distance([X[0, :5], X[1, :5]], X)
+    with pytest.raises(ValueError, match="Invalid subsequnce shape"):
+        paired_subsequence_distance([np.zeros(40)] * 4, X)
+    with pytest.raises(ValueError, match="dim"):
+        paired_subsequence_distance([X[i, :5] for i in range(4)], X.reshape(4, 1, 30), dim=1)
+    with pytest.raises(ValueError, match="single subsequence"):
+        subsequence_match([X[0, :5], X[1, :5]], X)
+    with pytest.raises(TypeError, match="threshold"):
+        subsequence_match(X[0, :5], X, threshold=object())
+    with pytest.raises(ValueError, match="threshold array length"):
+        subsequence_match(X[0, :5], X, threshold=[1.0, 2.0])
+    with pytest.raises(ValueError, match="threshold must be"):
+        subsequence_match(X[0, :5], X, threshold="median")
+    with pytest.raises(ValueError, match="exclude"):
+        subsequence_match(X[0, :5], X, threshold=1.0, exclude=-1)
+    with pytest.raises(ValueError, match="same number of samples"):
+        paired_subsequence_match([X[0, :5]], X)
+    with pytest.raises(ValueError, match="k must be less"):
+        argmin_subsequence_distance(X[:, :10], X, k=30)
+    with pytest.raises(ValueError, match="same number of samples"):
+        argmin_subsequence_distance(X[:2, :10], X)
+    with pytest.raises(ValueError, match="shorter than samples"):
+        argmin_subsequence_distance(np.zeros((4, 40)), X)
+    with pytest.raises(ValueError, match="same number of samples"):
+        distance_profile(X[:2, :10], X)
+    with pytest.raises(ValueError, match="larger than input"):
+        distance_profile(np.zeros(40), X, metric="euclidean")
+    with pytest.raises(NotImplementedError):
+        distance_profile(X[0, :5], X)  # the FFT 'mass' metric
+
+
+def test_sharded_requires_process_group():
+    from wildboar_gb300.distance import sharded
+
+    with pytest.raises(ValueError):
+        sharded.shard_bounds(3, -1, 2)

@@ -242,11 +242,6 @@ def distance_profile(y, x, *, dilation=1, padding=0, dim=0, metric="mass",
     (the SubsequenceMetric profile); the dilated / padded path and the FFT
     'mass' metric are not provided.
     """
-    if dilation != 1 or padding != 0:
-        raise NotImplementedError("only dilation=1 and padding=0 are provided")
-    if metric == "mass":
-        raise NotImplementedError("the 'mass' metric is not provided; use "
-                                  "metric='scaled_euclidean'")
     y = np.asarray(y, dtype=float).squeeze()
     xa = x
     if not _lib.is_torch_cuda(x):
@@ -265,6 +260,11 @@ def distance_profile(y, x, *, dilation=1, padding=0, dim=0, metric="mass",
         raise ValueError("y and x must have the same number of samples.")
     if dim >= X.shape[1]:
         raise ValueError(f"The parameter dim must be dim ({dim}) < n_dims ({X.shape[1]})")
+    if dilation != 1 or padding != 0:
+        raise NotImplementedError("only dilation=1 and padding=0 are provided")
+    if metric == "mass":
+        raise NotImplementedError("the 'mass' metric is not provided; use "
+                                  "metric='scaled_euclidean'")
     Metric_ = check_subsequence_metric(metric, scale=scale)
     metric_params = metric_params if metric_params is not None else {}
     m = Metric_(**metric_params)
