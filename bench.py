@@ -42,6 +42,12 @@ WORKLOAD = {
     "params": {"r": 0.1},
 }
 FP64_OPS_PER_CELL = 3  # v = x - y, v * v, min + v*v (mins run on the integer pipe)
+# DRAM bytes (read + write) of one launch of the headline kernel at 2000 x 2000,
+# L = 512, from one ncu capture of `python bench.py --no-cpu --no-forms --steps 2
+# --warmup 3` (dram__bytes_read.sum 17.12 MB + dram__bytes_write.sum 10.75 KB;
+# profiles/elastic_pairs_dtw_f64_2000x2000_L512.md).  The 32 MB output is still in
+# L2 when the kernel ends.
+HEADLINE_DRAM_BYTES = 17.12e6 + 10.75e3
 
 
 def _rank():
@@ -603,7 +609,10 @@ def run_gpu(args):
         "peak": fp64_peak / 1e12,
         "unit": "TFLOP/s (FP64 add+mul, peak measured by wb_alu_probe in this run)",
         "frac": achieved / fp64_peak,
-        "traffic": None,
+        # measured for the default 2000 x 2000 workload only
+        "traffic": HEADLINE_DRAM_BYTES if (wl["nx"], wl["ny"]) == (2000, 2000) else None,
+        "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+        "algorithmic_bytes": int(X.nbytes + Y.nbytes + wl["nx"] * wl["ny"] * 8),
         "kernel": "elastic_pairs_kernel<K_DTW>",
         "kernel_ms": k_avg,
         "ops_per_cell": FP64_OPS_PER_CELL,
