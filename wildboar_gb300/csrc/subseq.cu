@@ -80,19 +80,32 @@ __global__ void shapelet_norm_kernel(const SubseqJob J, double *norm) {
     }
 }
 
-// float threshold of the FP32 pre-filter for best FP64 sum `best`
-__device__ __forceinline__ float filter_threshold(double best, double e, int L) {
-    if (!(best < __longlong_as_double(0x7ff0000000000000LL)))
-        return __int_as_float(0x7f800000);
-    const double F = 1.0 + (double)(L + 4) * 5.9604644775390625e-08 * 1.01;
-    const double g = (double)(L + 4) * 1.1102230246251565e-16 * 1.01;
-    const double root = sqrt(best) * (1.0 + g) + e * sqrt((double)L);
-    return __double2float_ru(F * root * root * (1.0 + 1e-12));
+// Comparisons of the (non-negative or +inf) sums run on their bit patterns:
+// for x, y >= +0 the IEEE order is the signed 64-bit order, so the integer
+// pipe takes them and the FP64 pipe only does the sums.
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+
+// Float threshold of the FP32 pre-filter, computed in FP32 with every
+// operation rounded up (so it is at least the bound of the file header):
+// bf >= best (the FP64 sum rounded up), e >= 2^-24 (max|t| + max|s|); the
+// factor 1 + 2^-22 covers the FP64 rounding term g and F uses 6.1e-8 > 1.01
+// 2^-24.  FP32 keeps the per-tile recomputation off the FP64 pipe.
+__device__ __forceinline__ float filter_threshold(float bf, float e, int L) {
+    if (isinf(bf)) return __int_as_float(0x7f800000);
+    const float F = __fadd_ru(1.0f, __fmul_ru((float)(L + 4), 6.1e-8f));
+    const float sb = __fsqrt_ru(bf);
+    const float root = __fadd_ru(__fmul_ru(sb, 1.0000003f), __fmul_ru(e, __fsqrt_ru((float)L)));
+    return __fmul_ru(F, __fmul_ru(root, root));
+}
+
+// e = 2^-24 (max|t| + max|s|) rounded up, plus an absolute term for subnormals
+__device__ __forceinline__ float filter_e(float mt, float ms) {
+    return __fadd_ru(__fmul_ru(5.9604644775390625e-08f, __fadd_ru(mt, ms)), 1e-37f);
 }
 
 // float copies of packed shapelet values and the max |value| of each
 __global__ void shapelet_f32_kernel(const double *src, const int64_t *off, const int64_t *len,
-                                    int64_t m, float *dst, double *absmax) {
+                                    int64_t m, float *dst, float *absmax) {
     __shared__ double red[32];
     for (int64_t s = blockIdx.x; s < m; s += gridDim.x) {
         const int L = (int)len[s];
@@ -109,7 +122,7 @@ __global__ void shapelet_f32_kernel(const double *src, const int64_t *off, const
         if (threadIdx.x == 0) {
             double a = 0.0;
             for (int w = 0; w < (int)(blockDim.x >> 5); w++) a = fmax(a, red[w]);
-            absmax[s] = a;
+            absmax[s] = __double2float_ru(a);
         }
     }
 }
@@ -130,6 +143,7 @@ subseq_scan_kernel(const SubseqJob J, const double *norm, const double *mean_tab
     float *Tf = reinterpret_cast<float *>(T + nt);          // nt floats (unscaled filter)
     unsigned int *tmax = reinterpret_cast<unsigned int *>(Tf + nt + (nt & 1));
     const bool filt = !SCALED && J.shp_f32 != nullptr;
+    __shared__ int wqueue[kSubWarps][64];
     for (int64_t b = blockIdx.x; b < J.x.count * chunks; b += gridDim.x) {
         const int64_t si = b / chunks;
         const int64_t c0 = (b - si * chunks) * J.chunk;
@@ -148,7 +162,7 @@ subseq_scan_kernel(const SubseqJob J, const double *norm, const double *mean_tab
             }
         }
         __syncthreads();
-        const double MT = filt ? (double)__uint_as_float(*tmax) : 0.0;
+        const float MT = filt ? __uint_as_float(*tmax) : 0.0f;
         for (int64_t sh = c0 + wid; sh < c1; sh += kSubWarps) {
             const int64_t idx = J.order ? J.order[sh] : sh;
             const int L = (int)J.lengths[idx];
@@ -163,14 +177,63 @@ subseq_scan_kernel(const SubseqJob J, const double *norm, const double *mean_tab
             double best = INF;
             int bidx = 0;
             const float *Sf = filt ? J.shp_f32 + J.offsets[idx] : nullptr;
-            const double e = filt ? 5.9604644775390625e-08 * (MT + J.shp_absmax[idx]) + 1e-37
-                                  : 0.0;
+            const float e = filt ? filter_e(MT, J.shp_absmax[idx]) : 0.0f;
             float thr32 = __int_as_float(0x7f800000);
+            // Windows that pass the filter wait in a FIFO (ascending window
+            // order) and are summed in FP64 32 at a time, so the FP64 pipe
+            // works on full warps.  The order of evaluation stays ascending,
+            // so "first strictly smaller" keeps its meaning.
+            int *wq = wqueue[wid];
+            int qh = 0, qn = 0;
+            auto eval_batch = [&](int cnt) {
+                double dist = INF;
+                int w = 0x7fffffff;
+                if (lane < cnt) {
+                    w = wq[(qh + lane) & 63];
+                    dist = 0.0;
+                    if (SCALED) {
+                        const double mean = mt[w];
+                        const double sd = st[w];
+                        for (int k = 0; k < L; k++) {
+                            if (dbits(dist) >= dbits(best)) break;
+                            double x = __ldg(S + k);
+                            x = x - (T[w + k] - mean) / sd;
+                            dist = dist + x * x;
+                        }
+                    } else {
+                        for (int k = 0; k < L; k++) {
+                            if (dbits(dist) >= dbits(best)) break;
+                            double x = T[w + k];
+                            x = x - __ldg(S + k);
+                            dist = dist + x * x;
+                        }
+                    }
+                    if (!(dbits(dist) < dbits(best))) dist = INF;
+                }
+                // lexicographic (dist, window) minimum over the warp
+                double v = dist;
+                int vi = w;
+                for (int o = 16; o > 0; o >>= 1) {
+                    double ov = __shfl_xor_sync(0xffffffffu, v, o);
+                    int oi = __shfl_xor_sync(0xffffffffu, vi, o);
+                    if (dbits(ov) < dbits(v) || (dbits(ov) == dbits(v) && oi < vi)) {
+                        v = ov;
+                        vi = oi;
+                    }
+                }
+                if (dbits(v) < dbits(best)) {
+                    best = v;
+                    bidx = vi;
+                    if (filt) thr32 = filter_threshold(__double2float_ru(best), e, L);
+                }
+                qh = (qh + cnt) & 63;
+                qn -= cnt;
+                __syncwarp();
+            };
             for (int base = 0; base < nwin; base += 32) {
                 const int w = base + lane;
-                double dist = INF;
                 bool cand = w < nwin;
-                if (filt && cand && best < INF) {
+                if (filt && cand && dbits(best) < dbits(INF)) {
                     float d32 = 0.0f;
                     for (int k = 0; k < L; k++) {
                         const float y = __fsub_rn(Tf[w + k], __ldg(Sf + k));
@@ -181,44 +244,13 @@ subseq_scan_kernel(const SubseqJob J, const double *norm, const double *mean_tab
                         }
                     }
                 }
-                if (cand) {
-                    dist = 0.0;
-                    if (SCALED) {
-                        const double mean = mt[w];
-                        const double sd = st[w];
-                        for (int k = 0; k < L; k++) {
-                            if (dist >= best) break;
-                            double x = __ldg(S + k);
-                            x = x - (T[w + k] - mean) / sd;
-                            dist = dist + x * x;
-                        }
-                    } else {
-                        for (int k = 0; k < L; k++) {
-                            if (dist >= best) break;
-                            double x = T[w + k];
-                            x = x - __ldg(S + k);
-                            dist = dist + x * x;
-                        }
-                    }
-                    if (!(dist < best)) dist = INF;
-                }
-                // lexicographic (dist, window) minimum over the warp
-                double v = dist;
-                int vi = w;
-                for (int o = 16; o > 0; o >>= 1) {
-                    double ov = __shfl_xor_sync(0xffffffffu, v, o);
-                    int oi = __shfl_xor_sync(0xffffffffu, vi, o);
-                    if (ov < v || (ov == v && oi < vi)) {
-                        v = ov;
-                        vi = oi;
-                    }
-                }
-                if (v < best) {
-                    best = v;
-                    bidx = vi;
-                    if (filt) thr32 = filter_threshold(best, e, L);
-                }
+                const unsigned mask = __ballot_sync(0xffffffffu, cand);
+                if (cand) wq[(qh + qn + __popc(mask & ((1u << lane) - 1u))) & 63] = w;
+                qn += __popc(mask);
+                __syncwarp();
+                if (qn >= 32) eval_batch(32);
             }
+            if (qn > 0) eval_batch(qn);
             if (lane == 0) {
                 J.out_dist[si * J.m + idx] = sqrt(best);
                 J.out_idx[si * J.m + idx] = bidx;
@@ -246,7 +278,8 @@ subseq_scaled_tiled_kernel(const SubseqJob J, const double *norm, const double *
     double *T = wb_smem_sub;                      // nt
     double *best = T + nt;                        // chunk
     int *bidx = reinterpret_cast<int *>(best + J.chunk);  // chunk
-    double *Z = best + J.chunk + (J.chunk + 1) / 2;      // [max_len][32]
+    float *bestf = reinterpret_cast<float *>(bidx + J.chunk);  // chunk: best rounded up
+    double *Z = best + 2 * J.chunk;               // [max_len][32]
     float *Zf = reinterpret_cast<float *>(Z + (size_t)J.max_len * 32);  // [max_len][32]
     unsigned int *zmax = reinterpret_cast<unsigned int *>(Zf + (size_t)J.max_len * 32);
     const bool filt = J.shp_f32 != nullptr;
@@ -266,6 +299,7 @@ subseq_scaled_tiled_kernel(const SubseqJob J, const double *norm, const double *
         for (int i = threadIdx.x; i < nt; i += kSubThreads) T[i] = Tg[i];
         for (int q = threadIdx.x; q < cnt; q += kSubThreads) {
             best[q] = INF;
+            bestf[q] = __int_as_float(0x7f800000);
             bidx[q] = 0;
         }
         for (int base = 0; base < nwin; base += 32) {
@@ -283,7 +317,7 @@ subseq_scaled_tiled_kernel(const SubseqJob J, const double *norm, const double *
                 }
             }
             __syncthreads();
-            const double MZ = filt ? (double)__uint_as_float(*zmax) : 0.0;
+            const float MZ = filt ? __uint_as_float(*zmax) : 0.0f;
             const int w = base + lane;
             for (int q = wid; q < cnt; q += kSubWarps) {
                 const int64_t idx = J.order[first + q];
@@ -291,11 +325,11 @@ subseq_scaled_tiled_kernel(const SubseqJob J, const double *norm, const double *
                 const double bq = best[q];
                 double dist = INF;
                 bool cand = w < nwin;
-                if (filt && cand && bq < INF) {
+                if (filt && cand && dbits(bq) < dbits(INF)) {
                     // FP32 pre-filter (see the file header); e bounds the
                     // rounding of z and of the normalised shapelet to float
-                    const double e = 5.9604644775390625e-08 * (MZ + J.shp_absmax[idx]) + 1e-37;
-                    const float thr32 = filter_threshold(bq, e, L);
+                    const float thr32 =
+                        filter_threshold(bestf[q], filter_e(MZ, J.shp_absmax[idx]), L);
                     const float *Sf = J.shp_f32 + J.offsets[idx];
                     float d32 = 0.0f;
                     for (int k = 0; k < L; k++) {
@@ -310,25 +344,26 @@ subseq_scaled_tiled_kernel(const SubseqJob J, const double *norm, const double *
                 if (cand) {
                     dist = 0.0;
                     for (int k = 0; k < L; k++) {
-                        if (dist >= bq) break;
+                        if (dbits(dist) >= dbits(bq)) break;
                         double x = __ldg(S + k);
                         x = x - Z[k * 32 + lane];
                         dist = dist + x * x;
                     }
-                    if (!(dist < bq)) dist = INF;
+                    if (!(dbits(dist) < dbits(bq))) dist = INF;
                 }
                 double v = dist;
                 int vi = w;
                 for (int o = 16; o > 0; o >>= 1) {
                     double ov = __shfl_xor_sync(0xffffffffu, v, o);
                     int oi = __shfl_xor_sync(0xffffffffu, vi, o);
-                    if (ov < v || (ov == v && oi < vi)) {
+                    if (dbits(ov) < dbits(v) || (dbits(ov) == dbits(v) && oi < vi)) {
                         v = ov;
                         vi = oi;
                     }
                 }
-                if (lane == 0 && v < bq) {
+                if (lane == 0 && dbits(v) < dbits(bq)) {
                     best[q] = v;
+                    bestf[q] = __double2float_ru(v);
                     bidx[q] = vi;
                 }
                 __syncwarp();
@@ -373,32 +408,32 @@ subseq_paired_kernel(const SubseqJob J, const double *norm, const double *mean_t
                     const double mean = mt[w];
                     const double sd = st[w];
                     for (int k = 0; k < L; k++) {
-                        if (dist >= best) break;
+                        if (dbits(dist) >= dbits(best)) break;
                         double x = __ldg(S + k);
                         x = x - (__ldg(T + w + k) - mean) / sd;
                         dist = dist + x * x;
                     }
                 } else {
                     for (int k = 0; k < L; k++) {
-                        if (dist >= best) break;
+                        if (dbits(dist) >= dbits(best)) break;
                         double x = __ldg(T + w + k);
                         x = x - __ldg(S + k);
                         dist = dist + x * x;
                     }
                 }
-                if (!(dist < best)) dist = INF;
+                if (!(dbits(dist) < dbits(best))) dist = INF;
             }
             double v = dist;
             int vi = w;
             for (int o = 16; o > 0; o >>= 1) {
                 double ov = __shfl_xor_sync(0xffffffffu, v, o);
                 int oi = __shfl_xor_sync(0xffffffffu, vi, o);
-                if (ov < v || (ov == v && oi < vi)) {
+                if (dbits(ov) < dbits(v) || (dbits(ov) == dbits(v) && oi < vi)) {
                     v = ov;
                     vi = oi;
                 }
             }
-            if (v < best) {
+            if (dbits(v) < dbits(best)) {
                 best = v;
                 bidx = vi;
             }
@@ -480,8 +515,8 @@ int launch_subseq_profile(const SubseqJob &J, bool scaled, Workspace &ws, double
 }
 
 static size_t scaled_tiled_smem(const SubseqJob &J) {
-    return (size_t)J.x.len * 8 + (size_t)J.chunk * 8 + (size_t)((J.chunk + 1) / 2) * 8 +
-           (size_t)J.max_len * 32 * 8 + (size_t)J.max_len * 32 * 4 + 16;
+    return (size_t)J.x.len * 8 + (size_t)J.chunk * 16 + (size_t)J.max_len * 32 * 8 +
+           (size_t)J.max_len * 32 * 4 + 16;
 }
 
 static int sub_grid(int64_t n, int block) {
@@ -504,7 +539,7 @@ size_t subseq_workspace_bytes(const SubseqJob &J, bool scaled) {
 static int make_f32_copies(const SubseqJob &J, const double *src, Workspace &ws,
                            SubseqJob &out) {
     float *f = ws.take<float>((size_t)J.total_values);
-    double *mx = ws.take<double>((size_t)J.m);
+    float *mx = ws.take<float>((size_t)J.m);
     if (!f || !mx) return fail(WB_ENOMEM, "workspace reservation exceeded");
     shapelet_f32_kernel<<<(int)(J.m < 65535 ? J.m : 65535), 128, 0, ws.stream()>>>(
         src, J.offsets, J.lengths, J.m, f, mx);

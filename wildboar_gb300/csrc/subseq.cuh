@@ -33,7 +33,7 @@ struct SubseqJob {
     int std_as_given = 0;  // a zero std divides as is (distance profile's transient stats)
     // FP32 pre-filter of the minimum scans (set by launch_subseq)
     const float *shp_f32 = nullptr;      // packed shapelets (z-normalised when scaled)
-    const double *shp_absmax = nullptr;  // (m,) max |value| of each packed shapelet
+    const float *shp_absmax = nullptr;   // (m,) max |value| of each shapelet, rounded up
     double *out_dist = nullptr;          // (x.count, m)
     int64_t *out_idx = nullptr;          // (x.count, m)
 };
