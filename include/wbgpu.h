@@ -278,6 +278,42 @@ int wb_pairwise_distance_noalloc(const wb_series *x, const wb_series *y, int64_t
 /* size in bytes of the static scratch of wb_pairwise_distance_noalloc */
 int64_t wb_noalloc_scratch_bytes(void);
 
+/*
+ * wb_dtw_average_mm_step -- one epoch of the majorize-minimize DTW barycenter
+ * for a batch of groups; replaces the per-sample loop of _mm_dtw_average
+ * (distance/dtw.py:661-690): dtw_alignment (distance/dtw.py:246-290,
+ * _elastic.pyx:1011-1073; wdtw_alignment :293-327 when `weights` is given),
+ * the traceback of dtw_mapping (distance/dtw.py:362-426) and the z / V sums.
+ * Every pointer is device memory.  Pair q aligns the mean in row
+ * pair_group[q] of `means` (mean_len values per row) with sample member[q]
+ * (row member[q] of x, stride x_stride, n_timestep values).  The pairs of
+ * group gi are group_start[gi] .. group_start[gi + 1] - 1, in sample order;
+ * its new mean (the reference's z / V) goes to row groups[gi] of new_means
+ * (row gi when groups is NULL; new_means may be means).  `r` is the window
+ * fraction (warp max(floor(max(mean_len, n_timestep) r), 1)); `weights`
+ * (length >= max(mean_len, n_timestep)) weighs cell (i, j) by
+ * weights[|i - j|], NULL for dtw; sample_weight[q] weighs pair q (NULL: 1).
+ * last[q] (optional) receives the final alignment cell of pair q.
+ * new_means NULL: alignment and `last` only.
+ */
+int wb_dtw_average_mm_step(const double *x, int64_t x_stride, int64_t n_timestep,
+                           const double *means, int64_t mean_len, const int64_t *member,
+                           const int32_t *pair_group, const int64_t *group_start,
+                           const int32_t *groups, int64_t n_groups, int64_t n_pairs, double r,
+                           const double *weights, const double *sample_weight,
+                           double *new_means, double *last, void *stream);
+
+/*
+ * wb_group_mean -- x[group].mean(axis=0) of the euclidean KMeans update
+ * (_EuclideanCluster._update_centroid, distance/_neighbors.py:364-369):
+ * the rows member[group_start[gi] .. group_start[gi + 1] - 1] summed in that
+ * order, divided by their count, into row groups[gi] (or gi) of out.
+ * Device pointers.
+ */
+int wb_group_mean(const double *x, int64_t x_stride, int64_t n_timestep,
+                  const int64_t *member, const int64_t *group_start, const int32_t *groups,
+                  int64_t n_groups, double *out, void *stream);
+
 /* message of the last failed call on this thread ("" if none) */
 const char *wb_last_error(void);
 

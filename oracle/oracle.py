@@ -88,6 +88,7 @@ def lib():
         L.wbo_distance_1d.restype = ctypes.c_double
         L.wbo_fast_mean_std.argtypes = [dp, i64, dp, dp]
         L.wbo_dtw_alignment.argtypes = [dp, i64, dp, i64, i64, dp, dp]
+        L.wbo_mm_epoch.argtypes = [dp, i64, i64, dp, i64, i64, dp, dp, dp, dp, ip, dp]
         L.wbo_subsequence_matches.argtypes = [dp, ip, ip, dp, dp, i64, dp, i64, i64, i64,
                                               ctypes.c_int, pp, ctypes.c_double, dp, dp, i64,
                                               ctypes.c_int, ctypes.c_int]
@@ -360,3 +361,127 @@ def dtw_mapping(alignment):
                 j -= 1
         path.append((i, j))
     return path[::-1]
+
+
+# --------------------------------------------------------------------------
+# dtw_average (method="mm") and the estimators that use the distance path
+
+
+def jeong_weight(n, g=0.05):
+    """distance/dtw.py:330-359."""
+    return 1.0 / (1.0 + np.exp(-g * (np.arange(n, dtype=float) - n / 2.0)))
+
+
+def mm_epoch(X, mean, *, r=1.0, weights=None, sample_weight=None, return_last=False):
+    """One epoch of _mm_dtw_average (distance/dtw.py:668-682) in C: new mean."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    mean = np.ascontiguousarray(mean, dtype=np.float64)
+    N, T = X.shape
+    nm = mean.shape[0]
+    warp = max(int(math.floor(max(nm, T) * r)), 1)
+    out = np.empty(nm)
+    work = np.empty(nm * T)
+    path = np.empty(2 * (nm + T), dtype=np.int64)
+    last = np.empty(N) if return_last else None
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    sw = None if sample_weight is None else np.ascontiguousarray(sample_weight,
+                                                                  dtype=np.float64)
+    rc = lib().wbo_mm_epoch(_dp(X), N, T, _dp(mean), nm, warp, _dp(w), _dp(sw), _dp(out),
+                            _dp(work), _ip(path), _dp(last))
+    if rc != 0:
+        raise ValueError("invalid r")
+    return (out, last) if return_last else out
+
+
+def dtw_average_mm(X, *, r=1.0, g=None, init, sample_weight=None, tol=1e-5, max_epoch=50):
+    """dtw_average(method="mm") with an array init (distance/dtw.py:429-594,
+    661-690): returns (mean, cost)."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    mean = np.array(init, dtype=np.float64, copy=True)
+    if g is None:
+        metric, params, weights = "dtw", {"r": r}, None
+    else:
+        metric, params = "wdtw", {"r": r, "g": g}
+        weights = jeong_weight(max(mean.shape[0], X.shape[1]), g)
+
+    def costfn(m):
+        d = pairwise(m, X, metric=metric, metric_params=params)[0]
+        if sample_weight is None:
+            return np.mean(d)
+        return np.average(d, weights=sample_weight)
+
+    cost = costfn(mean)
+    for _ in range(max_epoch):
+        mean = mm_epoch(X, mean, r=r, weights=weights, sample_weight=sample_weight)
+        prev_cost = cost
+        cost = costfn(mean)
+        if abs(prev_cost - cost) < tol:
+            break
+    return mean, cost
+
+
+def kmeans(x, n_clusters, *, metric="euclidean", r=1.0, g=None, n_init="auto",
+           max_iter=300, tol=1e-3, random_state=None):
+    """KMeans.fit (distance/_neighbors.py:309-548): returns (labels, centers,
+    inertia, n_iter)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    rs = random_state if isinstance(random_state, np.random.RandomState) \
+        else np.random.RandomState(random_state)
+    if metric == "euclidean":
+        dmetric, dparams = "euclidean", {}
+    elif g is None:
+        dmetric, dparams = "dtw", {"r": r}
+    else:
+        dmetric, dparams = "wdtw", {"r": r, "g": g}
+
+    def assign(c):
+        idx, dist = argmin(x, c, k=1, metric=dmetric, metric_params=dparams)
+        return np.ravel(idx).astype(np.intp), dist
+
+    def fit_one():
+        cent = x[rs.choice(x.shape[0], size=n_clusters, replace=False)]
+        prev_cost, cost, reassign, it = np.inf, -np.inf, True, 0
+        assigned = dist = None
+        for it in range(max_iter):
+            assigned, dist = assign(cent)
+            prev_cost, cost = cost, paired(x, cent[assigned], metric=dmetric,
+                                           metric_params=dparams).sum() / x.shape[0]
+            if math.isclose(cost, prev_cost, rel_tol=tol):
+                reassign = False
+                break
+            for c in range(n_clusters):
+                grp = x[assigned == c]
+                if grp.shape[0] == 0:
+                    far = dist.min(axis=1).argmax()
+                    assigned[far] = c
+                    cent[c] = x[far]
+                elif grp.shape[0] == 1:
+                    cent[c] = grp
+                elif metric == "euclidean":
+                    cent[c] = grp.mean(axis=0)
+                else:
+                    rs.randint(np.iinfo(np.int32).max)
+                    cent[c] = dtw_average_mm(grp, r=r, g=g, init=cent[c])[0]
+        return it, cost, cent, assigned, reassign
+
+    best = None
+    for _ in range(1 if n_init == "auto" else n_init):
+        res = fit_one()
+        if best is None or res[1] < best[1]:
+            best = res
+    it, cost, cent, assigned, reassign = best
+    if reassign:
+        assigned, _ = assign(cent)
+    return assigned, cent, cost, it
+
+
+def knn_predict_proba(x_train, y_train, x, *, n_neighbors=5, metric="euclidean",
+                      metric_params=None):
+    """KNeighborsClassifier.predict_proba (distance/_neighbors.py:237-287), 2-D x."""
+    classes, yi = np.unique(y_train, return_inverse=True)
+    closest, _ = argmin(x, x_train, k=n_neighbors, metric=metric, metric_params=metric_params)
+    preds = yi[closest]
+    probs = np.empty((np.asarray(x).shape[0], len(classes)))
+    for i in range(len(classes)):
+        probs[:, i] = np.sum(preds == i, axis=1) / n_neighbors
+    return probs

@@ -1285,3 +1285,70 @@ int wbo_dtw_alignment(const double *X, idx_t n, const double *Y, idx_t m, idx_t 
 #undef OUT
     return 0;
 }
+
+/* One epoch of _mm_dtw_average (distance/dtw.py:661-690): for every sample i
+ * in order, the alignment of `mean` (nm values) with X[i] (T values,
+ * _dtw_alignment with warp r and optional weights), the traceback of
+ * dtw_mapping (distance/dtw.py:362-426: from the last cell, np.argmin over
+ * [diag, up, left], the first minimum winning; along the first row or column
+ * the only finite option), then V[m] += w and z[m] += X[i, x] * w over the
+ * path cells in row-major order (indicator.nonzero()); out_mean = z / V.
+ * `work` holds nm * T doubles, `path` 2 * (nm + T) indices. */
+int wbo_mm_epoch(const double *X, idx_t n_samples, idx_t T, const double *mean, idx_t nm,
+                 idx_t r, const double *weights, const double *sample_weight,
+                 double *out_mean, double *work, idx_t *path, double *last)
+{
+    double *z = (double *)calloc((size_t)nm, sizeof(double));
+    double *V = (double *)calloc((size_t)nm, sizeof(double));
+    if (!z || !V) {
+        free(z);
+        free(V);
+        return -2;
+    }
+    for (idx_t s = 0; s < n_samples; s++) {
+        const double *Xs = X + s * T;
+        if (wbo_dtw_alignment(mean, nm, Xs, T, r, weights, work) != 0) {
+            free(z);
+            free(V);
+            return -1;
+        }
+        if (last) last[s] = work[(nm - 1) * T + (T - 1)];
+        idx_t i = nm - 1, j = T - 1, len = 0;
+        while (i > 0 || j > 0) {
+            path[2 * len] = i;
+            path[2 * len + 1] = j;
+            len++;
+            double diag = (i > 0 && j > 0) ? work[(i - 1) * T + (j - 1)] : INF;
+            double up = i > 0 ? work[(i - 1) * T + j] : INF;
+            double left = j > 0 ? work[i * T + (j - 1)] : INF;
+            int move = 0;
+            double best = diag;
+            if (up < best) {
+                best = up;
+                move = 1;
+            }
+            if (left < best) move = 2;
+            if (move == 0) {
+                i--;
+                j--;
+            } else if (move == 1) {
+                i--;
+            } else {
+                j--;
+            }
+        }
+        path[2 * len] = 0;
+        path[2 * len + 1] = 0;
+        len++;
+        const double w = sample_weight ? sample_weight[s] : 1.0;
+        for (idx_t k = len - 1; k >= 0; k--) {
+            const idx_t pm = path[2 * k], px = path[2 * k + 1];
+            V[pm] += w;
+            z[pm] += Xs[px] * w;
+        }
+    }
+    for (idx_t k = 0; k < nm; k++) out_mean[k] = z[k] / V[k];
+    free(z);
+    free(V);
+    return 0;
+}

@@ -309,6 +309,82 @@ def main():
              "lengths": np.array([10, 10, 10, 10])},
             {"metric": metric, "metric_params": params, "kw": kw}, flat(res))
 
+    # dtw_average (method="mm"), KMeans and the neighbour estimators
+    # (distance/dtw.py:429-690, distance/_neighbors.py:17-588)
+    from wildboar.distance import KMeans, KNeighborsClassifier, NearestNeighbors
+    from wildboar.distance.dtw import dtw_average
+
+    XA = _walk(rng, (12, 30))
+    XM = _walk(rng, (5, 200))
+    XL = _walk(rng, (4, 540))
+    sw = rng.uniform(0.5, 2.0, 12)
+    for name, X_, kw in (
+            ("dtw_r1", XA, {"r": 1.0, "init": XA[3]}),
+            ("dtw_r02", XA, {"r": 0.2, "init": XA[0]}),
+            ("wdtw", XA, {"r": 0.5, "g": 0.1, "init": XA[5]}),
+            ("sample_weight", XA, {"r": 0.4, "init": XA[1], "sample_weight": sw}),
+            ("short_init", XA, {"r": 0.5, "init": XA[2, :24]}),
+            ("long_init", XA, {"r": 0.5, "init": np.concatenate([XA[4], XA[4, :6]])}),
+            ("epochs3", XA, {"r": 0.3, "init": XA[7], "tol": 0.0, "max_epoch": 3}),
+            ("random_init", XA, {"r": 0.6, "init": "random", "random_state": 7}),
+            ("len200", XM, {"r": 0.3, "init": XM[1]}),
+            ("len540", XL, {"r": 0.1, "init": XL[2]}),
+            ("wdtw_len540", XL, {"r": 0.05, "g": 0.05, "init": XL[0]})):
+        mean, cost = dtw_average(X_, return_cost=True, **kw)
+        inputs = {"x": X_}
+        args = {k: v for k, v in kw.items() if k not in ("init", "sample_weight")}
+        if isinstance(kw["init"], str):
+            args["init"] = kw["init"]
+        else:
+            inputs["init"] = kw["init"]
+        if "sample_weight" in kw:
+            inputs["sample_weight"] = kw["sample_weight"]
+        add(f"dtw_average_{name}", "dtw_average", inputs, args, {"mean": mean, "cost": cost})
+
+    XK = _walk(rng, (30, 25))
+    XK[:10] += 6.0
+    XK[10:20] -= 6.0
+    U = _walk(rng, (6, 20))
+    XD = np.concatenate([U, U, U + 0.01 * rng.standard_normal((6, 20))])
+    XT = _walk(rng, (7, 25))
+    for name, X_, kw in (
+            ("euclidean", XK, {"n_clusters": 3, "random_state": 1}),
+            ("dtw", XK, {"n_clusters": 3, "metric": "dtw", "r": 0.5, "random_state": 2}),
+            ("wdtw", XK, {"n_clusters": 2, "metric": "dtw", "r": 1.0, "g": 0.2,
+                          "random_state": 3}),
+            ("n_init2", XK, {"n_clusters": 3, "metric": "dtw", "r": 0.3, "n_init": 2,
+                             "max_iter": 5, "random_state": 4}),
+            ("empty_euclidean", XD, {"n_clusters": 6, "random_state": 6, "max_iter": 20}),
+            ("empty_dtw", XD, {"n_clusters": 6, "metric": "dtw", "r": 0.3,
+                               "random_state": 6, "max_iter": 20}),
+            ("empty_dtw13", XD, {"n_clusters": 6, "metric": "dtw", "r": 0.3,
+                                 "random_state": 13, "max_iter": 20})):
+        km = KMeans(**kw).fit(X_)
+        outputs = {"labels": km.labels_, "centers": km.cluster_centers_,
+                   "inertia": km.inertia_, "n_iter": km.n_iter_}
+        inputs = {"x": X_}
+        if X_.shape[1] == XT.shape[1]:
+            inputs["xt"] = XT
+            outputs["transform"] = km.transform(XT)
+        add(f"kmeans_{name}", "kmeans", inputs, kw, outputs)
+
+    ytr = rng.integers(0, 3, size=30)
+    for name, metric, params, k in (("dtw", "dtw", {"r": 0.3}, 3),
+                                    ("euclidean", "euclidean", None, 5),
+                                    ("msm", "msm", {"c": 0.5}, 4)):
+        clf = KNeighborsClassifier(n_neighbors=k, metric=metric, metric_params=params)
+        clf.fit(XK, ytr)
+        add(f"knn_{name}", "knn", {"x": XK, "y": ytr, "xt": XT},
+            {"metric": metric, "metric_params": params, "n_neighbors": k},
+            {"proba": clf.predict_proba(XT), "pred": clf.predict(XT)})
+    for name, metric, params in (("erp", "erp", {"g": 0.1}), ("dtw", "dtw", {"r": 0.2})):
+        nn = NearestNeighbors(n_neighbors=4, metric=metric, metric_params=params).fit(XK)
+        dist_tr, ind_tr = nn.kneighbors()
+        dist_te, ind_te = nn.kneighbors(XT)
+        add(f"kneighbors_{name}", "kneighbors", {"x": XK, "xt": XT},
+            {"metric": metric, "metric_params": params, "n_neighbors": 4},
+            {"dist_train": dist_tr, "ind_train": ind_tr, "dist": dist_te, "ind": ind_te})
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"reference_version": getattr(wildboar, "__version__", "?"),

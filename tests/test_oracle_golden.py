@@ -103,6 +103,52 @@ def run_oracle(case):
     if kind == "alignment":
         al = O.dtw_alignment(inp["x"], inp["y"], r=a["r"])
         return {"a": np.where(inp["mask"], al, 0.0)}
+    if kind == "dtw_average":
+        X = inp["x"]
+        if "init" in inp:
+            init = inp["init"]
+        else:  # init="random": dtw_average draws the row (distance/dtw.py:542-543)
+            init = X[np.random.RandomState(a["random_state"]).randint(X.shape[0])]
+        mean, cost = O.dtw_average_mm(X, r=a["r"], g=a.get("g"), init=init,
+                                      sample_weight=inp.get("sample_weight"),
+                                      tol=a.get("tol", 1e-5), max_epoch=a.get("max_epoch", 50))
+        return {"mean": mean, "cost": cost}
+    if kind == "kmeans":
+        labels, centers, inertia, n_iter = O.kmeans(
+            inp["x"], a["n_clusters"], metric=a.get("metric", "euclidean"), r=a.get("r", 1.0),
+            g=a.get("g"), n_init=a.get("n_init", "auto"), max_iter=a.get("max_iter", 300),
+            random_state=a["random_state"])
+        out = {"labels": labels, "centers": centers, "inertia": inertia, "n_iter": n_iter}
+        if "xt" in inp:
+            metric, params = "euclidean", {}
+            if a.get("metric") == "dtw":
+                metric = "dtw" if a.get("g") is None else "wdtw"
+                params = {"r": a.get("r", 1.0)}
+                if a.get("g") is not None:
+                    params["g"] = a["g"]
+            out["transform"] = O.pairwise(inp["xt"], centers, metric=metric,
+                                          metric_params=params)
+        return out
+    if kind == "knn":
+        proba = O.knn_predict_proba(inp["x"], inp["y"], inp["xt"], n_neighbors=a["n_neighbors"],
+                                    metric=metric, metric_params=a["metric_params"])
+        classes = np.unique(inp["y"])
+        return {"proba": proba, "pred": classes[np.argmax(proba, axis=1)]}
+    if kind == "kneighbors":
+        k = a["n_neighbors"]
+        X, Xt = inp["x"], inp["xt"]
+
+        def sorted_argmin(q, kk):
+            idx, dist = O.argmin(q, X, k=kk, metric=metric, metric_params=a["metric_params"])
+            order = np.argsort(dist, axis=1, kind="stable")
+            return np.take_along_axis(idx, order, 1), np.take_along_axis(dist, order, 1)
+
+        ind, dist = sorted_argmin(X, k + 1)
+        mask = ind != np.arange(X.shape[0])[:, None]
+        ind_tr = ind[mask].reshape(X.shape[0], -1)
+        dist_tr = dist[mask].reshape(X.shape[0], -1)
+        ind_te, dist_te = sorted_argmin(Xt, k)
+        return {"dist_train": dist_tr, "ind_train": ind_tr, "dist": dist_te, "ind": ind_te}
     raise AssertionError(kind)
 
 
@@ -110,6 +156,7 @@ ORACLE_KINDS = {"pairwise", "singleton", "paired", "argmin", "subsequence", "ali
                 "paired_subsequence"}
 ORACLE_KINDS |= {"argmin_subsequence", "distance_profile", "subsequence_match",
                  "paired_subsequence_match"}
+ORACLE_KINDS |= {"dtw_average", "kmeans", "knn", "kneighbors"}
 CASES = [c for c in _golden.cases() if c["kind"] in ORACLE_KINDS]
 
 

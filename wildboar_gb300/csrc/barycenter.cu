@@ -1,0 +1,339 @@
+// barycenter.cu -- the majorize-minimize DTW barycenter (dtw_average with
+// method="mm") and the group means of KMeans, FP64, bit-exact.
+//
+// One MM epoch of the reference (distance/dtw.py:661-690) aligns the current
+// mean with every sample (dtw_alignment, distance/_elastic.pyx:1011-1073),
+// walks the optimal path back (dtw_mapping, distance/dtw.py:362-426: from the
+// last cell, argmin of [diag, up, left] with the first minimum winning) and
+// then, for every mean element m, sums V[m] += w and z[m] += X[i, x] * w over
+// the path cells (m, x) of every sample i in sample order and, within a
+// sample, in ascending x; the new mean is z / V.
+//
+// Here:
+//  * mm_align_kernel: one warp per (mean, sample) pair runs the banded
+//    alignment recurrence as a wavefront: lane l owns S consecutive rows
+//    (mean elements) and handles column j = t - l at step t, receiving the
+//    row above its strip from lane l - 1 by shuffle (rows beyond 32 S go in
+//    passes through a boundary row in global memory).  Each cell keeps, in
+//    2 bits, the move the traceback would take from it -- the same three
+//    values the recurrence reads (up, left, diag), so no matrix is stored --
+//    and lane 0 then walks the path back and records, per row, the first
+//    and last column of the path in that row (a DTW path visits a contiguous
+//    run of columns in each row).  The final cell is also returned: for dtw
+//    with equal lengths it is the squared dtw distance of the pair.
+//  * mm_accumulate_kernel: one thread per (group, mean element) adds the
+//    path cells of the group's samples in the reference's order (sample
+//    order, ascending x), so z and V carry the reference's rounding, and
+//    writes z / V.  Without paths (KMeans with the euclidean metric) it is
+//    group.mean(axis=0): a sequential sum over the group's rows divided by
+//    the count, numpy's order for an axis-0 mean of a C-contiguous array.
+
+#include <algorithm>
+#include <cmath>
+
+#include "common.cuh"
+
+namespace wb {
+
+namespace {
+
+constexpr int kMmThreads = 128;
+constexpr int kMmWarps = kMmThreads / 32;
+
+template <int S>
+struct DirWord;
+template <>
+struct DirWord<4> { using T = uint8_t; };
+template <>
+struct DirWord<8> { using T = uint16_t; };
+template <>
+struct DirWord<16> { using T = uint32_t; };
+
+struct MmAlignJob {
+    const double *x = nullptr;      // samples, row s at x + s * x_stride
+    int64_t x_stride = 0;
+    int m = 0;                      // sample length (columns)
+    const double *means = nullptr;  // group means, row g at means + g * n
+    int n = 0;                      // mean length (rows)
+    const int64_t *member = nullptr;     // pair q aligns sample member[q]
+    const int32_t *pair_group = nullptr; // with mean pair_group[q]
+    int64_t q0 = 0, q1 = 0;         // pairs of this launch
+    int r = 1;                      // warp size max(floor(max(n, m) r), 1)
+    const double *weights = nullptr;  // weights[|i - j|] or nullptr
+    void *dir = nullptr;            // per pair (ceil(n / S), m) direction words
+    int64_t dir_pair_words = 0;
+    double *bnd = nullptr;          // per warp slot: boundary row (m doubles)
+    int32_t *path_lo = nullptr;     // (n_pairs, n)
+    int32_t *path_hi = nullptr;
+    double *last = nullptr;         // (n_pairs,) final cell, or nullptr
+};
+
+__device__ __forceinline__ long long dbits(double v) { return __double_as_longlong(v); }
+
+// move codes of the traceback: 0 diag, 1 up, 2 left (np.argmin's first minimum
+// over [diag, up, left]); values are non-negative or +inf, so integer order
+// of the bit patterns is their order
+__device__ __forceinline__ uint32_t move_code(long long diag, long long up, long long left) {
+    if (diag <= up && diag <= left) return 0u;
+    return up <= left ? 1u : 2u;
+}
+
+template <int S, bool W>
+__global__ void __launch_bounds__(kMmThreads) mm_align_kernel(const MmAlignJob J) {
+    using Word = typename DirWord<S>::T;
+    const double INF = __longlong_as_double(0x7ff0000000000000LL);
+    const int lane = threadIdx.x & 31;
+    const int slot = blockIdx.x * kMmWarps + (threadIdx.x >> 5);
+    const int n = J.n, m = J.m;
+    const int mx = imax(0, m - n) + J.r;   // columns j < i + mx
+    const int mn = imax(0, n - m);         // columns j >= i - mn - r + 1
+    double *bnd = J.bnd ? J.bnd + (int64_t)slot * m : nullptr;
+    for (int64_t q = J.q0 + slot; q < J.q1; q += (int64_t)gridDim.x * kMmWarps) {
+        const double *Y = J.x + J.member[q] * J.x_stride;
+        const double *X = J.means + (int64_t)J.pair_group[q] * n;
+        Word *dir = reinterpret_cast<Word *>(J.dir) + (q - J.q0) * J.dir_pair_words;
+        double fin = INF;
+        for (int p0 = 0; p0 < n; p0 += 32 * S) {
+            const int i0 = p0 + lane * S;
+            double a[S], left[S];
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+                a[k] = i0 + k < n ? X[i0 + k] : 0.0;
+                left[k] = INF;
+            }
+            double send = INF;       // this lane's last row at its last column
+            double prev_up0 = INF;   // row above the strip at the previous column
+            for (int t = 0; t < m + 31; t++) {
+                const double recv = __shfl_up_sync(0xffffffffu, send, 1);
+                const int j = t - lane;
+                if (j >= 0 && j < m) {
+                    double up0;
+                    if (lane == 0)
+                        up0 = p0 == 0 ? INF : bnd[j];
+                    else
+                        up0 = recv;
+                    const double y = Y[j];
+                    double up = up0, diag = prev_up0;
+                    uint32_t word = 0;
+#pragma unroll
+                    for (int k = 0; k < S; k++) {
+                        const int i = i0 + k;
+                        const double lf = left[k];
+                        double v = INF;
+                        if (i < n && j >= i - mn - J.r + 1 && j < i + mx) {
+                            const double d = a[k] - y;
+                            double c = d * d;
+                            if (W) c = c * J.weights[i > j ? i - j : j - i];
+                            if (i == 0 && j == 0) {
+                                v = c;
+                            } else {
+                                const long long bu = dbits(up), bl = dbits(lf), bd = dbits(diag);
+                                const long long mu = bl < bu ? bl : bu;
+                                v = __longlong_as_double(bd < mu ? bd : mu) + c;
+                                word |= move_code(bd, bu, bl) << (2 * k);
+                            }
+                        }
+                        if (i == n - 1 && j == m - 1) fin = v;
+                        diag = lf;
+                        left[k] = v;
+                        up = v;
+                    }
+                    if (i0 < n) dir[(int64_t)(i0 / S) * m + j] = (Word)word;
+                    send = up;
+                    prev_up0 = up0;
+                    if (lane == 31 && bnd) bnd[j] = up;
+                }
+            }
+            __syncwarp();
+        }
+        // the lane that owns row n - 1 saw the final cell
+        const int owner = ((n - 1) % (32 * S)) / S;
+        fin = __shfl_sync(0xffffffffu, fin, owner);
+        if (lane == 0) {
+            if (J.last) J.last[q] = fin;
+            int32_t *lo = J.path_lo + q * (int64_t)n;
+            int32_t *hi = J.path_hi + q * (int64_t)n;
+            int i = n - 1, j = m - 1;
+            hi[i] = j;
+            while (i > 0 || j > 0) {
+                uint32_t code;
+                if (i == 0)
+                    code = 2u;
+                else if (j == 0)
+                    code = 1u;
+                else
+                    code = (dir[(int64_t)(i / S) * m + j] >> (2 * (i % S))) & 3u;
+                if (code == 2u) {
+                    j -= 1;
+                } else {
+                    lo[i] = j;
+                    i -= 1;
+                    if (code == 0u) j -= 1;
+                    hi[i] = j;
+                }
+            }
+            lo[0] = 0;
+        }
+        __syncwarp();
+    }
+}
+
+// Thread (group gi, row): pairs group_start[gi] .. group_start[gi + 1] - 1 of
+// the group in sample order; path_lo / path_hi null: the single cell x = row.
+// The result goes to row groups[gi] (gi when groups is null) of out.
+__global__ void mm_accumulate_kernel(const double *x, int64_t x_stride, const int64_t *member,
+                                     const int64_t *group_start, const int32_t *groups,
+                                     int64_t n_groups, const int32_t *path_lo,
+                                     const int32_t *path_hi, const double *sample_weight,
+                                     int n, double *out, int64_t out_stride) {
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= n_groups * (int64_t)n) return;
+    const int64_t gi = tid / n;
+    const int row = (int)(tid - gi * n);
+    const int32_t g = groups ? groups[gi] : (int32_t)gi;
+    double z = 0.0, V = 0.0;
+    const int64_t qa = group_start[gi], qb = group_start[gi + 1];
+    for (int64_t q = qa; q < qb; q++) {
+        const int64_t s = member[q];
+        const double *Xs = x + s * x_stride;
+        int lo = row, hi = row;
+        if (path_lo) {
+            lo = path_lo[q * n + row];
+            hi = path_hi[q * n + row];
+        }
+        if (sample_weight) {
+            const double w = sample_weight[q];
+            for (int c = lo; c <= hi; c++) {
+                V = V + w;
+                z = z + Xs[c] * w;
+            }
+        } else {
+            for (int c = lo; c <= hi; c++) {
+                V = V + 1.0;
+                z = z + Xs[c];
+            }
+        }
+    }
+    out[g * out_stride + row] = z / V;
+}
+
+template <int S, bool W>
+int launch_align(const MmAlignJob &J, int grid, cudaStream_t st) {
+    mm_align_kernel<S, W><<<grid, kMmThreads, 0, st>>>(J);
+    WB_LAUNCH_CHECK("mm_align_kernel");
+    return WB_OK;
+}
+
+int pick_strip(int n) {
+    if (n <= 32 * 4) return 4;
+    if (n <= 32 * 8) return 8;
+    return 16;
+}
+
+}  // namespace
+
+}  // namespace wb
+
+using namespace wb;
+
+extern "C" int wb_dtw_average_mm_step(const double *x, int64_t x_stride, int64_t n_timestep,
+                                      const double *means, int64_t mean_len,
+                                      const int64_t *member, const int32_t *pair_group,
+                                      const int64_t *group_start, const int32_t *groups,
+                                      int64_t n_groups, int64_t n_pairs, double r,
+                                      const double *weights, const double *sample_weight,
+                                      double *new_means, double *last, void *stream) {
+    const cudaStream_t st = (cudaStream_t)stream;
+    if (n_pairs < 0 || n_groups < 0 || n_timestep < 1 || mean_len < 1)
+        return fail(WB_EINVAL, "dtw_average: invalid sizes");
+    if (!(r >= 0.0 && r <= 1.0)) return fail(WB_EINVAL, "dtw_average: r must be in [0, 1]");
+    if (n_timestep > INT32_MAX / 2 || mean_len > INT32_MAX / 2)
+        return fail(WB_EINVAL, "dtw_average: series too long");
+    if (n_pairs == 0) return WB_OK;
+    if (!x || !means || !member || !pair_group || !group_start)
+        return fail(WB_EINVAL, "dtw_average: null pointer");
+    const int n = (int)mean_len, m = (int)n_timestep;
+    const int64_t big = n > m ? n : m;
+    const double wv = std::floor((double)big * r);
+    const int warp = (int)(wv > 1.0 ? wv : 1.0);
+    const int S = pick_strip(n);
+    const int64_t word_bytes = S / 4;
+    const int64_t pair_words = (int64_t)((n + S - 1) / S) * m;
+    const int64_t pair_bytes = pair_words * word_bytes;
+    const bool passes = n > 32 * S;
+    const DeviceInfo &dev = device_info();
+    const int max_grid = dev.sm_count * 8;
+    // direction words per launch bounded to about 1 GiB
+    int64_t chunk = std::max<int64_t>(1, (1LL << 30) / std::max<int64_t>(pair_bytes, 1));
+    chunk = std::min<int64_t>(chunk, n_pairs);
+    const int grid = (int)std::min<int64_t>((chunk + kMmWarps - 1) / kMmWarps, max_grid);
+    Workspace ws(st);
+    const size_t need = align256(chunk * pair_bytes) +
+                        align256(passes ? (size_t)grid * kMmWarps * m * sizeof(double) : 0) +
+                        2 * align256((size_t)n_pairs * n * sizeof(int32_t)) + 4096;
+    WB_TRY(ws.reserve(need));
+    WB_TAKE(dirbuf, char, ws, chunk * pair_bytes);
+    double *bnd = nullptr;
+    if (passes) {
+        bnd = ws.take<double>((size_t)grid * kMmWarps * m);
+        if (!bnd) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    }
+    WB_TAKE(lo, int32_t, ws, (size_t)n_pairs * n);
+    WB_TAKE(hi, int32_t, ws, (size_t)n_pairs * n);
+    MmAlignJob J;
+    J.x = x;
+    J.x_stride = x_stride;
+    J.m = m;
+    J.means = means;
+    J.n = n;
+    J.member = member;
+    J.pair_group = pair_group;
+    J.r = warp;
+    J.weights = weights;
+    J.dir = dirbuf;
+    J.dir_pair_words = pair_words;
+    J.bnd = bnd;
+    J.path_lo = lo;
+    J.path_hi = hi;
+    J.last = last;
+    timer_begin("mm_align_kernel", st);
+    for (int64_t q0 = 0; q0 < n_pairs; q0 += chunk) {
+        J.q0 = q0;
+        J.q1 = std::min(n_pairs, q0 + chunk);
+        const bool w = weights != nullptr;
+        int s;
+        if (S == 4)
+            s = w ? launch_align<4, true>(J, grid, st) : launch_align<4, false>(J, grid, st);
+        else if (S == 8)
+            s = w ? launch_align<8, true>(J, grid, st) : launch_align<8, false>(J, grid, st);
+        else
+            s = w ? launch_align<16, true>(J, grid, st) : launch_align<16, false>(J, grid, st);
+        if (s != WB_OK) return s;
+    }
+    timer_end(st);
+    if (new_means && n_groups > 0) {
+        const int64_t threads = n_groups * (int64_t)n;
+        mm_accumulate_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(
+            x, x_stride, member, group_start, groups, n_groups, lo, hi, sample_weight, n,
+            new_means, n);
+        WB_LAUNCH_CHECK("mm_accumulate_kernel");
+    }
+    return WB_OK;
+}
+
+extern "C" int wb_group_mean(const double *x, int64_t x_stride, int64_t n_timestep,
+                             const int64_t *member, const int64_t *group_start,
+                             const int32_t *groups, int64_t n_groups, double *out,
+                             void *stream) {
+    const cudaStream_t st = (cudaStream_t)stream;
+    if (n_groups < 0 || n_timestep < 1 || n_timestep > INT32_MAX / 2)
+        return fail(WB_EINVAL, "group_mean: invalid sizes");
+    if (n_groups == 0) return WB_OK;
+    if (!x || !member || !group_start || !out) return fail(WB_EINVAL, "group_mean: null pointer");
+    const int n = (int)n_timestep;
+    const int64_t threads = n_groups * (int64_t)n;
+    mm_accumulate_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(
+        x, x_stride, member, group_start, groups, n_groups, nullptr, nullptr, nullptr, n, out, n);
+    WB_LAUNCH_CHECK("mm_accumulate_kernel");
+    return WB_OK;
+}

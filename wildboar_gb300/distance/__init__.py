@@ -11,6 +11,7 @@ from ._distance import (
     pairwise_subsequence_distance,
 )
 from ._metrics import _METRICS, _SUBSEQUENCE_METRICS
+from ._neighbors import KMeans, KNeighborsClassifier, NearestNeighbors
 from ._subsequence import (
     argmin_subsequence_distance,
     distance_profile,
@@ -31,6 +32,9 @@ __all__ = [
     "check_metric",
     "check_subsequence_metric",
     "InvalidParameterError",
+    "KMeans",
+    "KNeighborsClassifier",
+    "NearestNeighbors",
     "_METRICS",
     "_SUBSEQUENCE_METRICS",
 ]

@@ -1,0 +1,252 @@
+"""DTW barycenter averaging on the GPU (wildboar.distance.dtw.dtw_average).
+
+``dtw_average(method="mm")`` follows distance/dtw.py:429-594 and the
+majorize-minimize loop of ``_mm_dtw_average`` (:661-690).  Every epoch of
+every group runs on the device: the alignment, the traceback and the
+z / V sums are ``wb_dtw_average_mm_step`` (csrc/barycenter.cu), which keeps
+the reference's order of additions, so the means are bit-identical.  The
+cost of an epoch (``np.mean`` of the dtw distances of the new mean) is
+reduced on the host with numpy from distances computed on the device: for
+dtw between series of equal length the squared distance is the final cell
+of the next epoch's alignment (the same recurrence and band), so each epoch
+costs one alignment pass; wdtw (whose distance uses other weights than
+``wdtw_alignment``) and unequal lengths take a distance pass.
+
+``_mm_average_groups`` runs many groups (the clusters of a KMeans update) in
+lockstep: one launch per epoch covers every group that has not converged.
+"""
+
+import ctypes
+import math
+import numbers
+
+import numpy as np
+
+from .. import _lib
+from ._distance import InvalidParameterError, pairwise_distance
+from ._validation import check_array
+
+_lib.declare(
+    "wb_dtw_average_mm_step",
+    [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+     ctypes.c_int64, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+     ctypes.c_void_p, ctypes.c_void_p],
+)
+_lib.declare(
+    "wb_group_mean",
+    [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+     ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p],
+)
+
+
+def check_random_state(seed):
+    """sklearn.utils.check_random_state: None, an int or a RandomState."""
+    if seed is None or seed is np.random:
+        return np.random.mtrand._rand
+    if isinstance(seed, numbers.Integral) and not isinstance(seed, bool):
+        return np.random.RandomState(seed)
+    if isinstance(seed, np.random.RandomState):
+        return seed
+    raise ValueError("%r cannot be used to seed a numpy.random.RandomState instance" % seed)
+
+
+def _check_scalar(x, name, *, min_val=None, max_val=None, include_min=True, include_max=True):
+    if not isinstance(x, numbers.Real) or isinstance(x, bool):
+        raise TypeError(f"{name} must be an instance of float, not {type(x).__qualname__}.")
+    if min_val is not None and (x < min_val or (not include_min and x == min_val)):
+        raise ValueError(f"{name} == {x}, must be {'>=' if include_min else '>'} {min_val}.")
+    if max_val is not None and (x > max_val or (not include_max and x == max_val)):
+        raise ValueError(f"{name} == {x}, must be {'<=' if include_max else '<'} {max_val}.")
+    return x
+
+
+def jeong_weight(n, g=0.05):
+    """Weights of wdtw_alignment (distance/dtw.py:330-359), computed with numpy."""
+    return 1.0 / (1.0 + np.exp(-g * (np.arange(n, dtype=float) - n / 2.0)))
+
+
+def _torch():
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("dtw_average needs a CUDA device (wildboar_gb300 has no CPU path)")
+    return torch
+
+
+def _to_device(a, torch):
+    if isinstance(a, torch.Tensor):
+        return a.to(device="cuda", dtype=torch.float64).contiguous()
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda")
+
+
+def _layout(groups, active, torch, dev):
+    """Pair arrays of the active groups: member, pair_group, group_start, groups."""
+    members = [groups[g] for g in active]
+    counts = np.array([len(m) for m in members], dtype=np.int64)
+    start = np.zeros(len(active) + 1, dtype=np.int64)
+    np.cumsum(counts, out=start[1:])
+    member = np.concatenate(members).astype(np.int64) if members else np.zeros(0, np.int64)
+    pg = np.repeat(np.asarray(active, dtype=np.int32), counts)
+    return (torch.as_tensor(member, device=dev), torch.as_tensor(pg, device=dev),
+            torch.as_tensor(start, device=dev),
+            torch.as_tensor(np.asarray(active, dtype=np.int32), device=dev), start)
+
+
+def _step(Xd, means, lay, r, wdev, swdev, new_means, last, torch):
+    member, pg, gs, gid, _ = lay
+    n_groups = gid.shape[0]
+    n_pairs = member.shape[0]
+    st = _lib.lib().wb_dtw_average_mm_step(
+        Xd.data_ptr(), Xd.stride(0), Xd.shape[1], means.data_ptr(), means.shape[1],
+        member.data_ptr(), pg.data_ptr(), gs.data_ptr(), gid.data_ptr(), n_groups, n_pairs,
+        float(r), None if wdev is None else wdev.data_ptr(),
+        None if swdev is None else swdev.data_ptr(),
+        None if new_means is None else new_means.data_ptr(),
+        None if last is None else last.data_ptr(),
+        _lib.current_stream_handle())
+    _lib.check(st)
+
+
+def _group_cost(dist, sample_weight):
+    """costfn of dtw_average (distance/dtw.py:552-557) on host distances."""
+    if sample_weight is None:
+        return np.mean(dist)
+    return np.average(dist, weights=sample_weight)
+
+
+def _mm_average_groups(Xd, groups, init, *, r, g=None, sample_weight=None, tol=1e-5,
+                       max_epoch=50, verbose=False):
+    """MM barycenters of several groups of rows of the device matrix ``Xd``.
+
+    ``groups[i]`` are row indices of Xd (in the order the reference's group
+    array holds them), ``init`` the (n_groups, mean_len) initial means and
+    ``sample_weight`` None or one weight array per group.  Returns the means
+    (numpy, n_groups x mean_len) and the costs, as ``_mm_dtw_average``
+    returns them per group.
+    """
+    torch = _torch()
+    dev = Xd.device
+    G = len(groups)
+    init = np.ascontiguousarray(init, dtype=np.float64).reshape(G, -1)
+    nm, T = init.shape[1], Xd.shape[1]
+    cur = torch.as_tensor(init, device=dev).clone()
+    nxt = torch.empty_like(cur)
+    wdev = None
+    metric, metric_params = "dtw", {"r": r}
+    if g is not None:
+        wdev = torch.as_tensor(jeong_weight(max(nm, T), g), device=dev)
+        metric, metric_params = "wdtw", {"r": r, "g": g}
+    fused = g is None and nm == T
+    sw = [None] * G if sample_weight is None else sample_weight
+    costs = np.full(G, np.nan)
+    done = np.zeros(G, dtype=bool)
+
+    def swdev_of(lay_active):
+        if sample_weight is None:
+            return None
+        return torch.as_tensor(np.concatenate([np.asarray(sw[a], dtype=np.float64)
+                                               for a in lay_active]), device=dev)
+
+    def distance_costs(means_t, active):
+        out = {}
+        for a in active:
+            d = pairwise_distance(means_t[a], Xd[torch.as_tensor(groups[a], device=dev)],
+                                  metric=metric, metric_params=metric_params)
+            d = d.reshape(-1).cpu().numpy() if hasattr(d, "cpu") else np.atleast_1d(d)
+            out[a] = _group_cost(d, sw[a])
+        return out
+
+    active = [a for a in range(G)]
+    lay = _layout(groups, active, torch, dev)
+    if fused:
+        # one pass: cost of the current means, and the next means
+        last = torch.empty(lay[0].shape[0], dtype=torch.float64, device=dev)
+        _step(Xd, cur, lay, r, wdev, swdev_of(active), nxt, last, torch)
+        sq = np.sqrt(last.cpu().numpy())
+        start = lay[4]
+        cost = {a: _group_cost(sq[start[i]:start[i + 1]], sw[a]) for i, a in enumerate(active)}
+    else:
+        cost = distance_costs(cur, active)
+    for epoch in range(max_epoch):
+        if not active:
+            break
+        if fused:
+            # nxt holds the means of this epoch (from the alignment of cur)
+            idx = torch.as_tensor(active, device=dev)
+            cur[idx] = nxt[idx]
+            last = torch.empty(lay[0].shape[0], dtype=torch.float64, device=dev)
+            _step(Xd, cur, lay, r, wdev, swdev_of(active), nxt, last, torch)
+            sq = np.sqrt(last.cpu().numpy())
+            start = lay[4]
+            new_cost = {a: _group_cost(sq[start[i]:start[i + 1]], sw[a])
+                        for i, a in enumerate(active)}
+        else:
+            _step(Xd, cur, lay, r, wdev, swdev_of(active), cur, None, torch)
+            new_cost = distance_costs(cur, active)
+        still = []
+        for a in active:
+            prev_cost, cost[a] = cost[a], new_cost[a]
+            if abs(prev_cost - cost[a]) < tol:
+                if verbose:
+                    print(f"Complete at epoch={epoch} with cost={cost[a]}.")
+                done[a] = True
+            else:
+                still.append(a)
+        if len(still) != len(active):
+            active = still
+            lay = _layout(groups, active, torch, dev) if active else None
+    for a in range(G):
+        costs[a] = cost[a]
+    return cur.cpu().numpy(), costs
+
+
+def dtw_average(X, *, r=1.0, g=None, sample_weight=None, init="random", method="mm",
+                max_stable=5, learning_rate=0.1, decay=0.9, tol=1e-5, max_epoch=50,
+                return_cost=False, verbose=False, random_state=None):
+    """Compute the DTW barycenter average (distance/dtw.py:429-594).
+
+    ``method="mm"`` (the majorize-minimize mean, the reference's default and
+    the one KMeans uses) runs on the GPU and returns the reference's bits.
+    ``method="ssg"`` (stochastic subgradient, a sequential per-sample update)
+    is not provided.
+    """
+    X = check_array(X, allow_3d=False, ensure_2d=True, dtype=float)
+    if X.shape[0] < 2:
+        raise ValueError(
+            "Found array with %d sample(s) (shape=%r) while a minimum of 2 is required."
+            % (X.shape[0], X.shape))
+    r = _check_scalar(r, "r", min_val=0.0, max_val=1.0)
+    random_state = check_random_state(random_state)
+    if isinstance(init, str) and init == "random":
+        mean = X[random_state.randint(X.shape[0])].copy()
+    elif hasattr(init, "__len__") or hasattr(init, "__array__"):
+        mean = np.array(init, dtype=float, copy=True)
+    else:
+        raise ValueError("init must be array-like or 'random', not %r" % type(init).__qualname__)
+    if sample_weight is not None:
+        sample_weight = np.asarray(sample_weight, dtype=np.float64)
+        if sample_weight.ndim == 0:
+            sample_weight = np.full(X.shape[0], float(sample_weight))
+        if sample_weight.shape != (X.shape[0],):
+            raise ValueError(
+                "sample_weight.shape == {}, expected {}!".format(sample_weight.shape,
+                                                                  (X.shape[0],)))
+    if g is not None:
+        g = _check_scalar(g, "g", min_val=0, include_min=False)
+    if method == "ssg":
+        raise NotImplementedError("dtw_average(method='ssg') is not available on the GPU path")
+    if method != "mm":
+        raise ValueError("method must be 'mm' or 'ssg', got %r" % method)
+    torch = _torch()
+    Xd = _to_device(X, torch)
+    means, costs = _mm_average_groups(
+        Xd, [np.arange(X.shape[0])], mean.reshape(1, -1), r=r, g=g,
+        sample_weight=None if sample_weight is None else [sample_weight], tol=tol,
+        max_epoch=max_epoch, verbose=verbose)
+    if return_cost:
+        return means[0], costs[0]
+    return means[0]
+
+
+__all__ = ["dtw_average", "jeong_weight", "check_random_state", "InvalidParameterError"]
