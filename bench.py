@@ -383,6 +383,89 @@ def bench_subsequence(args, dev, flush):
             "algorithmic_window_elements": elems, **res}
 
 
+def c6_data(n_series=4096, L=256, K=32, seed=5):
+    """KMeans / barycenter inputs: float64 series from 32 sine / random-walk
+    prototypes + N(0, 0.1), the prototype labels."""
+    rng = np.random.default_rng(seed)
+    t = np.linspace(0, 1, L)
+    protos = []
+    for k in range(K):
+        if k % 2 == 0:
+            protos.append(np.sin(2 * np.pi * (1 + k / 4) * t + rng.uniform(0, 6.28)) * 3)
+        else:
+            protos.append(np.cumsum(rng.standard_normal(L)) * 0.3)
+    protos = np.asarray(protos)
+    labels = rng.integers(0, K, size=n_series)
+    return protos[labels] + 0.1 * rng.standard_normal((n_series, L)), labels
+
+
+def bench_barycenter(args, dev, flush):
+    """dtw_average (method="mm") epochs and KMeans(metric="dtw") on 4,096 float64
+    series of length 256 in 32 groups, r=0.2: one step is one MM epoch of all
+    32 groups (alignment + traceback + z / V sums, exact); then a full KMeans
+    fit through the public estimator.  CPU: the oracle's C epoch (one thread)
+    on a bounded sample."""
+    import torch
+
+    from oracle import oracle as O
+    from wildboar_gb300 import _lib
+    from wildboar_gb300.distance import KMeans
+    from wildboar_gb300.distance import dtw as D
+    from wildboar_gb300.distance._band import band_cells
+
+    N, L, K, r = args.c6_series, 256, 32, 0.2
+    X, labels = c6_data(N, L, K)
+    groups = [np.flatnonzero(labels == k) for k in range(K)]
+    init = X[[g[0] for g in groups]].copy()
+    Xd = torch.as_tensor(X, device=dev)
+    means = torch.as_tensor(init, device=dev)
+    nxt = torch.empty_like(means)
+    last = torch.empty(N, dtype=torch.float64, device=dev)
+    lay = D._layout(groups, list(range(K)), torch, Xd.device)
+    cells = N * band_cells(L, L, r)
+
+    def epoch():
+        D._step(Xd, means, lay, r, None, None, nxt, last, torch)
+
+    for _ in range(3):
+        epoch()
+    torch.cuda.synchronize()
+    l0 = _lib.launch_count()
+    ms = _timed(epoch, max(3, args.steps), flush)
+    launches = (_lib.launch_count() - l0) / max(3, args.steps)
+    got = nxt.cpu().numpy()
+    exact = all(np.array_equal(got[k], O.mm_epoch(X[groups[k]], init[k], r=r))
+                for k in (0, K // 2, K - 1))
+    # CPU: the oracle's epoch on a sample of one group's members
+    sample = groups[0][:args.c6_cpu_sample]
+    t0 = time.perf_counter()
+    O.mm_epoch(X[sample], init[0], r=r)
+    cpu_s = time.perf_counter() - t0
+    cpu_gcups = len(sample) * band_cells(L, L, r) / cpu_s / 1e9
+    # a full KMeans fit through the estimator (host data, returns host labels)
+    km = KMeans(K, metric="dtw", r=r, random_state=0)
+    km.fit(X[:256])  # warm-up on a small slice
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    km = KMeans(K, metric="dtw", r=r, random_state=0).fit(X)
+    torch.cuda.synchronize()
+    fit_s = time.perf_counter() - t0
+    return {
+        "config": f"{N} float64 series, L={L}, {K} groups (32 sine / random-walk prototypes "
+                  f"+ N(0, 0.1)), r={r}",
+        "mm_epoch_ms": ms,
+        "mm_epoch_gcups": cells / (ms * 1e-3) / 1e9,
+        "alignment_cells_per_epoch": cells,
+        "launches_per_epoch": launches,
+        "epoch_means_exact_vs_oracle": bool(exact),
+        "cpu_oracle_epoch": {"gcups": cpu_gcups, "cores": 1, "kind": "port",
+                             "sample": f"{len(sample)} series of one group, one epoch"},
+        "kmeans_fit_s": fit_s,
+        "kmeans_n_iter": int(km.n_iter_),
+        "kmeans_inertia": float(km.inertia_),
+    }
+
+
 def bench_euclid_tc(args, dev, flush):
     """Full-series euclidean 8192 x 8192 at length 1024: tensor-core 3xTF32
     GEMM form against the FP64 drop-in kernel on the same device data."""
@@ -527,6 +610,8 @@ def run_gpu(args):
             forms["euclidean_full_tc"] = bench_euclid_tc(args, dev, flush)
         if args.only in ("", "precision"):
             forms["precision_sweep"] = bench_precision(args, dev, flush)
+        if args.only in ("", "barycenter"):
+            forms["barycenter_kmeans"] = bench_barycenter(args, dev, flush)
         if rank == 0:
             print(json.dumps({"forms": forms}), flush=True)
         return
@@ -627,6 +712,7 @@ def run_gpu(args):
         forms["subsequence"] = bench_subsequence(args, dev, flush)
         forms["euclidean_full_tc"] = bench_euclid_tc(args, dev, flush)
         forms["precision_sweep"] = bench_precision(args, dev, flush)
+        forms["barycenter_kmeans"] = bench_barycenter(args, dev, flush)
         forms["both_beat_fp64_drop_in"] = bool(
             forms["batched_fp32"]["gcups"] > value and forms["fwd_bwd_fp32"]["gcups"] > value)
     line = {
@@ -679,8 +765,10 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true",
                     help="only the FP32 forms (profiling captures)")
     ap.add_argument("--only", default="", choices=["", "batched", "fwdbwd", "subseq", "euclid",
-                                                     "precision"],
+                                                     "precision", "barycenter"],
                     help="with --skip-fp64: run one form only")
+    ap.add_argument("--c6-series", type=int, default=4096)
+    ap.add_argument("--c6-cpu-sample", type=int, default=48)
     ap.add_argument("--c3-series", type=int, default=1000)
     ap.add_argument("--c3-shapelets", type=int, default=10000)
     ap.add_argument("--c3-full", type=int, default=8192)

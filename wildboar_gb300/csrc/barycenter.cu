@@ -17,7 +17,7 @@
 //    passes through a boundary row in global memory).  Each cell keeps, in
 //    2 bits, the move the traceback would take from it -- the same three
 //    values the recurrence reads (up, left, diag), so no matrix is stored --
-//    and lane 0 then walks the path back and records, per row, the first
+//    and the warp then walks the path back and records, per row, the first
 //    and last column of the path in that row (a DTW path visits a contiguous
 //    run of columns in each row).  The final cell is also returned: for dtw
 //    with equal lengths it is the squared dtw distance of the pair.
@@ -149,31 +149,45 @@ __global__ void __launch_bounds__(kMmThreads) mm_align_kernel(const MmAlignJob J
         // the lane that owns row n - 1 saw the final cell
         const int owner = ((n - 1) % (32 * S)) / S;
         fin = __shfl_sync(0xffffffffu, fin, owner);
-        if (lane == 0) {
-            if (J.last) J.last[q] = fin;
-            int32_t *lo = J.path_lo + q * (int64_t)n;
-            int32_t *hi = J.path_hi + q * (int64_t)n;
-            int i = n - 1, j = m - 1;
-            hi[i] = j;
-            while (i > 0 || j > 0) {
-                uint32_t code;
-                if (i == 0)
-                    code = 2u;
-                else if (j == 0)
-                    code = 1u;
-                else
-                    code = (dir[(int64_t)(i / S) * m + j] >> (2 * (i % S))) & 3u;
-                if (code == 2u) {
-                    j -= 1;
-                } else {
-                    lo[i] = j;
-                    i -= 1;
-                    if (code == 0u) j -= 1;
-                    hi[i] = j;
+        if (lane == 0 && J.last) J.last[q] = fin;
+        // The whole warp walks the path back in lockstep (i, j are
+        // warp-uniform): a window of 32 consecutive direction words of one
+        // strip (columns base .. base + 31) sits one per lane and the word
+        // of column j comes by shuffle, so a global load is paid once per
+        // window instead of once per step.  The path only moves up and left:
+        // a window is reloaded when the path leaves its strip or its columns.
+        int32_t *lo = J.path_lo + q * (int64_t)n;
+        int32_t *hi = J.path_hi + q * (int64_t)n;
+        int i = n - 1, j = m - 1;
+        int strip = -1, base = 0;
+        uint32_t wreg = 0;
+        if (lane == 0) hi[i] = j;
+        while (i > 0 || j > 0) {
+            uint32_t code;
+            if (i == 0) {
+                code = 2u;
+            } else if (j == 0) {
+                code = 1u;
+            } else {
+                if (i / S != strip || j < base) {
+                    strip = i / S;
+                    base = j >= 31 ? j - 31 : 0;
+                    const int col = base + lane;
+                    wreg = col < m ? (uint32_t)dir[(int64_t)strip * m + col] : 0u;
                 }
+                const uint32_t w = __shfl_sync(0xffffffffu, wreg, j - base);
+                code = (w >> (2 * (i % S))) & 3u;
             }
-            lo[0] = 0;
+            if (code == 2u) {
+                j -= 1;
+            } else {
+                if (lane == 0) lo[i] = j;
+                i -= 1;
+                if (code == 0u) j -= 1;
+                if (lane == 0) hi[i] = j;
+            }
         }
+        if (lane == 0) lo[0] = 0;
         __syncwarp();
     }
 }

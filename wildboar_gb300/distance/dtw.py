@@ -140,7 +140,6 @@ def _mm_average_groups(Xd, groups, init, *, r, g=None, sample_weight=None, tol=1
     fused = g is None and nm == T
     sw = [None] * G if sample_weight is None else sample_weight
     costs = np.full(G, np.nan)
-    done = np.zeros(G, dtype=bool)
 
     def swdev_of(lay_active):
         if sample_weight is None:
@@ -157,48 +156,57 @@ def _mm_average_groups(Xd, groups, init, *, r, g=None, sample_weight=None, tol=1
             out[a] = _group_cost(d, sw[a])
         return out
 
-    active = [a for a in range(G)]
+    active = list(range(G))
     lay = _layout(groups, active, torch, dev)
-    if fused:
-        # one pass: cost of the current means, and the next means
-        last = torch.empty(lay[0].shape[0], dtype=torch.float64, device=dev)
-        _step(Xd, cur, lay, r, wdev, swdev_of(active), nxt, last, torch)
-        sq = np.sqrt(last.cpu().numpy())
+    swd = swdev_of(active)
+    final = np.empty((G, nm))
+    last = torch.empty(lay[0].shape[0], dtype=torch.float64, device=dev) if fused else None
+
+    def fused_costs():
+        n_pairs = lay[0].shape[0]
+        sq = np.sqrt(last[:n_pairs].cpu().numpy())
         start = lay[4]
-        cost = {a: _group_cost(sq[start[i]:start[i + 1]], sw[a]) for i, a in enumerate(active)}
+        return {a: _group_cost(sq[start[i]:start[i + 1]], sw[a]) for i, a in enumerate(active)}
+
+    if fused:
+        # one pass gives the cost of the current means and the next means
+        _step(Xd, cur, lay, r, wdev, swd, nxt, last, torch)
+        cost = fused_costs()
     else:
         cost = distance_costs(cur, active)
     for epoch in range(max_epoch):
         if not active:
             break
         if fused:
-            # nxt holds the means of this epoch (from the alignment of cur)
-            idx = torch.as_tensor(active, device=dev)
-            cur[idx] = nxt[idx]
-            last = torch.empty(lay[0].shape[0], dtype=torch.float64, device=dev)
-            _step(Xd, cur, lay, r, wdev, swdev_of(active), nxt, last, torch)
-            sq = np.sqrt(last.cpu().numpy())
-            start = lay[4]
-            new_cost = {a: _group_cost(sq[start[i]:start[i + 1]], sw[a])
-                        for i, a in enumerate(active)}
+            # the rows of the active groups in nxt are this epoch's means
+            cur, nxt = nxt, cur
+            _step(Xd, cur, lay, r, wdev, swd, nxt, last, torch)
+            new_cost = fused_costs()
         else:
-            _step(Xd, cur, lay, r, wdev, swdev_of(active), cur, None, torch)
+            _step(Xd, cur, lay, r, wdev, swd, cur, None, torch)
             new_cost = distance_costs(cur, active)
-        still = []
+        still, finished = [], []
         for a in active:
             prev_cost, cost[a] = cost[a], new_cost[a]
             if abs(prev_cost - cost[a]) < tol:
                 if verbose:
                     print(f"Complete at epoch={epoch} with cost={cost[a]}.")
-                done[a] = True
+                finished.append(a)
             else:
                 still.append(a)
-        if len(still) != len(active):
+        if finished:
+            host = cur.cpu().numpy()
+            final[finished] = host[finished]
             active = still
-            lay = _layout(groups, active, torch, dev) if active else None
+            if active:
+                lay = _layout(groups, active, torch, dev)
+                swd = swdev_of(active)
+    if active:
+        host = cur.cpu().numpy()
+        final[active] = host[active]
     for a in range(G):
         costs[a] = cost[a]
-    return cur.cpu().numpy(), costs
+    return final, costs
 
 
 def dtw_average(X, *, r=1.0, g=None, sample_weight=None, init="random", method="mm",
