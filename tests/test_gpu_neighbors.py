@@ -3,10 +3,11 @@ on the GPU path.
 
 Parity: the reference's own outputs (golden fixtures made by running it,
 tests/golden/make_golden.py) through the public API, and the CPU oracle
-(oracle.dtw_average_mm / oracle.kmeans) on larger seeded cases: the
-alignment kernel's strip widths 4, 8 and 16 rows per lane, means longer than
-one pass of 512 rows, weights, sample weights, groups converging at
-different epochs.  Means, costs and distances within 1e-12 relative (the
+(oracle.dtw_average_mm / oracle.kmeans) on larger seeded cases: both
+alignment kernels (the row-strip wavefront with 4, 8 and 16 rows per lane and
+means longer than one pass of 512 rows; the anti-diagonal form with 1 to 16
+register slots per lane), weights, sample weights, unequal lengths, groups
+converging at different epochs.  Means, costs and distances within 1e-12 relative (the
 kernels perform the reference's operations in its order; 1e-12 absorbs libm
 differences between machines), labels, indices and iteration counts exact.
 """
@@ -155,3 +156,20 @@ def test_mm_step_launches_native_kernels():
     before = _lib.launch_count()
     dtw_average(X, r=0.5, init=X[0], max_epoch=2, tol=0.0)
     assert _lib.launch_count() - before >= 2
+
+
+# both alignment kernels (row-strip wavefront, anti-diagonal) on the same cases
+@pytest.mark.parametrize("form", ["strip", "antidiag"])
+@pytest.mark.parametrize("n,T,r,g", [(40, 40, 1.0, None), (200, 200, 0.2, None),
+                                     (300, 300, 1.0, None), (500, 480, 0.1, 0.05),
+                                     (64, 100, 0.4, None), (120, 70, 0.25, 0.2),
+                                     (33, 33, 0.0, None)])
+def test_alignment_forms_vs_oracle(monkeypatch, form, n, T, r, g):
+    monkeypatch.setenv("WB_MM_ALIGN", form)
+    rng = np.random.default_rng(7 * n + T)
+    X = _walk(rng, (6, T))
+    init = _walk(rng, n)
+    mean, cost = dtw_average(X, r=r, g=g, init=init, return_cost=True, max_epoch=4, tol=0.0)
+    om, oc = O.dtw_average_mm(X, r=r, g=g, init=init, max_epoch=4, tol=0.0)
+    np.testing.assert_allclose(mean, om, rtol=RTOL, atol=0)
+    np.testing.assert_allclose(cost, oc, rtol=RTOL, atol=0)

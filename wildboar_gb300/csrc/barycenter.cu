@@ -30,6 +30,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
 
 #include "common.cuh"
 
@@ -60,7 +62,7 @@ struct MmAlignJob {
     int64_t q0 = 0, q1 = 0;         // pairs of this launch
     int r = 1;                      // warp size max(floor(max(n, m) r), 1)
     const double *weights = nullptr;  // weights[|i - j|] or nullptr
-    void *dir = nullptr;            // per pair (ceil(n / S), m) direction words
+    void *dir = nullptr;            // per pair: (ceil(n / S), m) or (n + m - 1, 32) words
     int64_t dir_pair_words = 0;
     double *bnd = nullptr;          // per warp slot: boundary row (m doubles)
     int32_t *path_lo = nullptr;     // (n_pairs, n)
@@ -192,6 +194,192 @@ __global__ void __launch_bounds__(kMmThreads) mm_align_kernel(const MmAlignJob J
     }
 }
 
+// ---------------------------------------------------------------------------
+// Anti-diagonal form for narrow bands.  In the row-strip wavefront above a
+// lane's rows meet their band for only (band width + S) of the m + 31 steps,
+// and an FP64 warp instruction costs the FP64 pipe the same whatever its
+// active lanes, so a narrow band pays for the whole matrix.  Here the warp
+// walks the anti-diagonals d = i + j: the in-band cells of diagonal d are
+// rows ilo(d) .. ihi(d), and slot s = i - ilo(d) goes to lane s % 32,
+// register s / 32 (K registers).  A cell reads up (i - 1, j) and left
+// (i, j - 1) from diagonal d - 1 and diag (i - 1, j - 1) from d - 2; since
+// ilo grows by 0 or 1 per diagonal those are the previous diagonals' slots
+// shifted by -1, 0 or +1: one warp shuffle each.  Register slots past the
+// diagonal's cells are skipped by a warp-uniform test, so FP64 instructions
+// run only for in-band cells (up to 31 idle lanes per diagonal).  The move
+// codes go to one word per (diagonal, lane) (2 bits per register slot); the
+// traceback reads them through a shared-memory window of 16 diagonals.
+
+template <int K>
+struct AdWord { using T = uint32_t; };
+template <>
+struct AdWord<1> { using T = uint8_t; };
+template <>
+struct AdWord<2> { using T = uint8_t; };
+template <>
+struct AdWord<4> { using T = uint8_t; };
+template <>
+struct AdWord<8> { using T = uint16_t; };
+
+__host__ __device__ __forceinline__ int floordiv2(int a) { return a >= 0 ? a / 2 : -((1 - a) / 2); }
+
+// in-band rows of anti-diagonal d (band rows i: columns
+// [max(0, i - mn - r + 1), min(m, i + mx)))
+__host__ __device__ __forceinline__ void ad_bounds(int d, int n, int m, int r, int mx, int mn,
+                                                   int &ilo, int &ihi) {
+    int lo = d - m + 1 > 0 ? d - m + 1 : 0;
+    const int l2 = floordiv2(d - mx) + 1;
+    lo = l2 > lo ? l2 : lo;
+    int hi = n - 1 < d ? n - 1 : d;
+    const int h2 = floordiv2(d + mn + r - 1);
+    hi = h2 < hi ? h2 : hi;
+    ilo = lo;
+    ihi = hi;
+}
+
+// slot (lane + 32 k) + SH of the K-slot array P (SH in {-1, 0, +1}); slots
+// outside [0, 32 K) read +inf
+template <int K, int SH>
+__device__ __forceinline__ void ad_shift(const double (&P)[K], double (&out)[K], int lane) {
+    const double INF = __longlong_as_double(0x7ff0000000000000LL);
+    if constexpr (SH == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) out[k] = P[k];
+    } else {
+        double t[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) t[k] = __shfl_sync(0xffffffffu, P[k], (lane + SH) & 31);
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            if (SH < 0)
+                out[k] = lane == 0 ? (k == 0 ? INF : t[k == 0 ? 0 : k - 1]) : t[k];
+            else
+                out[k] = lane == 31 ? (k == K - 1 ? INF : t[k == K - 1 ? 0 : k + 1]) : t[k];
+        }
+    }
+}
+
+constexpr int kAdWindow = 16;
+
+template <int K, bool W>
+__global__ void __launch_bounds__(kMmThreads) mm_align_ad_kernel(const MmAlignJob J) {
+    using Word = typename AdWord<K>::T;
+    const double INF = __longlong_as_double(0x7ff0000000000000LL);
+    __shared__ uint32_t win_all[kMmWarps][kAdWindow * 32];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const int slot = blockIdx.x * kMmWarps + wid;
+    uint32_t *win = win_all[wid];
+    const int n = J.n, m = J.m, r = J.r;
+    const int mx = imax(0, m - n) + r;
+    const int mn = imax(0, n - m);
+    const int D = n + m - 1;
+    for (int64_t q = J.q0 + slot; q < J.q1; q += (int64_t)gridDim.x * kMmWarps) {
+        const double *Y = J.x + J.member[q] * J.x_stride;
+        const double *X = J.means + (int64_t)J.pair_group[q] * n;
+        Word *dir = reinterpret_cast<Word *>(J.dir) + (q - J.q0) * J.dir_pair_words;
+        double P1[K], P2[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            P1[k] = INF;
+            P2[k] = INF;
+        }
+        int lo1 = 0, lo2 = 0;
+        double fin = INF;
+        for (int d = 0; d < D; d++) {
+            int ilo, ihi;
+            ad_bounds(d, n, m, r, mx, mn, ilo, ihi);
+            const int cnt = ihi - ilo + 1;
+            const int d1 = ilo - lo1, d2 = ilo - lo2;
+            double up[K], left[K], diag[K];
+            if (d1 == 0) {
+                ad_shift<K, -1>(P1, up, lane);
+                ad_shift<K, 0>(P1, left, lane);
+            } else {
+                ad_shift<K, 0>(P1, up, lane);
+                ad_shift<K, 1>(P1, left, lane);
+            }
+            if (d2 == 0)
+                ad_shift<K, -1>(P2, diag, lane);
+            else if (d2 == 1)
+                ad_shift<K, 0>(P2, diag, lane);
+            else
+                ad_shift<K, 1>(P2, diag, lane);
+            uint32_t word = 0;
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                double v = INF;
+                if (32 * k < cnt) {
+                    const int s = lane + 32 * k;
+                    if (s < cnt) {
+                        const int i = ilo + s, j = d - i;
+                        const double dd = __ldg(X + i) - __ldg(Y + j);
+                        double c = dd * dd;
+                        if (W) c = c * __ldg(J.weights + (i > j ? i - j : j - i));
+                        if (d == 0) {
+                            v = c;
+                        } else {
+                            const long long bu = dbits(up[k]), bl = dbits(left[k]),
+                                            bd = dbits(diag[k]);
+                            const long long mu = bl < bu ? bl : bu;
+                            v = __longlong_as_double(bd < mu ? bd : mu) + c;
+                            word |= move_code(bd, bu, bl) << (2 * k);
+                        }
+                        if (d == D - 1) fin = v;
+                    }
+                }
+                P2[k] = P1[k];
+                P1[k] = v;
+            }
+            dir[(int64_t)d * 32 + lane] = (Word)word;
+            lo2 = lo1;
+            lo1 = ilo;
+        }
+        // the last diagonal has one cell, in slot 0
+        fin = __shfl_sync(0xffffffffu, fin, 0);
+        if (lane == 0 && J.last) J.last[q] = fin;
+        __syncwarp();
+        int32_t *lo = J.path_lo + q * (int64_t)n;
+        int32_t *hi = J.path_hi + q * (int64_t)n;
+        int i = n - 1, j = m - 1;
+        int wtop = -1;  // the window holds diagonals wtop - 15 .. wtop
+        if (lane == 0) hi[i] = j;
+        while (i > 0 || j > 0) {
+            uint32_t code;
+            if (i == 0) {
+                code = 2u;
+            } else if (j == 0) {
+                code = 1u;
+            } else {
+                const int d = i + j;
+                if (d > wtop || d <= wtop - kAdWindow) {
+                    __syncwarp();
+                    wtop = d;
+#pragma unroll
+                    for (int t = 0; t < kAdWindow; t++)
+                        win[t * 32 + lane] = d - t >= 0 ? (uint32_t)dir[(int64_t)(d - t) * 32 + lane]
+                                                        : 0u;
+                    __syncwarp();
+                }
+                int ilo, ihi;
+                ad_bounds(d, n, m, r, mx, mn, ilo, ihi);
+                const int s = i - ilo;
+                code = (win[(wtop - d) * 32 + (s & 31)] >> (2 * (s >> 5))) & 3u;
+            }
+            if (code == 2u) {
+                j -= 1;
+            } else {
+                if (lane == 0) lo[i] = j;
+                i -= 1;
+                if (code == 0u) j -= 1;
+                if (lane == 0) hi[i] = j;
+            }
+        }
+        if (lane == 0) lo[0] = 0;
+        __syncwarp();
+    }
+}
+
 // Thread (group gi, row): pairs group_start[gi] .. group_start[gi + 1] - 1 of
 // the group in sample order; path_lo / path_hi null: the single cell x = row.
 // The result goes to row groups[gi] (gi when groups is null) of out.
@@ -238,6 +426,13 @@ int launch_align(const MmAlignJob &J, int grid, cudaStream_t st) {
     return WB_OK;
 }
 
+template <int K, bool W>
+int launch_ad(const MmAlignJob &J, int grid, cudaStream_t st) {
+    mm_align_ad_kernel<K, W><<<grid, kMmThreads, 0, st>>>(J);
+    WB_LAUNCH_CHECK("mm_align_ad_kernel");
+    return WB_OK;
+}
+
 int pick_strip(int n) {
     if (n <= 32 * 4) return 4;
     if (n <= 32 * 8) return 8;
@@ -270,11 +465,38 @@ extern "C" int wb_dtw_average_mm_step(const double *x, int64_t x_stride, int64_t
     const int64_t big = n > m ? n : m;
     const double wv = std::floor((double)big * r);
     const int warp = (int)(wv > 1.0 ? wv : 1.0);
+    // FP64 warp-instruction slots of the two forms: the strip wavefront runs
+    // 32 S rows x (m + 31) steps per pass, the anti-diagonal form
+    // 32 ceil(cnt / 32) slots per diagonal
     const int S = pick_strip(n);
-    const int64_t word_bytes = S / 4;
-    const int64_t pair_words = (int64_t)((n + S - 1) / S) * m;
+    const int mxb = imax(0, m - n) + warp, mnb = imax(0, n - m);
+    int maxcnt = 0;
+    int64_t slots_ad = 0;
+    for (int d = 0; d < n + m - 1; d++) {
+        int ilo, ihi;
+        ad_bounds(d, n, m, warp, mxb, mnb, ilo, ihi);
+        const int cnt = ihi - ilo + 1;
+        maxcnt = cnt > maxcnt ? cnt : maxcnt;
+        slots_ad += 32LL * ((cnt + 31) / 32);
+    }
+    const int64_t slots_strip = (int64_t)((n + 32 * S - 1) / (32 * S)) * (m + 31) * 32 * S;
+    int K = 1;
+    while (32 * K < maxcnt) K *= 2;
+    bool antidiag = K <= 16 && slots_ad < slots_strip;
+    if (const char *f = std::getenv("WB_MM_ALIGN")) {
+        if (std::strcmp(f, "strip") == 0) antidiag = false;
+        if (std::strcmp(f, "antidiag") == 0 && K <= 16) antidiag = true;
+    }
+    int64_t pair_words, word_bytes;
+    if (antidiag) {
+        pair_words = (int64_t)(n + m - 1) * 32;
+        word_bytes = K <= 4 ? 1 : (K <= 8 ? 2 : 4);
+    } else {
+        pair_words = (int64_t)((n + S - 1) / S) * m;
+        word_bytes = S / 4;
+    }
     const int64_t pair_bytes = pair_words * word_bytes;
-    const bool passes = n > 32 * S;
+    const bool passes = !antidiag && n > 32 * S;
     const DeviceInfo &dev = device_info();
     const int max_grid = dev.sm_count * 8;
     // direction words per launch bounded to about 1 GiB
@@ -310,18 +532,27 @@ extern "C" int wb_dtw_average_mm_step(const double *x, int64_t x_stride, int64_t
     J.path_lo = lo;
     J.path_hi = hi;
     J.last = last;
-    timer_begin("mm_align_kernel", st);
+    timer_begin(antidiag ? "mm_align_ad_kernel" : "mm_align_kernel", st);
     for (int64_t q0 = 0; q0 < n_pairs; q0 += chunk) {
         J.q0 = q0;
         J.q1 = std::min(n_pairs, q0 + chunk);
         const bool w = weights != nullptr;
         int s;
-        if (S == 4)
+        if (antidiag) {
+            switch (K) {
+                case 1: s = w ? launch_ad<1, true>(J, grid, st) : launch_ad<1, false>(J, grid, st); break;
+                case 2: s = w ? launch_ad<2, true>(J, grid, st) : launch_ad<2, false>(J, grid, st); break;
+                case 4: s = w ? launch_ad<4, true>(J, grid, st) : launch_ad<4, false>(J, grid, st); break;
+                case 8: s = w ? launch_ad<8, true>(J, grid, st) : launch_ad<8, false>(J, grid, st); break;
+                default: s = w ? launch_ad<16, true>(J, grid, st) : launch_ad<16, false>(J, grid, st); break;
+            }
+        } else if (S == 4) {
             s = w ? launch_align<4, true>(J, grid, st) : launch_align<4, false>(J, grid, st);
-        else if (S == 8)
+        } else if (S == 8) {
             s = w ? launch_align<8, true>(J, grid, st) : launch_align<8, false>(J, grid, st);
-        else
+        } else {
             s = w ? launch_align<16, true>(J, grid, st) : launch_align<16, false>(J, grid, st);
+        }
         if (s != WB_OK) return s;
     }
     timer_end(st);
