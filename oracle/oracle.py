@@ -89,6 +89,9 @@ def lib():
         L.wbo_fast_mean_std.argtypes = [dp, i64, dp, dp]
         L.wbo_dtw_alignment.argtypes = [dp, i64, dp, i64, i64, dp, dp]
         L.wbo_mm_epoch.argtypes = [dp, i64, i64, dp, i64, i64, dp, dp, dp, dp, ip, dp]
+        L.wbo_scaled_dtw_subsequence.argtypes = [dp, ip, ip, dp, dp, i64, dp, i64, i64, i64,
+                                                 i64, ctypes.c_double, ctypes.c_int,
+                                                 ctypes.c_double, ctypes.c_int, dp, ip, dp, i64]
         L.wbo_subsequence_matches.argtypes = [dp, ip, ip, dp, dp, i64, dp, i64, i64, i64,
                                               ctypes.c_int, pp, ctypes.c_double, dp, dp, i64,
                                               ctypes.c_int, ctypes.c_int]
@@ -197,6 +200,9 @@ SUBSEQ_DEFAULTS = {
 def subsequence(shapelets, x, *, dim=0, metric="euclidean", metric_params=None,
                 n_threads=1):
     """(n_samples, n_shapelets) min distance and first argmin index."""
+    if metric == "scaled_dtw":
+        return scaled_dtw_subsequence(shapelets, x, r=(metric_params or {}).get("r", 1.0),
+                                      dim=dim)
     X = _ts(x)
     shp = [np.asarray(s, dtype=np.float64).ravel() for s in shapelets]
     lens = np.array([s.shape[0] for s in shp], dtype=np.int64)
@@ -254,6 +260,11 @@ def subsequence_matches(shapelets, x, threshold, *, dim=0, metric="euclidean",
     X = _ts(x)
     shp = [np.asarray(s, dtype=np.float64).ravel() for s in shapelets]
     lens = np.array([s.shape[0] for s in shp], dtype=np.int64)
+    if metric == "scaled_dtw":
+        r = (metric_params or {}).get("r", 1.0)
+        ld = int(X.shape[2] - lens.min() + 1)
+        dist, keep = scaled_dtw_matches(shp, X, threshold, r=r, dim=dim, transient=transient)
+        return dist[:, :ld], keep[:, :ld]
     offs = np.zeros(len(shp), dtype=np.int64)
     offs[1:] = np.cumsum(lens)[:-1]
     packed = np.ascontiguousarray(np.concatenate(shp))
@@ -485,3 +496,59 @@ def knn_predict_proba(x_train, y_train, x, *, n_neighbors=5, metric="euclidean",
     for i in range(len(classes)):
         probs[:, i] = np.sum(preds == i, axis=1) / n_neighbors
     return probs
+
+
+# --------------------------------------------------------------------------
+# scaled_dtw subsequence metric (UCR-suite scan)
+
+
+def _packed(shapelets):
+    shp = [np.asarray(s, dtype=np.float64).ravel() for s in shapelets]
+    lens = np.array([s.shape[0] for s in shp], dtype=np.int64)
+    offs = np.zeros(len(shp), dtype=np.int64)
+    offs[1:] = np.cumsum(lens)[:-1]
+    return shp, np.ascontiguousarray(np.concatenate(shp)), offs, lens
+
+
+def scaled_dtw_subsequence(shapelets, x, *, r=1.0, dim=0, paired=False):
+    """pairwise / paired_subsequence_distance with metric="scaled_dtw"
+    (ScaledDtwSubsequenceMetric, distance/_elastic.pyx:1928-2204, scan
+    :353-465): (min distance, first argmin window); (n_samples, m) or (m,)."""
+    X = _ts(x)
+    shp, packed, offs, lens = _packed(shapelets)
+    smean = np.array([np.mean(s) for s in shp])
+    sstd = np.array([np.std(s) for s in shp])
+    sstd[sstd <= 1e-13] = 0.0
+    shape = (len(shp),) if paired else (X.shape[0], len(shp))
+    dist = np.empty(shape)
+    idx = np.zeros(shape, dtype=np.int64)
+    lib().wbo_scaled_dtw_subsequence(_dp(packed), _ip(offs), _ip(lens), _dp(smean), _dp(sstd),
+                                     len(shp), _dp(X), X.shape[0], X.shape[1], X.shape[2], dim,
+                                     float(r), 1 if paired else 0, -1.0, 0, _dp(dist),
+                                     _ip(idx), None, 0)
+    return dist, idx
+
+
+def scaled_dtw_matches(shapelets, x, threshold, *, r=1.0, dim=0, transient=False):
+    """scaled_dtw_matches (distance/_elastic.pyx:468-620) of shapelet i in
+    x[i, dim]: (distance per window, keep flags), (n, n_timestep).
+    threshold=inf with transient=True is the distance profile
+    (_DistanceProfile: fast transient statistics, a zero std kept)."""
+    X = _ts(x)
+    shp, packed, offs, lens = _packed(shapelets)
+    if transient:
+        stats = [fast_mean_std(s) for s in shp]
+        smean = np.array([a for a, _ in stats])
+        sstd = np.array([b for _, b in stats])
+    else:
+        smean = np.array([np.mean(s) for s in shp])
+        sstd = np.array([np.std(s) for s in shp])
+        sstd[sstd <= 1e-13] = 0.0
+    ld = X.shape[2]
+    dist = np.ones((len(shp), ld)) if transient else np.full((len(shp), ld), np.nan)
+    keep = np.zeros((len(shp), ld))
+    lib().wbo_scaled_dtw_subsequence(_dp(packed), _ip(offs), _ip(lens), _dp(smean), _dp(sstd),
+                                     len(shp), _dp(X), X.shape[0], X.shape[1], X.shape[2], dim,
+                                     float(r), 1, float(threshold), 1 if transient else 0,
+                                     _dp(dist), None, _dp(keep), ld)
+    return dist, keep

@@ -1352,3 +1352,315 @@ int wbo_mm_epoch(const double *X, idx_t n_samples, idx_t T, const double *mean, 
     free(V);
     return 0;
 }
+
+/* ------------------------------------------------------------------------
+ * scaled_dtw subsequence metric: ScaledDtwSubsequenceMetric
+ * (distance/_elastic.pyx:1928-2204) with the UCR-suite scan
+ * scaled_dtw_subsequence_distance / scaled_dtw_matches (:353-620).
+ */
+
+/* the reference's ring deque (_elastic.pyx:37-95): push at `back`, moving
+ * down; the front element sits just above `front` */
+typedef struct {
+    idx_t *q;
+    idx_t cap, size, front, back;
+} sdq;
+
+static void sdq_reset(sdq *c) { c->size = 0; c->front = 0; c->back = c->cap - 1; }
+static void sdq_push_back(sdq *c, idx_t v)
+{
+    c->q[c->back] = v;
+    c->back -= 1;
+    if (c->back < 0) c->back = c->cap - 1;
+    c->size += 1;
+}
+static void sdq_pop_front(sdq *c)
+{
+    c->front -= 1;
+    if (c->front < 0) c->front = c->cap - 1;
+    c->size -= 1;
+}
+static void sdq_pop_back(sdq *c) { c->back = (c->back + 1) % c->cap; c->size -= 1; }
+static idx_t sdq_front(const sdq *c)
+{
+    idx_t t = c->front - 1;
+    if (t < 0) t = c->cap - 1;
+    return c->q[t];
+}
+static idx_t sdq_back(const sdq *c) { return c->q[(c->back + 1) % c->cap]; }
+
+/* find_min_max (_elastic.pyx:98-151): streaming envelope of T with warp r,
+ * including the reference's single front pop per step */
+static void sdtw_envelope(const double *T, idx_t length, idx_t r, double *lower, double *upper,
+                          sdq *dl, sdq *du)
+{
+    sdq_reset(du);
+    sdq_reset(dl);
+    sdq_push_back(du, 0);
+    sdq_push_back(dl, 0);
+    for (idx_t i = 1; i < length; i++) {
+        if (i > r) {
+            idx_t k = i - r - 1;
+            upper[k] = T[sdq_front(du)];
+            lower[k] = T[sdq_front(dl)];
+        }
+        double cur = T[i], prev = T[i - 1];
+        if (cur > prev) {
+            sdq_pop_back(du);
+            while (du->size != 0 && cur > T[sdq_back(du)]) sdq_pop_back(du);
+        } else {
+            sdq_pop_back(dl);
+            while (dl->size != 0 && cur < T[sdq_back(dl)]) sdq_pop_back(dl);
+        }
+        sdq_push_back(du, i);
+        sdq_push_back(dl, i);
+        if (i == 2 * r + 1 + sdq_front(du))
+            sdq_pop_front(du);
+        else if (i == 2 * r + 1 + sdq_front(dl))
+            sdq_pop_front(dl);
+    }
+    for (idx_t i = length; i < length + r + 1; i++) {
+        idx_t k = i - r - 1;
+        upper[k] = T[sdq_front(du)];
+        lower[k] = T[sdq_front(dl)];
+        if (i - sdq_front(du) >= 2 * r + 1) sdq_pop_front(du);
+        if (i - sdq_front(dl) >= 2 * r + 1) sdq_pop_front(dl);
+    }
+}
+
+static inline double sd2(double x, double y) { double s = x - y; return s * s; }
+
+/* constant_lower_bound (_elastic.pyx:159-237), LB_Kim of the first and last
+ * three points (the reference's second end term compares t_y1 with s_y1 twice) */
+/* (the reference reads T[1], T[2], T[L - 2], T[L - 3] and the same points
+ * of S whatever L is; for L < 3 those reads leave the arrays, here they are
+ * clamped to [0, L - 1]) */
+static inline idx_t sdtw_ix(idx_t k, idx_t L) { return k < 0 ? 0 : (k >= L ? L - 1 : k); }
+
+static double sdtw_kim(const double *S, double sm, double ss, const double *T, double tm,
+                       double ts, idx_t L, double best)
+{
+    if (ts == 0) return 0;
+    const idx_t a1 = sdtw_ix(1, L), a2 = sdtw_ix(2, L), b1 = sdtw_ix(L - 2, L),
+                b2 = sdtw_ix(L - 3, L);
+    double tx0 = (T[0] - tm) / ts, ty0 = (T[L - 1] - tm) / ts;
+    double sx0 = (S[0] - sm) / ss, sy0 = (S[L - 1] - sm) / ss;
+    double md = sd2(tx0, sx0) + sd2(ty0, sy0);
+    if (md >= best) return md;
+    double tx1 = (T[a1] - tm) / ts, sx1 = (S[a1] - sm) / ss;
+    md += dmin(dmin(sd2(tx1, sx0), sd2(tx0, sx1)), sd2(tx1, sx1));
+    if (md >= best) return md;
+    double ty1 = (T[b1] - tm) / ts, sy1 = (S[b1] - sm) / ss;
+    md += dmin(dmin(sd2(ty1, sy1), sd2(ty0, sy1)), sd2(ty1, sy1));
+    if (md >= best) return md;
+    double tx2 = (T[a2] - tm) / ts, sx2 = (S[a2] - sm) / ss;
+    md += dmin(dmin(dmin(sd2(tx0, sx2), dmin(sd2(tx1, sx2), sd2(tx2, sx2))), sd2(tx2, sx1)),
+               sd2(tx2, sx0));
+    if (md >= best) return md;
+    double ty2 = (T[b2] - tm) / ts, sy2 = (S[b2] - sm) / ss;
+    md += dmin(dmin(dmin(sd2(ty0, sy2), dmin(sd2(ty1, sy2), sd2(ty2, sy2))), sd2(ty2, sy1)),
+               sd2(ty2, sy0));
+    return md;
+}
+
+/* cumulative_bound (_elastic.pyx:240-270): LB_Keogh of T (normalised with
+ * mean/std) against an envelope normalised with lu_mean/lu_std */
+static double sdtw_keogh(const double *T, idx_t L, double mean, double std, double lu_mean,
+                         double lu_std, const double *lower, const double *upper, double *cb,
+                         double best)
+{
+    double md = 0;
+    for (idx_t i = 0; i < L; i++) {
+        if (md >= best) break;
+        double x = (T[i] - mean) / std;
+        double us = (upper[i] - lu_mean) / lu_std;
+        double ls = (lower[i] - lu_mean) / lu_std;
+        double d;
+        if (x > us) d = sd2(x, us);
+        else if (x < ls) d = sd2(x, ls);
+        else d = 0;
+        md += d;
+        cb[i] = d;
+    }
+    return md;
+}
+
+/* inner_scaled_dtw_subsequence_distance (_elastic.pyx:273-344): Sakoe-Chiba
+ * band |i - j| <= r, rows abandoned on row min + cb[i + r + 1] >= min_dist */
+static double sdtw_inner(const double *S, idx_t L, double sm, double ss, const double *X,
+                         double mean, double std, idx_t r, const double *cb, double *cost,
+                         double *cost_prev, double min_dist)
+{
+    int std_zero = std == 0, s_std_zero = ss == 0;
+    if (std_zero && s_std_zero) return 0;
+    for (idx_t i = 0; i < 2 * r + 1; i++) {
+        cost[i] = INF;
+        cost_prev[i] = INF;
+    }
+    idx_t k = 0;
+    for (idx_t i = 0; i < L; i++) {
+        k = imax(0, r - i);
+        double min_cost = INF;
+        for (idx_t j = imax(0, i - r); j < imin(L, i + r + 1); j++) {
+            double v;
+            if (i == 0 && j == 0) {
+                v = !s_std_zero ? (S[0] - sm) / ss : 0;
+                if (!std_zero) v -= (X[0] - mean) / std;
+                cost[k] = v * v;
+            } else {
+                double y = (j - 1 < 0 || k - 1 < 0) ? INF : cost[k - 1];
+                double x = (i - 1 < 0 || k + 1 > 2 * r) ? INF : cost_prev[k + 1];
+                double z = (i - 1 < 0 || j - 1 < 0) ? INF : cost_prev[k];
+                v = (S[i] - sm) / ss;
+                if (!std_zero) v -= (X[j] - mean) / std;
+                cost[k] = dmin(dmin(x, y), z) + v * v;
+            }
+            if (cost[k] < min_cost) min_cost = cost[k];
+            k += 1;
+        }
+        if (i + r < L - 1 && min_cost + cb[i + r + 1] >= min_dist)
+            return min_cost + cb[i + r + 1];
+        double *t = cost;
+        cost = cost_prev;
+        cost_prev = t;
+    }
+    return cost_prev[k - 1];
+}
+
+typedef struct {
+    double *xbuf, *tl, *tu, *cost, *cost_prev, *cb, *cb1, *cb2;
+} sdtw_work;
+
+/* the UCR scan of one series (scaled_dtw_subsequence_distance and
+ * scaled_dtw_matches share it): threshold < 0 gives the minimum (and its
+ * first window in *index); otherwise every window with distance <= threshold
+ * goes to distances[] / matches[] in order and the count is returned */
+static idx_t sdtw_scan(const double *S, idx_t L, double sm, double ss, const double *sl,
+                       const double *su, const double *T, idx_t n, idx_t r, sdtw_work *w,
+                       double threshold, double *min_out, idx_t *index, double *distances,
+                       idx_t *matches)
+{
+    double ex = 0, ex2 = 0, min_dist = INF;
+    int find_min = threshold < 0;
+    double thr = find_min ? 0 : threshold * threshold;
+    idx_t n_matches = 0;
+    for (idx_t i = 0; i < n; i++) {
+        double cv = T[i];
+        ex += cv;
+        ex2 += cv * cv;
+        idx_t pos = i % L;
+        w->xbuf[pos] = cv;
+        w->xbuf[pos + L] = cv;
+        if (i >= L - 1) {
+            idx_t j = (i + 1) % L;
+            idx_t I = i - (L - 1);
+            double mean = ex / L;
+            double tmp = ex2 / L - mean * mean;
+            double std = tmp > 0 ? sqrt(tmp) : 1.0;
+            double bound = find_min ? min_dist : thr;
+            double lb_kim = sdtw_kim(S, sm, ss, w->xbuf + j, mean, std, L, bound);
+            if (lb_kim < bound) {
+                double lb_k = sdtw_keogh(w->xbuf + j, L, mean, std, sm, ss, sl, su, w->cb1, bound);
+                if (lb_k < bound) {
+                    double lb_k2 = sdtw_keogh(S, L, sm, ss, mean, std, w->tl + I, w->tu + I,
+                                              w->cb2, bound);
+                    if (lb_k2 < bound) {
+                        const double *src = lb_k > lb_k2 ? w->cb1 : w->cb2;
+                        w->cb[L - 1] = src[L - 1];
+                        for (idx_t k = L - 2; k >= 0; k--) w->cb[k] = w->cb[k + 1] + src[k];
+                        double dist = sdtw_inner(S, L, sm, ss, w->xbuf + j, mean, std, r, w->cb,
+                                                 w->cost, w->cost_prev, bound);
+                        if (find_min) {
+                            if (dist < min_dist) {
+                                if (index) *index = (i + 1) - L;
+                                min_dist = dist;
+                            }
+                        } else if (dist <= thr) {
+                            if (matches) matches[n_matches] = (i + 1) - L;
+                            distances[n_matches] = sqrt(dist);
+                            n_matches++;
+                        }
+                    }
+                }
+            }
+            cv = w->xbuf[j];
+            ex -= cv;
+            ex2 -= cv * cv;
+        }
+    }
+    if (min_out) *min_out = sqrt(min_dist);
+    return n_matches;
+}
+
+static idx_t sdtw_warp(idx_t length, double r)
+{
+    /* _compute_warp_width (_elastic.pyx:1917-1921) */
+    if (r == 1) return length - 1;
+    return (idx_t)floor(length * r);
+}
+
+/* pairwise (paired = 0: every shapelet against every x[i, dim]) or paired
+ * (shapelet i against x[i, dim]) scaled_dtw subsequence scans.  threshold < 0:
+ * minimum distance and first argmin window into out_dist / out_idx
+ * ((xn, m) or (m,)); threshold >= 0 (paired only): the matched windows'
+ * distances at out_dist[i * ld + window] with out_keep = 1.  smean / sstd as
+ * ScaledSubsequenceMetric.from_array gives them (std <= EPSILON -> 0); a zero
+ * std is taken as 1 unless std_as_given (the transient statistics of the
+ * distance profile are used as they are). */
+int wbo_scaled_dtw_subsequence(const double *shp, const idx_t *off, const idx_t *len,
+                               const double *smean, const double *sstd, idx_t m,
+                               const double *X, idx_t xn, idx_t xd, idx_t xL, idx_t dim,
+                               double r, int paired, double threshold, int std_as_given,
+                               double *out_dist, idx_t *out_idx, double *out_keep, idx_t ld)
+{
+    idx_t cap = 2 * sdtw_warp(xL, r) + 2;
+    sdq du = {0}, dl = {0};
+    du.cap = dl.cap = cap;
+    du.q = (idx_t *)malloc(sizeof(idx_t) * cap);
+    dl.q = (idx_t *)malloc(sizeof(idx_t) * cap);
+    idx_t maxL = 0;
+    for (idx_t s = 0; s < m; s++) maxL = imax(maxL, len[s]);
+    sdtw_work w;
+    w.xbuf = (double *)malloc(sizeof(double) * 2 * xL);
+    w.tl = (double *)malloc(sizeof(double) * xL);
+    w.tu = (double *)malloc(sizeof(double) * xL);
+    w.cost = (double *)malloc(sizeof(double) * (2 * xL + 1));
+    w.cost_prev = (double *)malloc(sizeof(double) * (2 * xL + 1));
+    w.cb = (double *)malloc(sizeof(double) * xL);
+    w.cb1 = (double *)malloc(sizeof(double) * xL);
+    w.cb2 = (double *)malloc(sizeof(double) * xL);
+    double *sl = (double *)malloc(sizeof(double) * (maxL > 0 ? maxL : 1));
+    double *su = (double *)malloc(sizeof(double) * (maxL > 0 ? maxL : 1));
+    double *dbuf = (double *)malloc(sizeof(double) * xL);
+    idx_t *ibuf = (idx_t *)malloc(sizeof(idx_t) * xL);
+    idx_t npairs = paired ? m : xn * m;
+    for (idx_t p = 0; p < npairs; p++) {
+        idx_t si = paired ? p : p / m, sh = paired ? p : p % m;
+        const double *S = shp + off[sh];
+        idx_t L = len[sh];
+        idx_t wr = sdtw_warp(L, r);
+        double sm = smean[sh];
+        double ss = (sstd[sh] != 0 || std_as_given) ? sstd[sh] : 1.0;
+        sdtw_envelope(S, L, wr, sl, su, &dl, &du);
+        const double *T = X + (si * xd + dim) * xL;
+        sdtw_envelope(T, xL, wr, w.tl, w.tu, &dl, &du);
+        if (threshold < 0) {
+            double d;
+            idx_t idx = 0;
+            sdtw_scan(S, L, sm, ss, sl, su, T, xL, wr, &w, -1.0, &d, &idx, NULL, NULL);
+            out_dist[p] = d;
+            out_idx[p] = idx;
+        } else {
+            idx_t cnt = sdtw_scan(S, L, sm, ss, sl, su, T, xL, wr, &w, threshold, NULL, NULL,
+                                  dbuf, ibuf);
+            for (idx_t k = 0; k < cnt; k++) {
+                out_dist[p * ld + ibuf[k]] = dbuf[k];
+                out_keep[p * ld + ibuf[k]] = 1.0;
+            }
+        }
+    }
+    free(du.q); free(dl.q);
+    free(w.xbuf); free(w.tl); free(w.tu); free(w.cost); free(w.cost_prev);
+    free(w.cb); free(w.cb1); free(w.cb2); free(sl); free(su); free(dbuf); free(ibuf);
+    return 0;
+}

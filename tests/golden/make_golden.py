@@ -385,6 +385,49 @@ def main():
             {"metric": metric, "metric_params": params, "n_neighbors": 4},
             {"dist_train": dist_tr, "ind_train": ind_tr, "dist": dist_te, "ind": ind_te})
 
+    # scaled_dtw: the UCR-suite scan (distance/_elastic.pyx:159-620, 1928-2204)
+    XS = _walk(rng, (5, 120))
+    XS[3, 40:60] = XS[3, 40]  # a constant stretch (ties in the envelope deques)
+    shp_s = [XS[1, 10:30].copy(), rng.standard_normal(15), XS[0, 50:90] + 0.1,
+             XS[2, 5:8].copy(), np.full(12, 2.5), XS[4, 0:120].copy()[::4].copy(),
+             XS[3, 35:70].copy()]
+    lens_s = np.array([len(s) for s in shp_s])
+    for r in (0.0, 0.1, 0.3, 1.0):
+        params = {"r": r}
+        d, i = pairwise_subsequence_distance(shp_s, XS, metric="scaled_dtw",
+                                             metric_params=params, return_index=True)
+        add(f"subseq_scaled_dtw_r{r}", "subsequence",
+            {"x": XS, "shapelets": np.concatenate(shp_s), "lengths": lens_s},
+            {"metric": "scaled_dtw", "metric_params": params}, {"d": d, "idx": i})
+    shp_p = [XS[k, 7 + 3 * k:27 + 3 * k].copy() + 0.05 * rng.standard_normal(20)
+             for k in range(5)]
+    for r in (0.2, 1.0):
+        d, i = paired_subsequence_distance(shp_p, XS, metric="scaled_dtw",
+                                           metric_params={"r": r}, return_index=True)
+        add(f"paired_scaled_dtw_r{r}", "paired_subsequence",
+            {"x": XS, "shapelets": np.concatenate(shp_p),
+             "lengths": np.array([20] * 5)},
+            {"metric": "scaled_dtw", "metric_params": {"r": r}}, {"d": d, "idx": i})
+    qs = XS[2, 30:52].copy() + 0.05 * rng.standard_normal(22)
+    for r in (0.1, 0.5):
+        dp = distance_profile(qs, XS, metric="scaled_dtw", metric_params={"r": r})
+        add(f"profile_scaled_dtw_r{r}", "distance_profile", {"x": XS, "y": qs},
+            {"metric": "scaled_dtw", "metric_params": {"r": r}}, {"d": dp})
+    for params, kw in (({"r": 0.1}, {"threshold": 2.0}), ({"r": 0.3}, {}),
+                       ({"r": 0.2}, {"threshold": 3.0, "max_matches": 4}),
+                       ({"r": 1.0}, {"threshold": 2.5, "exclude": 3})):
+        res = subsequence_match(qs, XS, metric="scaled_dtw", metric_params=params,
+                                return_distance=True, **kw)
+        tag = f"r{params['r']}_" + "_".join(f"{k}{v}" for k, v in kw.items())
+        add(f"match_scaled_dtw_{tag}", "subsequence_match", {"x": XS, "y": qs},
+            {"metric": "scaled_dtw", "metric_params": params, "kw": kw}, flat(res))
+    res = paired_subsequence_match(shp_p, XS, metric="scaled_dtw", metric_params={"r": 0.2},
+                                   return_distance=True, threshold=2.0)
+    add("paired_match_scaled_dtw_r0.2_threshold2.0", "paired_subsequence_match",
+        {"x": XS, "shapelets": np.concatenate(shp_p), "lengths": np.array([20] * 5)},
+        {"metric": "scaled_dtw", "metric_params": {"r": 0.2}, "kw": {"threshold": 2.0}},
+        flat(res))
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"reference_version": getattr(wildboar, "__version__", "?"),
