@@ -51,6 +51,7 @@ extern "C" {
 #define WB_MSM 10
 #define WB_TWE 11
 #define WB_SCALED_EUCLIDEAN 32
+#define WB_SCALED_DTW 33     /* subsequence metric only (the UCR-suite scan) */
 
 /* dtypes */
 #define WB_F64 0
@@ -119,13 +120,16 @@ int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_t dim,
  * packed float64 values; offsets/lengths index them.  means/stds are the
  * np.mean / np.std of each shapelet (std <= 1e-13 given as 0): the scaled
  * metric uses both, edr with a NaN epsilon uses stds (epsilon = std / 4).
- * metric is WB_EUCLIDEAN, WB_SCALED_EUCLIDEAN or an elastic id (dtw, wdtw,
- * ddtw, wddtw, adtw, lcss, edr, erp, msm, twe) with `params` (NULL allowed for
- * the euclidean ones).  Shapelet arrays live on the same side as x.  Replaces
+ * metric is WB_EUCLIDEAN, WB_SCALED_EUCLIDEAN, WB_SCALED_DTW (params->r;
+ * means and stds required) or an elastic id (dtw, wdtw, ddtw, wddtw, adtw,
+ * lcss, edr, erp, msm, twe) with `params` (NULL allowed for the euclidean
+ * ones).  Shapelet arrays live on the same side as x.  Replaces
  * _pairwise_subsequence_distance (distance/_cdistance.pyx:956-1037) with
- * euclidean_distance / scaled_euclidean_distance (distance/_metric.pyx:561-682)
- * and the elastic *_subsequence_distance functions (distance/_elastic.pyx:
- * 622-1866), including their early abandoning at the running minimum.
+ * euclidean_distance / scaled_euclidean_distance (distance/_metric.pyx:561-682),
+ * the elastic *_subsequence_distance functions (distance/_elastic.pyx:
+ * 622-1866), including their early abandoning at the running minimum, and
+ * the UCR-suite scaled_dtw_subsequence_distance (distance/_elastic.pyx:
+ * 159-465) with its LB_Kim / LB_Keogh pruning decisions.
  */
 int wb_pairwise_subsequence_distance(const double *shapelets, const int64_t *offsets,
                                      const int64_t *lengths, const double *means,
@@ -154,7 +158,11 @@ int wb_paired_subsequence_distance(const double *shapelets, const int64_t *offse
  * erp / msm / twe; NaN past the pair's last window) and out_key[i * ld + w]
  * the largest per-row minimum of the recurrence (the value the reference's
  * early abandoning compares with its threshold; -inf for the euclidean
- * metrics, whose key may be NULL).  ld >= x.n_timestep - min length + 1.
+ * metrics, whose key may be NULL).  For WB_SCALED_DTW out_raw is the squared
+ * dtw cost and out_key the largest of LB_Kim, the two LB_Keogh bounds and
+ * the per-row "row minimum + cumulative bound" (scaled_dtw_matches,
+ * distance/_elastic.pyx:468-620): a window matches threshold t iff
+ * key < t^2 and raw <= t^2.  ld >= x.n_timestep - min length + 1.
  * Shapelets may share storage (equal offsets).  stds of 0 are taken as 1
  * (persistent subsequences, _cdistance.pyx:283-343) unless std_as_given
  * (the distance profile's transient statistics, _cdistance.pyx:1680-1699,

@@ -179,3 +179,48 @@ def test_min_scan_near_ties_vs_oracle(metric):
     od, oi = O.subsequence(shp, X, metric=metric)
     np.testing.assert_array_equal(i, oi)
     np.testing.assert_array_equal(d, od)
+
+
+@pytest.mark.parametrize("r", [0.0, 0.05, 0.2, 1.0])
+def test_scaled_dtw_scan_vs_oracle(r):
+    # the UCR scan: lower bounds prune windows against the running best; the
+    # GPU's 32-window replay must take the reference's decisions
+    from wildboar_gb300.distance import (paired_subsequence_distance,
+                                         pairwise_subsequence_distance)
+
+    rng = np.random.default_rng(45)
+    X = np.cumsum(rng.standard_normal((12, 300)), axis=1)
+    X[5, 100:140] = X[5, 100]
+    shp = [X[k % 12, 20 + 7 * k:20 + 7 * k + L].copy() + 0.02 * rng.standard_normal(L)
+           for k, L in enumerate((8, 16, 16, 33, 64, 5, 100, 23))]
+    shp.append(rng.standard_normal(40))
+    d, i = pairwise_subsequence_distance(shp, X, metric="scaled_dtw", metric_params={"r": r},
+                                         return_index=True)
+    od, oi = O.scaled_dtw_subsequence(shp, X, r=r)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_allclose(d, od, rtol=RTOL, atol=0)
+    d, i = paired_subsequence_distance(shp[:9] + shp[:3], X, metric="scaled_dtw",
+                                       metric_params={"r": r}, return_index=True)
+    od, oi = O.scaled_dtw_subsequence(shp[:9] + shp[:3], X, r=r, paired=True)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_allclose(d, od, rtol=RTOL, atol=0)
+
+
+@pytest.mark.parametrize("r", [0.1, 1.0])
+def test_scaled_dtw_profile_and_matches_vs_oracle(r):
+    rng = np.random.default_rng(46)
+    X = np.cumsum(rng.standard_normal((7, 200)), axis=1)
+    q = X[3, 50:80].copy() + rng.standard_normal(30) * 0.05
+    dp = distance_profile(q, X, metric="scaled_dtw", metric_params={"r": r})
+    od, _ = O.scaled_dtw_matches([q] * 7, X, np.inf, r=r, transient=True)
+    np.testing.assert_allclose(dp, od[:, :171], rtol=RTOL, atol=0)
+    thr = float(np.nanpercentile(dp, 15))
+    res = subsequence_match(q, X, thr, metric="scaled_dtw", metric_params={"r": r},
+                            return_distance=True)
+    counts, idx, dist = _flat(res)
+    d2, keep = O.scaled_dtw_matches([q] * 7, X, thr, r=r)
+    keep = keep[:, :171]
+    np.testing.assert_array_equal(counts, (keep > 0).sum(axis=1))
+    np.testing.assert_array_equal(idx, np.concatenate(
+        [np.flatnonzero(keep[i] > 0) for i in range(7)]))
+    np.testing.assert_allclose(dist, d2[:, :171][keep > 0], rtol=RTOL, atol=0)

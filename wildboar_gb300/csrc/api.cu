@@ -847,6 +847,72 @@ static int subseq_elastic(const double *shapelets, const int64_t *offsets,
     return WB_OK;
 }
 
+// scaled_dtw: staging and outputs around subseq_scaled_dtw (scaled_dtw.cu)
+static int subseq_sdtw_entry(const double *shapelets, const int64_t *offsets,
+                             const int64_t *lengths, const double *means, const double *stds,
+                             int64_t m, const wb_series *x, int64_t dim, const wb_params *p,
+                             double *out_dist, int64_t *out_idx, int32_t out_on_device,
+                             cudaStream_t s, const std::vector<int64_t> &hlen, int64_t total,
+                             bool paired, double *prof_raw, double *prof_key, int64_t prof_ld,
+                             int std_as_given) {
+    if (!(p->r >= 0.0 && p->r <= 1.0)) return fail(WB_EINVAL, "r must be in [0, 1]");
+    const bool dev_in = x->on_device != 0;
+    const bool profile = prof_raw != nullptr;
+    const size_t n_out = profile ? (size_t)m * prof_ld : (paired ? (size_t)m : (size_t)x->n * m);
+    Workspace ws(s);
+    size_t need = subseq_scaled_dtw_bytes(m, total, x->n, (int)x->n_timestep, hlen, p->r,
+                                          x->n_timestep, paired) +
+                  stage_bytes(x) + (dev_in ? 0 : align256(total * 8) + 4 * align256(m * 8)) +
+                  (out_on_device ? 0 : 2 * align256(n_out * 8));
+    WB_TRY(ws.reserve(need));
+    SeriesSet X;
+    WB_TRY(stage(x, dim, ws, X));
+    const double *dshp = shapelets, *dmean = means, *dstd = stds;
+    const int64_t *doff = offsets, *dlen = lengths;
+    if (!dev_in) {
+        WB_TAKE(hs, double, ws, total);
+        WB_TAKE(ho, int64_t, ws, m);
+        WB_TAKE(hl, int64_t, ws, m);
+        WB_TAKE(hm, double, ws, m);
+        WB_TAKE(hd, double, ws, m);
+        WB_CUDA(cudaMemcpyAsync(hs, shapelets, total * 8, cudaMemcpyHostToDevice, s));
+        WB_CUDA(cudaMemcpyAsync(ho, offsets, m * 8, cudaMemcpyHostToDevice, s));
+        WB_CUDA(cudaMemcpyAsync(hl, lengths, m * 8, cudaMemcpyHostToDevice, s));
+        WB_CUDA(cudaMemcpyAsync(hm, means, m * 8, cudaMemcpyHostToDevice, s));
+        WB_CUDA(cudaMemcpyAsync(hd, stds, m * 8, cudaMemcpyHostToDevice, s));
+        dshp = hs;
+        doff = ho;
+        dlen = hl;
+        dmean = hm;
+        dstd = hd;
+    }
+    double *od = profile ? prof_raw : out_dist, *ok = prof_key;
+    int64_t *oi = out_idx;
+    if (!out_on_device) {
+        od = ws.take<double>(n_out);
+        if (profile)
+            ok = ws.take<double>(n_out);
+        else
+            oi = ws.take<int64_t>(n_out);
+        if (!od || (profile ? !ok : !oi)) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    }
+    WB_TRY(subseq_scaled_dtw(dshp, doff, dlen, dmean, dstd, m, hlen, total, X, x->n_timestep,
+                             p->r, paired, std_as_given, profile ? nullptr : od,
+                             profile ? nullptr : oi, profile ? od : nullptr,
+                             profile ? ok : nullptr, prof_ld, ws, s));
+    if (!out_on_device) {
+        if (profile) {
+            WB_CUDA(cudaMemcpyAsync(prof_raw, od, n_out * 8, cudaMemcpyDeviceToHost, s));
+            WB_CUDA(cudaMemcpyAsync(prof_key, ok, n_out * 8, cudaMemcpyDeviceToHost, s));
+        } else {
+            WB_CUDA(cudaMemcpyAsync(out_dist, od, n_out * 8, cudaMemcpyDeviceToHost, s));
+            WB_CUDA(cudaMemcpyAsync(out_idx, oi, n_out * 8, cudaMemcpyDeviceToHost, s));
+        }
+    }
+    WB_CUDA(cudaStreamSynchronize(s));
+    return WB_OK;
+}
+
 // Shared by the pairwise (every series against every shapelet) and paired
 // (series i against shapelet i) subsequence entries.
 static int subseq_entry(const double *shapelets, const int64_t *offsets, const int64_t *lengths,
@@ -863,9 +929,11 @@ static int subseq_entry(const double *shapelets, const int64_t *offsets, const i
                                    std::to_string(x->n) + " samples.");
     WB_TRY(check_dim(x, dim));
     const bool elastic = is_elastic(metric) && metric != WB_WLCSS;
-    if (metric != WB_EUCLIDEAN && metric != WB_SCALED_EUCLIDEAN && !elastic)
+    const bool sdtw = metric == WB_SCALED_DTW;
+    if (metric != WB_EUCLIDEAN && metric != WB_SCALED_EUCLIDEAN && !elastic && !sdtw)
         return fail(WB_EUNSUPPORTED, "unsupported subsequence metric id " + std::to_string(metric));
-    if (elastic && !params) return fail(WB_EINVAL, "params is NULL");
+    if ((elastic || sdtw) && !params) return fail(WB_EINVAL, "params is NULL");
+    if (sdtw && (!means || !stds)) return fail(WB_EINVAL, "scaled metric needs means and stds");
     if (m < 0) return fail(WB_EINVAL, "negative number of shapelets");
     if (m == 0 || x->n == 0) return WB_OK;
     if (!shapelets || !offsets || !lengths || (!profile && (!out_dist || !out_idx)))
@@ -898,6 +966,10 @@ static int subseq_entry(const double *shapelets, const int64_t *offsets, const i
         return subseq_elastic(shapelets, offsets, lengths, stds, m, x, dim, metric, params,
                               out_dist, out_idx, out_on_device, s, hlen, total, paired,
                               prof_raw, prof_key, prof_ld, std_as_given);
+    if (sdtw)
+        return subseq_sdtw_entry(shapelets, offsets, lengths, means, stds, m, x, dim, params,
+                                 out_dist, out_idx, out_on_device, s, hlen, total, paired,
+                                 prof_raw, prof_key, prof_ld, std_as_given);
     const size_t n_out = profile ? (size_t)m * prof_ld : (paired ? (size_t)m : (size_t)x->n * m);
     std::vector<int64_t> order(m);
     std::iota(order.begin(), order.end(), 0);

@@ -1,6 +1,8 @@
 // elastic.cuh -- job description of the FP64 elastic-distance kernels.
 #pragma once
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace wb {
@@ -117,6 +119,17 @@ int launch_elastic_subseq(const SubseqElasticJob &J, int kind, double *gring, in
                           cudaStream_t s);
 int launch_shapelet_slopes(const double *shp, const int64_t *off, const int64_t *len,
                            int64_t m, double *out, cudaStream_t s);
+
+// scaled_dtw subsequence metric (scaled_dtw.cu); shapelet arrays on the device
+int subseq_scaled_dtw(const double *shp, const int64_t *off, const int64_t *len,
+                      const double *means, const double *stds, int64_t m,
+                      const std::vector<int64_t> &hlen, int64_t total, const SeriesSet &X,
+                      int64_t n_timestep, double r, bool paired, int std_as_given,
+                      double *out_dist, int64_t *out_idx, double *prof_raw, double *prof_key,
+                      int64_t prof_ld, Workspace &ws, cudaStream_t s);
+size_t subseq_scaled_dtw_bytes(int64_t m, int64_t total, int64_t n_series, int n,
+                               const std::vector<int64_t> &hlen, double r, int64_t n_timestep,
+                               bool paired);
 
 // argmin_subsequence_distance (argmin_subseq.cu)
 struct ArgminSubseqJob;

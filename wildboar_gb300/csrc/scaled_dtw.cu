@@ -1,0 +1,527 @@
+// scaled_dtw.cu -- the scaled_dtw subsequence metric (ScaledDtwSubsequenceMetric,
+// distance/_elastic.pyx:1928-2204) with the UCR-suite scan of
+// scaled_dtw_subsequence_distance / scaled_dtw_matches (:159-620), FP64.
+//
+// The reference scans the windows of a series in order.  For window I it
+// takes the running mean / std of the stream (sums ex, ex2 updated by adding
+// the newest and subtracting the oldest value; std 1 when the variance is
+// not positive), and skips the window when LB_Kim (first / last three
+// points), then LB_Keogh of the window against the shapelet's envelope, then
+// LB_Keogh of the shapelet against the window's slice of the series
+// envelope reaches the best distance so far; otherwise it runs a
+// Sakoe-Chiba-banded dtw on the z-normalised values that gives up as soon
+// as a row minimum plus the cumulative bound of the remaining rows reaches
+// the best.  Each test is "value >= best" on a sum of non-negative terms, so
+// the reference's decision for a window equals comparing the window's full
+// values with the best at that point:
+//   key(I) = max(LB_Kim, LB_Keogh, LB_Keogh2, max over rows of
+//                (row minimum + cumulative bound)),   raw(I) = the dtw,
+// window I is evaluated iff key(I) < best, and then replaces the best iff
+// raw(I) < best.  Here one warp takes one (shapelet, series) pair, its lanes
+// compute (key, raw) of 32 consecutive windows -- each lane stops early once
+// a value reaches the best at the start of the 32 (the best only decreases,
+// so such a window fails the exact test too) -- and the 32 decisions are
+// replayed in window order.  For thresholds (subsequence_match, the distance
+// profile) the same (key, raw) pair decides: a window matches threshold t
+// iff key < t^2 and raw <= t^2.
+//
+// Prepasses: the envelopes (find_min_max, :98-151, restated with the same
+// ring deques -- including its single front pop per step -- so the
+// envelopes carry the reference's values) of every shapelet and, per
+// shapelet length, of every series; the running window statistics per
+// (series, length); the z-normalised shapelet and shapelet envelope.
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "elastic.cuh"
+
+namespace wb {
+
+namespace {
+
+constexpr int kSdThreads = 128;
+
+// persistent grid: 8 blocks per SM, lane scratch bounded to about 512 MiB
+inline int64_t sdtw_grid(int slots, int sm_count) {
+    const int64_t per_block = (int64_t)slots * kSdThreads * 8;
+    return std::max<int64_t>(
+        1, std::min<int64_t>((int64_t)8 * sm_count, (512LL << 20) / per_block));
+}
+
+// _compute_warp_width (distance/_elastic.pyx:1917-1921)
+inline int sdtw_warp(int64_t length, double r) {
+    if (r == 1.0) return (int)(length - 1);
+    return (int)std::floor((double)length * r);
+}
+
+// the reference's ring deque (distance/_elastic.pyx:37-95): elements are
+// pushed at `back`, which moves down; the front element sits just above
+// `front`
+struct DevDeque {
+    int *q;
+    int cap, size, front, back;
+    __device__ void reset() {
+        size = 0;
+        front = 0;
+        back = cap - 1;
+    }
+    __device__ void push_back(int v) {
+        q[back] = v;
+        back -= 1;
+        if (back < 0) back = cap - 1;
+        size += 1;
+    }
+    __device__ void pop_front() {
+        front -= 1;
+        if (front < 0) front = cap - 1;
+        size -= 1;
+    }
+    __device__ void pop_back() {
+        back = (back + 1) % cap;
+        size -= 1;
+    }
+    __device__ int front_v() const { return q[front - 1 < 0 ? cap - 1 : front - 1]; }
+    __device__ int back_v() const { return q[(back + 1) % cap]; }
+};
+
+// find_min_max (distance/_elastic.pyx:98-151)
+__device__ void sdtw_envelope(const double *T, int length, int r, double *lower, double *upper,
+                              DevDeque &dl, DevDeque &du) {
+    du.reset();
+    dl.reset();
+    du.push_back(0);
+    dl.push_back(0);
+    for (int i = 1; i < length; i++) {
+        if (i > r) {
+            const int k = i - r - 1;
+            upper[k] = T[du.front_v()];
+            lower[k] = T[dl.front_v()];
+        }
+        const double cur = T[i], prev = T[i - 1];
+        if (cur > prev) {
+            du.pop_back();
+            while (du.size != 0 && cur > T[du.back_v()]) du.pop_back();
+        } else {
+            dl.pop_back();
+            while (dl.size != 0 && cur < T[dl.back_v()]) dl.pop_back();
+        }
+        du.push_back(i);
+        dl.push_back(i);
+        if (i == 2 * r + 1 + du.front_v())
+            du.pop_front();
+        else if (i == 2 * r + 1 + dl.front_v())
+            dl.pop_front();
+    }
+    for (int i = length; i < length + r + 1; i++) {
+        const int k = i - r - 1;
+        upper[k] = T[du.front_v()];
+        lower[k] = T[dl.front_v()];
+        if (i - du.front_v() >= 2 * r + 1) du.pop_front();
+        if (i - dl.front_v() >= 2 * r + 1) dl.pop_front();
+    }
+}
+
+// Per shapelet: z-normalised values and envelope (the reference normalises
+// them on the fly with the same two operations).  sstd: 0 is taken as 1
+// unless std_as_given.
+__global__ void sdtw_shapelet_prep_kernel(const double *shp, const int64_t *off,
+                                          const int64_t *len, const double *mean,
+                                          const double *sstd, int64_t m, double r,
+                                          int std_as_given, int cap, int *dq, double *Sn,
+                                          double *SnL, double *SnU, double *sstd_eff) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= m) return;
+    const double *S = shp + off[s];
+    const int L = (int)len[s];
+    const int w = r == 1.0 ? L - 1 : (int)floor((double)L * r);
+    const double sm = mean[s];
+    const double ss = (sstd[s] != 0.0 || std_as_given) ? sstd[s] : 1.0;
+    sstd_eff[s] = ss;
+    DevDeque dl{dq + s * 2 * cap, cap, 0, 0, 0}, du{dq + s * 2 * cap + cap, cap, 0, 0, 0};
+    double *lo = SnL + off[s], *up = SnU + off[s];
+    sdtw_envelope(S, L, w, lo, up, dl, du);
+    for (int k = 0; k < L; k++) {
+        Sn[off[s] + k] = (S[k] - sm) / ss;
+        up[k] = (up[k] - sm) / ss;
+        lo[k] = (lo[k] - sm) / ss;
+    }
+}
+
+// Per prep item (series, shapelet length L, warp w): the series envelope
+// and the running window statistics of scaled_dtw_subsequence_distance
+// (:380-398, 455-460).
+// item_len null: every item has length L_all; items are the series 0 .. n_items - 1
+__global__ void sdtw_series_prep_kernel(SeriesSet X, const int64_t *item_len, int L_all,
+                                        int64_t n_items, double r, int cap, int *dq, double *tl,
+                                        double *tu, double *wmean, double *wstd) {
+    const int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= n_items) return;
+    const int n = X.len;
+    const double *T = X.base + it * X.stride;
+    const int L = item_len ? (int)item_len[it] : L_all;
+    const int w = r == 1.0 ? L - 1 : (int)floor((double)L * r);
+    DevDeque dl{dq + it * 2 * cap, cap, 0, 0, 0}, du{dq + it * 2 * cap + cap, cap, 0, 0, 0};
+    sdtw_envelope(T, n, w, tl + it * n, tu + it * n, dl, du);
+    double ex = 0.0, ex2 = 0.0;
+    double *mo = wmean + it * n, *so = wstd + it * n;
+    for (int i = 0; i < n; i++) {
+        const double v = T[i];
+        ex = ex + v;
+        ex2 = ex2 + v * v;
+        if (i >= L - 1) {
+            const int I = i - (L - 1);
+            const double mu = ex / (double)L;
+            const double tmp = ex2 / (double)L - mu * mu;
+            mo[I] = mu;
+            so[I] = tmp > 0.0 ? sqrt(tmp) : 1.0;
+            const double o = T[I];
+            ex = ex - o;
+            ex2 = ex2 - o * o;
+        }
+    }
+}
+
+struct SdtwScanJob {
+    SeriesSet x;
+    const int64_t *off = nullptr;   // packed shapelet offsets (Sn, SnL, SnU)
+    const int64_t *len = nullptr;
+    const double *Sn = nullptr, *SnL = nullptr, *SnU = nullptr;
+    const double *sstd_eff = nullptr;  // the shapelet std the scan uses (0 kept when given)
+    double r = 1.0;
+    // tasks: pairwise: shapelets task_shp[0 .. n_shp) x all series, prep item =
+    // series; paired: task t = (shapelet t, series t), prep item t
+    const int32_t *task_shp = nullptr;
+    int64_t n_shp = 0;
+    int paired = 0;
+    int64_t m = 0;  // shapelets in the output row
+    const double *tl = nullptr, *tu = nullptr, *wmean = nullptr, *wstd = nullptr;
+    double *out_dist = nullptr;
+    int64_t *out_idx = nullptr;
+    double *prof_raw = nullptr, *prof_key = nullptr;
+    int64_t prof_ld = 0;
+    int64_t scr_stride = 0;  // threads of the launch (scratch stride)
+    int xn_off = 0, cb_off = 0, c0_off = 0, c1_off = 0;  // scratch slots per lane
+};
+
+__device__ __forceinline__ double sq(double a) { return a * a; }
+__device__ __forceinline__ double dmin2(double a, double b) { return b < a ? b : a; }
+
+// LB_Kim of constant_lower_bound (:159-237), all six terms (the reference's
+// early returns only stop at a partial sum that already fails).  For L < 3
+// the reference reads outside the arrays; indices are clamped here.
+__device__ double sdtw_kim(const double *Sn, const double *W, double tm, double ts, int L) {
+    const int a1 = L > 1 ? 1 : L - 1, a2 = L > 2 ? 2 : L - 1;
+    const int b1 = L - 2 >= 0 ? L - 2 : 0, b2 = L - 3 >= 0 ? L - 3 : 0;
+    const double tx0 = (W[0] - tm) / ts, ty0 = (W[L - 1] - tm) / ts;
+    const double sx0 = Sn[0], sy0 = Sn[L - 1];
+    double md = sq(tx0 - sx0) + sq(ty0 - sy0);
+    const double tx1 = (W[a1] - tm) / ts, sx1 = Sn[a1];
+    md = md + dmin2(dmin2(sq(tx1 - sx0), sq(tx0 - sx1)), sq(tx1 - sx1));
+    const double ty1 = (W[b1] - tm) / ts, sy1 = Sn[b1];
+    md = md + dmin2(dmin2(sq(ty1 - sy1), sq(ty0 - sy1)), sq(ty1 - sy1));
+    const double tx2 = (W[a2] - tm) / ts, sx2 = Sn[a2];
+    md = md + dmin2(dmin2(dmin2(sq(tx0 - sx2), dmin2(sq(tx1 - sx2), sq(tx2 - sx2))),
+                          sq(tx2 - sx1)),
+                    sq(tx2 - sx0));
+    const double ty2 = (W[b2] - tm) / ts, sy2 = Sn[b2];
+    md = md + dmin2(dmin2(dmin2(sq(ty0 - sy2), dmin2(sq(ty1 - sy2), sq(ty2 - sy2))),
+                          sq(ty2 - sy1)),
+                    sq(ty2 - sy0));
+    return md;
+}
+
+// one term of cumulative_bound (:240-270)
+__device__ __forceinline__ double keogh_term(double x, double us, double ls) {
+    if (x > us) return sq(x - us);
+    if (x < ls) return sq(x - ls);
+    return 0.0;
+}
+
+template <bool PROFILE>
+__global__ void __launch_bounds__(kSdThreads) sdtw_scan_kernel(const SdtwScanJob J,
+                                                               double *scr) {
+    const double INF = __longlong_as_double(0x7ff0000000000000LL);
+    const double QNAN = __longlong_as_double(0x7ff8000000000000LL);
+    const int lane = threadIdx.x & 31;
+    const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t warp = gtid >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t st = J.scr_stride;
+    double *xn = scr + gtid + (int64_t)J.xn_off * st;
+    double *cb = scr + gtid + (int64_t)J.cb_off * st;
+    double *cc[2] = {scr + gtid + (int64_t)J.c0_off * st, scr + gtid + (int64_t)J.c1_off * st};
+    const int n = J.x.len;
+    const int64_t ntask = J.paired ? J.m : J.n_shp * J.x.count;
+    for (int64_t task = warp; task < ntask; task += nwarps) {
+        int64_t sh, si, item, oidx;
+        if (J.paired) {
+            sh = si = item = oidx = task;
+        } else {
+            sh = J.task_shp[task / J.x.count];
+            si = task - (task / J.x.count) * J.x.count;
+            item = si;
+            oidx = si * J.m + sh;
+        }
+        const int L = (int)J.len[sh];
+        const int w = J.r == 1.0 ? L - 1 : (int)floor((double)L * J.r);
+        const double *Sn = J.Sn + J.off[sh];
+        const double *SnL = J.SnL + J.off[sh];
+        const double *SnU = J.SnU + J.off[sh];
+        const bool ss_zero = J.sstd_eff[sh] == 0.0;
+        const double *T = J.x.base + si * J.x.stride;
+        const double *tl = J.tl + item * n, *tu = J.tu + item * n;
+        const double *wm = J.wmean + item * n, *ws = J.wstd + item * n;
+        const int nwin = n - L + 1;
+        if (PROFILE) {
+            for (int64_t I = nwin + lane; I < J.prof_ld; I += 32) {
+                J.prof_raw[oidx * J.prof_ld + I] = QNAN;
+                J.prof_key[oidx * J.prof_ld + I] = QNAN;
+            }
+        }
+        double best = INF;
+        int bidx = 0;
+        for (int base = 0; base < nwin; base += 32) {
+            const int I = base + lane;
+            const double bound = PROFILE ? INF : best;
+            double key = INF, raw = INF;
+            if (I < nwin) {
+                const double tm = wm[I], ts = ws[I];
+                const double *W = T + I;
+                key = sdtw_kim(Sn, W, tm, ts, L);
+                if (key < bound) {
+                    double lbk = 0.0;
+                    for (int k = 0; k < L; k++) {
+                        const double x = (W[k] - tm) / ts;
+                        xn[(int64_t)k * st] = x;
+                        lbk = lbk + keogh_term(x, SnU[k], SnL[k]);
+                    }
+                    key = key > lbk ? key : lbk;
+                    if (lbk < bound) {
+                        double lbk2 = 0.0;
+                        for (int k = 0; k < L; k++)
+                            lbk2 = lbk2 + keogh_term(Sn[k], (tu[I + k] - tm) / ts,
+                                                     (tl[I + k] - tm) / ts);
+                        key = key > lbk2 ? key : lbk2;
+                        if (lbk2 < bound) {
+                            // cb[k] = cb[k + 1] + term[k], from the larger bound
+                            const bool first = lbk > lbk2;
+                            double acc = 0.0;
+                            for (int k = L - 1; k >= 0; k--) {
+                                const double d =
+                                    first ? keogh_term(xn[(int64_t)k * st], SnU[k], SnL[k])
+                                          : keogh_term(Sn[k], (tu[I + k] - tm) / ts,
+                                                       (tl[I + k] - tm) / ts);
+                                acc = k == L - 1 ? d : acc + d;
+                                cb[(int64_t)k * st] = acc;
+                            }
+                            // inner_scaled_dtw_subsequence_distance (:273-344)
+                            const int W2 = 2 * w + 1;
+                            for (int k = 0; k < W2; k++) {
+                                cc[0][(int64_t)k * st] = INF;
+                                cc[1][(int64_t)k * st] = INF;
+                            }
+                            int cur = 0;
+                            int kk = 0;
+                            bool gave_up = false;
+                            double kmax = -INF;
+                            for (int i = 0; i < L; i++) {
+                                double *c = cc[cur];
+                                const double *pv = cc[cur ^ 1];
+                                kk = w - i > 0 ? w - i : 0;
+                                double minc = INF;
+                                const int j0 = i - w > 0 ? i - w : 0;
+                                const int j1 = i + w + 1 < L ? i + w + 1 : L;
+                                double left = INF;
+                                double pk = (i >= 1) ? pv[(int64_t)kk * st] : INF;
+                                const double si_v = Sn[i];
+                                for (int j = j0; j < j1; j++) {
+                                    double v;
+                                    if (i == 0 && j == 0) {
+                                        v = ss_zero ? 0.0 : Sn[0];
+                                        v = v - xn[0];
+                                        v = v * v;
+                                    } else {
+                                        const double y = (j - 1 < 0 || kk - 1 < 0) ? INF : left;
+                                        const double pk1 = (kk + 1 <= 2 * w && i >= 1)
+                                                               ? pv[(int64_t)(kk + 1) * st]
+                                                               : INF;
+                                        const double x = (i - 1 < 0 || kk + 1 > 2 * w) ? INF : pk1;
+                                        const double z = (i - 1 < 0 || j - 1 < 0) ? INF : pk;
+                                        const double dv = si_v - xn[(int64_t)j * st];
+                                        v = dmin2(dmin2(x, y), z) + dv * dv;
+                                        pk = pk1;
+                                    }
+                                    c[(int64_t)kk * st] = v;
+                                    left = v;
+                                    if (v < minc) minc = v;
+                                    kk += 1;
+                                }
+                                if (i + w < L - 1) {
+                                    const double val = minc + cb[(int64_t)(i + w + 1) * st];
+                                    kmax = kmax > val ? kmax : val;
+                                    if (val >= bound) {
+                                        gave_up = true;
+                                        break;
+                                    }
+                                }
+                                cur ^= 1;
+                            }
+                            key = key > kmax ? key : kmax;
+                            if (!gave_up) raw = cc[cur ^ 1][(int64_t)(kk - 1) * st];
+                        }
+                    }
+                }
+                if (PROFILE) {
+                    J.prof_raw[oidx * J.prof_ld + I] = raw;
+                    J.prof_key[oidx * J.prof_ld + I] = key;
+                }
+            }
+            if (!PROFILE) {
+                // replay the 32 windows in order against the running best
+                for (int t = 0; t < 32; t++) {
+                    const double kt = __shfl_sync(0xffffffffu, key, t);
+                    const double rt = __shfl_sync(0xffffffffu, raw, t);
+                    if (base + t < nwin && kt < best && rt < best) {
+                        best = rt;
+                        bidx = base + t;
+                    }
+                }
+            }
+        }
+        if (!PROFILE && lane == 0) {
+            J.out_dist[oidx] = sqrt(best);
+            J.out_idx[oidx] = bidx;
+        }
+    }
+}
+
+}  // namespace
+
+// Host driver; shapelet arrays (shp, off, len, means, stds) are device
+// pointers here, X is staged.
+int subseq_scaled_dtw(const double *shp, const int64_t *off, const int64_t *len,
+                      const double *means, const double *stds, int64_t m,
+                      const std::vector<int64_t> &hlen, int64_t total, const SeriesSet &X,
+                      int64_t n_timestep, double r,
+                      bool paired, int std_as_given, double *out_dist, int64_t *out_idx,
+                      double *prof_raw, double *prof_key, int64_t prof_ld, Workspace &ws,
+                      cudaStream_t s) {
+    if (!(r >= 0.0 && r <= 1.0)) return fail(WB_EINVAL, "r must be in [0, 1]");
+    const int n = X.len;
+    const int cap = 2 * sdtw_warp(n_timestep, r) + 2;
+    const bool profile = prof_raw != nullptr;
+    int max_len = 1, max_w = 0;
+    for (int64_t i = 0; i < m; i++) {
+        max_len = std::max<int>(max_len, (int)hlen[i]);
+        max_w = std::max(max_w, sdtw_warp(hlen[i], r));
+    }
+    // shapelet prep
+    WB_TAKE(Sn, double, ws, total);
+    WB_TAKE(SnL, double, ws, total);
+    WB_TAKE(SnU, double, ws, total);
+    WB_TAKE(sstd_eff, double, ws, m);
+    WB_TAKE(dq_s, int, ws, (size_t)m * 2 * cap);
+    sdtw_shapelet_prep_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(
+        shp, off, len, means, stds, m, r, std_as_given, cap, dq_s, Sn, SnL, SnU, sstd_eff);
+    WB_LAUNCH_CHECK("sdtw_shapelet_prep_kernel");
+    // per-lane scratch: xn[max_len], cb[max_len], two cost rows [2 w + 1]
+    const int slots = 2 * max_len + 2 * (2 * max_w + 1);
+    const DeviceInfo &dev = device_info();
+    SdtwScanJob J;
+    J.x = X;
+    J.off = off;
+    J.len = len;
+    J.Sn = Sn;
+    J.SnL = SnL;
+    J.SnU = SnU;
+    J.sstd_eff = sstd_eff;
+    J.r = r;
+    J.paired = paired ? 1 : 0;
+    J.m = m;
+    J.xn_off = 0;
+    J.cb_off = max_len;
+    J.c0_off = 2 * max_len;
+    J.c1_off = 2 * max_len + 2 * max_w + 1;
+    J.prof_raw = prof_raw;
+    J.prof_key = prof_key;
+    J.prof_ld = prof_ld;
+    J.out_dist = out_dist;
+    J.out_idx = out_idx;
+
+    // per-item buffers (items: the series; paired: the pairs) and the lane
+    // scratch, reserved once and reused by every length group
+    const int64_t items = paired ? m : X.count;
+    WB_TAKE(dq, int, ws, (size_t)items * 2 * cap);
+    WB_TAKE(tl, double, ws, (size_t)items * n);
+    WB_TAKE(tu, double, ws, (size_t)items * n);
+    WB_TAKE(wm, double, ws, (size_t)items * n);
+    WB_TAKE(wsd, double, ws, (size_t)items * n);
+    const int64_t grid = sdtw_grid(slots, dev.sm_count);
+    WB_TAKE(scr, double, ws, (size_t)grid * kSdThreads * slots);
+    J.tl = tl;
+    J.tu = tu;
+    J.wmean = wm;
+    J.wstd = wsd;
+    J.scr_stride = grid * kSdThreads;
+
+    auto launch_scan = [&](int L_all, int64_t warps, const int32_t *task_shp,
+                           int64_t n_shp) -> int {
+        sdtw_series_prep_kernel<<<(unsigned)((items + 63) / 64), 64, 0, s>>>(
+            X, paired ? len : nullptr, L_all, items, r, cap, dq, tl, tu, wm, wsd);
+        WB_LAUNCH_CHECK("sdtw_series_prep_kernel");
+        J.task_shp = task_shp;
+        J.n_shp = n_shp;
+        const int64_t g = std::max<int64_t>(
+            1, std::min<int64_t>(grid, (warps * 32 + kSdThreads - 1) / kSdThreads));
+        timer_begin("sdtw_scan_kernel", s);
+        if (profile)
+            sdtw_scan_kernel<true><<<(unsigned)g, kSdThreads, 0, s>>>(J, scr);
+        else
+            sdtw_scan_kernel<false><<<(unsigned)g, kSdThreads, 0, s>>>(J, scr);
+        timer_end(s);
+        WB_LAUNCH_CHECK("sdtw_scan_kernel");
+        return WB_OK;
+    };
+
+    if (paired) return launch_scan(0, m, nullptr, 0);
+    // pairwise: one launch pair per shapelet length (the series prep depends on it)
+    std::vector<int64_t> order(m);
+    for (int64_t i = 0; i < m; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int64_t a, int64_t b) { return hlen[a] < hlen[b]; });
+    WB_TAKE(d_order, int32_t, ws, m);
+    std::vector<int32_t> ord32(m);
+    for (int64_t i = 0; i < m; i++) ord32[i] = (int32_t)order[i];
+    WB_CUDA(cudaMemcpyAsync(d_order, ord32.data(), m * 4, cudaMemcpyHostToDevice, s));
+    for (int64_t t = 0; t < m;) {
+        int64_t u = t;
+        while (u < m && hlen[order[u]] == hlen[order[t]]) u++;
+        WB_TRY(launch_scan((int)hlen[order[t]], (u - t) * X.count, d_order + t, u - t));
+        t = u;
+    }
+    // ord32 feeds an asynchronous copy
+    WB_CUDA(cudaStreamSynchronize(s));
+    return WB_OK;
+}
+
+size_t subseq_scaled_dtw_bytes(int64_t m, int64_t total, int64_t n_series, int n,
+                               const std::vector<int64_t> &hlen, double r, int64_t n_timestep,
+                               bool paired) {
+    int max_len = 1, max_w = 0;
+    for (int64_t i = 0; i < m; i++) {
+        max_len = std::max<int>(max_len, (int)hlen[i]);
+        max_w = std::max(max_w, sdtw_warp(hlen[i], r));
+    }
+    const int cap = 2 * sdtw_warp(n_timestep, r) + 2;
+    const int slots = 2 * max_len + 2 * (2 * max_w + 1);
+    const int64_t items = paired ? m : n_series;
+    const int64_t grid = sdtw_grid(slots, device_info().sm_count);
+    return 3 * align256(total * 8) + align256(m * 8) + align256((size_t)m * 2 * cap * 4) +
+           align256((size_t)items * 2 * cap * 4) + 4 * align256((size_t)items * n * 8) +
+           align256((size_t)grid * kSdThreads * slots * 8) + align256(m * 4) + 4096;
+}
+
+}  // namespace wb

@@ -332,6 +332,15 @@ class DtwSubsequenceMetric(_ElasticSubsequence):
         self.r = r
 
 
+class ScaledDtwSubsequenceMetric(DtwSubsequenceMetric):
+    """ScaledDtwSubsequenceMetric, distance/_elastic.pyx:1928-2204: z-normalised
+    dtw with the UCR-suite scan (LB_Kim, LB_Keogh both ways, cumulative-bound
+    abandoning) and its warp width (r == 1: length - 1, else floor(length r))."""
+
+    metric_id = 33
+    scaled = True
+
+
 class AmercingDtwSubsequenceMetric(DtwSubsequenceMetric):
     """AmercingDtwSubsequenceMetric, distance/_elastic.pyx:2293-2351 (p unchecked)."""
 
@@ -475,6 +484,7 @@ _SUBSEQUENCE_METRICS = {
     "euclidean": EuclideanSubsequenceMetric,
     "scaled_euclidean": ScaledEuclideanSubsequenceMetric,
     "dtw": DtwSubsequenceMetric,
+    "scaled_dtw": ScaledDtwSubsequenceMetric,
     "wdtw": WeightedDtwSubsequenceMetric,
     "ddtw": DerivativeDtwSubsequenceMetric,
     "wddtw": WeightedDerivativeDtwSubsequenceMetric,

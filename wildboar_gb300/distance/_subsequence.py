@@ -30,7 +30,8 @@ from ._distance import (
 )
 from ._metrics import check_scalar
 
-_SQRT = {0, 1, 2, 3, 4, 5, 32}          # euclidean, dtw family, scaled_euclidean
+_SQRT = {0, 1, 2, 3, 4, 5, 32, 33}      # euclidean, dtw family, scaled_euclidean / dtw
+_SCALED_DTW = 33
 _EUCLID = {0, 32}
 _LCSS, _EDR = 6, 8
 
@@ -143,6 +144,11 @@ def _match_mask(metric_id, raw, key, dist, L, T, t):
     with np.errstate(invalid="ignore"):
         if metric_id in _EUCLID:
             return raw <= t * t
+        if metric_id == _SCALED_DTW:
+            # scaled_dtw_matches: every bound and the abandoning test fail on
+            # ">= t^2" (distance/_elastic.pyx:520-600)
+            t2 = t * t
+            return (key < t2) & (raw <= t2)
         if metric_id in (1, 2, 3, 4, 5):  # dtw, wdtw, ddtw, wddtw, adtw
             t2 = t * t
             return ~(key > t2) & (raw <= t2)
@@ -271,9 +277,16 @@ def distance_profile(y, x, *, dilation=1, padding=0, dim=0, metric="mass",
     shapelets = [np.ascontiguousarray(r, dtype=float) for r in y2]
     # _DistanceProfile reads y[i, 0] and x[i, 0] whatever dim is
     # (distance/_cdistance.pyx:1680-1699)
-    raw, _, lens = _profile_raw(shapelets, X, 0, m, transient=True)
+    raw, key, lens = _profile_raw(shapelets, X, 0, m, transient=True)
     nwin = X.shape[-1] - y2.shape[1] + 1
     dp = _distances(m.metric_id, raw[:, :nwin], float(y2.shape[1]))
+    if m.metric_id == _SCALED_DTW:
+        # the profile is scaled_dtw_matches with an infinite threshold over a
+        # profile of ones: windows it does not keep stay 1
+        L = float(y2.shape[1])
+        keep = _match_mask(m.metric_id, raw[:, :nwin], key[:, :nwin], dp, L,
+                           X.shape[-1], math.inf)
+        dp = np.where(keep, dp, 1.0)
     return np.squeeze(dp)
 
 
