@@ -312,6 +312,35 @@ int wb_dtw_average_mm_step(const double *x, int64_t x_stride, int64_t n_timestep
                            double *new_means, double *last, void *stream);
 
 /*
+ * wb_dtw_envelope -- _dtw_envelop (distance/_elastic.pyx:1076-1092, the
+ * streaming find_min_max of :98-151 with deques of capacity 2 warp + 2) of
+ * every row of x (n, n_timestep): lower / upper are (n, n_timestep).
+ * 0 <= warp < n_timestep.  All arrays on the side `on_device` says.
+ */
+int wb_dtw_envelope(const double *x, int64_t n, int64_t n_timestep, int64_t warp,
+                    double *lower, double *upper, int32_t on_device, void *stream);
+
+/*
+ * wb_lb_keogh -- DtwKeoghLowerBound.transform (distance/lb.py:390-432):
+ * out[i, j] = max(left, right) for query q[i] and fitted series x[j] (both
+ * (., n_timestep) rows), left = sqrt(LB_Keogh of q[i] against the envelope
+ * of x[j]) and right = sqrt(LB_Keogh of x[j] against the envelope of q[i])
+ * (_dtw_lb_keogh, distance/_elastic.pyx:1095-1115), warp as the caller
+ * computes it (distance/lb.py:372-376).  kind: 0 both, 1 left only,
+ * 2 right only (the other side is -inf).  out is (nq, nx).
+ */
+int wb_lb_keogh(const double *q, int64_t nq, const double *x, int64_t nx, int64_t n_timestep,
+                int64_t warp, int32_t kind, double *out, int32_t on_device, void *stream);
+
+/*
+ * wb_lb_kim -- DtwKimLowerBound.transform (distance/lb.py:224-311): the
+ * constant-time bound of every query y[i] against every fitted x[j];
+ * out is (ny, nx).
+ */
+int wb_lb_kim(const double *y, int64_t ny, const double *x, int64_t nx, int64_t n_timestep,
+              double *out, int32_t on_device, void *stream);
+
+/*
  * wb_group_mean -- x[group].mean(axis=0) of the euclidean KMeans update
  * (_EuclideanCluster._update_centroid, distance/_neighbors.py:364-369):
  * the rows member[group_start[gi] .. group_start[gi + 1] - 1] summed in that

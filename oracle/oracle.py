@@ -89,6 +89,8 @@ def lib():
         L.wbo_fast_mean_std.argtypes = [dp, i64, dp, dp]
         L.wbo_dtw_alignment.argtypes = [dp, i64, dp, i64, i64, dp, dp]
         L.wbo_mm_epoch.argtypes = [dp, i64, i64, dp, i64, i64, dp, dp, dp, dp, ip, dp]
+        L.wbo_dtw_envelope.argtypes = [dp, i64, i64, i64, dp, dp]
+        L.wbo_lb_keogh.argtypes = [dp, i64, dp, i64, i64, i64, ctypes.c_int, dp]
         L.wbo_scaled_dtw_subsequence.argtypes = [dp, ip, ip, dp, dp, i64, dp, i64, i64, i64,
                                                  i64, ctypes.c_double, ctypes.c_int,
                                                  ctypes.c_double, ctypes.c_int, dp, ip, dp, i64]
@@ -552,3 +554,62 @@ def scaled_dtw_matches(shapelets, x, threshold, *, r=1.0, dim=0, transient=False
                                      float(r), 1, float(threshold), 1 if transient else 0,
                                      _dp(dist), None, _dp(keep), ld)
     return dist, keep
+
+
+# --------------------------------------------------------------------------
+# lower bounds (distance/lb.py)
+
+
+def _warp_size(n, r):
+    w = max(math.floor(n * r), 1)
+    return w - 1 if w == n else w
+
+
+def dtw_envelope(X, warp):
+    """_dtw_envelop (distance/_elastic.pyx:1076-1092) of every row."""
+    X = np.ascontiguousarray(np.atleast_2d(X), dtype=np.float64)
+    lo = np.empty_like(X)
+    up = np.empty_like(X)
+    if lib().wbo_dtw_envelope(_dp(X), X.shape[0], X.shape[1], int(warp), _dp(lo), _dp(up)):
+        raise ValueError("invalid r")
+    return lo, up
+
+
+def lb_keogh(Q, X, *, r=1.0, kind="both"):
+    """DtwKeoghLowerBound(r, kind).fit(X).transform(Q) (distance/lb.py:314-432)."""
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    out = np.empty((Q.shape[0], X.shape[0]))
+    lib().wbo_lb_keogh(_dp(Q), Q.shape[0], _dp(X), X.shape[0], X.shape[1],
+                       _warp_size(X.shape[1], r), {"both": 0, "left": 1, "right": 2}[kind],
+                       _dp(out))
+    return out
+
+
+def lb_kim(Q, X):
+    """DtwKimLowerBound().fit(X).transform(Q) (distance/lb.py:198-311),
+    restated with numpy: per query, vectorised over the fitted series."""
+    X = np.asarray(X, dtype=np.float64)
+    Q = np.asarray(Q, dtype=np.float64)
+    n = X.shape[-1]
+
+    def sq(a, b):
+        v = a - b
+        return v * v
+
+    out = np.empty((Q.shape[0], X.shape[0]))
+    for i in range(Q.shape[0]):
+        a0, a0e, b0, b0e = X[:, 0], X[:, -1], Q[i, 0], Q[i, -1]
+        d = sq(a0, b0) + sq(a0e, b0e)
+        if n > 1:
+            a1, a1e, b1, b1e = X[:, 1], X[:, -2], Q[i, 1], Q[i, -2]
+            d += np.minimum(sq(a1, b0), np.minimum(sq(a0, b1), sq(a1, b1)))
+            d += np.minimum(sq(a1e, b1), np.minimum(sq(a0e, b1e), sq(a1e, b1e)))
+            if n > 2:
+                a2, a2e, b2, b2e = X[:, 2], X[:, -3], Q[i, 2], Q[i, -3]
+                d += np.minimum(sq(a0, b2), np.minimum(sq(a1, b2), np.minimum(
+                    sq(a2, b2), np.minimum(sq(a2, b1), sq(a2, b0)))))
+                d += np.minimum(sq(a0e, b2e), np.minimum(sq(a1e, b2e), np.minimum(
+                    sq(a2e, b2e), np.minimum(sq(a2e, b1e), sq(a2e, b0e)))))
+        out[i] = d
+    return out

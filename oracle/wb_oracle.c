@@ -1664,3 +1664,50 @@ int wbo_scaled_dtw_subsequence(const double *shp, const idx_t *off, const idx_t 
     free(w.cb); free(w.cb1); free(w.cb2); free(sl); free(su); free(dbuf); free(ibuf);
     return 0;
 }
+
+/* ------------------------------------------------------------------------
+ * lower bounds of distance/lb.py */
+
+/* _dtw_envelop (distance/_elastic.pyx:1076-1092): deques of capacity 2r + 2 */
+int wbo_dtw_envelope(const double *x, idx_t n, idx_t L, idx_t r, double *lower, double *upper)
+{
+    if (!(0 <= r && r < L)) return -1;
+    sdq du = {0}, dl = {0};
+    du.cap = dl.cap = 2 * r + 2;
+    du.q = (idx_t *)malloc(sizeof(idx_t) * du.cap);
+    dl.q = (idx_t *)malloc(sizeof(idx_t) * dl.cap);
+    for (idx_t i = 0; i < n; i++)
+        sdtw_envelope(x + i * L, L, r, lower + i * L, upper + i * L, &dl, &du);
+    free(du.q);
+    free(dl.q);
+    return 0;
+}
+
+/* DtwKeoghLowerBound.transform (distance/lb.py:390-432): kind 0 both,
+ * 1 left (query vs fitted envelope), 2 right (fitted vs query envelope);
+ * each side sqrt(cumulative_bound at mean 0, std 1) (_dtw_lb_keogh,
+ * _elastic.pyx:1095-1115); out (nq, nx) = max(left, right) */
+int wbo_lb_keogh(const double *q, idx_t nq, const double *x, idx_t nx, idx_t L, idx_t r,
+                 int kind, double *out)
+{
+    double *xl = (double *)malloc(sizeof(double) * nx * L);
+    double *xu = (double *)malloc(sizeof(double) * nx * L);
+    double *ql = (double *)malloc(sizeof(double) * L);
+    double *qu = (double *)malloc(sizeof(double) * L);
+    double *cb = (double *)malloc(sizeof(double) * L);
+    if (wbo_dtw_envelope(x, nx, L, r, xl, xu) != 0) return -1;
+    for (idx_t i = 0; i < nq; i++) {
+        const double *qi = q + i * L;
+        if (kind != 1) wbo_dtw_envelope(qi, 1, L, r, ql, qu);
+        for (idx_t j = 0; j < nx; j++) {
+            double d1 = -INF, d2 = -INF;
+            if (kind != 2)
+                d1 = sqrt(sdtw_keogh(qi, L, 0, 1, 0, 1, xl + j * L, xu + j * L, cb, INF));
+            if (kind != 1)
+                d2 = sqrt(sdtw_keogh(x + j * L, L, 0, 1, 0, 1, ql, qu, cb, INF));
+            out[i * nx + j] = d2 > d1 ? d2 : d1;
+        }
+    }
+    free(xl); free(xu); free(ql); free(qu); free(cb);
+    return 0;
+}

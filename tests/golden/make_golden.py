@@ -428,6 +428,23 @@ def main():
         {"metric": "scaled_dtw", "metric_params": {"r": 0.2}, "kw": {"threshold": 2.0}},
         flat(res))
 
+    # lower-bound producers (distance/lb.py:198-432)
+    from wildboar.distance.lb import DtwKeoghLowerBound, DtwKimLowerBound
+
+    XB = _walk(rng, (9, 60))
+    XB[2, 10:30] = XB[2, 10]  # constant stretch: ties in the envelope deques
+    XB[5, :] = np.repeat(_walk(rng, 12), 5)
+    QB = _walk(rng, (5, 60))
+    QB[1, 30:50] = 0.25
+    for r, kind in ((0.1, "both"), (0.0, "both"), (1.0, "both"), (0.3, "left"),
+                    (0.05, "right")):
+        lbk = DtwKeoghLowerBound(r=r, kind=kind).fit(XB)
+        add(f"lb_keogh_r{r}_{kind}", "lb_keogh", {"x": XB, "q": QB}, {"r": r, "kind": kind},
+            {"out": lbk.transform(QB), "lower": lbk.lower_, "upper": lbk.upper_})
+    for L in (60, 2, 1):
+        add(f"lb_kim_L{L}", "lb_kim", {"x": XB[:, :L], "q": QB[:, :L]}, {},
+            {"out": DtwKimLowerBound().fit(XB[:, :L]).transform(QB[:, :L])})
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"reference_version": getattr(wildboar, "__version__", "?"),

@@ -149,6 +149,13 @@ def run_oracle(case):
         dist_tr = dist[mask].reshape(X.shape[0], -1)
         ind_te, dist_te = sorted_argmin(Xt, k)
         return {"dist_train": dist_tr, "ind_train": ind_tr, "dist": dist_te, "ind": ind_te}
+    if kind == "lb_keogh":
+        X = inp["x"]
+        lo, up = O.dtw_envelope(X, O._warp_size(X.shape[1], a["r"]))
+        return {"out": O.lb_keogh(inp["q"], X, r=a["r"], kind=a["kind"]), "lower": lo,
+                "upper": up}
+    if kind == "lb_kim":
+        return {"out": O.lb_kim(inp["q"], inp["x"])}
     raise AssertionError(kind)
 
 
@@ -156,7 +163,7 @@ ORACLE_KINDS = {"pairwise", "singleton", "paired", "argmin", "subsequence", "ali
                 "paired_subsequence"}
 ORACLE_KINDS |= {"argmin_subsequence", "distance_profile", "subsequence_match",
                  "paired_subsequence_match"}
-ORACLE_KINDS |= {"dtw_average", "kmeans", "knn", "kneighbors"}
+ORACLE_KINDS |= {"dtw_average", "kmeans", "knn", "kneighbors", "lb_keogh", "lb_kim"}
 CASES = [c for c in _golden.cases() if c["kind"] in ORACLE_KINDS]
 
 
