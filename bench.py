@@ -466,6 +466,67 @@ def bench_barycenter(args, dev, flush):
     }
 
 
+def bench_ucr(args, dev, flush):
+    """scaled_dtw subsequence distance (the UCR-suite scan) of 1,000 shapelets
+    (L~U{16..128}) against series of length 1,024, r=0.1; and the LB_Keogh
+    lower-bound matrix of 1,000 queries against 10,000 series of length 256,
+    r=0.1.  CPU: the oracle (one core) on bounded samples."""
+    import torch
+
+    from oracle import oracle as O
+    from wildboar_gb300.distance import pairwise_subsequence_distance
+    from wildboar_gb300.distance.lb import DtwKeoghLowerBound
+
+    res = {}
+    X, shp = c3_data(args.c7_series, 1000)
+    Xd = torch.as_tensor(X, device=dev)
+
+    def scan():
+        return pairwise_subsequence_distance(shp, Xd, metric="scaled_dtw",
+                                             metric_params={"r": 0.1}, return_index=True)
+
+    scan()
+    torch.cuda.synchronize()
+    ms = _timed(scan, 1, flush)
+    d, i = scan()
+    od, oi = O.scaled_dtw_subsequence(shp[:50], X[:2], r=0.1)
+    t0 = time.perf_counter()
+    O.scaled_dtw_subsequence(shp[:100], X[:3], r=0.1)
+    cpu_pair_s = (time.perf_counter() - t0) / 300
+    pairs = len(shp) * X.shape[0]
+    res["scaled_dtw_subsequence"] = {
+        "config": f"{len(shp)} shapelets (L~U{{16..128}}) x {X.shape[0]} series, T=1024, r=0.1",
+        "ms": ms,
+        "pairs_per_s": pairs / (ms * 1e-3),
+        "argmin_exact_on_sample": bool(np.array_equal(i[:2, :50].cpu().numpy(), oi)),
+        "max_rel_err_on_sample": float(np.max(np.abs(d[:2, :50].cpu().numpy() - od) /
+                                              np.maximum(od, 1e-300))),
+        "cpu_oracle": {"pairs_per_s": 1.0 / cpu_pair_s, "cores": 1, "kind": "port",
+                       "sample": "100 shapelets x 3 series"},
+    }
+    rng = np.random.default_rng(8)
+    DB = np.cumsum(rng.standard_normal((10000, 256)), axis=1)
+    Q = np.cumsum(rng.standard_normal((1000, 256)), axis=1)
+    lbk = DtwKeoghLowerBound(r=0.1).fit(DB)
+    lbk.transform(Q[:8])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = lbk.transform(Q)
+    wall = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ref = O.lb_keogh(Q[:4], DB, r=0.1)
+    cpu_s = (time.perf_counter() - t0) / 4 * Q.shape[0]
+    res["lb_keogh"] = {
+        "config": "1000 queries x 10000 series, L=256, r=0.1, both sides, host arrays",
+        "wall_ms": wall * 1e3,
+        "bounds_per_s": Q.shape[0] * DB.shape[0] / wall,
+        "exact_on_sample": bool(np.array_equal(out[:4], ref)),
+        "cpu_oracle": {"bounds_per_s": Q.shape[0] * DB.shape[0] / cpu_s, "cores": 1,
+                       "kind": "port", "sample": "4 queries x 10000 series"},
+    }
+    return res
+
+
 def bench_euclid_tc(args, dev, flush):
     """Full-series euclidean 8192 x 8192 at length 1024: tensor-core 3xTF32
     GEMM form against the FP64 drop-in kernel on the same device data."""
@@ -612,6 +673,8 @@ def run_gpu(args):
             forms["precision_sweep"] = bench_precision(args, dev, flush)
         if args.only in ("", "barycenter"):
             forms["barycenter_kmeans"] = bench_barycenter(args, dev, flush)
+        if args.only in ("", "ucr"):
+            forms["ucr_lower_bounds"] = bench_ucr(args, dev, flush)
         if rank == 0:
             print(json.dumps({"forms": forms}), flush=True)
         return
@@ -713,6 +776,7 @@ def run_gpu(args):
         forms["euclidean_full_tc"] = bench_euclid_tc(args, dev, flush)
         forms["precision_sweep"] = bench_precision(args, dev, flush)
         forms["barycenter_kmeans"] = bench_barycenter(args, dev, flush)
+        forms["ucr_lower_bounds"] = bench_ucr(args, dev, flush)
         forms["both_beat_fp64_drop_in"] = bool(
             forms["batched_fp32"]["gcups"] > value and forms["fwd_bwd_fp32"]["gcups"] > value)
     line = {
@@ -765,9 +829,11 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true",
                     help="only the FP32 forms (profiling captures)")
     ap.add_argument("--only", default="", choices=["", "batched", "fwdbwd", "subseq", "euclid",
-                                                     "precision", "barycenter"],
+                                                     "precision", "barycenter", "ucr"],
                     help="with --skip-fp64: run one form only")
     ap.add_argument("--c6-series", type=int, default=4096)
+    ap.add_argument("--c7-series", type=int, default=200,
+                    help="series for the scaled_dtw subsequence form")
     ap.add_argument("--c6-cpu-sample", type=int, default=48)
     ap.add_argument("--c3-series", type=int, default=1000)
     ap.add_argument("--c3-shapelets", type=int, default=10000)
