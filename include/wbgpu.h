@@ -341,6 +341,42 @@ int wb_lb_kim(const double *y, int64_t ny, const double *x, int64_t nx, int64_t 
               double *out, int32_t on_device, void *stream);
 
 /*
+ * wb_nearest_pivot -- batched nearest-pivot assignment for proximity trees
+ * (_partition_pivots, tree/_cptree.pyx:869-894, find_min_branch :273-290).
+ * Group g holds samples[sample_ptr[g] .. sample_ptr[g + 1]) and pivots
+ * pivots[pivot_ptr[g] .. pivot_ptr[g + 1]) (row indices of x, dim `dim`) and
+ * uses metric slot group_slot[g] (slot_metric[slot], slot_params[slot]).
+ * out_branch / out_dist, aligned with `samples`, receive the position within
+ * the group's pivots of the first pivot at the strictly smallest (full, not
+ * early-abandoned) distance and that distance; a sample without a finite
+ * distance keeps the previous sample's branch (-1 for a group's first), as
+ * the running pivot of _partition_pivots does.  Index arrays and outputs are
+ * host arrays; x may be on either side.
+ */
+int wb_nearest_pivot(const wb_series *x, int64_t dim, int64_t n_groups, const int64_t *sample_ptr,
+                     const int64_t *samples, const int64_t *pivot_ptr, const int64_t *pivots,
+                     const int32_t *group_slot, const int32_t *slot_metric,
+                     const wb_params *slot_params, int32_t n_slots, int64_t *out_branch,
+                     double *out_dist, void *stream);
+
+/*
+ * wb_subsequence_distance_views -- the shapelet transform's attribute values
+ * (transient_distance / persistent_distance, distance/_cdistance.pyx:265-299)
+ * for subsequence views of x: view v is x[view_sample[v], view_dim[v],
+ * view_start[v] : view_start[v] + view_length[v]] with the statistics its
+ * SubsequenceView holds (view_mean, view_std from _ts_view_update_statistics,
+ * :167-185; a zero std is used as 1).  Every view against every series of
+ * `target` at `dim`: out_dist / out_idx are (target.n, m) on the target's
+ * side.  View arrays are host arrays.
+ */
+int wb_subsequence_distance_views(const wb_series *x, const int64_t *view_sample,
+                                  const int64_t *view_dim, const int64_t *view_start,
+                                  const int64_t *view_length, const double *view_mean,
+                                  const double *view_std, int64_t m, const wb_series *target,
+                                  int64_t dim, int32_t metric, const wb_params *params,
+                                  double *out_dist, int64_t *out_idx, void *stream);
+
+/*
  * wb_group_mean -- x[group].mean(axis=0) of the euclidean KMeans update
  * (_EuclideanCluster._update_centroid, distance/_neighbors.py:364-369):
  * the rows member[group_start[gi] .. group_start[gi + 1] - 1] summed in that

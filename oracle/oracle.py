@@ -200,11 +200,15 @@ SUBSEQ_DEFAULTS = {
 
 
 def subsequence(shapelets, x, *, dim=0, metric="euclidean", metric_params=None,
-                n_threads=1):
-    """(n_samples, n_shapelets) min distance and first argmin index."""
+                n_threads=1, stats=None):
+    """(n_samples, n_shapelets) min distance and first argmin index.
+
+    stats: (means, stds) of the shapelets as the caller holds them (e.g. a
+    SubsequenceView's _ts_view_update_statistics) instead of np.mean / np.std.
+    """
     if metric == "scaled_dtw":
         return scaled_dtw_subsequence(shapelets, x, r=(metric_params or {}).get("r", 1.0),
-                                      dim=dim)
+                                      dim=dim, stats=stats)
     X = _ts(x)
     shp = [np.asarray(s, dtype=np.float64).ravel() for s in shapelets]
     lens = np.array([s.shape[0] for s in shp], dtype=np.int64)
@@ -215,6 +219,9 @@ def subsequence(shapelets, x, *, dim=0, metric="euclidean", metric_params=None,
     smean = np.array([np.mean(s) for s in shp])
     sstd = np.array([np.std(s) for s in shp])
     sstd[sstd <= 1e-13] = 0.0
+    if stats is not None:
+        smean = np.ascontiguousarray(stats[0], dtype=np.float64)
+        sstd = np.ascontiguousarray(stats[1], dtype=np.float64)
     dist = np.empty((X.shape[0], len(shp)))
     idx = np.zeros((X.shape[0], len(shp)), dtype=np.int64)
     pd = dict(SUBSEQ_DEFAULTS.get(metric, {}))
@@ -512,7 +519,7 @@ def _packed(shapelets):
     return shp, np.ascontiguousarray(np.concatenate(shp)), offs, lens
 
 
-def scaled_dtw_subsequence(shapelets, x, *, r=1.0, dim=0, paired=False):
+def scaled_dtw_subsequence(shapelets, x, *, r=1.0, dim=0, paired=False, stats=None):
     """pairwise / paired_subsequence_distance with metric="scaled_dtw"
     (ScaledDtwSubsequenceMetric, distance/_elastic.pyx:1928-2204, scan
     :353-465): (min distance, first argmin window); (n_samples, m) or (m,)."""
@@ -521,6 +528,9 @@ def scaled_dtw_subsequence(shapelets, x, *, r=1.0, dim=0, paired=False):
     smean = np.array([np.mean(s) for s in shp])
     sstd = np.array([np.std(s) for s in shp])
     sstd[sstd <= 1e-13] = 0.0
+    if stats is not None:
+        smean = np.ascontiguousarray(stats[0], dtype=np.float64)
+        sstd = np.ascontiguousarray(stats[1], dtype=np.float64)
     shape = (len(shp),) if paired else (X.shape[0], len(shp))
     dist = np.empty(shape)
     idx = np.zeros(shape, dtype=np.int64)
