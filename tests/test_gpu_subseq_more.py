@@ -224,3 +224,26 @@ def test_scaled_dtw_profile_and_matches_vs_oracle(r):
     np.testing.assert_array_equal(idx, np.concatenate(
         [np.flatnonzero(keep[i] > 0) for i in range(7)]))
     np.testing.assert_allclose(dist, d2[:, :171][keep > 0], rtol=RTOL, atol=0)
+
+
+@pytest.mark.parametrize("left,right", [("euclidean", "dtw"),
+                                        ("scaled_euclidean", "scaled_dtw")])
+def test_subsequence_match_equivalent(left, right):
+    # the reference's test_subsequence_match_equivalent
+    # (tests/wildboar/distance/test_distance.py:1440-1477) on random walks:
+    # a warp window of 0 makes dtw the euclidean distance
+    rng = np.random.default_rng(47)
+    x = np.cumsum(rng.standard_normal((10, 150)), axis=1)
+    q = x[9, 40:60].copy()
+
+    def run(metric):
+        return subsequence_match(q, x[0:9], return_distance=True, max_matches=20, exclude=4,
+                                 metric=metric,
+                                 metric_params={"r": 0.0} if "dtw" in metric else {})
+
+    li, ld = run(left)
+    ri, rd = run(right)
+    for a, b in zip(ld, rd):
+        np.testing.assert_almost_equal(a, b)
+    for a, b in zip(li, ri):
+        np.testing.assert_array_equal(a, b)
