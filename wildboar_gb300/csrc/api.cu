@@ -982,7 +982,8 @@ static int subseq_entry(const double *shapelets, const int64_t *offsets, const i
         group_of[i] = (int32_t)group_len.size() - 1;
     }
 
-    // scaled metric: chunks of <= 64 shapelets of one length for the tiled kernel
+    // scaled metric: chunks of <= kScaledTileChunk shapelets of one length for
+    // the tiled kernel (the z-normalised tiles are shared by a chunk)
     std::vector<int64_t> ch_first;
     std::vector<int32_t> ch_count, ch_group;
     int max_len = 0;
@@ -991,7 +992,8 @@ static int subseq_entry(const double *shapelets, const int64_t *offsets, const i
     if (tiled) {
         for (int64_t t = 0; t < m;) {
             int64_t u = t;
-            while (u < m && u - t < 64 && group_of[order[u]] == group_of[order[t]]) u++;
+            while (u < m && u - t < kScaledTileChunk && group_of[order[u]] == group_of[order[t]])
+                u++;
             ch_first.push_back(t);
             ch_count.push_back((int32_t)(u - t));
             ch_group.push_back(group_of[order[t]]);
@@ -1007,7 +1009,7 @@ static int subseq_entry(const double *shapelets, const int64_t *offsets, const i
     J.std_as_given = std_as_given;
     J.total_values = total;
     J.win_stride = (int)x->n_timestep;
-    J.chunk = 64;
+    J.chunk = kScaledTileChunk;
     Workspace ws(s);
     size_t need = stage_bytes(x) + align256(m * 8) * 3 + align256(m * 4) +
                   align256(group_len.size() * 4) +

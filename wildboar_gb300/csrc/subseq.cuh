@@ -42,6 +42,8 @@ size_t subseq_workspace_bytes(const SubseqJob &J, bool scaled);
 // longest shapelet the tiled scaled kernel takes (its z-normalised window
 // tile is L x 32 doubles of shared memory)
 constexpr int kScaledTileMaxLen = 384;
+// shapelets of one length sharing the z-normalised window tiles of a block
+constexpr int kScaledTileChunk = 256;
 int launch_subseq(const SubseqJob &J, bool scaled, Workspace &ws);
 // paired jobs: every window's full sum at raw[pair * ld + window]
 int launch_subseq_profile(const SubseqJob &J, bool scaled, Workspace &ws, double *raw,
