@@ -445,6 +445,35 @@ def main():
         add(f"lb_kim_L{L}", "lb_kim", {"x": XB[:, :L], "q": QB[:, :L]}, {},
             {"out": DtwKimLowerBound().fit(XB[:, :L]).transform(QB[:, :L])})
 
+    # edge cases of the rows above: ties everywhere, minimal bands, single windows
+    XE = _walk(rng, (4, 16))
+    XT2 = np.stack([XE[0], XE[0], XE[0] + 0.0, XE[1]])
+    for name, X_, kw in (("ties_r0", XT2, {"r": 0.0, "init": XE[0]}),
+                         ("ties_r1", XT2, {"r": 1.0, "init": XE[2]}),
+                         ("two_rows", XE[:2], {"r": 0.5, "init": XE[3]}),
+                         ("const_init", XE, {"r": 0.3, "init": np.zeros(16)})):
+        mean, cost = dtw_average(X_, return_cost=True, **kw)
+        add(f"dtw_average_edge_{name}", "dtw_average", {"x": X_, "init": kw["init"]},
+            {"r": kw["r"]}, {"mean": mean, "cost": cost})
+    km = KMeans(n_clusters=4, metric="dtw", r=0.2, random_state=5).fit(XE)
+    add("kmeans_edge_k_eq_n", "kmeans", {"x": XE},
+        {"n_clusters": 4, "metric": "dtw", "r": 0.2, "random_state": 5},
+        {"labels": km.labels_, "centers": km.cluster_centers_, "inertia": km.inertia_,
+         "n_iter": km.n_iter_})
+    shp_e = [XS[0].copy(), XS[1, 7:10].copy(), XS[2, 0:119].copy()]
+    for r in (1.0, 0.2):
+        d, i = pairwise_subsequence_distance(shp_e, XS, metric="scaled_dtw",
+                                             metric_params={"r": r}, return_index=True)
+        add(f"subseq_scaled_dtw_edge_r{r}", "subsequence",
+            {"x": XS, "shapelets": np.concatenate(shp_e),
+             "lengths": np.array([len(s) for s in shp_e])},
+            {"metric": "scaled_dtw", "metric_params": {"r": r}}, {"d": d, "idx": i})
+    for L in (1, 2, 3):
+        lbk = DtwKeoghLowerBound(r=0.5).fit(XB[:, :L])
+        add(f"lb_keogh_L{L}", "lb_keogh", {"x": XB[:, :L], "q": QB[:, :L]},
+            {"r": 0.5, "kind": "both"},
+            {"out": lbk.transform(QB[:, :L]), "lower": lbk.lower_, "upper": lbk.upper_})
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"reference_version": getattr(wildboar, "__version__", "?"),
