@@ -377,6 +377,21 @@ int wb_subsequence_distance_views(const wb_series *x, const int64_t *view_sample
                                   double *out_dist, int64_t *out_idx, void *stream);
 
 /*
+ * wb_dtw_average_ssg_epoch -- the sample loop of one epoch of the stochastic
+ * subgradient DTW mean (_ssg_dtw_average, distance/dtw.py:597-658): for
+ * step i, the path of (mean, x[order[i]]) (dtw_alignment / wdtw_alignment and
+ * dtw_mapping as wb_dtw_average_mm_step), z[m] = sum over its cells (m, x)
+ * of (mean[m] - x[order[i], x] w), mean -= lr[i] z, with
+ * w = sample_weight[order[i]] (NULL: 1).  x, mean and weights are device
+ * pointers (mean updated in place); order, lr and sample_weight are host
+ * arrays of n_steps (order, lr) and n samples (sample_weight).
+ */
+int wb_dtw_average_ssg_epoch(const double *x, int64_t x_stride, int64_t n_timestep,
+                             double *mean, int64_t mean_len, const int64_t *order,
+                             const double *lr, int64_t n_steps, double r, const double *weights,
+                             const double *sample_weight, void *stream);
+
+/*
  * wb_group_mean -- x[group].mean(axis=0) of the euclidean KMeans update
  * (_EuclideanCluster._update_centroid, distance/_neighbors.py:364-369):
  * the rows member[group_start[gi] .. group_start[gi + 1] - 1] summed in that

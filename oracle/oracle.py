@@ -623,3 +623,49 @@ def lb_kim(Q, X):
                     sq(a2e, b2e), np.minimum(sq(a2e, b1e), sq(a2e, b0e)))))
         out[i] = d
     return out
+
+
+def dtw_average_ssg(X, *, r=1.0, g=None, init, sample_weight=None, max_epoch=50,
+                    learning_rate=0.1, decay=0.9, max_stable=5, random_state):
+    """_ssg_dtw_average (distance/dtw.py:597-658) with the oracle's alignment
+    and traceback; random_state is the RandomState the reference passes on."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    mean = np.array(init, dtype=np.float64, copy=True)
+    if g is None:
+        metric, params, weights = "dtw", {"r": r}, None
+    else:
+        metric, params = "wdtw", {"r": r, "g": g}
+        weights = jeong_weight(max(mean.shape[0], X.shape[1]), g)
+
+    def costfn(m):
+        d = pairwise(m, X, metric=metric, metric_params=params)[0]
+        if sample_weight is None:
+            return np.mean(d)
+        return np.average(d, weights=sample_weight)
+
+    best_mean = None
+    order = np.arange(X.shape[0])
+    min_cost = np.inf
+    n_stable = 0
+    z = np.empty(mean.shape[0])
+    for epoch in range(max_epoch):
+        if n_stable > max_stable:
+            break
+        random_state.shuffle(order)
+        for i, o in enumerate(order):
+            z.fill(0)
+            path = dtw_mapping(dtw_alignment(mean, X[o], r=r, weights=weights))
+            w = 1.0 if sample_weight is None else sample_weight[o]
+            for m_, x_ in path:
+                z[m_] += mean[m_] - X[o, x_] * w
+            mean -= learning_rate * z
+            if epoch == 0:
+                learning_rate = decay**i * learning_rate
+        cost = costfn(mean)
+        if cost < min_cost:
+            min_cost = cost
+            n_stable = 0
+            best_mean = mean.copy()
+        else:
+            n_stable += 1
+    return best_mean, min_cost

@@ -474,6 +474,25 @@ def main():
             {"r": 0.5, "kind": "both"},
             {"out": lbk.transform(QB[:, :L]), "lower": lbk.lower_, "upper": lbk.upper_})
 
+    # dtw_average(method="ssg") (distance/dtw.py:597-658)
+    XG = _walk(rng, (10, 24))
+    swg = rng.uniform(0.5, 1.5, 10)
+    for name, kw in (("dtw", {"r": 0.5, "random_state": 3, "max_epoch": 8}),
+                     ("wdtw", {"r": 1.0, "g": 0.1, "random_state": 4, "max_epoch": 6}),
+                     ("sample_weight", {"r": 0.3, "random_state": 5, "max_epoch": 6,
+                                        "sample_weight": swg}),
+                     ("stable", {"r": 0.2, "random_state": 6, "max_epoch": 40,
+                                 "max_stable": 1, "learning_rate": 0.05, "decay": 0.8})):
+        mean, cost = dtw_average(XG, method="ssg", return_cost=True, **kw)
+        inputs = {"x": XG}
+        if "sample_weight" in kw:
+            inputs["sample_weight"] = kw["sample_weight"]
+        args = {k: v for k, v in kw.items() if k != "sample_weight"}
+        args["method"] = "ssg"
+        args["init"] = "random"
+        add(f"dtw_average_ssg_{name}", "dtw_average", inputs, args,
+            {"mean": mean, "cost": cost})
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"reference_version": getattr(wildboar, "__version__", "?"),

@@ -39,7 +39,8 @@ def _cases(kind):
 def test_dtw_average_golden(case):
     a = dict(case["args"])
     inp = case["inputs"]
-    kw = {k: a[k] for k in ("r", "g", "tol", "max_epoch", "random_state") if k in a}
+    kw = {k: a[k] for k in ("r", "g", "tol", "max_epoch", "random_state", "method",
+                            "learning_rate", "decay", "max_stable") if k in a}
     init = inp["init"] if "init" in inp else a["init"]
     mean, cost = dtw_average(inp["x"], init=init, sample_weight=inp.get("sample_weight"),
                              return_cost=True, **kw)
@@ -171,5 +172,19 @@ def test_alignment_forms_vs_oracle(monkeypatch, form, n, T, r, g):
     init = _walk(rng, n)
     mean, cost = dtw_average(X, r=r, g=g, init=init, return_cost=True, max_epoch=4, tol=0.0)
     om, oc = O.dtw_average_mm(X, r=r, g=g, init=init, max_epoch=4, tol=0.0)
+    np.testing.assert_allclose(mean, om, rtol=RTOL, atol=0)
+    np.testing.assert_allclose(cost, oc, rtol=RTOL, atol=0)
+
+
+@pytest.mark.parametrize("form", ["strip", "antidiag"])
+def test_dtw_average_ssg_vs_oracle(monkeypatch, form):
+    monkeypatch.setenv("WB_MM_ALIGN", form)
+    rng = np.random.default_rng(31)
+    X = _walk(rng, (12, 90))
+    mean, cost = dtw_average(X, method="ssg", r=0.2, max_epoch=5, random_state=9,
+                             return_cost=True)
+    rs = np.random.RandomState(9)
+    init = X[rs.randint(12)]
+    om, oc = O.dtw_average_ssg(X, r=0.2, init=init, max_epoch=5, random_state=rs)
     np.testing.assert_allclose(mean, om, rtol=RTOL, atol=0)
     np.testing.assert_allclose(cost, oc, rtol=RTOL, atol=0)

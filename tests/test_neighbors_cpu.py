@@ -24,7 +24,6 @@ def test_kmeans_rejects_3d():
 
 
 @pytest.mark.parametrize("kw,exc", [({"r": 1.5}, ValueError), ({"method": "foo"}, ValueError),
-                                    ({"method": "ssg"}, NotImplementedError),
                                     ({"g": 0.0}, ValueError), ({"init": 3}, ValueError),
                                     ({"sample_weight": np.ones(3)}, ValueError)])
 def test_dtw_average_rejects_bad_args(kw, exc):
@@ -63,3 +62,12 @@ def test_jeong_weight_formula():
     w = jeong_weight(10, 0.3)
     want = 1.0 / (1.0 + np.exp(-0.3 * (np.arange(10, dtype=float) - 5.0)))
     np.testing.assert_array_equal(w, want)
+
+
+def test_dtw_average_ssg_needs_the_device():
+    import torch
+
+    if torch.cuda.is_available():  # pragma: no cover
+        pytest.skip("a GPU is present")
+    with pytest.raises(RuntimeError):
+        dtw_average(X, method="ssg", random_state=0)

@@ -105,10 +105,18 @@ def run_oracle(case):
         return {"a": np.where(inp["mask"], al, 0.0)}
     if kind == "dtw_average":
         X = inp["x"]
+        rs = np.random.RandomState(a["random_state"]) if "random_state" in a else None
         if "init" in inp:
             init = inp["init"]
         else:  # init="random": dtw_average draws the row (distance/dtw.py:542-543)
-            init = X[np.random.RandomState(a["random_state"]).randint(X.shape[0])]
+            init = X[rs.randint(X.shape[0])]
+        if a.get("method") == "ssg":
+            kw = {k: a[k] for k in ("max_epoch", "learning_rate", "decay", "max_stable")
+                  if k in a}
+            mean, cost = O.dtw_average_ssg(X, r=a["r"], g=a.get("g"), init=init,
+                                           sample_weight=inp.get("sample_weight"),
+                                           random_state=rs, **kw)
+            return {"mean": mean, "cost": cost}
         mean, cost = O.dtw_average_mm(X, r=a["r"], g=a.get("g"), init=init,
                                       sample_weight=inp.get("sample_weight"),
                                       tol=a.get("tol", 1e-5), max_epoch=a.get("max_epoch", 50))

@@ -445,6 +445,95 @@ int pick_strip(int n) {
 
 using namespace wb;
 
+namespace wb {
+namespace {
+
+// which alignment kernel, and its direction-word layout, for (n x m) pairs
+struct AlignPlan {
+    int n = 0, m = 0, warp = 1;
+    bool antidiag = false;
+    int S = 16, K = 1;
+    int64_t pair_words = 0, word_bytes = 4;
+    bool passes = false;
+};
+
+AlignPlan plan_alignment(int n, int m, double r) {
+    AlignPlan P;
+    P.n = n;
+    P.m = m;
+    const int64_t big = n > m ? n : m;
+    const double wv = std::floor((double)big * r);
+    P.warp = (int)(wv > 1.0 ? wv : 1.0);
+    // FP64 warp-instruction slots of the two forms: the strip wavefront runs
+    // 32 S rows x (m + 31) steps per pass, the anti-diagonal form
+    // 32 ceil(cnt / 32) slots per diagonal
+    P.S = pick_strip(n);
+    const int mxb = imax(0, m - n) + P.warp, mnb = imax(0, n - m);
+    int maxcnt = 0;
+    int64_t slots_ad = 0;
+    for (int d = 0; d < n + m - 1; d++) {
+        int ilo, ihi;
+        ad_bounds(d, n, m, P.warp, mxb, mnb, ilo, ihi);
+        const int cnt = ihi - ilo + 1;
+        maxcnt = cnt > maxcnt ? cnt : maxcnt;
+        slots_ad += 32LL * ((cnt + 31) / 32);
+    }
+    const int64_t slots_strip =
+        (int64_t)((n + 32 * P.S - 1) / (32 * P.S)) * (m + 31) * 32 * P.S;
+    while (32 * P.K < maxcnt) P.K *= 2;
+    P.antidiag = P.K <= 16 && slots_ad < slots_strip;
+    if (const char *f = std::getenv("WB_MM_ALIGN")) {
+        if (std::strcmp(f, "strip") == 0) P.antidiag = false;
+        if (std::strcmp(f, "antidiag") == 0 && P.K <= 16) P.antidiag = true;
+    }
+    if (P.antidiag) {
+        P.pair_words = (int64_t)(n + m - 1) * 32;
+        P.word_bytes = P.K <= 4 ? 1 : (P.K <= 8 ? 2 : 4);
+    } else {
+        P.pair_words = (int64_t)((n + P.S - 1) / P.S) * m;
+        P.word_bytes = P.S / 4;
+    }
+    P.passes = !P.antidiag && n > 32 * P.S;
+    return P;
+}
+
+int run_alignment(const AlignPlan &P, const MmAlignJob &J, int grid, cudaStream_t st) {
+    const bool w = J.weights != nullptr;
+    if (P.antidiag) {
+        switch (P.K) {
+            case 1: return w ? launch_ad<1, true>(J, grid, st) : launch_ad<1, false>(J, grid, st);
+            case 2: return w ? launch_ad<2, true>(J, grid, st) : launch_ad<2, false>(J, grid, st);
+            case 4: return w ? launch_ad<4, true>(J, grid, st) : launch_ad<4, false>(J, grid, st);
+            case 8: return w ? launch_ad<8, true>(J, grid, st) : launch_ad<8, false>(J, grid, st);
+            default:
+                return w ? launch_ad<16, true>(J, grid, st) : launch_ad<16, false>(J, grid, st);
+        }
+    }
+    if (P.S == 4) return w ? launch_align<4, true>(J, grid, st) : launch_align<4, false>(J, grid, st);
+    if (P.S == 8) return w ? launch_align<8, true>(J, grid, st) : launch_align<8, false>(J, grid, st);
+    return w ? launch_align<16, true>(J, grid, st) : launch_align<16, false>(J, grid, st);
+}
+
+// One stochastic-subgradient step of _ssg_dtw_average (distance/dtw.py:
+// 622-633) from the path of (mean, sample): z[m] = sum over the path cells
+// (m, x) in order of (mean[m] - X[x] w), then mean[m] -= lr z[m].  One thread
+// per mean element (each reads and writes only its own element).
+__global__ void ssg_update_kernel(const double *X, const int32_t *lo, const int32_t *hi, int n,
+                                  double w, int weighted, double lr, double *mean) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double mv = mean[i];
+    double z = 0.0;
+    for (int c = lo[i]; c <= hi[i]; c++) {
+        const double xv = weighted ? X[c] * w : X[c];
+        z = z + (mv - xv);
+    }
+    mean[i] = mv - lr * z;
+}
+
+}  // namespace
+}  // namespace wb
+
 extern "C" int wb_dtw_average_mm_step(const double *x, int64_t x_stride, int64_t n_timestep,
                                       const double *means, int64_t mean_len,
                                       const int64_t *member, const int32_t *pair_group,
@@ -462,41 +551,8 @@ extern "C" int wb_dtw_average_mm_step(const double *x, int64_t x_stride, int64_t
     if (!x || !means || !member || !pair_group || !group_start)
         return fail(WB_EINVAL, "dtw_average: null pointer");
     const int n = (int)mean_len, m = (int)n_timestep;
-    const int64_t big = n > m ? n : m;
-    const double wv = std::floor((double)big * r);
-    const int warp = (int)(wv > 1.0 ? wv : 1.0);
-    // FP64 warp-instruction slots of the two forms: the strip wavefront runs
-    // 32 S rows x (m + 31) steps per pass, the anti-diagonal form
-    // 32 ceil(cnt / 32) slots per diagonal
-    const int S = pick_strip(n);
-    const int mxb = imax(0, m - n) + warp, mnb = imax(0, n - m);
-    int maxcnt = 0;
-    int64_t slots_ad = 0;
-    for (int d = 0; d < n + m - 1; d++) {
-        int ilo, ihi;
-        ad_bounds(d, n, m, warp, mxb, mnb, ilo, ihi);
-        const int cnt = ihi - ilo + 1;
-        maxcnt = cnt > maxcnt ? cnt : maxcnt;
-        slots_ad += 32LL * ((cnt + 31) / 32);
-    }
-    const int64_t slots_strip = (int64_t)((n + 32 * S - 1) / (32 * S)) * (m + 31) * 32 * S;
-    int K = 1;
-    while (32 * K < maxcnt) K *= 2;
-    bool antidiag = K <= 16 && slots_ad < slots_strip;
-    if (const char *f = std::getenv("WB_MM_ALIGN")) {
-        if (std::strcmp(f, "strip") == 0) antidiag = false;
-        if (std::strcmp(f, "antidiag") == 0 && K <= 16) antidiag = true;
-    }
-    int64_t pair_words, word_bytes;
-    if (antidiag) {
-        pair_words = (int64_t)(n + m - 1) * 32;
-        word_bytes = K <= 4 ? 1 : (K <= 8 ? 2 : 4);
-    } else {
-        pair_words = (int64_t)((n + S - 1) / S) * m;
-        word_bytes = S / 4;
-    }
-    const int64_t pair_bytes = pair_words * word_bytes;
-    const bool passes = !antidiag && n > 32 * S;
+    const AlignPlan P = plan_alignment(n, m, r);
+    const int64_t pair_bytes = P.pair_words * P.word_bytes;
     const DeviceInfo &dev = device_info();
     const int max_grid = dev.sm_count * 8;
     // direction words per launch bounded to about 1 GiB
@@ -505,12 +561,12 @@ extern "C" int wb_dtw_average_mm_step(const double *x, int64_t x_stride, int64_t
     const int grid = (int)std::min<int64_t>((chunk + kMmWarps - 1) / kMmWarps, max_grid);
     Workspace ws(st);
     const size_t need = align256(chunk * pair_bytes) +
-                        align256(passes ? (size_t)grid * kMmWarps * m * sizeof(double) : 0) +
+                        align256(P.passes ? (size_t)grid * kMmWarps * m * sizeof(double) : 0) +
                         2 * align256((size_t)n_pairs * n * sizeof(int32_t)) + 4096;
     WB_TRY(ws.reserve(need));
     WB_TAKE(dirbuf, char, ws, chunk * pair_bytes);
     double *bnd = nullptr;
-    if (passes) {
+    if (P.passes) {
         bnd = ws.take<double>((size_t)grid * kMmWarps * m);
         if (!bnd) return fail(WB_ENOMEM, "workspace reservation exceeded");
     }
@@ -524,36 +580,19 @@ extern "C" int wb_dtw_average_mm_step(const double *x, int64_t x_stride, int64_t
     J.n = n;
     J.member = member;
     J.pair_group = pair_group;
-    J.r = warp;
+    J.r = P.warp;
     J.weights = weights;
     J.dir = dirbuf;
-    J.dir_pair_words = pair_words;
+    J.dir_pair_words = P.pair_words;
     J.bnd = bnd;
     J.path_lo = lo;
     J.path_hi = hi;
     J.last = last;
-    timer_begin(antidiag ? "mm_align_ad_kernel" : "mm_align_kernel", st);
+    timer_begin(P.antidiag ? "mm_align_ad_kernel" : "mm_align_kernel", st);
     for (int64_t q0 = 0; q0 < n_pairs; q0 += chunk) {
         J.q0 = q0;
         J.q1 = std::min(n_pairs, q0 + chunk);
-        const bool w = weights != nullptr;
-        int s;
-        if (antidiag) {
-            switch (K) {
-                case 1: s = w ? launch_ad<1, true>(J, grid, st) : launch_ad<1, false>(J, grid, st); break;
-                case 2: s = w ? launch_ad<2, true>(J, grid, st) : launch_ad<2, false>(J, grid, st); break;
-                case 4: s = w ? launch_ad<4, true>(J, grid, st) : launch_ad<4, false>(J, grid, st); break;
-                case 8: s = w ? launch_ad<8, true>(J, grid, st) : launch_ad<8, false>(J, grid, st); break;
-                default: s = w ? launch_ad<16, true>(J, grid, st) : launch_ad<16, false>(J, grid, st); break;
-            }
-        } else if (S == 4) {
-            s = w ? launch_align<4, true>(J, grid, st) : launch_align<4, false>(J, grid, st);
-        } else if (S == 8) {
-            s = w ? launch_align<8, true>(J, grid, st) : launch_align<8, false>(J, grid, st);
-        } else {
-            s = w ? launch_align<16, true>(J, grid, st) : launch_align<16, false>(J, grid, st);
-        }
-        if (s != WB_OK) return s;
+        WB_TRY(run_alignment(P, J, grid, st));
     }
     timer_end(st);
     if (new_means && n_groups > 0) {
@@ -563,6 +602,68 @@ extern "C" int wb_dtw_average_mm_step(const double *x, int64_t x_stride, int64_t
             new_means, n);
         WB_LAUNCH_CHECK("mm_accumulate_kernel");
     }
+    return WB_OK;
+}
+
+extern "C" int wb_dtw_average_ssg_epoch(const double *x, int64_t x_stride, int64_t n_timestep,
+                                        double *mean, int64_t mean_len, const int64_t *order,
+                                        const double *lr, int64_t n_steps, double r,
+                                        const double *weights, const double *sample_weight,
+                                        void *stream) {
+    const cudaStream_t st = (cudaStream_t)stream;
+    if (n_steps < 0 || n_timestep < 1 || mean_len < 1)
+        return fail(WB_EINVAL, "dtw_average: invalid sizes");
+    if (!(r >= 0.0 && r <= 1.0)) return fail(WB_EINVAL, "dtw_average: r must be in [0, 1]");
+    if (n_timestep > INT32_MAX / 2 || mean_len > INT32_MAX / 2)
+        return fail(WB_EINVAL, "dtw_average: series too long");
+    if (n_steps == 0) return WB_OK;
+    if (!x || !mean || !order || !lr) return fail(WB_EINVAL, "dtw_average: null pointer");
+    const int n = (int)mean_len, m = (int)n_timestep;
+    const AlignPlan P = plan_alignment(n, m, r);
+    const int64_t pair_bytes = P.pair_words * P.word_bytes;
+    Workspace ws(st);
+    const size_t need = align256(pair_bytes) +
+                        align256(P.passes ? (size_t)kMmWarps * m * sizeof(double) : 0) +
+                        2 * align256((size_t)n * sizeof(int32_t)) +
+                        align256((size_t)n_steps * 8) + align256(4) + 4096;
+    WB_TRY(ws.reserve(need));
+    WB_TAKE(dirbuf, char, ws, pair_bytes);
+    double *bnd = nullptr;
+    if (P.passes) {
+        bnd = ws.take<double>((size_t)kMmWarps * m);
+        if (!bnd) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    }
+    WB_TAKE(lo, int32_t, ws, n);
+    WB_TAKE(hi, int32_t, ws, n);
+    WB_TAKE(dorder, int64_t, ws, n_steps);
+    WB_TAKE(zero, int32_t, ws, 1);
+    WB_CUDA(cudaMemcpyAsync(dorder, order, n_steps * 8, cudaMemcpyHostToDevice, st));
+    WB_CUDA(cudaMemsetAsync(zero, 0, 4, st));
+    MmAlignJob J;
+    J.x = x;
+    J.x_stride = x_stride;
+    J.m = m;
+    J.means = mean;
+    J.n = n;
+    J.pair_group = zero;
+    J.r = P.warp;
+    J.weights = weights;
+    J.dir = dirbuf;
+    J.dir_pair_words = P.pair_words;
+    J.bnd = bnd;
+    J.path_lo = lo;
+    J.path_hi = hi;
+    J.q0 = 0;
+    J.q1 = 1;
+    for (int64_t i = 0; i < n_steps; i++) {
+        J.member = dorder + i;
+        WB_TRY(run_alignment(P, J, 1, st));
+        const double w = sample_weight ? sample_weight[order[i]] : 1.0;
+        ssg_update_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(
+            x + order[i] * x_stride, lo, hi, n, w, sample_weight ? 1 : 0, lr[i], mean);
+        WB_LAUNCH_CHECK("ssg_update_kernel");
+    }
+    WB_CUDA(cudaStreamSynchronize(st));
     return WB_OK;
 }
 

@@ -34,6 +34,12 @@ _lib.declare(
      ctypes.c_void_p, ctypes.c_void_p],
 )
 _lib.declare(
+    "wb_dtw_average_ssg_epoch",
+    [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p,
+     ctypes.c_void_p, ctypes.c_void_p],
+)
+_lib.declare(
     "wb_group_mean",
     [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
      ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p],
@@ -209,15 +215,67 @@ def _mm_average_groups(Xd, groups, init, *, r, g=None, sample_weight=None, tol=1
     return final, costs
 
 
+def _ssg_dtw_average(Xd, mean, *, r, g, sample_weight, max_epoch, learning_rate, decay,
+                     max_stable, verbose, random_state):
+    """_ssg_dtw_average (distance/dtw.py:597-658): the shuffles, learning-rate
+    schedule, costs and best-mean bookkeeping on the host, every epoch's
+    sample loop one call on the device (wb_dtw_average_ssg_epoch)."""
+    torch = _torch()
+    dev = Xd.device
+    N, T = Xd.shape
+    nm = mean.shape[0]
+    mean_d = torch.as_tensor(np.ascontiguousarray(mean, dtype=np.float64), device=dev).clone()
+    wdev = None
+    metric, metric_params = "dtw", {"r": r}
+    if g is not None:
+        wdev = torch.as_tensor(jeong_weight(max(nm, T), g), device=dev)
+        metric, metric_params = "wdtw", {"r": r, "g": g}
+    sw = None if sample_weight is None else np.ascontiguousarray(sample_weight, np.float64)
+    best_mean = None
+    order = np.arange(N)
+    min_cost = np.inf
+    n_stable = 0
+    for epoch in range(max_epoch):
+        if n_stable > max_stable:
+            if verbose:
+                print(f"Completed at epoch={epoch} with cost={min_cost}.")
+            break
+        random_state.shuffle(order)
+        lrs = np.empty(N)
+        for i in range(N):
+            lrs[i] = learning_rate
+            if epoch == 0:
+                learning_rate = decay**i * learning_rate
+        o = np.ascontiguousarray(order, dtype=np.int64)
+        st = _lib.lib().wb_dtw_average_ssg_epoch(
+            Xd.data_ptr(), Xd.stride(0), T, mean_d.data_ptr(), nm, _lib.ptr(o), _lib.ptr(lrs),
+            N, float(r), None if wdev is None else wdev.data_ptr(), _lib.ptr(sw),
+            _lib.current_stream_handle())
+        _lib.check(st)
+        d = pairwise_distance(mean_d, Xd, metric=metric, metric_params=metric_params)
+        d = d.reshape(-1).cpu().numpy()
+        cost = _group_cost(d, sw)
+        if cost < min_cost:
+            if verbose:
+                print(f"New min cost={cost} at epoch={epoch} with "
+                      f"learning_rate={learning_rate}.")
+            min_cost = cost
+            n_stable = 0
+            best_mean = mean_d.cpu().numpy().copy()
+        else:
+            n_stable += 1
+    return best_mean, min_cost
+
+
 def dtw_average(X, *, r=1.0, g=None, sample_weight=None, init="random", method="mm",
                 max_stable=5, learning_rate=0.1, decay=0.9, tol=1e-5, max_epoch=50,
                 return_cost=False, verbose=False, random_state=None):
     """Compute the DTW barycenter average (distance/dtw.py:429-594).
 
     ``method="mm"`` (the majorize-minimize mean, the reference's default and
-    the one KMeans uses) runs on the GPU and returns the reference's bits.
-    ``method="ssg"`` (stochastic subgradient, a sequential per-sample update)
-    is not provided.
+    the one KMeans uses) and ``method="ssg"`` (the stochastic subgradient mean,
+    a sequential per-sample update, distance/dtw.py:597-658) run on the GPU and
+    return the reference's bits.
     """
     X = check_array(X, allow_3d=False, ensure_2d=True, dtype=float)
     if X.shape[0] < 2:
@@ -242,12 +300,16 @@ def dtw_average(X, *, r=1.0, g=None, sample_weight=None, init="random", method="
                                                                   (X.shape[0],)))
     if g is not None:
         g = _check_scalar(g, "g", min_val=0, include_min=False)
-    if method == "ssg":
-        raise NotImplementedError("dtw_average(method='ssg') is not available on the GPU path")
-    if method != "mm":
+    if method not in ("mm", "ssg"):
         raise ValueError("method must be 'mm' or 'ssg', got %r" % method)
     torch = _torch()
     Xd = _to_device(X, torch)
+    if method == "ssg":
+        mean, cost = _ssg_dtw_average(
+            Xd, mean, r=r, g=g, sample_weight=sample_weight, max_epoch=max_epoch,
+            learning_rate=learning_rate, decay=decay, max_stable=max_stable, verbose=verbose,
+            random_state=random_state)
+        return (mean, cost) if return_cost else mean
     means, costs = _mm_average_groups(
         Xd, [np.arange(X.shape[0])], mean.reshape(1, -1), r=r, g=g,
         sample_weight=None if sample_weight is None else [sample_weight], tol=tol,
