@@ -392,6 +392,26 @@ int wb_dtw_average_ssg_epoch(const double *x, int64_t x_stride, int64_t n_timest
                              const double *sample_weight, void *stream);
 
 /*
+ * wb_dtw_alignment -- the cumulative cost matrix of dtw_alignment /
+ * wdtw_alignment (distance/dtw.py:246-327, _elastic.pyx:1011-1073): out is
+ * (n, m) with the band's cells and +inf elsewhere (the reference leaves the
+ * cells off the band and its boundary markers unset).  r is the window
+ * fraction (warp max(floor(max(n, m) r), 1)); weights (length >= max(n, m))
+ * weigh cell (i, j) by weights[|i - j|], NULL for dtw.
+ */
+int wb_dtw_alignment(const double *x, int64_t n, const double *y, int64_t m, double r,
+                     const double *weights, double *out, int32_t on_device, void *stream);
+
+/*
+ * wb_lb_keogh_terms -- _dtw_lb_keogh (distance/_elastic.pyx:1095-1115) of one
+ * series against an envelope: cb[k] the excursion of x[k] outside
+ * [lower[k], upper[k]] squared, *dist the square root of their sum.
+ */
+int wb_lb_keogh_terms(const double *x, const double *lower, const double *upper,
+                      int64_t n_timestep, double *cb, double *dist, int32_t on_device,
+                      void *stream);
+
+/*
  * wb_group_mean -- x[group].mean(axis=0) of the euclidean KMeans update
  * (_EuclideanCluster._update_centroid, distance/_neighbors.py:364-369):
  * the rows member[group_start[gi] .. group_start[gi + 1] - 1] summed in that

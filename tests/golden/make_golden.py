@@ -493,6 +493,36 @@ def main():
         add(f"dtw_average_ssg_{name}", "dtw_average", inputs, args,
             {"mean": mean, "cost": cost})
 
+    # single-pair helpers of distance/dtw.py:43-426
+    from wildboar.distance.dtw import (ddtw_distance, dtw_distance, dtw_envelop,
+                                       dtw_lb_keogh, dtw_mapping, wddtw_distance,
+                                       wdtw_alignment, wdtw_distance)
+
+    ha = _walk(rng, 35)
+    hb = _walk(rng, 35)
+    hc = _walk(rng, 28)
+    def band_mask(n, m, r):
+        warp = max(math.floor(max(n, m) * r), 1)
+        mask = np.zeros((n, m), dtype=bool)
+        for i in range(n):
+            mask[i, max(0, i - max(0, n - m) - warp + 1):min(m, i + max(0, m - n) + warp)] = True
+        return mask
+
+    for r in (0.1, 1.0):
+        lo, up = dtw_envelop(ha, r=r)
+        d1, cb1 = dtw_lb_keogh(hb, ha, r=r)
+        d2, cb2 = dtw_lb_keogh(hb, lower=lo, upper=up)
+        wmask = band_mask(35, 28, r)
+        wal = wdtw_alignment(ha, hc, r=r, g=0.3)
+        add(f"dtw_helpers_r{r}", "dtw_helpers", {"a": ha, "b": hb, "c": hc, "mask": wmask},
+            {"r": r},
+            {"dtw": dtw_distance(ha, hb, r=r), "ddtw": ddtw_distance(ha, hc, r=r),
+             "wdtw": wdtw_distance(hc, hb, r=r, g=0.1),
+             "wddtw": wddtw_distance(ha, hb, r=r, g=0.2), "lower": lo, "upper": up,
+             "lb": d1, "cb": cb1, "lb2": d2, "cb2": cb2,
+             "mapping": dtw_mapping(ha, hc, r=r),
+             "walign": np.where(wmask, wal, 0.0)})
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"reference_version": getattr(wildboar, "__version__", "?"),

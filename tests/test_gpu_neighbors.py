@@ -188,3 +188,40 @@ def test_dtw_average_ssg_vs_oracle(monkeypatch, form):
     om, oc = O.dtw_average_ssg(X, r=0.2, init=init, max_epoch=5, random_state=rs)
     np.testing.assert_allclose(mean, om, rtol=RTOL, atol=0)
     np.testing.assert_allclose(cost, oc, rtol=RTOL, atol=0)
+
+
+@_cases("dtw_helpers")
+def test_dtw_helpers_golden(case):
+    from wildboar_gb300.distance import dtw as D
+
+    a, inp, out = case["args"], case["inputs"], case["outputs"]
+    r, ha, hb, hc = a["r"], inp["a"], inp["b"], inp["c"]
+    np.testing.assert_allclose(D.dtw_distance(ha, hb, r=r), out["dtw"], rtol=RTOL, atol=0)
+    np.testing.assert_allclose(D.ddtw_distance(ha, hc, r=r), out["ddtw"], rtol=RTOL, atol=0)
+    np.testing.assert_allclose(D.wdtw_distance(hc, hb, r=r, g=0.1), out["wdtw"], rtol=RTOL,
+                               atol=0)
+    np.testing.assert_allclose(D.wddtw_distance(ha, hb, r=r, g=0.2), out["wddtw"], rtol=RTOL,
+                               atol=0)
+    lo, up = D.dtw_envelop(ha, r=r)
+    np.testing.assert_array_equal(lo, out["lower"])
+    np.testing.assert_array_equal(up, out["upper"])
+    d1, cb1 = D.dtw_lb_keogh(hb, ha, r=r)
+    d2, cb2 = D.dtw_lb_keogh(hb, lower=lo, upper=up)
+    np.testing.assert_allclose(d1, out["lb"], rtol=RTOL, atol=0)
+    np.testing.assert_allclose(cb1, out["cb"], rtol=RTOL, atol=0)
+    np.testing.assert_allclose(d2, out["lb2"], rtol=RTOL, atol=0)
+    np.testing.assert_allclose(cb2, out["cb2"], rtol=RTOL, atol=0)
+    np.testing.assert_array_equal(D.dtw_mapping(ha, hc, r=r), out["mapping"])
+    wal = D.wdtw_alignment(ha, hc, r=r, g=0.3)
+    np.testing.assert_allclose(np.where(inp["mask"], wal, 0.0), out["walign"], rtol=RTOL,
+                               atol=0)
+
+
+@_cases("alignment")
+def test_dtw_alignment_golden(case):
+    from wildboar_gb300.distance import dtw as D
+
+    inp = case["inputs"]
+    al = D.dtw_alignment(inp["x"], inp["y"], r=case["args"]["r"])
+    np.testing.assert_allclose(np.where(inp["mask"], al, 0.0), case["outputs"]["a"],
+                               rtol=RTOL, atol=0)

@@ -164,6 +164,31 @@ def run_oracle(case):
                 "upper": up}
     if kind == "lb_kim":
         return {"out": O.lb_kim(inp["q"], inp["x"])}
+    if kind == "dtw_helpers":
+        r, ha, hb, hc = a["r"], inp["a"], inp["b"], inp["c"]
+        warp = max(math.floor(ha.shape[0] * r), 1)
+        warp = warp - 1 if warp == ha.shape[0] else warp
+        lo, up = O.dtw_envelope(ha, warp)
+        lo, up = lo[0], up[0]
+        # cumulative_bound at mean 0, std 1 (distance/_elastic.pyx:240-270): a
+        # sequential sum of the excursion terms
+        cb = np.where(hb > up, (hb - up) ** 2, np.where(hb < lo, (hb - lo) ** 2, 0.0))
+        acc = 0.0
+        for v in cb.tolist():
+            acc += v
+        lb = math.sqrt(acc)
+        path = O.dtw_mapping(O.dtw_alignment(ha, hc, r=r))
+        mapping = np.zeros((ha.shape[0], hc.shape[0]), dtype=bool)
+        for i, j in path:
+            mapping[i, j] = True
+        wal = O.dtw_alignment(ha, hc, r=r, weights=O.jeong_weight(35, 0.3))
+        return {"dtw": O.distance_1d(ha, hb, metric="dtw", metric_params={"r": r}),
+                "ddtw": O.distance_1d(ha, hc, metric="ddtw", metric_params={"r": r}),
+                "wdtw": O.distance_1d(hc, hb, metric="wdtw", metric_params={"r": r, "g": 0.1}),
+                "wddtw": O.distance_1d(ha, hb, metric="wddtw",
+                                       metric_params={"r": r, "g": 0.2}),
+                "lower": lo, "upper": up, "lb": lb, "cb": cb, "lb2": lb, "cb2": cb,
+                "mapping": mapping, "walign": np.where(inp["mask"], wal, 0.0)}
     raise AssertionError(kind)
 
 
@@ -171,7 +196,8 @@ ORACLE_KINDS = {"pairwise", "singleton", "paired", "argmin", "subsequence", "ali
                 "paired_subsequence"}
 ORACLE_KINDS |= {"argmin_subsequence", "distance_profile", "subsequence_match",
                  "paired_subsequence_match"}
-ORACLE_KINDS |= {"dtw_average", "kmeans", "knn", "kneighbors", "lb_keogh", "lb_kim"}
+ORACLE_KINDS |= {"dtw_average", "kmeans", "knn", "kneighbors", "lb_keogh", "lb_kim",
+                 "dtw_helpers"}
 CASES = [c for c in _golden.cases() if c["kind"] in ORACLE_KINDS]
 
 

@@ -68,6 +68,7 @@ struct MmAlignJob {
     int32_t *path_lo = nullptr;     // (n_pairs, n)
     int32_t *path_hi = nullptr;
     double *last = nullptr;         // (n_pairs,) final cell, or nullptr
+    double *full = nullptr;         // (n, m) cost matrix of pair q0 (dtw_alignment), or nullptr
 };
 
 __device__ __forceinline__ long long dbits(double v) { return __double_as_longlong(v); }
@@ -136,6 +137,8 @@ __global__ void __launch_bounds__(kMmThreads) mm_align_kernel(const MmAlignJob J
                             }
                         }
                         if (i == n - 1 && j == m - 1) fin = v;
+                        if (J.full && q == J.q0 && i < n && j >= i - mn - J.r + 1 && j < i + mx)
+                            J.full[(int64_t)i * m + j] = v;
                         diag = lf;
                         left[k] = v;
                         up = v;
@@ -326,6 +329,7 @@ __global__ void __launch_bounds__(kMmThreads) mm_align_ad_kernel(const MmAlignJo
                             word |= move_code(bd, bu, bl) << (2 * k);
                         }
                         if (d == D - 1) fin = v;
+                        if (J.full && q == J.q0) J.full[(int64_t)i * m + j] = v;
                     }
                 }
                 P2[k] = P1[k];
@@ -531,8 +535,89 @@ __global__ void ssg_update_kernel(const double *X, const int32_t *lo, const int3
     mean[i] = mv - lr * z;
 }
 
+__global__ void fill_kernel(double *p, int64_t n, double v) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) p[t] = v;
+}
+
 }  // namespace
 }  // namespace wb
+
+extern "C" int wb_dtw_alignment(const double *x, int64_t n, const double *y, int64_t m, double r,
+                                const double *weights, double *out, int32_t on_device,
+                                void *stream) {
+    const cudaStream_t st = (cudaStream_t)stream;
+    if (n < 1 || m < 1 || n > INT32_MAX / 2 || m > INT32_MAX / 2)
+        return fail(WB_EINVAL, "dtw_alignment: invalid sizes");
+    if (!(r >= 0.0 && r <= 1.0)) return fail(WB_EINVAL, "r must be in [0, 1]");
+    if (!x || !y || !out) return fail(WB_EINVAL, "NULL array");
+    const AlignPlan P = plan_alignment((int)n, (int)m, r);
+    const int64_t big = std::max(n, m);
+    const size_t cells = (size_t)n * m;
+    Workspace ws(st);
+    const size_t need = align256(P.pair_words * P.word_bytes) +
+                        align256(P.passes ? (size_t)kMmWarps * m * 8 : 0) +
+                        2 * align256((size_t)n * 4) + align256(8) + align256(4) +
+                        (on_device ? 0 : align256(n * 8) + align256(m * 8) +
+                                             align256(cells * 8) +
+                                             (weights ? align256(big * 8) : 0)) +
+                        4096;
+    WB_TRY(ws.reserve(need));
+    WB_TAKE(dirbuf, char, ws, P.pair_words * P.word_bytes);
+    double *bnd = nullptr;
+    if (P.passes) {
+        bnd = ws.take<double>((size_t)kMmWarps * m);
+        if (!bnd) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    }
+    WB_TAKE(lo, int32_t, ws, n);
+    WB_TAKE(hi, int32_t, ws, n);
+    WB_TAKE(member, int64_t, ws, 1);
+    WB_TAKE(group, int32_t, ws, 1);
+    WB_CUDA(cudaMemsetAsync(member, 0, 8, st));
+    WB_CUDA(cudaMemsetAsync(group, 0, 4, st));
+    const double *dx = x, *dy = y, *dw = weights;
+    double *dout = out;
+    if (!on_device) {
+        WB_TAKE(hx, double, ws, n);
+        WB_TAKE(hy, double, ws, m);
+        WB_TAKE(ho, double, ws, cells);
+        WB_CUDA(cudaMemcpyAsync(hx, x, n * 8, cudaMemcpyHostToDevice, st));
+        WB_CUDA(cudaMemcpyAsync(hy, y, m * 8, cudaMemcpyHostToDevice, st));
+        if (weights) {
+            WB_TAKE(hw, double, ws, big);
+            WB_CUDA(cudaMemcpyAsync(hw, weights, big * 8, cudaMemcpyHostToDevice, st));
+            dw = hw;
+        }
+        dx = hx;
+        dy = hy;
+        dout = ho;
+    }
+    fill_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(
+        dout, (int64_t)cells, HUGE_VAL);
+    WB_LAUNCH_CHECK("fill_kernel");
+    MmAlignJob J;
+    J.x = dy;
+    J.x_stride = m;
+    J.m = (int)m;
+    J.means = dx;
+    J.n = (int)n;
+    J.member = member;
+    J.pair_group = group;
+    J.r = P.warp;
+    J.weights = dw;
+    J.dir = dirbuf;
+    J.dir_pair_words = P.pair_words;
+    J.bnd = bnd;
+    J.path_lo = lo;
+    J.path_hi = hi;
+    J.full = dout;
+    J.q0 = 0;
+    J.q1 = 1;
+    WB_TRY(run_alignment(P, J, 1, st));
+    if (!on_device) WB_CUDA(cudaMemcpyAsync(out, dout, cells * 8, cudaMemcpyDeviceToHost, st));
+    WB_CUDA(cudaStreamSynchronize(st));
+    return WB_OK;
+}
 
 extern "C" int wb_dtw_average_mm_step(const double *x, int64_t x_stride, int64_t n_timestep,
                                       const double *means, int64_t mean_len,

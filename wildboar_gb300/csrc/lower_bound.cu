@@ -133,6 +133,20 @@ __global__ void lb_kim_kernel(const double *y, int64_t ny, const double *x, int6
     out[t] = d;
 }
 
+// _dtw_lb_keogh (distance/_elastic.pyx:1095-1115) of one series: the terms
+// cb[k] and sqrt of their sum in order (one thread: the sum is sequential)
+__global__ void lb_terms_kernel(const double *x, const double *lo, const double *up, int L,
+                                double *cb, double *dist) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    double s = 0.0;
+    for (int k = 0; k < L; k++) {
+        const double d = lb_term(x[k], up[k], lo[k]);
+        cb[k] = d;
+        s = s + d;
+    }
+    dist[0] = sqrt(s);
+}
+
 int dev_in(const double *src, size_t count, int on_device, Workspace &ws, const double **dst) {
     if (on_device) {
         *dst = src;
@@ -274,6 +288,35 @@ extern "C" int wb_lb_kim(const double *y, int64_t ny, const double *x, int64_t n
     lb_kim_kernel<<<(unsigned)((t + 255) / 256), 256, 0, s>>>(dy, ny, dx, nx, L, o);
     WB_LAUNCH_CHECK("lb_kim_kernel");
     if (!on_device) WB_CUDA(cudaMemcpyAsync(out, o, co * 8, cudaMemcpyDeviceToHost, s));
+    WB_CUDA(cudaStreamSynchronize(s));
+    return WB_OK;
+}
+
+extern "C" int wb_lb_keogh_terms(const double *x, const double *lower, const double *upper,
+                                 int64_t n_timestep, double *cb, double *dist,
+                                 int32_t on_device, void *stream) {
+    const cudaStream_t s = (cudaStream_t)stream;
+    if (n_timestep < 1 || n_timestep > INT32_MAX / 4) return fail(WB_EINVAL, "invalid sizes");
+    if (!x || !lower || !upper || !cb || !dist) return fail(WB_EINVAL, "NULL array");
+    const size_t L = (size_t)n_timestep;
+    Workspace ws(s);
+    WB_TRY(ws.reserve((on_device ? 0 : 4 * align256(L * 8) + align256(8)) + 1024));
+    const double *dx, *dl, *du;
+    WB_TRY(dev_in(x, L, on_device, ws, &dx));
+    WB_TRY(dev_in(lower, L, on_device, ws, &dl));
+    WB_TRY(dev_in(upper, L, on_device, ws, &du));
+    double *dcb = cb, *dd = dist;
+    if (!on_device) {
+        dcb = ws.take<double>(L);
+        dd = ws.take<double>(1);
+        if (!dcb || !dd) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    }
+    lb_terms_kernel<<<1, 32, 0, s>>>(dx, dl, du, (int)L, dcb, dd);
+    WB_LAUNCH_CHECK("lb_terms_kernel");
+    if (!on_device) {
+        WB_CUDA(cudaMemcpyAsync(cb, dcb, L * 8, cudaMemcpyDeviceToHost, s));
+        WB_CUDA(cudaMemcpyAsync(dist, dd, 8, cudaMemcpyDeviceToHost, s));
+    }
     WB_CUDA(cudaStreamSynchronize(s));
     return WB_OK;
 }

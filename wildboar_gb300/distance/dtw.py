@@ -25,6 +25,7 @@ import numpy as np
 from .. import _lib
 from ._distance import InvalidParameterError, pairwise_distance
 from ._validation import check_array
+from .lb import dtw_envelope as _envelope_rows
 
 _lib.declare(
     "wb_dtw_average_mm_step",
@@ -38,6 +39,16 @@ _lib.declare(
     [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p,
      ctypes.c_void_p, ctypes.c_void_p],
+)
+_lib.declare(
+    "wb_dtw_alignment",
+    [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_double,
+     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p],
+)
+_lib.declare(
+    "wb_lb_keogh_terms",
+    [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+     ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p],
 )
 _lib.declare(
     "wb_group_mean",
@@ -319,4 +330,148 @@ def dtw_average(X, *, r=1.0, g=None, sample_weight=None, init="random", method="
     return means[0]
 
 
-__all__ = ["dtw_average", "jeong_weight", "check_random_state", "InvalidParameterError"]
+# --------------------------------------------------------------------------
+# single-pair helpers of distance/dtw.py:38-426
+
+
+def _compute_warp_size(x_size, r, *, y_size=0):
+    """distance/dtw.py:38-40."""
+    _check_scalar(r, "r", min_val=0, max_val=1)
+    return max(math.floor(max(x_size, y_size) * r), 1)
+
+
+def _row(x, name):
+    x = check_array(x, allow_3d=False, ensure_2d=False, dtype=float, input_name=name)
+    return np.ascontiguousarray(np.ravel(x), dtype=np.float64)
+
+
+def dtw_distance(x, y, *, r=1.0):
+    """Dynamic time warping distance of two series (distance/dtw.py:43-67)."""
+    return pairwise_distance(_row(x, "x"), _row(y, "y"), metric="dtw", metric_params={"r": r})
+
+
+def ddtw_distance(x, y, *, r=1.0):
+    """Derivative dtw distance (distance/dtw.py:70-94)."""
+    return pairwise_distance(_row(x, "x"), _row(y, "y"), metric="ddtw", metric_params={"r": r})
+
+
+def wdtw_distance(x, y, *, r=1.0, g=0.05):
+    """Weighted dtw distance (distance/dtw.py:97-123)."""
+    return pairwise_distance(_row(x, "x"), _row(y, "y"), metric="wdtw",
+                             metric_params={"r": r, "g": g})
+
+
+def wddtw_distance(x, y, *, r=1.0, g=0.05):
+    """Weighted derivative dtw distance (distance/dtw.py:126-152)."""
+    return pairwise_distance(_row(x, "x"), _row(y, "y"), metric="wddtw",
+                             metric_params={"r": r, "g": g})
+
+
+def dtw_envelop(x, *, r=1.0):
+    """LB_Keogh envelope (lower, upper) of one series (distance/dtw.py:155-184)."""
+    x = _row(x, "x")
+    warp = _compute_warp_size(x.shape[0], r)
+    if warp == x.shape[0]:
+        warp -= 1
+    lo, up = _envelope_rows(x.reshape(1, -1), warp)
+    return lo[0], up[0]
+
+
+def dtw_lb_keogh(x, y=None, *, lower=None, upper=None, r=1.0):
+    """LB_Keogh of x against y's envelope (or a given one): (bound, cb)
+    (distance/dtw.py:187-243)."""
+    x = _row(x, "x")
+    if y is not None:
+        y = _row(y, "y")
+        if y.shape[0] != x.shape[0]:
+            raise ValueError(
+                "x (%d) and y (%d) must have the same number of timesteps"
+                % (x.shape[0], y.shape[0]))
+        lower, upper = dtw_envelop(y, r=r)
+    elif lower is None or upper is None:
+        raise ValueError("both y, lower and upper can't be None")
+    lower = _row(lower, "lower")
+    upper = _row(upper, "upper")
+    if lower.shape[0] != upper.shape[0] or lower.shape[0] != x.shape[0]:
+        raise ValueError(
+            "lower (%d), upper (%d) and x (%d) have the same number of timesteps"
+            % (lower.shape[0], upper.shape[0], x.shape[0]))
+    cb = np.empty(x.shape[0])
+    dist = np.empty(1)
+    st = _lib.lib().wb_lb_keogh_terms(_lib.ptr(x), _lib.ptr(lower), _lib.ptr(upper),
+                                      x.shape[0], _lib.ptr(cb), _lib.ptr(dist), 0, None)
+    _lib.check(st)
+    return float(dist[0]), cb
+
+
+def dtw_alignment(x, y, *, r=1.0, weight=None, out=None):
+    """Cumulative cost matrix of dtw (distance/dtw.py:246-290).  Cells off the
+    band are +inf (the reference leaves them unset)."""
+    x = _row(x, "x")
+    y = _row(y, "y")
+    warp_size = _compute_warp_size(x.shape[0], r, y_size=y.shape[0])
+    if not 0 < warp_size <= max(x.shape[0], y.shape[0]):
+        raise ValueError("invalid r")
+    if weight is not None:
+        weight = _row(weight, "weight")
+        if weight.shape[0] != max(x.shape[0], y.shape[0]):
+            raise ValueError(
+                "weight must have the same size as max(x.size, y.size) %d, got %d"
+                % (max(x.shape[0], y.shape[0]), weight.shape[0]))
+    if out is None:
+        out = np.empty((x.shape[0], y.shape[0]))
+    elif out.shape[0] < x.shape[0] or out.shape[1] < y.shape[0]:
+        raise ValueError("out has wrong shape, got [%d, %d]" % out.shape)
+    res = np.empty((x.shape[0], y.shape[0]))
+    st = _lib.lib().wb_dtw_alignment(_lib.ptr(x), x.shape[0], _lib.ptr(y), y.shape[0],
+                                     float(r), _lib.ptr(weight), _lib.ptr(res), 0, None)
+    _lib.check(st)
+    out[:x.shape[0], :y.shape[0]] = res
+    return out
+
+
+def wdtw_alignment(x, y, *, r=1.0, g=0.5, out=None):
+    """Weighted dtw cost matrix (distance/dtw.py:293-327)."""
+    x = _row(x, "x")
+    y = _row(y, "y")
+    return dtw_alignment(x, y, r=r, weight=jeong_weight(max(x.shape[0], y.shape[0]), g),
+                         out=out)
+
+
+def dtw_mapping(x=None, y=None, *, alignment=None, r=1, return_index=False):
+    """Optimal warping path as a boolean indicator (distance/dtw.py:362-426):
+    from the last cell, the argmin of [diag, up, left], the first minimum
+    winning."""
+    if alignment is None:
+        if x is None or y is None:
+            raise ValueError("if alignment=None, neither x or y can be None")
+        alignment = dtw_alignment(x, y, r=r)
+    else:
+        alignment = np.asarray(alignment, dtype=float)
+        if alignment.ndim != 2:
+            raise ValueError("alignment must be a 2-D array")
+    indicator = np.zeros(alignment.shape, dtype=bool)
+    i = alignment.shape[0] - 1
+    j = alignment.shape[1] - 1
+    while i > 0 or j > 0:
+        indicator[i, j] = True
+        option_diag = alignment[i - 1, j - 1] if i > 0 and j > 0 else np.inf
+        option_up = alignment[i - 1, j] if i > 0 else np.inf
+        option_left = alignment[i, j - 1] if j > 0 else np.inf
+        move = int(np.argmin([option_diag, option_up, option_left]))
+        if move == 0:
+            i -= 1
+            j -= 1
+        elif move == 1:
+            i -= 1
+        else:
+            j -= 1
+    indicator[0, 0] = True
+    if return_index:
+        return indicator, indicator.nonzero()
+    return indicator
+
+
+__all__ = ["dtw_average", "jeong_weight", "check_random_state", "InvalidParameterError",
+           "dtw_distance", "ddtw_distance", "wdtw_distance", "wddtw_distance", "dtw_envelop",
+           "dtw_lb_keogh", "dtw_alignment", "wdtw_alignment", "dtw_mapping"]
