@@ -527,6 +527,51 @@ def bench_ucr(args, dev, flush):
     return res
 
 
+def bench_argmin(args, dev, flush):
+    """argmin_distance (k=5) of 2,000 random-walk queries against 2,000 series of
+    length 512, dtw r=0.1 (the headline data): the recurrence with its abandon
+    keys plus the heap replay.  GCUPS over the algorithmic band cells (the
+    reference's early abandoning skips some of them; the count does not).  CPU:
+    the oracle's argmin (with the reference's early abandoning) on all host
+    threads, on a row sample."""
+    import torch
+
+    from oracle import oracle as O
+    from wildboar_gb300.distance import argmin_distance
+
+    wl = WORKLOAD
+    X, Y = make_data(0, wl["nx"], wl["ny"], wl["L"], seed=11)
+    Xd = torch.as_tensor(X, device=dev)
+    Yd = torch.as_tensor(Y, device=dev)
+    cells = X.shape[0] * Y.shape[0] * band_cells(wl["L"], wl["L"], wl["params"]["r"])
+
+    def call():
+        return argmin_distance(Xd, Yd, k=5, metric="dtw", metric_params=wl["params"],
+                               return_distance=True)
+
+    call()
+    torch.cuda.synchronize()
+    ms = _timed(call, max(1, min(args.steps, 2)), flush)
+    idx, dist = call()
+    oi, od = O.argmin(X[:4], Y, k=5, metric="dtw", metric_params=wl["params"],
+                      n_threads=os.cpu_count() or 1)
+    n_threads = os.cpu_count() or 1
+    rows = max(n_threads, 32)
+    t0 = time.perf_counter()
+    O.argmin(X[:rows], Y, k=5, metric="dtw", metric_params=wl["params"], n_threads=n_threads)
+    cpu_s = time.perf_counter() - t0
+    return {
+        "config": f"{X.shape[0]} queries x {Y.shape[0]} series, L={wl['L']}, dtw r=0.1, k=5",
+        "ms": ms,
+        "gcups_algorithmic": cells / (ms * 1e-3) / 1e9,
+        "indices_exact_on_sample": bool(np.array_equal(idx[:4].cpu().numpy(), oi)),
+        "cpu_oracle": {"gcups_algorithmic": rows * Y.shape[0] *
+                       band_cells(wl["L"], wl["L"], wl["params"]["r"]) / cpu_s / 1e9,
+                       "cores": n_threads, "kind": "port",
+                       "sample": f"{rows} queries x {Y.shape[0]} series"},
+    }
+
+
 def bench_euclid_tc(args, dev, flush):
     """Full-series euclidean 8192 x 8192 at length 1024: tensor-core 3xTF32
     GEMM form against the FP64 drop-in kernel on the same device data."""
@@ -675,6 +720,8 @@ def run_gpu(args):
             forms["barycenter_kmeans"] = bench_barycenter(args, dev, flush)
         if args.only in ("", "ucr"):
             forms["ucr_lower_bounds"] = bench_ucr(args, dev, flush)
+        if args.only in ("", "argmin"):
+            forms["argmin_knn"] = bench_argmin(args, dev, flush)
         if rank == 0:
             print(json.dumps({"forms": forms}), flush=True)
         return
@@ -777,6 +824,7 @@ def run_gpu(args):
         forms["precision_sweep"] = bench_precision(args, dev, flush)
         forms["barycenter_kmeans"] = bench_barycenter(args, dev, flush)
         forms["ucr_lower_bounds"] = bench_ucr(args, dev, flush)
+        forms["argmin_knn"] = bench_argmin(args, dev, flush)
         forms["both_beat_fp64_drop_in"] = bool(
             forms["batched_fp32"]["gcups"] > value and forms["fwd_bwd_fp32"]["gcups"] > value)
     line = {
@@ -829,7 +877,8 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true",
                     help="only the FP32 forms (profiling captures)")
     ap.add_argument("--only", default="", choices=["", "batched", "fwdbwd", "subseq", "euclid",
-                                                     "precision", "barycenter", "ucr"],
+                                                     "precision", "barycenter", "ucr",
+                                                     "argmin"],
                     help="with --skip-fp64: run one form only")
     ap.add_argument("--c6-series", type=int, default=4096)
     ap.add_argument("--c7-series", type=int, default=200,

@@ -259,3 +259,40 @@ def test_native_library_runs():
     before = _lib.launch_count()
     pairwise_distance(np.ones((2, 5)), np.zeros((3, 5)), metric="dtw")
     assert _lib.launch_count() > before
+
+
+ARGMIN_LONG = [("dtw", {"r": 0.1}), ("dtw", {"r": 1.0}), ("wdtw", {"g": 0.1}), ("ddtw", {"r": 0.3}),
+              ("adtw", {"p": 0.5}), ("edr", {"epsilon": 0.5}), ("edr", {}), ("erp", {"g": 0.2}),
+              ("msm", {"c": 0.5}), ("twe", {"penalty": 0.5, "stiffness": 0.01}),
+              ("lcss", {"epsilon": 0.5}), ("adtw", {"p": -0.2})]
+
+
+@pytest.mark.parametrize("metric,params", ARGMIN_LONG,
+                         ids=[f"{m}-{i}" for i, (m, _) in enumerate(ARGMIN_LONG)])
+@pytest.mark.parametrize("k", [1, 3, 10])
+def test_argmin_many_candidates_vs_oracle(metric, params, k):
+    # 300 candidates, a close one late in the scan: the heap replay of the
+    # reference's early abandoning over a long candidate list
+    rng = np.random.default_rng(70 + k)
+    X = _walk(rng, (21, 60))
+    Y = _walk(rng, (300, 60))
+    Y[250] = X[3] + 0.01 * rng.standard_normal(60)  # a close candidate late in the scan
+    idx, dist = argmin_distance(X, Y, k=k, metric=metric, metric_params=params,
+                                return_distance=True)
+    oidx, odist = O.argmin(X, Y, k=k, metric=metric, metric_params=params)
+    np.testing.assert_array_equal(idx, oidx)
+    np.testing.assert_allclose(dist, odist, rtol=RTOL, atol=0)
+
+
+def test_argmin_many_candidates_lower_bound_vs_oracle():
+    rng = np.random.default_rng(4)
+    X = _walk(rng, (13, 64))
+    Y = _walk(rng, (200, 64))
+    full = O.pairwise(X, Y, metric="dtw", metric_params={"r": 0.2})
+    lb = full * rng.uniform(0.2, 1.05, size=full.shape)
+    idx, dist = argmin_distance(X, Y, k=5, metric="dtw", metric_params={"r": 0.2},
+                                lower_bound=lb, return_distance=True)
+    oidx, odist = O.argmin(X, Y, k=5, metric="dtw", metric_params={"r": 0.2},
+                           lower_bound=lb)
+    np.testing.assert_array_equal(idx, oidx)
+    np.testing.assert_allclose(dist, odist, rtol=RTOL, atol=0)
