@@ -243,13 +243,17 @@ def bench_batched(args, dev, flush):
     xs, ys = x[idx].cpu().numpy(), y[idx].cpu().numpy()
     lxs, lys = lx[idx].cpu().numpy(), ly[idx].cpu().numpy()
     err = 0.0
+    cpu_cells = 0
+    t0 = time.perf_counter()
     for t, i in enumerate(idx):
         acc = 0.0
         for k in range(d):
             acc += O.distance_1d(xs[t, k, : lxs[t, k]].astype(np.float64),
                                  ys[t, k, : lys[t, k]].astype(np.float64), metric="dtw",
                                  metric_params={"r": r})
+            cpu_cells += band_cells(int(lxs[t, k]), int(lys[t, k]), r)
         err = max(err, abs(out[i] - acc / d) / (acc / d))
+    cpu_s = time.perf_counter() - t0
     return {
         "gcups": cells / (ms * 1e-3) / 1e9,
         "ms_per_step": ms,
@@ -260,6 +264,9 @@ def bench_batched(args, dev, flush):
         "plan_and_autotune_s": plan_s,
         "max_rel_err_vs_fp64": err,
         "err_sample_pairs": int(len(idx)),
+        "cpu_oracle": {"gcups": cpu_cells / cpu_s / 1e9, "cores": 1, "kind": "port",
+                       "sample": f"the {len(idx)} error-sample pairs x {d} dims, FP64, "
+                                 "one call per pair and dim"},
     }
 
 
@@ -371,12 +378,17 @@ def bench_subsequence(args, dev, flush):
         d, i = call()
         d = d.cpu().numpy()
         i = i.cpu().numpy()
+        t0 = time.perf_counter()
         od, oi = O.subsequence(shp, X[:2], metric=metric, n_threads=os.cpu_count() or 1)
+        cpu_s = time.perf_counter() - t0
         res[metric] = {
             "ms": ms,
             "g_window_elements_per_s": elems / (ms * 1e-3) / 1e9,
             "argmin_exact_on_sample": bool(np.array_equal(i[:2], oi)),
             "max_rel_err_on_sample": float(np.max(np.abs(d[:2] - od) / np.maximum(od, 1e-300))),
+            "cpu_oracle": {"g_window_elements_per_s": 2 * elems / X.shape[0] / cpu_s / 1e9,
+                           "cores": os.cpu_count() or 1, "kind": "port",
+                           "sample": f"all {len(shp)} shapelets x 2 series"},
         }
     return {"config": f"{args.c3_shapelets} shapelets (L~U{{16..128}}, z-normalised "
                       f"random-walk fragments) x {args.c3_series} series, T={T}, float64",
@@ -599,8 +611,19 @@ def bench_euclid_tc(args, dev, flush):
     ny = (Yd * Yd).sum(1, keepdim=True).t()
     norm_err = ((D * D - D64 * D64).abs() / (nx + ny)).max().item()
     flops = 2.0 * n * n * L
+    # CPU: the oracle's euclidean pairwise (the reference's sequential sums) on
+    # all host threads, a row sample
+    from oracle import oracle as O
+
+    rows = max(os.cpu_count() or 1, 16)
+    t0 = time.perf_counter()
+    O.pairwise(X[:rows], Y, metric="euclidean", n_threads=os.cpu_count() or 1)
+    cpu_s = time.perf_counter() - t0
     return {
         "config": f"{n} x {n} series, L={L}, float64 in, float64 out",
+        "cpu_oracle": {"gflops_useful": 2.0 * rows * n * L / cpu_s / 1e9,
+                       "cores": os.cpu_count() or 1, "kind": "port",
+                       "sample": f"{rows} rows x {n} series"},
         "tc_ms": ms_tc,
         "tc_tflops_useful": flops / (ms_tc * 1e-3) / 1e12,
         "tc_tflops_issued_3xtf32": 3 * flops / (ms_tc * 1e-3) / 1e12,
