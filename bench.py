@@ -541,11 +541,14 @@ def bench_ucr(args, dev, flush):
 
 def bench_argmin(args, dev, flush):
     """argmin_distance (k=5) of 2,000 random-walk queries against 2,000 series of
-    length 512, dtw r=0.1 (the headline data): the recurrence with its abandon
-    keys plus the heap replay.  GCUPS over the algorithmic band cells (the
-    reference's early abandoning skips some of them; the count does not).  CPU:
-    the oracle's argmin (with the reference's early abandoning) on all host
-    threads, on a row sample."""
+    length 512, dtw r=0.1 (the headline data).  Default form: candidates in
+    chunks of doubling size, each pair stopped once it crosses the k-th
+    distance of the replayed prefix (the reference's own early abandoning,
+    made safe for out-of-order evaluation), then the heap replay; beside it
+    the all-pairs form (every pair's recurrence with its abandon key).  GCUPS
+    over the algorithmic band cells of all pairs (abandoned cells included in
+    the count).  CPU: the oracle's argmin (with the reference's early
+    abandoning) on all host threads, on a row sample."""
     import torch
 
     from oracle import oracle as O
@@ -561,10 +564,22 @@ def bench_argmin(args, dev, flush):
         return argmin_distance(Xd, Yd, k=5, metric="dtw", metric_params=wl["params"],
                                return_distance=True)
 
-    call()
-    torch.cuda.synchronize()
-    ms = _timed(call, max(1, min(args.steps, 2)), flush)
-    idx, dist = call()
+    prev = os.environ.pop("WB_GPU_ARGMIN", None)
+    try:
+        call()
+        torch.cuda.synchronize()
+        ms = _timed(call, max(1, min(args.steps, 2)), flush)
+        idx, dist = call()
+        os.environ["WB_GPU_ARGMIN"] = "all"
+        call()
+        torch.cuda.synchronize()
+        ms_all = _timed(call, max(1, min(args.steps, 2)), flush)
+        fidx, fdist = call()
+    finally:
+        if prev is None:
+            os.environ.pop("WB_GPU_ARGMIN", None)
+        else:
+            os.environ["WB_GPU_ARGMIN"] = prev
     oi, od = O.argmin(X[:4], Y, k=5, metric="dtw", metric_params=wl["params"],
                       n_threads=os.cpu_count() or 1)
     n_threads = os.cpu_count() or 1
@@ -576,7 +591,11 @@ def bench_argmin(args, dev, flush):
         "config": f"{X.shape[0]} queries x {Y.shape[0]} series, L={wl['L']}, dtw r=0.1, k=5",
         "ms": ms,
         "gcups_algorithmic": cells / (ms * 1e-3) / 1e9,
+        "all_pairs_ms": ms_all,
+        "all_pairs_gcups": cells / (ms_all * 1e-3) / 1e9,
         "indices_exact_on_sample": bool(np.array_equal(idx[:4].cpu().numpy(), oi)),
+        "forms_bit_identical": bool(torch.equal(idx, fidx) and torch.equal(
+            dist.view(torch.int64), fdist.view(torch.int64))),
         "cpu_oracle": {"gcups_algorithmic": rows * Y.shape[0] *
                        band_cells(wl["L"], wl["L"], wl["params"]["r"]) / cpu_s / 1e9,
                        "cores": n_threads, "kind": "port",

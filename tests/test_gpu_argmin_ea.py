@@ -1,0 +1,123 @@
+"""GPU parity of argmin_distance's early-abandoned candidate chunks.
+
+For dtw, wdtw, ddtw, wddtw and adtw (penalty >= 0) with a narrow band the
+library walks the candidates in chunks of doubling size and stops a pair as
+soon as its running largest row minimum exceeds the k-th distance of the
+replayed prefix.  ``WB_GPU_ARGMIN=<c>`` sets the first chunk (small chunks
+exercise many bound updates on small inputs), ``WB_GPU_ARGMIN=all`` turns the
+chunks off.  Every form must give the oracle's indices (heap order included)
+and distances, and the two GPU forms must agree bit for bit.
+"""
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():  # pragma: no cover
+    pytest.skip("needs a CUDA device", allow_module_level=True)
+
+from oracle import oracle as O  # noqa: E402
+from wildboar_gb300.distance import argmin_distance  # noqa: E402
+
+RTOL = 1e-12
+
+EA_METRICS = [("dtw", {"r": 0.1}), ("dtw", {"r": 0.3}), ("wdtw", {"g": 0.1, "r": 0.2}),
+              ("ddtw", {"r": 0.2}), ("wddtw", {"g": 0.05, "r": 0.25}),
+              ("adtw", {"p": 0.5, "r": 0.2}), ("adtw", {"p": 0.0, "r": 0.1})]
+
+
+def _walk(rng, shape):
+    return np.cumsum(rng.standard_normal(shape), axis=-1)
+
+
+def _both(monkeypatch, first_chunk, X, Y, **kw):
+    monkeypatch.setenv("WB_GPU_ARGMIN", str(first_chunk))
+    ea = argmin_distance(X, Y, return_distance=True, **kw)
+    monkeypatch.setenv("WB_GPU_ARGMIN", "all")
+    full = argmin_distance(X, Y, return_distance=True, **kw)
+    monkeypatch.delenv("WB_GPU_ARGMIN")
+    return ea, full
+
+
+@pytest.mark.parametrize("metric,params", EA_METRICS,
+                         ids=[f"{m}-{i}" for i, (m, _) in enumerate(EA_METRICS)])
+@pytest.mark.parametrize("k,first", [(1, 1), (3, 5), (10, 16)])
+def test_argmin_ea_vs_oracle(monkeypatch, metric, params, k, first):
+    rng = np.random.default_rng(100 + k)
+    X = _walk(rng, (19, 60))
+    Y = _walk(rng, (260, 60))
+    Y[200] = X[4] + 0.01 * rng.standard_normal(60)  # a close candidate late in the scan
+    Y[230] = Y[200]                                 # and a tie after it
+    (idx, dist), (fidx, fdist) = _both(monkeypatch, first, X, Y, k=k, metric=metric,
+                                       metric_params=params)
+    oidx, odist = O.argmin(X, Y, k=k, metric=metric, metric_params=params)
+    np.testing.assert_array_equal(idx, oidx)
+    np.testing.assert_allclose(dist, odist, rtol=RTOL, atol=0)
+    np.testing.assert_array_equal(idx, fidx)
+    assert np.array_equal(dist.view(np.uint64), fdist.view(np.uint64))
+
+
+@pytest.mark.parametrize("metric,params", [("dtw", {"r": 0.15}), ("wdtw", {"g": 0.2}),
+                                           ("adtw", {"p": 1.0, "r": 0.1})])
+def test_argmin_ea_unequal_lengths_vs_oracle(monkeypatch, metric, params):
+    rng = np.random.default_rng(9)
+    X = _walk(rng, (11, 48))
+    Y = _walk(rng, (150, 71))
+    (idx, dist), (fidx, fdist) = _both(monkeypatch, 3, X, Y, k=4, metric=metric,
+                                       metric_params=params)
+    oidx, odist = O.argmin(X, Y, k=4, metric=metric, metric_params=params)
+    np.testing.assert_array_equal(idx, oidx)
+    np.testing.assert_allclose(dist, odist, rtol=RTOL, atol=0)
+    np.testing.assert_array_equal(idx, fidx)
+    assert np.array_equal(dist.view(np.uint64), fdist.view(np.uint64))
+
+
+def test_argmin_ea_lower_bound_vs_oracle(monkeypatch):
+    rng = np.random.default_rng(12)
+    X = _walk(rng, (13, 64))
+    Y = _walk(rng, (220, 64))
+    full = O.pairwise(X, Y, metric="dtw", metric_params={"r": 0.2})
+    lb = full * rng.uniform(0.2, 1.05, size=full.shape)
+    (idx, dist), (fidx, fdist) = _both(monkeypatch, 4, X, Y, k=5, metric="dtw",
+                                       metric_params={"r": 0.2}, lower_bound=lb)
+    oidx, odist = O.argmin(X, Y, k=5, metric="dtw", metric_params={"r": 0.2},
+                           lower_bound=lb)
+    np.testing.assert_array_equal(idx, oidx)
+    np.testing.assert_allclose(dist, odist, rtol=RTOL, atol=0)
+    np.testing.assert_array_equal(idx, fidx)
+    assert np.array_equal(dist.view(np.uint64), fdist.view(np.uint64))
+
+
+def test_argmin_ea_k_above_first_chunks(monkeypatch):
+    # k larger than the first chunks: the bound stays infinite until the
+    # heap is full
+    rng = np.random.default_rng(5)
+    X = _walk(rng, (7, 40))
+    Y = _walk(rng, (90, 40))
+    (idx, dist), _ = _both(monkeypatch, 2, X, Y, k=40, metric="dtw", metric_params={"r": 0.2})
+    oidx, odist = O.argmin(X, Y, k=40, metric="dtw", metric_params={"r": 0.2})
+    np.testing.assert_array_equal(idx, oidx)
+    np.testing.assert_allclose(dist, odist, rtol=RTOL, atol=0)
+
+
+def test_argmin_ea_default_schedule_bitwise(monkeypatch):
+    # the default schedule at a size where it chunks (2 000 queries), against
+    # the all-pairs form, plus a row sample against the oracle
+    rng = np.random.default_rng(21)
+    X = _walk(rng, (2000, 128))
+    Y = _walk(rng, (1200, 128))
+    monkeypatch.delenv("WB_GPU_ARGMIN", raising=False)
+    idx, dist = argmin_distance(X, Y, k=5, metric="dtw", metric_params={"r": 0.1},
+                                return_distance=True)
+    monkeypatch.setenv("WB_GPU_ARGMIN", "all")
+    fidx, fdist = argmin_distance(X, Y, k=5, metric="dtw", metric_params={"r": 0.1},
+                                  return_distance=True)
+    np.testing.assert_array_equal(idx, fidx)
+    assert np.array_equal(dist.view(np.uint64), fdist.view(np.uint64))
+    rows = [0, 777, 1999]
+    oidx, odist = O.argmin(X[rows], Y, k=5, metric="dtw", metric_params={"r": 0.1})
+    np.testing.assert_array_equal(idx[rows], oidx)
+    np.testing.assert_allclose(dist[rows], odist, rtol=RTOL, atol=0)

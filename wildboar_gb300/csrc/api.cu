@@ -622,12 +622,34 @@ extern "C" int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_
         probe.rows.len -= 2;
         probe.cols.len -= 2;
     }
+    // early-abandoned chunks of candidates (argmin_ea.cu) where the metric
+    // and band allow them: chunk sizes double from a first chunk that gives
+    // every lane a few pairs, so the k-th distances tighten early
+    std::vector<int64_t> chunks;
+    {
+        ElasticJob ea = probe;
+        double dummy_key = 0.0;
+        ea.key = metric == WB_EUCLIDEAN ? nullptr : &dummy_key;
+        ea.all_zero = derivative(metric) && std::min(xl, yl) < 3;
+        if (!argmin_ea_disabled() && argmin_ea_supported(ea)) {
+            int64_t c = std::max<int64_t>(64, (4 * argmin_ea_lanes(ea) + x->n - 1) / x->n);
+            if (argmin_ea_first_chunk() > 0) c = argmin_ea_first_chunk();
+            for (int64_t a = 0; a < y->n; c *= 2) {
+                chunks.push_back(a);
+                a = std::min<int64_t>(y->n, a + c);
+            }
+            chunks.push_back(y->n);
+            if (chunks.size() < 3) chunks.clear();  // one chunk: nothing to abandon
+        }
+    }
+    const bool use_ea = !chunks.empty();
     size_t need = stage_bytes(x) + stage_bytes(y) +
                   table_bytes(metric, params, probeR, probeC, x->n, y->n, xl, yl) +
-                  elastic_workspace_bytes(probe) + 2 * align256(pairs * 8) +
+                  (use_ea ? 0 : elastic_workspace_bytes(probe)) + 2 * align256(pairs * 8) +
                   2 * align256((size_t)x->n * k * 8) +
                   (lower_bound && !out_on_device ? align256(pairs * 8) : 0) +
-                  (out_on_device ? 0 : 2 * align256((size_t)x->n * k * 8));
+                  (out_on_device ? 0 : 2 * align256((size_t)x->n * k * 8)) +
+                  (use_ea ? 2 * align256((size_t)x->n * 8) + align256(chunks.size() * 8) : 0);
     WB_TRY(ws.reserve(need));
     WB_TRY(stage(x, dim, ws, J.rows));
     WB_TRY(stage(y, dim, ws, J.cols));
@@ -640,7 +662,7 @@ extern "C" int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_
     J.mode = PM_ALL;
     int never_push = 0;
     if (derivative(metric) && std::min(xl, yl) < 3) never_push = 1;
-    if (!never_push) WB_TRY(launch_elastic(J, ws, nullptr));
+    if (!never_push && !use_ea) WB_TRY(launch_elastic(J, ws, nullptr));
 
     const double *lb = lower_bound;
     if (lower_bound && !out_on_device) {
@@ -665,7 +687,29 @@ extern "C" int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_
     A.out_dist = out_on_device ? distances : ws.take<double>((size_t)x->n * k);
     if (!A.heap_idx || !A.heap_val || !A.out_idx || !A.out_dist)
         return fail(WB_ENOMEM, "workspace reservation exceeded");
-    WB_TRY(launch_argmin_replay(A, s));
+    if (use_ea) {
+        A.state_n = ws.take<int64_t>(x->n);
+        A.state_dist = ws.take<double>(x->n);
+        auto *counters = ws.take<unsigned long long>(chunks.size());
+        if (!A.state_n || !A.state_dist || !counters)
+            return fail(WB_ENOMEM, "workspace reservation exceeded");
+        WB_CUDA(cudaMemsetAsync(counters, 0, chunks.size() * 8, s));
+        WB_TRY(launch_fill(A.state_dist, HUGE_VAL, x->n, s));
+        timer_begin("argmin_ea_kernel", s);
+        for (size_t c = 0; c + 1 < chunks.size(); c++) {
+            const int64_t a = chunks[c], b = chunks[c + 1];
+            WB_TRY(launch_argmin_ea(J, metric, xl, yl, a, b - a, y->n, A.state_dist, lb,
+                                    counters + c, s));
+            A.j0 = a;
+            A.j1 = b;
+            A.resume = c > 0;
+            A.finish = c + 2 == chunks.size();
+            WB_TRY(launch_argmin_replay(A, s));
+        }
+        timer_end(s);
+    } else {
+        WB_TRY(launch_argmin_replay(A, s));
+    }
     if (!out_on_device) {
         WB_CUDA(cudaMemcpyAsync(indices, A.out_idx, (size_t)x->n * k * 8,
                                 cudaMemcpyDeviceToHost, s));

@@ -25,8 +25,13 @@ __global__ void argmin_replay_kernel(const ArgminJob J) {
         const double *lb = J.lower_bound ? J.lower_bound + i * J.ny : nullptr;
         double distance = INF;
         int64_t n = 0;
+        if (J.resume) {
+            n = J.state_n[i];
+            distance = J.state_dist[i];
+        }
+        const int64_t j1 = J.j1 < 0 ? J.ny : J.j1;
         if (!J.never_push) {
-            for (int64_t j = 0; j < J.ny; j++) {
+            for (int64_t j = J.j0; j < j1; j++) {
                 if (lb && lb[j] >= distance) continue;
                 if (krow) {
                     double thr = abandon_threshold(J.metric, distance, J.xl, J.yl);
@@ -39,6 +44,11 @@ __global__ void argmin_replay_kernel(const ArgminJob J) {
                 }
             }
         }
+        if (J.state_n) {
+            J.state_n[i] = n;
+            J.state_dist[i] = distance;
+        }
+        if (!J.finish) continue;
         for (int64_t t = 0; t < J.k; t++) {
             J.out_idx[i * J.k + t] = t < n ? hi[t] : 0;
             J.out_dist[i * J.k + t] = t < n ? hv[t] : 0.0;

@@ -144,6 +144,11 @@ int wb_argmin_subsequence_impl(const double *s, const int64_t *s_len, int64_t s_
 // (compensated) (elastic_strip.cu)
 bool strip_supported(const ElasticJob &J);
 bool strip_forced();
+// WB_GPU_ARGMIN=all: argmin evaluates every candidate pair in full (no
+// early-abandoned chunks); WB_GPU_ARGMIN=<c>: first chunk of c candidates
+// (default: enough pairs for every lane).  All forms give the same results.
+bool argmin_ea_disabled();
+int64_t argmin_ea_first_chunk();
 size_t strip_workspace_bytes(const ElasticJob &J, bool fp32);
 int launch_strip(const ElasticJob &J, Workspace &ws, bool fp32);
 
@@ -173,7 +178,25 @@ struct ArgminJob {
     double *out_dist = nullptr;
     int64_t *heap_idx = nullptr;    // (nx, k) scratch
     double *heap_val = nullptr;     // (nx, k) scratch
+    // replay of candidates [j0, j1) only (j1 < 0: all), resuming the heaps
+    // and k-th distances left by the previous range when `resume` is set;
+    // outputs written when `finish` is set
+    int64_t j0 = 0, j1 = -1;
+    int resume = 0, finish = 1;
+    int64_t *state_n = nullptr;     // (nx,) heap sizes between ranges
+    double *state_dist = nullptr;   // (nx,) k-th distance (inf until the heap is full)
 };
 int launch_argmin_replay(const ArgminJob &job, cudaStream_t s);
+
+// early-abandoned candidate chunks (argmin_ea.cu): dtw / wdtw / ddtw / wddtw
+// / adtw with a non-negative penalty and a band whose ring fits in shared
+// memory.  Writes out / key of pairs (i, j in [j0, j0 + nc)) with row stride
+// ny; an abandoned pair gets distance inf and its partial key, which exceeds
+// the threshold the replay compares it with.
+bool argmin_ea_supported(const ElasticJob &job);
+int64_t argmin_ea_lanes(const ElasticJob &job);
+int launch_argmin_ea(const ElasticJob &job, int metric, int xl, int yl, int64_t j0, int64_t nc,
+                     int64_t ny, const double *cur_dist, const double *lower_bound,
+                     unsigned long long *counter, cudaStream_t s);
 
 }  // namespace wb
