@@ -5,7 +5,8 @@ library walks the candidates in chunks of doubling size and stops a pair as
 soon as its running largest row minimum exceeds the k-th distance of the
 replayed prefix.  ``WB_GPU_ARGMIN=<c>`` sets the first chunk (small chunks
 exercise many bound updates on small inputs), ``WB_GPU_ARGMIN=all`` turns the
-chunks off.  Every form must give the oracle's indices (heap order included)
+chunks off, ``WB_GPU_ARGMIN_FORM=strip`` runs the register-strip form (wide
+bands) for any band.  Every form must give the oracle's indices (heap order included)
 and distances, and the two GPU forms must agree bit for bit.
 """
 
@@ -60,9 +61,40 @@ def test_argmin_ea_vs_oracle(monkeypatch, metric, params, k, first):
     assert np.array_equal(dist.view(np.uint64), fdist.view(np.uint64))
 
 
+@pytest.mark.parametrize("metric,params", EA_METRICS,
+                         ids=[f"{m}-{i}" for i, (m, _) in enumerate(EA_METRICS)])
+@pytest.mark.parametrize("k,first", [(1, 3), (6, 9)])
+def test_argmin_ea_strip_form_vs_oracle(monkeypatch, metric, params, k, first):
+    monkeypatch.setenv("WB_GPU_ARGMIN_FORM", "strip")
+    test_argmin_ea_vs_oracle(monkeypatch, metric, params, k, first)
+
+
+@pytest.mark.parametrize("metric,params", [("dtw", {"r": 1.0}), ("dtw", {"r": 0.5}),
+                                           ("wdtw", {"g": 0.05}), ("wddtw", {"g": 0.1}),
+                                           ("adtw", {"p": 0.25, "r": 1.0}),
+                                           ("ddtw", {"r": 0.7})])
+def test_argmin_ea_wide_band_vs_oracle(monkeypatch, metric, params):
+    # series long enough that the ring leaves fewer than two blocks per SM:
+    # the strip form by default
+    rng = np.random.default_rng(31)
+    X = _walk(rng, (9, 170))
+    Y = _walk(rng, (120, 170))
+    Y[100] = X[2] + 0.01 * rng.standard_normal(170)
+    (idx, dist), (fidx, fdist) = _both(monkeypatch, 4, X, Y, k=3, metric=metric,
+                                       metric_params=params)
+    oidx, odist = O.argmin(X, Y, k=3, metric=metric, metric_params=params)
+    np.testing.assert_array_equal(idx, oidx)
+    np.testing.assert_allclose(dist, odist, rtol=RTOL, atol=0)
+    np.testing.assert_array_equal(idx, fidx)
+    assert np.array_equal(dist.view(np.uint64), fdist.view(np.uint64))
+
+
+@pytest.mark.parametrize("form", ["default", "strip"])
 @pytest.mark.parametrize("metric,params", [("dtw", {"r": 0.15}), ("wdtw", {"g": 0.2}),
                                            ("adtw", {"p": 1.0, "r": 0.1})])
-def test_argmin_ea_unequal_lengths_vs_oracle(monkeypatch, metric, params):
+def test_argmin_ea_unequal_lengths_vs_oracle(monkeypatch, form, metric, params):
+    if form == "strip":
+        monkeypatch.setenv("WB_GPU_ARGMIN_FORM", "strip")
     rng = np.random.default_rng(9)
     X = _walk(rng, (11, 48))
     Y = _walk(rng, (150, 71))
@@ -75,7 +107,10 @@ def test_argmin_ea_unequal_lengths_vs_oracle(monkeypatch, metric, params):
     assert np.array_equal(dist.view(np.uint64), fdist.view(np.uint64))
 
 
-def test_argmin_ea_lower_bound_vs_oracle(monkeypatch):
+@pytest.mark.parametrize("form", ["default", "strip"])
+def test_argmin_ea_lower_bound_vs_oracle(monkeypatch, form):
+    if form == "strip":
+        monkeypatch.setenv("WB_GPU_ARGMIN_FORM", "strip")
     rng = np.random.default_rng(12)
     X = _walk(rng, (13, 64))
     Y = _walk(rng, (220, 64))
@@ -121,3 +156,22 @@ def test_argmin_ea_default_schedule_bitwise(monkeypatch):
     oidx, odist = O.argmin(X[rows], Y, k=5, metric="dtw", metric_params={"r": 0.1})
     np.testing.assert_array_equal(idx[rows], oidx)
     np.testing.assert_allclose(dist[rows], odist, rtol=RTOL, atol=0)
+
+
+@pytest.mark.parametrize("metric,params", [("dtw", {"r": 1.0}), ("lcss", {"epsilon": 0.5}),
+                                           ("msm", {"c": 0.5}), ("wdtw", {"g": 0.05})])
+def test_argmin_long_series_wide_band_vs_oracle(monkeypatch, metric, params):
+    # L = 512 with a full band: the all-pairs form runs the ring kernel with a
+    # global ring (its workspace is sized for the keyed kernel), the chunked
+    # form the strip kernel
+    rng = np.random.default_rng(41)
+    X = _walk(rng, (5, 512))
+    Y = _walk(rng, (40, 512))
+    Y[33] = X[1] + 0.01 * rng.standard_normal(512)
+    (idx, dist), (fidx, fdist) = _both(monkeypatch, 2, X, Y, k=3, metric=metric,
+                                       metric_params=params)
+    oidx, odist = O.argmin(X, Y, k=3, metric=metric, metric_params=params)
+    np.testing.assert_array_equal(idx, oidx)
+    np.testing.assert_allclose(dist, odist, rtol=RTOL, atol=0)
+    np.testing.assert_array_equal(idx, fidx)
+    assert np.array_equal(dist.view(np.uint64), fdist.view(np.uint64))

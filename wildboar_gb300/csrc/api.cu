@@ -618,6 +618,10 @@ extern "C" int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_
     probe.rows = probeR;
     probe.cols = probeC;
     probe.mode = PM_ALL;
+    // the recurrence also writes abandon keys: the kernel choice (and so its
+    // workspace) depends on it
+    double dummy_key = 0.0;
+    probe.key = metric == WB_EUCLIDEAN ? nullptr : &dummy_key;
     if (derivative(metric) && std::min(xl, yl) >= 3) {
         probe.rows.len -= 2;
         probe.cols.len -= 2;
@@ -626,13 +630,15 @@ extern "C" int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_
     // and band allow them: chunk sizes double from a first chunk that gives
     // every lane a few pairs, so the k-th distances tighten early
     std::vector<int64_t> chunks;
+    size_t ea_ring_bytes = 0;
     {
         ElasticJob ea = probe;
-        double dummy_key = 0.0;
-        ea.key = metric == WB_EUCLIDEAN ? nullptr : &dummy_key;
         ea.all_zero = derivative(metric) && std::min(xl, yl) < 3;
         if (!argmin_ea_disabled() && argmin_ea_supported(ea)) {
-            int64_t c = std::max<int64_t>(64, (4 * argmin_ea_lanes(ea) + x->n - 1) / x->n);
+            ea_ring_bytes = argmin_ea_ring_bytes(ea);
+            // (rounded down: the first chunk abandons nothing, so its pairs
+            // take equally long and should fill whole rounds of lanes)
+            int64_t c = std::max<int64_t>(64, 4 * argmin_ea_lanes(ea) / x->n);
             if (argmin_ea_first_chunk() > 0) c = argmin_ea_first_chunk();
             for (int64_t a = 0; a < y->n; c *= 2) {
                 chunks.push_back(a);
@@ -649,7 +655,9 @@ extern "C" int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_
                   2 * align256((size_t)x->n * k * 8) +
                   (lower_bound && !out_on_device ? align256(pairs * 8) : 0) +
                   (out_on_device ? 0 : 2 * align256((size_t)x->n * k * 8)) +
-                  (use_ea ? 2 * align256((size_t)x->n * 8) + align256(chunks.size() * 8) : 0);
+                  (use_ea ? 2 * align256((size_t)x->n * 8) + align256(chunks.size() * 8) +
+                                ea_ring_bytes
+                          : 0);
     WB_TRY(ws.reserve(need));
     WB_TRY(stage(x, dim, ws, J.rows));
     WB_TRY(stage(y, dim, ws, J.cols));
@@ -691,7 +699,8 @@ extern "C" int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_
         A.state_n = ws.take<int64_t>(x->n);
         A.state_dist = ws.take<double>(x->n);
         auto *counters = ws.take<unsigned long long>(chunks.size());
-        if (!A.state_n || !A.state_dist || !counters)
+        double *ea_ring = ea_ring_bytes ? ws.take<double>(ea_ring_bytes / 8) : nullptr;
+        if (!A.state_n || !A.state_dist || !counters || (ea_ring_bytes && !ea_ring))
             return fail(WB_ENOMEM, "workspace reservation exceeded");
         WB_CUDA(cudaMemsetAsync(counters, 0, chunks.size() * 8, s));
         WB_TRY(launch_fill(A.state_dist, HUGE_VAL, x->n, s));
@@ -699,7 +708,7 @@ extern "C" int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_
         for (size_t c = 0; c + 1 < chunks.size(); c++) {
             const int64_t a = chunks[c], b = chunks[c + 1];
             WB_TRY(launch_argmin_ea(J, metric, xl, yl, a, b - a, y->n, A.state_dist, lb,
-                                    counters + c, s));
+                                    counters + c, ea_ring, s));
             A.j0 = a;
             A.j1 = b;
             A.resume = c > 0;

@@ -146,7 +146,8 @@ bool strip_supported(const ElasticJob &J);
 bool strip_forced();
 // WB_GPU_ARGMIN=all: argmin evaluates every candidate pair in full (no
 // early-abandoned chunks); WB_GPU_ARGMIN=<c>: first chunk of c candidates
-// (default: enough pairs for every lane).  All forms give the same results.
+// (default: enough pairs for every lane); WB_GPU_ARGMIN_FORM=strip: the
+// strip form of the chunks for any band.  All forms give the same results.
 bool argmin_ea_disabled();
 int64_t argmin_ea_first_chunk();
 size_t strip_workspace_bytes(const ElasticJob &J, bool fp32);
@@ -189,14 +190,15 @@ struct ArgminJob {
 int launch_argmin_replay(const ArgminJob &job, cudaStream_t s);
 
 // early-abandoned candidate chunks (argmin_ea.cu): dtw / wdtw / ddtw / wddtw
-// / adtw with a non-negative penalty and a band whose ring fits in shared
-// memory.  Writes out / key of pairs (i, j in [j0, j0 + nc)) with row stride
-// ny; an abandoned pair gets distance inf and its partial key, which exceeds
-// the threshold the replay compares it with.
+// / adtw with a non-negative penalty.  Writes out / key of pairs (i, j in
+// [j0, j0 + nc)) with row stride ny; an abandoned pair gets distance inf and
+// its partial key, which exceeds the threshold the replay compares it with.
+// Wide bands need a device ring of argmin_ea_ring_bytes (0 for narrow ones).
 bool argmin_ea_supported(const ElasticJob &job);
 int64_t argmin_ea_lanes(const ElasticJob &job);
+size_t argmin_ea_ring_bytes(const ElasticJob &job);
 int launch_argmin_ea(const ElasticJob &job, int metric, int xl, int yl, int64_t j0, int64_t nc,
                      int64_t ny, const double *cur_dist, const double *lower_bound,
-                     unsigned long long *counter, cudaStream_t s);
+                     unsigned long long *counter, double *ring, cudaStream_t s);
 
 }  // namespace wb
