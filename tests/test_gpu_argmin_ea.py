@@ -175,3 +175,52 @@ def test_argmin_long_series_wide_band_vs_oracle(monkeypatch, metric, params):
     np.testing.assert_allclose(dist, odist, rtol=RTOL, atol=0)
     np.testing.assert_array_equal(idx, fidx)
     assert np.array_equal(dist.view(np.uint64), fdist.view(np.uint64))
+
+
+STRIP_EA_METRICS = [("edr", {"epsilon": 0.5}), ("edr", {}), ("edr", {"epsilon": 0.3, "r": 0.2}),
+                    ("erp", {"g": 0.2}), ("erp", {"g": 0.0, "r": 0.3}), ("msm", {"c": 0.5}),
+                    ("msm", {"c": 1.0, "r": 0.2}), ("twe", {"penalty": 0.5, "stiffness": 0.01}),
+                    ("twe", {"penalty": 1.0, "stiffness": 0.001, "r": 0.25})]
+
+
+@pytest.mark.parametrize("metric,params", STRIP_EA_METRICS,
+                         ids=[f"{m}-{i}" for i, (m, _) in enumerate(STRIP_EA_METRICS)])
+@pytest.mark.parametrize("k,first", [(1, 2), (4, 7)])
+def test_argmin_strip_ea_vs_oracle(monkeypatch, metric, params, k, first):
+    # edr / erp / msm / twe: the generic strip form with chunks and bounds
+    test_argmin_ea_vs_oracle(monkeypatch, metric, params, k, first)
+
+
+@pytest.mark.parametrize("metric,params", [("edr", {}), ("erp", {"g": 0.1}),
+                                           ("msm", {"c": 0.7}),
+                                           ("twe", {"penalty": 0.3, "stiffness": 0.05})])
+def test_argmin_strip_ea_unequal_lengths_vs_oracle(monkeypatch, metric, params):
+    rng = np.random.default_rng(19)
+    X = _walk(rng, (8, 52))
+    Y = _walk(rng, (110, 37))
+    (idx, dist), (fidx, fdist) = _both(monkeypatch, 3, X, Y, k=4, metric=metric,
+                                       metric_params=params)
+    oidx, odist = O.argmin(X, Y, k=4, metric=metric, metric_params=params)
+    np.testing.assert_array_equal(idx, oidx)
+    np.testing.assert_allclose(dist, odist, rtol=RTOL, atol=0)
+    np.testing.assert_array_equal(idx, fidx)
+    assert np.array_equal(dist.view(np.uint64), fdist.view(np.uint64))
+
+
+@pytest.mark.parametrize("metric,params", [("lcss", {"epsilon": 0.5}),
+                                           ("wlcss", {"epsilon": 0.4, "g": 0.1}),
+                                           ("adtw", {"p": -0.2, "r": 1.0})])
+def test_argmin_keyed_strip_sweep_vs_oracle(monkeypatch, metric, params):
+    # lcss / wlcss / negative-penalty adtw with a band too wide for a shared
+    # ring: one chunk through the strip sweep with keys, no bound
+    rng = np.random.default_rng(23)
+    X = _walk(rng, (6, 240))
+    Y = _walk(rng, (45, 240))
+    Y[30] = X[2] + 0.01 * rng.standard_normal(240)
+    (idx, dist), (fidx, fdist) = _both(monkeypatch, 5, X, Y, k=3, metric=metric,
+                                       metric_params=params)
+    oidx, odist = O.argmin(X, Y, k=3, metric=metric, metric_params=params)
+    np.testing.assert_array_equal(idx, oidx)
+    np.testing.assert_allclose(dist, odist, rtol=RTOL, atol=0)
+    np.testing.assert_array_equal(idx, fidx)
+    assert np.array_equal(dist.view(np.uint64), fdist.view(np.uint64))

@@ -640,12 +640,12 @@ extern "C" int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_
             // take equally long and should fill whole rounds of lanes)
             int64_t c = std::max<int64_t>(64, 4 * argmin_ea_lanes(ea) / x->n);
             if (argmin_ea_first_chunk() > 0) c = argmin_ea_first_chunk();
+            if (!argmin_ea_chunked(ea)) c = y->n;  // one chunk without a bound
             for (int64_t a = 0; a < y->n; c *= 2) {
                 chunks.push_back(a);
                 a = std::min<int64_t>(y->n, a + c);
             }
             chunks.push_back(y->n);
-            if (chunks.size() < 3) chunks.clear();  // one chunk: nothing to abandon
         }
     }
     const bool use_ea = !chunks.empty();

@@ -41,17 +41,6 @@ namespace wb {
 
 constexpr int kEaThreads = 128;
 
-struct EaChunk {
-    int64_t j0 = 0, nc = 0;                 // candidates [j0, j0 + nc)
-    int64_t nq = 0;                         // queries
-    int64_t ny = 0;                         // row stride of out / key / lower_bound
-    const double *cur_dist = nullptr;       // k-th distance after the replayed prefix
-    const double *lower_bound = nullptr;    // (nq, ny) or null
-    unsigned long long *counter = nullptr;  // next pair of the chunk
-    int metric = WB_DTW;
-    int xl = 0, yl = 0;
-};
-
 // KIND: K_DTW (dtw, ddtw on slopes), K_WDTW (wdtw, wddtw), K_ADTW (penalty >= 0)
 template <int KIND>
 __global__ void __launch_bounds__(kEaThreads)
@@ -258,9 +247,10 @@ constexpr int kEaStripRows = 16;
 // Plan of the early-abandoning kernels: the shared-memory ring form when at
 // least two blocks of rings fit per SM, else the strip form.
 struct EaPlan {
-    int form = 0;  // 0: not applicable, 1: shared-memory ring, 2: strips
+    int form = 0;  // 0: not applicable, 1: shared-memory ring, 2: dtw strips, 3: generic strips
     int P = 0;
     int blocks_per_sm = 0;
+    bool chunked = false;  // the metric's threshold grows with the k-th distance
 };
 
 template <int KIND>
@@ -273,7 +263,6 @@ static int strip_blocks_per_sm() {
 
 static EaPlan ea_plan(const ElasticJob &J) {
     EaPlan pl;
-    if (J.kind != K_DTW && J.kind != K_WDTW && J.kind != K_ADTW) return pl;
     if (J.all_zero || J.mode != PM_ALL || !J.key) return pl;
     if (J.rows.len < 1 || J.cols.len < 1) return pl;
     const DeviceInfo &dev = device_info();
@@ -282,6 +271,17 @@ static EaPlan ea_plan(const ElasticJob &J) {
     int b = 0;
     if (per_block <= (size_t)dev.max_smem_optin && per_block + 2048 <= (size_t)dev.smem_per_sm)
         b = (int)(((size_t)dev.smem_per_sm - 1024) / (per_block + 1024));
+    if (J.kind != K_DTW && J.kind != K_WDTW && J.kind != K_ADTW) {
+        if (!strip_ea_supported(J)) return pl;
+        pl.chunked = J.kind == K_EDR || J.kind == K_ERP || J.kind == K_MSM || J.kind == K_TWE;
+        // lcss / wlcss / negative-penalty adtw cannot abandon out of order; the
+        // strip sweep only replaces the all-pairs kernel's global ring
+        if (!pl.chunked && b >= 1) return pl;
+        pl.blocks_per_sm = strip_ea_blocks_per_sm(J);
+        if (pl.blocks_per_sm >= 1) pl.form = 3;
+        return pl;
+    }
+    pl.chunked = true;
     const char *force = getenv("WB_GPU_ARGMIN_FORM");
     const bool strip_forced = force && strcmp(force, "strip") == 0;
     if (b >= 2 && !strip_forced) {
@@ -318,10 +318,16 @@ int64_t argmin_ea_lanes(const ElasticJob &J) {
     return (int64_t)ea_plan(J).blocks_per_sm * device_info().sm_count * kEaThreads;
 }
 
+bool argmin_ea_chunked(const ElasticJob &J) { return ea_plan(J).chunked; }
+
+// per-lane ring of the strip forms: columns 0 .. m (the generic sweep may
+// write column m's boundary value)
+static int64_t ea_ring_ld(const ElasticJob &J) { return (int64_t)J.cols.len + 1; }
+
 size_t argmin_ea_ring_bytes(const ElasticJob &J) {
     const EaPlan pl = ea_plan(J);
-    if (pl.form != 2) return 0;
-    return align256((size_t)argmin_ea_lanes(J) * (size_t)J.cols.len * sizeof(double));
+    if (pl.form < 2) return 0;
+    return align256((size_t)argmin_ea_lanes(J) * (size_t)ea_ring_ld(J) * sizeof(double));
 }
 
 int launch_argmin_ea(const ElasticJob &J, int metric, int xl, int yl, int64_t j0, int64_t nc,
@@ -329,7 +335,7 @@ int launch_argmin_ea(const ElasticJob &J, int metric, int xl, int yl, int64_t j0
                      unsigned long long *counter, double *ring, cudaStream_t s) {
     const EaPlan pl = ea_plan(J);
     if (pl.form == 0) return fail(WB_EINVAL, "no early-abandoning argmin kernel for this job");
-    if (pl.form == 2 && !ring) return fail(WB_EINVAL, "strip ring missing");
+    if (pl.form >= 2 && !ring) return fail(WB_EINVAL, "strip ring missing");
     EaChunk C;
     C.j0 = j0;
     C.nc = nc;
@@ -360,8 +366,10 @@ int launch_argmin_ea(const ElasticJob &J, int metric, int xl, int yl, int64_t j0
             case K_WDTW: return run(argmin_ea_kernel<K_WDTW>);
             case K_ADTW: return run(argmin_ea_kernel<K_ADTW>);
         }
+    } else if (pl.form == 3) {
+        return launch_strip_ea(J, C, ring, ea_ring_ld(J), grid, s);
     } else {
-        const int64_t ld = J.cols.len;
+        const int64_t ld = ea_ring_ld(J);
         auto run = [&](auto kfn) -> int {
             kfn<<<grid, kEaThreads, 0, s>>>(J, C, ring, ld);
             WB_LAUNCH_CHECK("argmin_ea_strip_kernel");

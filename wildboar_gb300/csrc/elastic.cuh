@@ -189,12 +189,37 @@ struct ArgminJob {
 };
 int launch_argmin_replay(const ArgminJob &job, cudaStream_t s);
 
+// One chunk of argmin candidates for the early-abandoning kernels.
+struct EaChunk {
+    int64_t j0 = 0, nc = 0;                 // candidates [j0, j0 + nc)
+    int64_t nq = 0;                         // queries
+    int64_t ny = 0;                         // row stride of out / key / lower_bound
+    const double *cur_dist = nullptr;       // k-th distance after the replayed prefix
+    const double *lower_bound = nullptr;    // (nq, ny) or null
+    unsigned long long *counter = nullptr;  // next pair of the chunk
+    int metric = WB_DTW;
+    int xl = 0, yl = 0;
+};
+
+// Generic strip form (elastic_strip.cu) of the early-abandoning kernels:
+// edr / erp / msm / twe (chunked: their thresholds grow with the k-th
+// distance) and, with one chunk and no bound, the keyed all-pairs sweep of
+// lcss / wlcss / adtw with a negative penalty for wide bands.  The ring is
+// per lane [lane][column] (ring_ld >= cols.len).
+bool strip_ea_supported(const ElasticJob &job);
+int strip_ea_blocks_per_sm(const ElasticJob &job);
+int launch_strip_ea(const ElasticJob &job, const EaChunk &chunk, double *ring, int64_t ring_ld,
+                    int grid, cudaStream_t s);
+
 // early-abandoned candidate chunks (argmin_ea.cu): dtw / wdtw / ddtw / wddtw
-// / adtw with a non-negative penalty.  Writes out / key of pairs (i, j in
+// / adtw with a non-negative penalty, and through the generic strip form
+// edr / erp / msm / twe (and unchunked lcss / wlcss / adtw for wide bands).  Writes out / key of pairs (i, j in
 // [j0, j0 + nc)) with row stride ny; an abandoned pair gets distance inf and
 // its partial key, which exceeds the threshold the replay compares it with.
 // Wide bands need a device ring of argmin_ea_ring_bytes (0 for narrow ones).
 bool argmin_ea_supported(const ElasticJob &job);
+// candidates may be split in chunks with bounds (else one chunk, no bound)
+bool argmin_ea_chunked(const ElasticJob &job);
 int64_t argmin_ea_lanes(const ElasticJob &job);
 size_t argmin_ea_ring_bytes(const ElasticJob &job);
 int launch_argmin_ea(const ElasticJob &job, int metric, int xl, int yl, int64_t j0, int64_t nc,

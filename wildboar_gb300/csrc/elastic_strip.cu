@@ -30,7 +30,7 @@
 #include <cstring>
 #include <type_traits>
 
-#include "elastic.cuh"
+#include "argmin.cuh"
 
 namespace wb {
 
@@ -147,12 +147,13 @@ struct Rows {
 // One strip column.  P[k]: cell (i0 + k, c - 1) on entry, (i0 + k, c) on exit;
 // bup = cell (i0 - 1, c), bdiag = cell (i0 - 1, c - 1).  MASK: some rows of
 // the strip are outside their band at this column or past the series end.
-template <int KIND, int S, class A, bool MASK>
+template <int KIND, int S, class A, bool MASK, bool KEY = false>
 __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
                                        typename A::V bdiag, const Rows<S, A> &Rw,
                                        typename A::E yc, typename A::E yp, typename A::E colv,
                                        float ycf, float ypf, int c, int i0, int lo, int hi,
-                                       int valid, const PairCtx<A> &C) {
+                                       int valid, const PairCtx<A> &C,
+                                       typename A::V (&rmin)[S]) {
     using V = typename A::V;
     using E = typename A::E;
     constexpr bool DTWF = Kt<KIND>::dtwf;
@@ -220,27 +221,42 @@ __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
                 else nv = DTWF ? A::inf() : A::zero();
             }
         }
+        if constexpr (KEY) {
+            // the row minimum of the two-row recurrences: in-band cells only
+            if (!MASK || (d >= lo && d <= hi && k < valid))
+                rmin[k] = KIND == K_ADTW_ANY ? A::vmin_any(rmin[k], nv) : A::vmin(rmin[k], nv);
+        }
         dg = lf;
         up = nv;
         P[k] = nv;
     }
 }
 
-// The recurrence of one pair; returns cell (n - 1, m - 1).
+// The recurrence of one pair, resumable strip by strip: sweep_begin writes
+// the row above the first strip into the ring, sweep_strip sweeps one strip
+// (and with KEY the minimum of each of its rows over the row's band, the
+// abandon key's terms); sweep_pair runs them all and returns cell
+// (n - 1, m - 1).
+template <class A>
+struct SweepState {
+    typename A::V result, cy, stale_next;
+    typename A::E xprev;
+    float xprevf;
+    int i0, pstart, pend;
+};
+
+// true when the first row already completes the pair (st.result holds it)
 template <int KIND, int S, class A>
-__device__ __forceinline__ typename A::V sweep_pair(const double *__restrict__ X, int n,
-                                    const double *__restrict__ Y, int m, int r,
-                                    const PairCtx<A> &C, typename A::R *__restrict__ ring,
-                                    int64_t nth) {
+__device__ __forceinline__ bool sweep_begin(const double *__restrict__ X, int n,
+                                            const double *__restrict__ Y, int m, int r,
+                                            const PairCtx<A> &C, typename A::R *__restrict__ ring,
+                                            int64_t nth, SweepState<A> &st) {
     using V = typename A::V;
     using E = typename A::E;
-    constexpr bool DTWF = Kt<KIND>::dtwf;
-    constexpr int FR = Kt<KIND>::first_row, FC = Kt<KIND>::first_col;
-    const int mx = imax(0, m - n) + r, mn = imax(0, n - m);
-    const int lo = -(mn + r - 1), hi = mx - 1;
+    constexpr int FR = Kt<KIND>::first_row;
+    const int mx = imax(0, m - n) + r;
     const int lim = imin(m, mx);
     const V INF = A::inf(), ZERO = A::zero();
-    const V ROOB = DTWF ? INF : ZERO;
     const double x0d = X[0];
     const E x0 = A::el(x0d);
     const float x0f = (float)x0d;
@@ -257,7 +273,8 @@ __device__ __forceinline__ typename A::V sweep_pair(const double *__restrict__ X
                 cy = A::add(cy, msm_cost<A>(xif, xpf, y0f, C.c));
                 xpf = xif;
             }
-            return cy;
+            st.result = cy;
+            return true;
         }
     }
 
@@ -300,115 +317,155 @@ __device__ __forceinline__ typename A::V sweep_pair(const double *__restrict__ X
         for (int j = 0; j < lim; j++) ring[(int64_t)j * nth] = A::pack(init);
         if (mx < m) ring[(int64_t)mx * nth] = A::pack(init);
     }
-    if (n == FR) return acc;  // one row: lim == m, acc is cell (0, m - 1)
-
-    V result = ZERO;
-    int pstart = 0, pend = mx < m ? mx + 1 : lim;
-    E xprev = FR == 1 ? x0 : A::el(0.0);  // x_{i0 - 1} (twe: 0 above row 0)
-    float xprevf = x0f;
-    V stale_next = ZERO;  // msm: cell (i0 - 2, js(i0) - 1)
-    for (int i0 = FR; i0 < n; i0 += S) {
-        const int rows = imin(S, n - i0);
-        Rows<S, A> Rw;
-        V cyk[S];
-        V cy_prev = cy;
-#pragma unroll
-        for (int k = 0; k < S; k++) {
-            const double xd = (k < rows) ? X[i0 + k] : 0.0;
-            Rw.x[k] = A::el(xd);
-            if constexpr (KIND == K_ERP) Rw.rx[k] = A::absv(A::sub(Rw.x[k], C.g));
-            if constexpr (KIND == K_TWE) {
-                Rw.px[k] = (k == 0) ? xprev : Rw.x[k > 0 ? k - 1 : 0];
-                Rw.rx[k] = A::absv(A::sub(Rw.px[k], Rw.x[k]));
-            }
-            if constexpr (KIND == K_MSM) {
-                Rw.xf[k] = (float)xd;
-                Rw.pxf[k] = (k == 0) ? xprevf : Rw.xf[k > 0 ? k - 1 : 0];
-                cy = A::add(cy, msm_cost<A>(Rw.xf[k], Rw.pxf[k], y0f, C.c));
-                cyk[k] = cy;
-            }
-        }
-        const int cstart = imax(FC, i0 - mn - r + 1);
-        const int cend = imin(m, i0 + rows - 1 + mx);
-        int bstart = cend, bend = cend;
-        if (rows == S) {
-            bstart = imax(cstart, i0 + S - 1 + lo);
-            bend = imin(cend, i0 + hi + 1);
-            if (bstart >= bend) bstart = bend = cend;
-        }
-        const bool at_boundary = (cstart == FC);
-        V P[S];
-#pragma unroll
-        for (int k = 0; k < S; k++) {
-            V v;
-            if (at_boundary) {
-                if constexpr (KIND == K_ERP) v = C.gx_sum;
-                else if constexpr (KIND == K_MSM) v = cyk[k];
-                else if constexpr (DTWF || KIND == K_TWE) v = INF;
-                else v = ZERO;
-            } else {
-                if constexpr (KIND == K_MSM) v = stale_next;
-                else v = DTWF ? INF : ZERO;
-            }
-            P[k] = v;
-        }
-        V bdiag;
-        if (at_boundary) {
-            if constexpr (KIND == K_ERP) bdiag = i0 == 0 ? ZERO : C.gx_sum;
-            else if constexpr (KIND == K_TWE) bdiag = i0 == 0 ? ZERO : INF;
-            else if constexpr (KIND == K_MSM) bdiag = cy_prev;
-            else bdiag = DTWF ? INF : ZERO;
-        } else {
-            bdiag = A::unpack(ring[(int64_t)(cstart - 1) * nth]);
-        }
-        const bool last = (i0 + rows == n);
-        const int cnext = imax(FC, i0 + S - mn - r + 1);  // msm: next strip's first column
-        auto ld_up = [&](int c) -> V {
-            return (c >= pstart && c < pend) ? A::unpack(ring[(int64_t)c * nth]) : ROOB;
-        };
-        auto ld_y = [&](int c) -> double { return c < cend ? __ldg(Y + c) : 0.0; };
-        V nb0 = ld_up(cstart), nb1 = ld_up(cstart + 1);
-        double ny0 = ld_y(cstart), ny1 = ld_y(cstart + 1);
-        E yp = cstart > 0 ? A::el(__ldg(Y + cstart - 1)) : A::el(0.0);
-        float ypf = cstart > 0 ? (float)__ldg(Y + cstart - 1) : 0.0f;
-        for (int c = cstart; c < cend; c++) {
-            const V bup = nb0;
-            const double ycd = ny0;
-            nb0 = nb1;
-            ny0 = ny1;
-            nb1 = ld_up(c + 2);
-            ny1 = ld_y(c + 2);
-            const E yc = A::el(ycd);
-            const float ycf = (float)ycd;
-            E colv = A::el(0.0);
-            if constexpr (KIND == K_ERP) colv = A::el(__ldg(C.gY + c));
-            if constexpr (KIND == K_TWE) colv = A::absv(A::sub(yp, yc));
-            if (c >= bstart && c < bend)
-                column<KIND, S, A, false>(P, bup, bdiag, Rw, yc, yp, colv, ycf, ypf, c, i0, lo,
-                                          hi, rows, C);
-            else
-                column<KIND, S, A, true>(P, bup, bdiag, Rw, yc, yp, colv, ycf, ypf, c, i0, lo,
-                                         hi, rows, C);
-            if constexpr (KIND == K_MSM) {
-                if (c == cnext - 1) stale_next = P[S - 2];
-            }
-            if (last && c == m - 1) {
-#pragma unroll
-                for (int k = 0; k < S; k++)
-                    if (k < rows) result = P[k];  // ends at P[rows - 1], no indexed P
-            }
-            ring[(int64_t)c * nth] = A::pack(P[S - 1]);
-            bdiag = bup;
-            yp = yc;
-            ypf = ycf;
-        }
-        pstart = cstart;
-        pend = cend;
-        // carried into the next strip (only the last strip has rows < S)
-        if constexpr (KIND == K_TWE) xprev = Rw.x[S - 1];
-        if constexpr (KIND == K_MSM) xprevf = Rw.xf[S - 1];
+    if (n == FR) {  // one row: lim == m, acc is cell (0, m - 1)
+        st.result = acc;
+        return true;
     }
-    return result;
+    st.result = ZERO;
+    st.cy = cy;
+    st.stale_next = ZERO;  // msm: cell (i0 - 2, js(i0) - 1)
+    st.xprev = FR == 1 ? x0 : A::el(0.0);  // x_{i0 - 1} (twe: 0 above row 0)
+    st.xprevf = x0f;
+    st.i0 = FR;
+    st.pstart = 0;
+    st.pend = mx < m ? mx + 1 : lim;
+    return false;
+}
+
+// rows st.i0 .. st.i0 + rows - 1; returns rows
+template <int KIND, int S, class A, bool KEY>
+__device__ __forceinline__ int sweep_strip(const double *__restrict__ X, int n,
+                                           const double *__restrict__ Y, int m, int r,
+                                           const PairCtx<A> &C, typename A::R *__restrict__ ring,
+                                           int64_t nth, SweepState<A> &st,
+                                           typename A::V (&rmin)[S]) {
+    using V = typename A::V;
+    using E = typename A::E;
+    constexpr bool DTWF = Kt<KIND>::dtwf;
+    constexpr int FC = Kt<KIND>::first_col;
+    const int mx = imax(0, m - n) + r, mn = imax(0, n - m);
+    const int lo = -(mn + r - 1), hi = mx - 1;
+    const V INF = A::inf(), ZERO = A::zero();
+    const V ROOB = DTWF ? INF : ZERO;
+    const float y0f = (float)__ldg(Y);
+    const int i0 = st.i0;
+    const int pstart = st.pstart, pend = st.pend;
+    const int rows = imin(S, n - i0);
+    Rows<S, A> Rw;
+    V cyk[S];
+    V cy = st.cy;
+    const V cy_prev = cy;
+#pragma unroll
+    for (int k = 0; k < S; k++) {
+        const double xd = (k < rows) ? X[i0 + k] : 0.0;
+        Rw.x[k] = A::el(xd);
+        if constexpr (KIND == K_ERP) Rw.rx[k] = A::absv(A::sub(Rw.x[k], C.g));
+        if constexpr (KIND == K_TWE) {
+            Rw.px[k] = (k == 0) ? st.xprev : Rw.x[k > 0 ? k - 1 : 0];
+            Rw.rx[k] = A::absv(A::sub(Rw.px[k], Rw.x[k]));
+        }
+        if constexpr (KIND == K_MSM) {
+            Rw.xf[k] = (float)xd;
+            Rw.pxf[k] = (k == 0) ? st.xprevf : Rw.xf[k > 0 ? k - 1 : 0];
+            cy = A::add(cy, msm_cost<A>(Rw.xf[k], Rw.pxf[k], y0f, C.c));
+            cyk[k] = cy;
+        }
+        if constexpr (KEY) rmin[k] = KIND == K_MSM ? cyk[k] : INF;
+    }
+    st.cy = cy;
+    const int cstart = imax(FC, i0 - mn - r + 1);
+    const int cend = imin(m, i0 + rows - 1 + mx);
+    int bstart = cend, bend = cend;
+    if (rows == S) {
+        bstart = imax(cstart, i0 + S - 1 + lo);
+        bend = imin(cend, i0 + hi + 1);
+        if (bstart >= bend) bstart = bend = cend;
+    }
+    const bool at_boundary = (cstart == FC);
+    V P[S];
+#pragma unroll
+    for (int k = 0; k < S; k++) {
+        V v;
+        if (at_boundary) {
+            if constexpr (KIND == K_ERP) v = C.gx_sum;
+            else if constexpr (KIND == K_MSM) v = cyk[k];
+            else if constexpr (DTWF || KIND == K_TWE) v = INF;
+            else v = ZERO;
+        } else {
+            if constexpr (KIND == K_MSM) v = st.stale_next;
+            else v = DTWF ? INF : ZERO;
+        }
+        P[k] = v;
+    }
+    V bdiag;
+    if (at_boundary) {
+        if constexpr (KIND == K_ERP) bdiag = i0 == 0 ? ZERO : C.gx_sum;
+        else if constexpr (KIND == K_TWE) bdiag = i0 == 0 ? ZERO : INF;
+        else if constexpr (KIND == K_MSM) bdiag = cy_prev;
+        else bdiag = DTWF ? INF : ZERO;
+    } else {
+        bdiag = A::unpack(ring[(int64_t)(cstart - 1) * nth]);
+    }
+    const bool last = (i0 + rows == n);
+    const int cnext = imax(FC, i0 + S - mn - r + 1);  // msm: next strip's first column
+    auto ld_up = [&](int c) -> V {
+        return (c >= pstart && c < pend) ? A::unpack(ring[(int64_t)c * nth]) : ROOB;
+    };
+    auto ld_y = [&](int c) -> double { return c < cend ? __ldg(Y + c) : 0.0; };
+    V nb0 = ld_up(cstart), nb1 = ld_up(cstart + 1);
+    double ny0 = ld_y(cstart), ny1 = ld_y(cstart + 1);
+    E yp = cstart > 0 ? A::el(__ldg(Y + cstart - 1)) : A::el(0.0);
+    float ypf = cstart > 0 ? (float)__ldg(Y + cstart - 1) : 0.0f;
+    for (int c = cstart; c < cend; c++) {
+        const V bup = nb0;
+        const double ycd = ny0;
+        nb0 = nb1;
+        ny0 = ny1;
+        nb1 = ld_up(c + 2);
+        ny1 = ld_y(c + 2);
+        const E yc = A::el(ycd);
+        const float ycf = (float)ycd;
+        E colv = A::el(0.0);
+        if constexpr (KIND == K_ERP) colv = A::el(__ldg(C.gY + c));
+        if constexpr (KIND == K_TWE) colv = A::absv(A::sub(yp, yc));
+        if (c >= bstart && c < bend)
+            column<KIND, S, A, false, KEY>(P, bup, bdiag, Rw, yc, yp, colv, ycf, ypf, c, i0,
+                                           lo, hi, rows, C, rmin);
+        else
+            column<KIND, S, A, true, KEY>(P, bup, bdiag, Rw, yc, yp, colv, ycf, ypf, c, i0, lo,
+                                          hi, rows, C, rmin);
+        if constexpr (KIND == K_MSM) {
+            if (c == cnext - 1) st.stale_next = P[S - 2];
+        }
+        if (last && c == m - 1) {
+#pragma unroll
+            for (int k = 0; k < S; k++)
+                if (k < rows) st.result = P[k];  // ends at P[rows - 1], no indexed P
+        }
+        ring[(int64_t)c * nth] = A::pack(P[S - 1]);
+        bdiag = bup;
+        yp = yc;
+        ypf = ycf;
+    }
+    st.pstart = cstart;
+    st.pend = cend;
+    // carried into the next strip (only the last strip has rows < S)
+    if constexpr (KIND == K_TWE) st.xprev = Rw.x[S - 1];
+    if constexpr (KIND == K_MSM) st.xprevf = Rw.xf[S - 1];
+    st.i0 = i0 + rows;
+    return rows;
+}
+
+template <int KIND, int S, class A>
+__device__ __forceinline__ typename A::V sweep_pair(const double *__restrict__ X, int n,
+                                    const double *__restrict__ Y, int m, int r,
+                                    const PairCtx<A> &C, typename A::R *__restrict__ ring,
+                                    int64_t nth) {
+    SweepState<A> st;
+    if (sweep_begin<KIND, S, A>(X, n, Y, m, r, C, ring, nth, st)) return st.result;
+    typename A::V unused[S];
+    while (st.i0 < n) sweep_strip<KIND, S, A, false>(X, n, Y, m, r, C, ring, nth, st, unused);
+    return st.result;
 }
 
 __device__ __forceinline__ double finish_value(const ElasticJob &J, double v) {
@@ -479,6 +536,153 @@ __global__ void __launch_bounds__(kStripThreads)
         J.out[rs * J.out_ld + cs] = d;
         if (J.mode == PM_UPPER) J.out[cs * J.out_ld + rs] = d;
     }
+}
+
+// --------------------------------------------------------------------------
+// argmin chunks with early abandoning, one pair per lane at a time (the lane
+// queue of argmin_ea.cu): after every strip the lane folds the strip's row
+// minima into the pair's key and stops the pair once the key exceeds the
+// threshold bound of the chunk (the reference abandons it then as well).
+template <int KIND, int S>
+__global__ void __launch_bounds__(kStripThreads)
+    strip_ea_kernel(const ElasticJob J, const EaChunk Ch, double *ring_base, int64_t ring_ld) {
+    using A = ArF64;
+    using V = A::V;
+    const int64_t gtid = (int64_t)blockIdx.x * kStripThreads + threadIdx.x;
+    double *ring = ring_base + gtid * ring_ld;
+    const int n = J.rows.len, m = J.cols.len;
+    const double INF = WB_SINF64;
+    const int64_t total = Ch.nq * Ch.nc;
+
+    int64_t p = (int64_t)atomicAdd(Ch.counter, 1ULL);
+    int64_t qi = 0, cj = 0;
+    const double *X = nullptr, *Y = nullptr;
+    double bound = INF, kmax = -INF;
+    PairCtx<A> C;
+    SweepState<A> st;
+    bool finished = false;
+
+    auto next_pair = [&]() {
+        while (p < total) {
+            qi = p / Ch.nc;
+            cj = Ch.j0 + (p - qi * Ch.nc);
+            const double d = Ch.cur_dist[qi];
+            const int64_t o = qi * Ch.ny + cj;
+            if (Ch.lower_bound && Ch.lower_bound[o] >= d) {
+                // the replay skips it: lb >= D_a >= every later k-th distance
+                J.out[o] = INF;
+                J.key[o] = INF;
+                p = (int64_t)atomicAdd(Ch.counter, 1ULL);
+                continue;
+            }
+            bound = abandon_threshold(Ch.metric, d, Ch.xl, Ch.yl);
+            C.eps = J.eps;
+            if constexpr (KIND == K_EDR) {
+                if (J.std_rows) C.eps = cy_max(J.std_rows[qi], J.std_cols[cj]) / 4.0;
+            }
+            C.g = J.g;
+            C.pen = KIND == K_TWE ? J.penalty + J.stiffness : J.p;
+            C.s2 = J.stiffness * 2.0;
+            C.c = (float)J.c;
+            C.gx_sum = 0.0;
+            C.gy_sum = 0.0;
+            C.gY = nullptr;
+            if constexpr (KIND == K_ERP) {
+                C.gx_sum = J.gsum_rows[qi];
+                C.gy_sum = J.gsum_cols[cj];
+                C.gY = J.gtab_cols + cj * (int64_t)m;
+            }
+            C.w = J.weights;
+            C.stab = J.stab;
+            X = J.rows.base + qi * J.rows.stride;
+            Y = J.cols.base + cj * J.cols.stride;
+            kmax = -INF;
+            finished = sweep_begin<KIND, S, A>(X, n, Y, m, J.band, C, ring, 1, st);
+            return;
+        }
+    };
+    next_pair();
+
+    while (p < total) {
+        if (!finished) {
+            V rmin[S];
+            const int rows = sweep_strip<KIND, S, A, true>(X, n, Y, m, J.band, C, ring, 1, st,
+                                                           rmin);
+#pragma unroll
+            for (int k = 0; k < S; k++)
+                if (k < rows) kmax = fmax(kmax, rmin[k]);
+            finished = st.i0 >= n;
+        }
+        if (finished || kmax > bound) {
+            const int64_t o = qi * Ch.ny + cj;
+            J.out[o] = finished ? finish_value(J, st.result) : INF;
+            J.key[o] = kmax;
+            p = (int64_t)atomicAdd(Ch.counter, 1ULL);
+            next_pair();
+        }
+    }
+}
+
+constexpr int kStripEaRowsLight = 16;  // edr, lcss, wlcss, adtw
+constexpr int kStripEaRowsHeavy = 8;   // erp, msm, twe
+
+bool strip_ea_supported(const ElasticJob &J) {
+    switch (J.kind) {
+        case K_EDR:
+        case K_ERP:
+        case K_TWE:
+        case K_LCSS:
+        case K_WLCSS:
+        case K_ADTW_ANY:
+            break;
+        case K_MSM:
+            if (J.cols.len < 2) return false;  // one column: no strips, no key
+            break;
+        default:
+            return false;
+    }
+    return !J.all_zero && J.mode == PM_ALL && J.key && J.rows.len >= 1 && J.cols.len >= 1;
+}
+
+template <int KIND, int S>
+static int strip_ea_occupancy() {
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, strip_ea_kernel<KIND, S>, kStripThreads,
+                                                  0);
+    return nb;
+}
+
+int strip_ea_blocks_per_sm(const ElasticJob &J) {
+    switch (J.kind) {
+        case K_EDR: return strip_ea_occupancy<K_EDR, kStripEaRowsLight>();
+        case K_LCSS: return strip_ea_occupancy<K_LCSS, kStripEaRowsLight>();
+        case K_WLCSS: return strip_ea_occupancy<K_WLCSS, kStripEaRowsLight>();
+        case K_ADTW_ANY: return strip_ea_occupancy<K_ADTW_ANY, kStripEaRowsLight>();
+        case K_ERP: return strip_ea_occupancy<K_ERP, kStripEaRowsHeavy>();
+        case K_MSM: return strip_ea_occupancy<K_MSM, kStripEaRowsHeavy>();
+        case K_TWE: return strip_ea_occupancy<K_TWE, kStripEaRowsHeavy>();
+    }
+    return 0;
+}
+
+int launch_strip_ea(const ElasticJob &J, const EaChunk &Ch, double *ring, int64_t ring_ld,
+                    int grid, cudaStream_t s) {
+    if (Ch.nq * Ch.nc == 0) return WB_OK;
+    auto run = [&](auto kfn) -> int {
+        kfn<<<grid, kStripThreads, 0, s>>>(J, Ch, ring, ring_ld);
+        WB_LAUNCH_CHECK("strip_ea_kernel");
+        return WB_OK;
+    };
+    switch (J.kind) {
+        case K_EDR: return run(strip_ea_kernel<K_EDR, kStripEaRowsLight>);
+        case K_LCSS: return run(strip_ea_kernel<K_LCSS, kStripEaRowsLight>);
+        case K_WLCSS: return run(strip_ea_kernel<K_WLCSS, kStripEaRowsLight>);
+        case K_ADTW_ANY: return run(strip_ea_kernel<K_ADTW_ANY, kStripEaRowsLight>);
+        case K_ERP: return run(strip_ea_kernel<K_ERP, kStripEaRowsHeavy>);
+        case K_MSM: return run(strip_ea_kernel<K_MSM, kStripEaRowsHeavy>);
+        case K_TWE: return run(strip_ea_kernel<K_TWE, kStripEaRowsHeavy>);
+    }
+    return fail(WB_EINVAL, "no strip early-abandoning kernel for this metric kind");
 }
 
 // --------------------------------------------------------------------------
