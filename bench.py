@@ -580,6 +580,38 @@ def bench_argmin(args, dev, flush):
             os.environ.pop("WB_GPU_ARGMIN", None)
         else:
             os.environ["WB_GPU_ARGMIN"] = prev
+    # the metric's default band (r=1) on half the queries: the strip form
+    Xw = Xd[:1000]
+    cells_w = Xw.shape[0] * Y.shape[0] * band_cells(wl["L"], wl["L"], 1.0)
+
+    def call_w():
+        return argmin_distance(Xw, Yd, k=5, metric="dtw", metric_params={"r": 1.0},
+                               return_distance=True)
+
+    try:
+        call_w()
+        torch.cuda.synchronize()
+        ms_w = _timed(call_w, 1, flush)
+        widx, wdist = call_w()
+        os.environ["WB_GPU_ARGMIN"] = "all"
+        call_w()
+        torch.cuda.synchronize()
+        ms_w_all = _timed(call_w, 1, flush)
+        wfidx, wfdist = call_w()
+    finally:
+        if prev is None:
+            os.environ.pop("WB_GPU_ARGMIN", None)
+        else:
+            os.environ["WB_GPU_ARGMIN"] = prev
+    wide = {
+        "config": f"1000 queries x {Y.shape[0]} series, L={wl['L']}, dtw r=1.0, k=5",
+        "ms": ms_w,
+        "gcups_algorithmic": cells_w / (ms_w * 1e-3) / 1e9,
+        "all_pairs_ms": ms_w_all,
+        "all_pairs_gcups": cells_w / (ms_w_all * 1e-3) / 1e9,
+        "forms_bit_identical": bool(torch.equal(widx, wfidx) and torch.equal(
+            wdist.view(torch.int64), wfdist.view(torch.int64))),
+    }
     oi, od = O.argmin(X[:4], Y, k=5, metric="dtw", metric_params=wl["params"],
                       n_threads=os.cpu_count() or 1)
     n_threads = os.cpu_count() or 1
@@ -600,6 +632,7 @@ def bench_argmin(args, dev, flush):
                        band_cells(wl["L"], wl["L"], wl["params"]["r"]) / cpu_s / 1e9,
                        "cores": n_threads, "kind": "port",
                        "sample": f"{rows} queries x {Y.shape[0]} series"},
+        "wide_band": wide,
     }
 
 
