@@ -247,3 +247,31 @@ def test_subsequence_match_equivalent(left, right):
         np.testing.assert_almost_equal(a, b)
     for a, b in zip(li, ri):
         np.testing.assert_array_equal(a, b)
+
+
+LONG_SCAN = [("dtw", {"r": 0.1}), ("dtw", {"r": 1.0}), ("wdtw", {"g": 0.1}), ("ddtw", {"r": 0.3}),
+             ("adtw", {"p": 0.5}), ("adtw", {"p": -0.2}), ("edr", {}), ("edr", {"epsilon": 0.4}),
+             ("erp", {"g": 0.1}), ("msm", {"c": 0.5}), ("twe", {"penalty": 0.5,
+                                                               "stiffness": 0.01}),
+             ("lcss", {"epsilon": 0.5})]
+
+
+@pytest.mark.parametrize("metric,params", LONG_SCAN,
+                         ids=[f"{m}-{i}" for i, (m, _) in enumerate(LONG_SCAN)])
+def test_elastic_subsequence_long_scan_vs_oracle(metric, params):
+    # several rounds of 32 windows per (series, shapelet), near matches planted
+    # late in some series: the rounds abandon at the best earlier window
+    from wildboar_gb300.distance import pairwise_subsequence_distance
+
+    rng = np.random.default_rng(55)
+    X = np.cumsum(rng.standard_normal((6, 300)), axis=1)
+    shp = [np.cumsum(rng.standard_normal(int(n))) for n in rng.integers(8, 41, size=24)]
+    for k in range(0, 24, 5):
+        s = k % 6
+        pos = 200 + 3 * k
+        X[s, pos:pos + len(shp[k])] = shp[k] + 0.05 * rng.standard_normal(len(shp[k]))
+    d, i = pairwise_subsequence_distance(shp, X, metric=metric, metric_params=params,
+                                         return_index=True)
+    od, oi = O.subsequence(shp, X, metric=metric, metric_params=params)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_allclose(d, od, rtol=RTOL, atol=0)

@@ -382,31 +382,45 @@ elastic_subseq_kernel(const SubseqElasticJob J, double *gring, int P) {
         for (int base = 0; base < nwin; base += 32) {
             const int w = base + lane;
             double d = INF, key = INF;
+            // The round's windows stop at the threshold of the best window of
+            // the earlier rounds: the thresholds inside the round are no larger
+            // (lcss's threshold falls as the distance grows: no bound), and an
+            // abandoned window's partial key already exceeds the threshold its
+            // replay compares it with.  Adjacent windows overlap, so a round
+            // far from every good match abandons in all its lanes together.
+            const double bound =
+                (J.prof_raw || KIND == K_LCSS) ? INF
+                                               : subseq_threshold(J.metric, min_dist, L,
+                                                                  J.t_len_thr);
             if (w < nwin) {
                 const double *Y = T + w;
                 double raw;
                 if constexpr (KIND == K_DTW)
-                    raw = rec_dtw<false>(ring, P, S, L, Y, L, band, nullptr, key);
+                    raw = rec_dtw<false, RingG, true>(ring, P, S, L, Y, L, band, nullptr, key,
+                                                      bound);
                 else if constexpr (KIND == K_WDTW)
-                    raw = rec_dtw<true>(ring, P, S, L, Y, L, band, J.weights, key);
+                    raw = rec_dtw<true, RingG, true>(ring, P, S, L, Y, L, band, J.weights, key,
+                                                     bound);
                 else if constexpr (KIND == K_ADTW)
-                    raw = rec_adtw<true>(ring, P, S, L, Y, L, band, J.p, key);
+                    raw = rec_adtw<true, RingG, true>(ring, P, S, L, Y, L, band, J.p, key,
+                                                      bound);
                 else if constexpr (KIND == K_ADTW_ANY)
-                    raw = rec_adtw<false>(ring, P, S, L, Y, L, band, J.p, key);
+                    raw = rec_adtw<false, RingG, true>(ring, P, S, L, Y, L, band, J.p, key,
+                                                       bound);
                 else if constexpr (KIND == K_LCSS)
                     raw = rec_lcss<false>(ring, P, S, L, Y, L, band, eps, nullptr, key);
                 else if constexpr (KIND == K_EDR)
-                    raw = rec_edr(ring, P, S, L, Y, L, band, eps, key);
+                    raw = rec_edr<RingG, true>(ring, P, S, L, Y, L, band, eps, key, bound);
                 else if constexpr (KIND == K_ERP) {
                     double gy_sum = 0.0;
                     for (int k = 0; k < L; k++) gy_sum = gy_sum + ldg(J.gtab + si * J.t_len + w + k);
-                    raw = rec_erp(ring, P, S, L, Y, L, band, J.g, gx_sum, gy_sum,
-                                  J.gtab + si * J.t_len + w, key);
+                    raw = rec_erp<RingG, true>(ring, P, S, L, Y, L, band, J.g, gx_sum, gy_sum,
+                                               J.gtab + si * J.t_len + w, key, bound);
                 } else if constexpr (KIND == K_MSM)
-                    raw = rec_msm(ring, P, S, L, Y, L, band, J.c, key);
+                    raw = rec_msm<RingG, true>(ring, P, S, L, Y, L, band, J.c, key, bound);
                 else
-                    raw = rec_twe<RingG, false>(ring, P, S, L, Y, L, band, J.penalty,
-                                                J.stiffness, nullptr, J.stab, key);
+                    raw = rec_twe<RingG, false, true>(ring, P, S, L, Y, L, band, J.penalty,
+                                                      J.stiffness, nullptr, J.stab, key, bound);
                 if (KIND == K_LCSS) d = 1.0 - raw / (double)L;
                 else if (KIND == K_EDR) d = raw / (double)L;
                 else d = raw;

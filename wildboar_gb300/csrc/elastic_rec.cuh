@@ -1,7 +1,9 @@
 // elastic_rec.cuh -- the FP64 two-row recurrences of the elastic metrics,
 // thread-per-pair with the live band in a ring (shared or global memory).
 // Shared by the pairwise / argmin kernels (elastic_f64.cu) and the
-// subsequence kernels (elastic_f64.cu, argmin_subseq.cu).  Every cell performs
+// subsequence kernels (elastic_f64.cu, argmin_subseq.cu).  With EA the
+// recurrence stops after the first row that lifts the abandon key (the largest
+// row minimum so far) above `bound`, returning +inf with that partial key.  Every cell performs
 // the reference's IEEE double operations in the reference's order; the
 // including file is compiled with -fmad=false.
 #pragma once
@@ -33,10 +35,10 @@ __device__ __forceinline__ double ldg(const double *p) { return __ldg(p); }
 
 // --------------------------------------------------------------------------
 // dtw / wdtw / ddtw / wddtw: dtw_distance, distance/_elastic.pyx:869-940
-template <bool W, class R>
+template <bool W, class R, bool EA = false>
 __device__ double rec_dtw(R ring, int P, const double *__restrict__ X, int n,
                           const double *__restrict__ Y, int m, int r,
-                          const double *__restrict__ w, double &key) {
+                          const double *__restrict__ w, double &key, double bound = HUGE_VAL) {
     const int mx = imax(0, m - n) + r;
     const int mn = imax(0, n - m);
     const double INF = WB_INF;
@@ -76,16 +78,22 @@ __device__ double rec_dtw(R ring, int P, const double *__restrict__ X, int n,
         }
         if (je < m) ring.st(q, INF);
         kmax = fmax(kmax, rmin);
+        if constexpr (EA) {
+            if (kmax > bound) {  // abandoned: the caller's bound is crossed
+                key = kmax;
+                return WB_INF;
+            }
+        }
     }
     key = kmax;
     return ring.ld((m - 1) % P);
 }
 
 // adtw: adtw_distance, distance/_elastic.pyx:943-1008
-template <bool NONNEG, class R>
+template <bool NONNEG, class R, bool EA = false>
 __device__ double rec_adtw(R ring, int P, const double *__restrict__ X, int n,
                            const double *__restrict__ Y, int m, int r, double pen,
-                           double &key) {
+                           double &key, double bound = HUGE_VAL) {
     const int mx = imax(0, m - n) + r;
     const int mn = imax(0, n - m);
     const double INF = WB_INF;
@@ -127,6 +135,12 @@ __device__ double rec_adtw(R ring, int P, const double *__restrict__ X, int n,
         }
         if (je < m) ring.st(q, INF);
         kmax = fmax(kmax, rmin);
+        if constexpr (EA) {
+            if (kmax > bound) {  // abandoned: the caller's bound is crossed
+                key = kmax;
+                return WB_INF;
+            }
+        }
     }
     key = kmax;
     return ring.ld((m - 1) % P);
@@ -175,10 +189,10 @@ __device__ double rec_lcss(R ring, int P, const double *__restrict__ X, int n,
 }
 
 // edr: edr_distance, distance/_elastic.pyx:1437-1497
-template <class R>
+template <class R, bool EA = false>
 __device__ double rec_edr(R ring, int P, const double *__restrict__ X, int n,
                           const double *__restrict__ Y, int m, int r, double eps,
-                          double &key) {
+                          double &key, double bound = HUGE_VAL) {
     const int mx = imax(0, m - n) + r;
     const int mn = imax(0, n - m);
     const double INF = WB_INF;
@@ -213,17 +227,23 @@ __device__ double rec_edr(R ring, int P, const double *__restrict__ X, int n,
         }
         if (je < m) ring.st(q, 0.0);
         kmax = fmax(kmax, rmin);
+        if constexpr (EA) {
+            if (kmax > bound) {  // abandoned: the caller's bound is crossed
+                key = kmax;
+                return WB_INF;
+            }
+        }
     }
     key = kmax;
     return ring.ld((m - 1) % P);
 }
 
 // erp: erp_distance, distance/_elastic.pyx:1273-1347
-template <class R>
+template <class R, bool EA = false>
 __device__ double rec_erp(R ring, int P, const double *__restrict__ X, int n,
                           const double *__restrict__ Y, int m, int r, double g,
                           double gx_sum, double gy_sum, const double *__restrict__ gY,
-                          double &key) {
+                          double &key, double bound = HUGE_VAL) {
     const int mx = imax(0, m - n) + r;
     const int mn = imax(0, n - m);
     const double INF = WB_INF;
@@ -265,6 +285,12 @@ __device__ double rec_erp(R ring, int P, const double *__restrict__ X, int n,
         }
         if (je < m) ring.st(q, 0.0);
         kmax = fmax(kmax, rmin);
+        if constexpr (EA) {
+            if (kmax > bound) {  // abandoned: the caller's bound is crossed
+                key = kmax;
+                return WB_INF;
+            }
+        }
     }
     key = kmax;
     return ring.ld((m - 1) % P);
@@ -280,10 +306,10 @@ __device__ __forceinline__ double msm_cost(float x, float y, float z, float c) {
 }
 
 // msm: msm_distance, distance/_elastic.pyx:1592-1647
-template <class R>
+template <class R, bool EA = false>
 __device__ double rec_msm(R ring, int P, const double *__restrict__ X, int n,
                           const double *__restrict__ Y, int m, int r, double cd,
-                          double &key) {
+                          double &key, double bound = HUGE_VAL) {
     const int mx = imax(0, m - n) + r;
     const int mn = imax(0, n - m);
     const double INF = WB_INF;
@@ -346,6 +372,12 @@ __device__ double rec_msm(R ring, int P, const double *__restrict__ X, int n,
         }
         if (je < m) ring.st(q, 0.0);
         kmax = fmax(kmax, rmin);
+        if constexpr (EA) {
+            if (kmax > bound) {  // abandoned: the caller's bound is crossed
+                key = kmax;
+                return WB_INF;
+            }
+        }
         xprevf = xif;
     }
     key = kmax;
@@ -356,11 +388,12 @@ __device__ double rec_msm(R ring, int P, const double *__restrict__ X, int n,
 // twe: twe_distance, distance/_elastic.pyx:1733-1829.  DYTAB: |y_{j-1} - y_j|
 // from a per-series table; otherwise computed (windows of a longer series
 // start with y_{-1} = 0, which no whole-series table holds).
-template <class R, bool DYTAB = true>
+template <class R, bool DYTAB = true, bool EA = false>
 __device__ double rec_twe(R ring, int P, const double *__restrict__ X, int n,
                           const double *__restrict__ Y, int m, int r, double penalty,
                           double stiffness, const double *__restrict__ dY,
-                          const double *__restrict__ stab, double &key) {
+                          const double *__restrict__ stab, double &key,
+                          double bound = HUGE_VAL) {
     const int mx = imax(0, m - n) + r;
     const int mn = imax(0, n - m);
     const double INF = WB_INF;
@@ -408,6 +441,12 @@ __device__ double rec_twe(R ring, int P, const double *__restrict__ X, int n,
         }
         if (je < m) ring.st(q, 0.0);
         kmax = fmax(kmax, rmin);
+        if constexpr (EA) {
+            if (kmax > bound) {  // abandoned: the caller's bound is crossed
+                key = kmax;
+                return WB_INF;
+            }
+        }
         xp = xi;
     }
     key = kmax;
