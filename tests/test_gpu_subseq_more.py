@@ -275,3 +275,30 @@ def test_elastic_subsequence_long_scan_vs_oracle(metric, params):
     od, oi = O.subsequence(shp, X, metric=metric, metric_params=params)
     np.testing.assert_array_equal(i, oi)
     np.testing.assert_allclose(d, od, rtol=RTOL, atol=0)
+
+
+@pytest.mark.parametrize("metric,params", LONG_SCAN,
+                         ids=[f"{m}-{i}" for i, (m, _) in enumerate(LONG_SCAN)])
+@pytest.mark.parametrize("scale", [False, True])
+def test_argmin_subsequence_long_scan_vs_oracle(monkeypatch, metric, params, scale):
+    # many rounds of windows with near matches early and late: the rounds
+    # abandon at the heap threshold of the earlier rounds
+    rng = np.random.default_rng(57)
+    X = np.cumsum(rng.standard_normal((9, 400)), axis=1)
+    lens = rng.integers(10, 45, size=9)
+    Y = [np.cumsum(rng.standard_normal(int(L))) for L in lens]
+    for s in range(9):
+        L = len(Y[s])
+        for pos in (20 + 7 * s, 300 + 5 * s):
+            X[s, pos:pos + L] = Y[s] + 0.05 * rng.standard_normal(L)
+    idx, dist = argmin_subsequence_distance(Y, X, k=3, metric=metric, metric_params=params,
+                                            scale=scale, return_distance=True)
+    oi, od = O.argmin_subsequence(Y, X, k=3, metric=metric, metric_params=params, scale=scale)
+    np.testing.assert_array_equal(idx, oi)
+    np.testing.assert_allclose(dist, od, rtol=RTOL, atol=0)
+    # every window in full: the same heaps bit for bit
+    monkeypatch.setenv("WB_GPU_ARGMIN", "all")
+    fidx, fdist = argmin_subsequence_distance(Y, X, k=3, metric=metric, metric_params=params,
+                                              scale=scale, return_distance=True)
+    np.testing.assert_array_equal(idx, fidx)
+    assert np.array_equal(np.asarray(dist).view(np.uint64), np.asarray(fdist).view(np.uint64))

@@ -51,6 +51,7 @@ struct ArgminSubseqJob {
     double *heap_val = nullptr;
     int64_t *out_idx = nullptr;   // (n, k)
     double *out_dist = nullptr;
+    int no_abandon = 0;           // evaluate every window in full (WB_GPU_ARGMIN=all)
 };
 
 // fast_mean_std, utils/_stats.pyx:22-42 (x*x where the reference calls pow)
@@ -92,9 +93,20 @@ argmin_subseq_kernel(const ArgminSubseqJob J, double *gring, int P) {
                 for (int q = 0; q < Lc; q++) gx_sum = gx_sum + fabs(S[q] - J.g);
             if (KIND == K_EDR && isnan(J.eps)) sx = row_std(S, Lc);
             double distance = INF;
+            // windows abandon at the threshold of the heap after the earlier
+            // rounds (it only falls within a round); lcss / wlcss thresholds
+            // fall as the k-th distance grows and adtw's square of a negative
+            // root is no bound: those evaluate every window in full
+            constexpr bool EA = KIND == K_DTW || KIND == K_WDTW || KIND == K_ADTW ||
+                                KIND == K_EDR || KIND == K_ERP || KIND == K_MSM ||
+                                KIND == K_TWE;
             for (int base = 0; base < nwin; base += 32) {
                 const int w = base + lane;
                 double d = INF, key = INF;
+                const double bound =
+                    (EA && !J.no_abandon)
+                        ? abandon_threshold(J.metric, __shfl_sync(0xffffffffu, distance, 0), L, L)
+                        : INF;
                 if (w < nwin) {
                     const double *Y = J.W ? J.W + ((pi - J.p0) * J.w_ld + w) * J.w_stride
                                           : J.x.base + pi * J.x.stride + w;
@@ -110,11 +122,14 @@ argmin_subseq_kernel(const ArgminSubseqJob J, double *gring, int P) {
                         d = sqrt(raw);
                     } else {
                         if constexpr (KIND == K_DTW)
-                            raw = rec_dtw<false>(ring, P, S, Lc, Y, Lc, band, nullptr, key);
+                            raw = rec_dtw<false, RingG, EA>(ring, P, S, Lc, Y, Lc, band, nullptr, key,
+                                                            bound);
                         else if constexpr (KIND == K_WDTW)
-                            raw = rec_dtw<true>(ring, P, S, Lc, Y, Lc, band, J.weights, key);
+                            raw = rec_dtw<true, RingG, EA>(ring, P, S, Lc, Y, Lc, band, J.weights,
+                                                           key, bound);
                         else if constexpr (KIND == K_ADTW)
-                            raw = rec_adtw<true>(ring, P, S, Lc, Y, Lc, band, J.p, key);
+                            raw = rec_adtw<true, RingG, EA>(ring, P, S, Lc, Y, Lc, band, J.p, key,
+                                                            bound);
                         else if constexpr (KIND == K_ADTW_ANY)
                             raw = rec_adtw<false>(ring, P, S, Lc, Y, Lc, band, J.p, key);
                         else if constexpr (KIND == K_LCSS)
@@ -126,19 +141,20 @@ argmin_subseq_kernel(const ArgminSubseqJob J, double *gring, int P) {
                         else if constexpr (KIND == K_EDR) {
                             double eps = J.eps;
                             if (isnan(eps)) eps = fmax(sx, row_std(Y, Lc)) / 4.0;
-                            raw = rec_edr(ring, P, S, Lc, Y, Lc, band, eps, key);
+                            raw = rec_edr<RingG, EA>(ring, P, S, Lc, Y, Lc, band, eps, key, bound);
                         } else if constexpr (KIND == K_ERP) {
                             const double *gY = J.W ? J.G + ((pi - J.p0) * J.w_ld + w) * J.w_stride
                                                    : J.gtab + pi * J.t_len + w;
                             double gy_sum = 0.0;
                             for (int q = 0; q < Lc; q++) gy_sum = gy_sum + gY[q];
-                            raw = rec_erp(ring, P, S, Lc, Y, Lc, band, J.g, gx_sum, gy_sum, gY,
-                                          key);
+                            raw = rec_erp<RingG, EA>(ring, P, S, Lc, Y, Lc, band, J.g, gx_sum, gy_sum,
+                                                     gY, key, bound);
                         } else if constexpr (KIND == K_MSM)
-                            raw = rec_msm(ring, P, S, Lc, Y, Lc, band, J.c, key);
+                            raw = rec_msm<RingG, EA>(ring, P, S, Lc, Y, Lc, band, J.c, key, bound);
                         else
-                            raw = rec_twe<RingG, false>(ring, P, S, Lc, Y, Lc, band, J.penalty,
-                                                        J.stiffness, nullptr, J.stab, key);
+                            raw = rec_twe<RingG, false, EA>(ring, P, S, Lc, Y, Lc, band, J.penalty,
+                                                            J.stiffness, nullptr, J.stab, key,
+                                                            bound);
                         if (KIND == K_LCSS || KIND == K_WLCSS) d = 1.0 - raw / (double)Lc;
                         else if (KIND == K_EDR) d = raw / (double)Lc;
                         else if (KIND == K_ERP || KIND == K_MSM || KIND == K_TWE) d = raw;
@@ -490,6 +506,7 @@ int wb_argmin_subsequence_impl(const double *s, const int64_t *s_len, int64_t s_
     WB_TAKE(hval, double, ws, (size_t)n * k);
     J.heap_idx = hidx;
     J.heap_val = hval;
+    J.no_abandon = argmin_ea_disabled() ? 1 : 0;
     int64_t *oi = indices;
     double *od = distances;
     if (!out_on_device) {

@@ -145,7 +145,8 @@ int wb_argmin_subsequence_impl(const double *s, const int64_t *s_len, int64_t s_
 bool strip_supported(const ElasticJob &J);
 bool strip_forced();
 // WB_GPU_ARGMIN=all: argmin evaluates every candidate pair in full (no
-// early-abandoned chunks); WB_GPU_ARGMIN=<c>: first chunk of c candidates
+// early-abandoned chunks; argmin_subsequence: every window in full);
+// WB_GPU_ARGMIN=<c>: first chunk of c candidates
 // (default: enough pairs for every lane); WB_GPU_ARGMIN_FORM=strip: the
 // strip form of the chunks for any band.  All forms give the same results.
 bool argmin_ea_disabled();
