@@ -395,6 +395,54 @@ def bench_subsequence(args, dev, flush):
             "algorithmic_window_elements": elems, **res}
 
 
+def bench_subsequence_elastic(args, dev, flush):
+    """pairwise_subsequence_distance with elastic metrics (dtw r=0.1, dtw r=1,
+    lcss): 1,000 of the C3 shapelets against 100 series of length 1,024.
+    GCUPS over the algorithmic band cells of every window (abandoned cells
+    included in the count).  CPU: the oracle (the reference's sequential scan
+    with its early abandoning) on all host threads, one series."""
+    import torch
+
+    from oracle import oracle as O
+    from wildboar_gb300.distance import pairwise_subsequence_distance
+
+    X, shp = c3_data(100, 1000)
+    T = X.shape[1]
+    Xd = torch.as_tensor(X, device=dev)
+    res = {}
+    for name, metric, params in (("dtw_r0.1", "dtw", {"r": 0.1}), ("dtw_r1", "dtw", {"r": 1.0}),
+                                 ("lcss", "lcss", {"epsilon": 0.5})):
+        r = params.get("r", 1.0)
+        cells = X.shape[0] * sum((T - len(s) + 1) * band_cells(len(s), len(s), r) for s in shp)
+
+        def call():
+            return pairwise_subsequence_distance(shp, Xd, metric=metric, metric_params=params,
+                                                 return_index=True)
+        call()
+        torch.cuda.synchronize()
+        ms = _timed(call, 1, flush)
+        d, i = call()
+        n_threads = os.cpu_count() or 1
+        ns = 200  # CPU sample: the first 200 shapelets against the first series
+        cells_s = sum((T - len(s) + 1) * band_cells(len(s), len(s), r) for s in shp[:ns])
+        t0 = time.perf_counter()
+        od, oi = O.subsequence(shp[:ns], X[:1], metric=metric, metric_params=params,
+                               n_threads=n_threads)
+        cpu_s = time.perf_counter() - t0
+        res[name] = {
+            "ms": ms,
+            "gcups_algorithmic": cells / (ms * 1e-3) / 1e9,
+            "argmin_exact_on_sample": bool(np.array_equal(i[:1, :ns].cpu().numpy(), oi)),
+            "max_rel_err_on_sample": float(np.max(np.abs(d[:1, :ns].cpu().numpy() - od) /
+                                                  np.maximum(np.abs(od), 1e-300))),
+            "cpu_oracle": {"gcups_algorithmic": cells_s / cpu_s / 1e9,
+                           "cores": n_threads, "kind": "port",
+                           "sample": f"{ns} shapelets x 1 series"},
+        }
+    return {"config": f"{len(shp)} shapelets (L~U{{16..128}}, z-normalised random-walk "
+                      f"fragments) x {X.shape[0]} series, T={T}, float64", **res}
+
+
 def c6_data(n_series=4096, L=256, K=32, seed=5):
     """KMeans / barycenter inputs: float64 series from 32 sine / random-walk
     prototypes + N(0, 0.1), the prototype labels."""
@@ -797,6 +845,8 @@ def run_gpu(args):
             forms["ucr_lower_bounds"] = bench_ucr(args, dev, flush)
         if args.only in ("", "argmin"):
             forms["argmin_knn"] = bench_argmin(args, dev, flush)
+        if args.only in ("", "subseq_elastic"):
+            forms["subsequence_elastic"] = bench_subsequence_elastic(args, dev, flush)
         if rank == 0:
             print(json.dumps({"forms": forms}), flush=True)
         return
@@ -900,6 +950,7 @@ def run_gpu(args):
         forms["barycenter_kmeans"] = bench_barycenter(args, dev, flush)
         forms["ucr_lower_bounds"] = bench_ucr(args, dev, flush)
         forms["argmin_knn"] = bench_argmin(args, dev, flush)
+        forms["subsequence_elastic"] = bench_subsequence_elastic(args, dev, flush)
         forms["both_beat_fp64_drop_in"] = bool(
             forms["batched_fp32"]["gcups"] > value and forms["fwd_bwd_fp32"]["gcups"] > value)
     line = {
@@ -953,7 +1004,7 @@ def main():
                     help="only the FP32 forms (profiling captures)")
     ap.add_argument("--only", default="", choices=["", "batched", "fwdbwd", "subseq", "euclid",
                                                      "precision", "barycenter", "ucr",
-                                                     "argmin"],
+                                                     "argmin", "subseq_elastic"],
                     help="with --skip-fp64: run one form only")
     ap.add_argument("--c6-series", type=int, default=4096)
     ap.add_argument("--c7-series", type=int, default=200,
