@@ -224,3 +224,40 @@ def test_argmin_keyed_strip_sweep_vs_oracle(monkeypatch, metric, params):
     np.testing.assert_allclose(dist, odist, rtol=RTOL, atol=0)
     np.testing.assert_array_equal(idx, fidx)
     assert np.array_equal(dist.view(np.uint64), fdist.view(np.uint64))
+
+
+@pytest.mark.parametrize("metric,params", [("dtw", {"r": 0.2}), ("msm", {"c": 0.5}),
+                                           ("dtw", {"r": 1.0})])
+def test_argmin_ea_multivariate_dim_vs_oracle(monkeypatch, metric, params):
+    # (n, d, L) inputs (the reference's argmin accepts dim 0 only): the
+    # chunked kernels read dimension 0 through the series stride d * L
+    rng = np.random.default_rng(61)
+    X = _walk(rng, (7, 3, 130))
+    Y = _walk(rng, (90, 3, 130))
+    (idx, dist), (fidx, fdist) = _both(monkeypatch, 3, X, Y, k=4, metric=metric,
+                                       metric_params=params, dim=0)
+    oidx, odist = O.argmin(X[:, 0, :], Y[:, 0, :], k=4, metric=metric, metric_params=params)
+    np.testing.assert_array_equal(idx, oidx)
+    np.testing.assert_allclose(dist, odist, rtol=RTOL, atol=0)
+    np.testing.assert_array_equal(idx, fidx)
+    assert np.array_equal(dist.view(np.uint64), fdist.view(np.uint64))
+
+
+def test_argmin_ea_device_inputs(monkeypatch):
+    # torch device tensors (outputs stay on the device) through the chunks
+    rng = np.random.default_rng(62)
+    X = _walk(rng, (300, 96))
+    Y = _walk(rng, (700, 96))
+    Xd = torch.as_tensor(X, device="cuda")
+    Yd = torch.as_tensor(Y, device="cuda")
+    monkeypatch.setenv("WB_GPU_ARGMIN", "16")
+    idx, dist = argmin_distance(Xd, Yd, k=5, metric="dtw", metric_params={"r": 0.1},
+                                return_distance=True)
+    hidx, hdist = argmin_distance(X, Y, k=5, metric="dtw", metric_params={"r": 0.1},
+                                  return_distance=True)
+    np.testing.assert_array_equal(idx.cpu().numpy(), hidx)
+    assert np.array_equal(dist.cpu().numpy().view(np.uint64), hdist.view(np.uint64))
+    rows = [0, 150, 299]
+    oidx, odist = O.argmin(X[rows], Y, k=5, metric="dtw", metric_params={"r": 0.1})
+    np.testing.assert_array_equal(hidx[rows], oidx)
+    np.testing.assert_allclose(hdist[rows], odist, rtol=RTOL, atol=0)
