@@ -113,6 +113,18 @@ inline int compute_r(int64_t length, double r) {
 // the comparison runs on the integer pipe instead of the FP64 pipe.  Equal
 // values have equal bits, so the result is the value Cython's
 // "b < a ? b : a" would give.
+// Bit pattern of an epsilon compared with v = |x - y| (non-negative, never
+// NaN) on the integer pipe: v <= eps iff bits(v) <= eps_bits(eps), and the
+// same for <.  Negative doubles have negative patterns (never reached by v);
+// NaN, which no comparison satisfies, maps to -1.0 and -0.0 to +0.0 (equal
+// as doubles, different patterns).
+__device__ __forceinline__ long long eps_bits(double eps) {
+    if (isnan(eps)) eps = -1.0;
+    if (eps == 0.0) eps = 0.0;
+    return __double_as_longlong(eps);
+}
+__device__ __forceinline__ long long dbits_of(double v) { return __double_as_longlong(v); }
+
 __device__ __forceinline__ double nn_min(double a, double b) {
     long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
     return __longlong_as_double(ib < ia ? ib : ia);

@@ -162,6 +162,7 @@ __device__ double rec_lcss(R ring, int P, const double *__restrict__ X, int n,
     }
     if (mx < m) ring.st(mx % P, 0.0);
     double kmax = -INF;
+    const long long eb = eps_bits(eps);  // v <= eps on the integer pipe
     for (int i = 0; i < n; i++) {
         const int js = imax(0, i - mn - r + 1);
         const int je = imin(m, i + mx);
@@ -174,7 +175,7 @@ __device__ double rec_lcss(R ring, int P, const double *__restrict__ X, int n,
             double up = ring.ld(q);
             double v = fabs(xi - ldg(Y + j));
             double wt = W ? ldg(w + abs(i - j)) : 1.0;
-            double nv = (v <= eps) ? wt + diag : nn_max(left, up);
+            double nv = (dbits_of(v) <= eb) ? wt + diag : nn_max(left, up);
             ring.st(q, nv);
             rmin = nn_min(rmin, nv);
             diag = up;
@@ -204,6 +205,7 @@ __device__ double rec_edr(R ring, int P, const double *__restrict__ X, int n,
     }
     if (mx < m) ring.st(mx % P, 0.0);
     double kmax = -INF;
+    const long long eb = eps_bits(eps);  // v < eps on the integer pipe
     for (int i = 0; i < n; i++) {
         const int js = imax(0, i - mn - r + 1);
         const int je = imin(m, i + mx);
@@ -215,10 +217,10 @@ __device__ double rec_edr(R ring, int P, const double *__restrict__ X, int n,
         for (int j = js; j < je; j++) {
             double up = ring.ld(q);
             double v = fabs(xi - ldg(Y + j));
-            double a = diag + (v < eps ? 0.0 : 1.0);
-            double b = up + 1.0;
-            double c = left + 1.0;
-            double nv = nn_min(nn_min(a, b), c);
+            double a = diag + (dbits_of(v) < eb ? 0.0 : 1.0);
+            // min(up + 1, left + 1) == min(up, left) + 1 exactly (rounding is
+            // monotone and the same operand is added): one addition fewer
+            double nv = nn_min(a, nn_min(up, left) + 1.0);
             ring.st(q, nv);
             rmin = nn_min(rmin, nv);
             diag = up;

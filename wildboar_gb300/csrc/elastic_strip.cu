@@ -127,6 +127,7 @@ struct Kt {
 template <class A>
 struct PairCtx {
     typename A::E eps, g, pen, s2;
+    long long eb;                  // eps_bits(eps) (FP64 lcss / edr comparisons)
     float c;                       // msm cost
     typename A::V gx_sum, gy_sum;  // erp gap sums
     const double *gY;              // erp: |y_j - g| of the column series
@@ -183,13 +184,23 @@ __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
             E wt = A::el(1.0);
             if constexpr (KIND == K_WLCSS)
                 wt = weight<A>(C.w, (!MASK || k < valid) ? abs(d) : 0);
-            nv = (v <= C.eps) ? A::add(dg, wt) : A::vmax(lf, up);
+            bool match;
+            if constexpr (is_f64<A>()) match = dbits_of(v) <= C.eb;  // integer pipe
+            else match = v <= C.eps;
+            nv = match ? A::add(dg, wt) : A::vmax(lf, up);
         } else if constexpr (KIND == K_EDR) {
             const E v = A::absv(A::sub(Rw.x[k], yc));
-            const V a = A::add(dg, v < C.eps ? A::el(0.0) : A::el(1.0));
-            const V b = A::add(up, A::el(1.0));
-            const V cc = A::add(lf, A::el(1.0));
-            nv = A::vmin(A::vmin(a, b), cc);
+            if constexpr (is_f64<A>()) {
+                // the comparison on the integer pipe; min(up + 1, left + 1) ==
+                // min(up, left) + 1 exactly (monotone rounding, same operand)
+                const V a = A::add(dg, dbits_of(v) < C.eb ? 0.0 : 1.0);
+                nv = A::vmin(a, A::add(A::vmin(up, lf), 1.0));
+            } else {
+                const V a = A::add(dg, v < C.eps ? A::el(0.0) : A::el(1.0));
+                const V b = A::add(up, A::el(1.0));
+                const V cc = A::add(lf, A::el(1.0));
+                nv = A::vmin(A::vmin(a, b), cc);
+            }
         } else if constexpr (KIND == K_ERP) {
             const V a = A::add(dg, A::absv(A::sub(Rw.x[k], yc)));
             const V b = A::add(up, Rw.rx[k]);
@@ -493,10 +504,12 @@ __global__ void __launch_bounds__(kStripThreads)
     auto run = [&](int64_t rs, int64_t cs) -> double {
         if (J.all_zero) return 0.0;
         PairCtx<A> C;
-        C.eps = A::el(J.eps);
+        double epsd = J.eps;
         if constexpr (KIND == K_EDR) {
-            if (J.std_rows) C.eps = A::el(cy_max(J.std_rows[rs], J.std_cols[cs]) / 4.0);
+            if (J.std_rows) epsd = cy_max(J.std_rows[rs], J.std_cols[cs]) / 4.0;
         }
+        C.eps = A::el(epsd);
+        C.eb = eps_bits(epsd);
         C.g = A::el(J.g);
         C.pen = A::el(KIND == K_TWE ? J.penalty + J.stiffness : J.p);
         C.s2 = A::el(J.stiffness * 2.0);
@@ -580,6 +593,7 @@ __global__ void __launch_bounds__(kStripThreads)
             if constexpr (KIND == K_EDR) {
                 if (J.std_rows) C.eps = cy_max(J.std_rows[qi], J.std_cols[cj]) / 4.0;
             }
+            C.eb = eps_bits(C.eps);
             C.g = J.g;
             C.pen = KIND == K_TWE ? J.penalty + J.stiffness : J.p;
             C.s2 = J.stiffness * 2.0;
