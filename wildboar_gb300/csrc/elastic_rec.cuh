@@ -117,20 +117,21 @@ __device__ double rec_adtw(R ring, int P, const double *__restrict__ X, int n,
         const double xi = X[i];
         q = js % P;
         double diag = js > 0 ? ring.ld(wrap_dec(q, P)) : INF;
-        double left = INF;  // prev_cost + penalty with prev_cost = inf
+        double prev = INF;  // the left cell: prev_cost = inf before the band
         double rmin = INF;
         for (int j = js; j < je; j++) {
             double up = ring.ld(q);
-            double a = up + pen;
             double d = xi - ldg(Y + j);
+            // min(up + p, prev + p) == min(up, prev) + p exactly (rounding is
+            // monotone and the same operand is added): one addition per cell
             double mv;
-            if (NONNEG) mv = nn_min(nn_min(a, left), diag);
-            else mv = cy_min(cy_min(a, left), diag);
+            if (NONNEG) mv = nn_min(nn_min(up, prev) + pen, diag);
+            else mv = cy_min(cy_min(up, prev) + pen, diag);
             double nv = mv + d * d;
             ring.st(q, nv);
             rmin = NONNEG ? nn_min(rmin, nv) : (nv < rmin ? nv : rmin);
             diag = up;
-            left = nv + pen;
+            prev = nv;
             q = wrap_inc(q, P);
         }
         if (je < m) ring.st(q, INF);

@@ -172,12 +172,19 @@ __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
                 cst = A::mul(cst, weight<A>(C.w, (!MASK || k < valid) ? abs(d) : 0));
             nv = A::add(A::vmin(A::vmin(up, lf), dg), cst);
         } else if constexpr (KIND == K_ADTW || KIND == K_ADTW_ANY) {
-            const V a = A::add(up, C.pen);
-            const V l = A::add(lf, C.pen);
             const E v = A::sub(Rw.x[k], yc);
             V mv;
-            if constexpr (KIND == K_ADTW) mv = A::vmin(A::vmin(a, l), dg);
-            else mv = A::vmin_any(A::vmin_any(a, l), dg);
+            if constexpr (is_f64<A>()) {
+                // min(up + p, left + p) == min(up, left) + p exactly (monotone
+                // rounding, same operand): one addition fewer per cell
+                if constexpr (KIND == K_ADTW) mv = A::vmin(A::add(A::vmin(up, lf), C.pen), dg);
+                else mv = A::vmin_any(A::add(A::vmin_any(up, lf), C.pen), dg);
+            } else {
+                const V a = A::add(up, C.pen);
+                const V l = A::add(lf, C.pen);
+                if constexpr (KIND == K_ADTW) mv = A::vmin(A::vmin(a, l), dg);
+                else mv = A::vmin_any(A::vmin_any(a, l), dg);
+            }
             nv = A::add(mv, A::mul(v, v));
         } else if constexpr (KIND == K_LCSS || KIND == K_WLCSS) {
             const E v = A::absv(A::sub(Rw.x[k], yc));
