@@ -125,6 +125,17 @@ __device__ __forceinline__ long long eps_bits(double eps) {
 }
 __device__ __forceinline__ long long dbits_of(double v) { return __double_as_longlong(v); }
 
+// (double)m for a non-negative float, exact, on the integer pipe for zero and
+// normal floats (sign 0, exponent field e in 1..254: the double has exponent
+// field e + 1023 - 127 and the 23 mantissa bits shifted up by 29); subnormal,
+// infinite and NaN values go through the conversion instruction.
+__device__ __forceinline__ double f2d_nonneg(float m) {
+    const unsigned int u = __float_as_uint(m);
+    if (u - 0x00800000u >= 0x7f000000u && u != 0u) return (double)m;
+    const unsigned long long b = u ? ((unsigned long long)u << 29) + (896ull << 52) : 0ull;
+    return __longlong_as_double((long long)b);
+}
+
 __device__ __forceinline__ double nn_min(double a, double b) {
     long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
     return __longlong_as_double(ib < ia ? ib : ia);

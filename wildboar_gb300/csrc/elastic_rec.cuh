@@ -305,7 +305,7 @@ __device__ __forceinline__ double msm_cost(float x, float y, float z, float c) {
     if ((y <= x && x <= z) || (y >= x && x >= z)) return (double)c;
     float a = fabsf(__fsub_rn(x, y));
     float b = fabsf(__fsub_rn(x, z));
-    return (double)c + (double)(b < a ? b : a);
+    return (double)c + f2d_nonneg(b < a ? b : a);  // exact widening, integer pipe
 }
 
 // msm: msm_distance, distance/_elastic.pyx:1592-1647

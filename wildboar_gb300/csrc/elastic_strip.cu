@@ -105,7 +105,7 @@ __device__ __forceinline__ typename A::E msm_cost(float x, float y, float z, flo
     if ((y <= x && x <= z) || (y >= x && x >= z)) return (typename A::E)c;
     const float a = fabsf(__fsub_rn(x, y));
     const float b = fabsf(__fsub_rn(x, z));
-    if constexpr (is_f64<A>()) return (double)c + (double)(b < a ? b : a);
+    if constexpr (is_f64<A>()) return (double)c + f2d_nonneg(b < a ? b : a);  // exact widening
     else return __fadd_rn(c, b < a ? b : a);
 }
 
