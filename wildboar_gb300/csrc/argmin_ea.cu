@@ -106,9 +106,11 @@ argmin_ea_kernel(const ElasticJob J, const EaChunk C, int P) {
                 nv = nn_min(nn_min(up, left), diag) + (d * d) * ldg(J.weights + wi);
                 left = nv;
             } else {
-                const double a = up + J.p;
-                nv = nn_min(nn_min(a, left), diag) + d * d;
-                left = first ? nv : nv + J.p;
+                // left holds the previous cell; min(up + p, left + p) ==
+                // min(up, left) + p exactly; row 0 moves left without p
+                const double t = nn_min(up, left) + J.p;
+                nv = nn_min(first ? left : t, diag) + d * d;
+                left = nv;
             }
             ring.st(q, nv);
             rmin = nn_min(rmin, nv);
@@ -207,9 +209,10 @@ argmin_ea_strip_kernel(const ElasticJob J, const EaChunk C, double *ring_base, i
                     wi = in_band ? wi : 0;
                     nv = nn_min(nn_min(up, lf), dg) + (v * v) * ldg(J.weights + wi);
                 } else {
-                    const double a = up + J.p;
-                    const double l = (k == 0 && i0 == 0) ? lf : lf + J.p;
-                    nv = nn_min(nn_min(a, l), dg) + v * v;
+                    // min(up + p, lf + p) == min(up, lf) + p exactly; row 0
+                    // (up = +inf) moves left without p
+                    const double t = nn_min(up, lf) + J.p;
+                    nv = nn_min((k == 0 && i0 == 0) ? lf : t, dg) + v * v;
                 }
                 nv = in_band ? nv : INF;
                 rmin[k] = nn_min(rmin[k], nv);
