@@ -124,6 +124,11 @@ __device__ __forceinline__ long long eps_bits(double eps) {
     return __double_as_longlong(eps);
 }
 __device__ __forceinline__ long long dbits_of(double v) { return __double_as_longlong(v); }
+// bit pattern of |d|: clearing the sign bit is an integer operation, where a
+// stand-alone fabs could take an FP64 instruction
+__device__ __forceinline__ long long abs_bits(double d) {
+    return __double_as_longlong(d) & 0x7fffffffffffffffLL;
+}
 
 // (double)m for a non-negative float, exact, on the integer pipe for zero and
 // normal floats (sign 0, exponent field e in 1..254: the double has exponent

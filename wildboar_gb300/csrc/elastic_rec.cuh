@@ -174,9 +174,9 @@ __device__ double rec_lcss(R ring, int P, const double *__restrict__ X, int n,
         double rmin = INF;
         for (int j = js; j < je; j++) {
             double up = ring.ld(q);
-            double v = fabs(xi - ldg(Y + j));
+            const long long vb = abs_bits(xi - ldg(Y + j));  // |x - y| as bits
             double wt = W ? ldg(w + abs(i - j)) : 1.0;
-            double nv = (dbits_of(v) <= eb) ? wt + diag : nn_max(left, up);
+            double nv = (vb <= eb) ? wt + diag : nn_max(left, up);
             ring.st(q, nv);
             rmin = nn_min(rmin, nv);
             diag = up;
@@ -217,8 +217,8 @@ __device__ double rec_edr(R ring, int P, const double *__restrict__ X, int n,
         double rmin = INF;
         for (int j = js; j < je; j++) {
             double up = ring.ld(q);
-            double v = fabs(xi - ldg(Y + j));
-            double a = diag + (dbits_of(v) < eb ? 0.0 : 1.0);
+            const long long vb = abs_bits(xi - ldg(Y + j));  // |x - y| as bits
+            double a = diag + (vb < eb ? 0.0 : 1.0);
             // min(up + 1, left + 1) == min(up, left) + 1 exactly (rounding is
             // monotone and the same operand is added): one addition fewer
             double nv = nn_min(a, nn_min(up, left) + 1.0);

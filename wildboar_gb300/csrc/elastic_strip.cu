@@ -192,7 +192,7 @@ __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
             if constexpr (KIND == K_WLCSS)
                 wt = weight<A>(C.w, (!MASK || k < valid) ? abs(d) : 0);
             bool match;
-            if constexpr (is_f64<A>()) match = dbits_of(v) <= C.eb;  // integer pipe
+            if constexpr (is_f64<A>()) match = abs_bits(A::sub(Rw.x[k], yc)) <= C.eb;  // integer pipe
             else match = v <= C.eps;
             nv = match ? A::add(dg, wt) : A::vmax(lf, up);
         } else if constexpr (KIND == K_EDR) {
@@ -200,7 +200,7 @@ __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
             if constexpr (is_f64<A>()) {
                 // the comparison on the integer pipe; min(up + 1, left + 1) ==
                 // min(up, left) + 1 exactly (monotone rounding, same operand)
-                const V a = A::add(dg, dbits_of(v) < C.eb ? 0.0 : 1.0);
+                const V a = A::add(dg, abs_bits(A::sub(Rw.x[k], yc)) < C.eb ? 0.0 : 1.0);
                 nv = A::vmin(a, A::add(A::vmin(up, lf), 1.0));
             } else {
                 const V a = A::add(dg, v < C.eps ? A::el(0.0) : A::el(1.0));
