@@ -261,3 +261,39 @@ def test_argmin_ea_device_inputs(monkeypatch):
     oidx, odist = O.argmin(X[rows], Y, k=5, metric="dtw", metric_params={"r": 0.1})
     np.testing.assert_array_equal(hidx[rows], oidx)
     np.testing.assert_allclose(hdist[rows], odist, rtol=RTOL, atol=0)
+
+
+@pytest.mark.parametrize("metric,params,first", [("dtw", {"r": 0.2}, "5"), ("msm", {"c": 0.5}, "5"),
+                                                 ("lcss", {"epsilon": 0.5}, "all"),
+                                                 ("euclidean", {}, "all")])
+def test_argmin_query_batches(monkeypatch, metric, params, first):
+    # queries in several batches (a pair budget of 7 query rows of 150
+    # candidates), with a lower bound: the same result as one batch
+    rng = np.random.default_rng(63)
+    X = _walk(rng, (31, 64))
+    Y = _walk(rng, (150, 64))
+    lb = None
+    if metric == "dtw":
+        full = O.pairwise(X, Y, metric=metric, metric_params=params)
+        lb = full * rng.uniform(0.3, 1.02, size=full.shape)
+    monkeypatch.setenv("WB_GPU_ARGMIN", first)
+    monkeypatch.setenv("WB_GPU_ARGMIN_BATCH", str(7 * 150))
+    idx, dist = argmin_distance(X, Y, k=4, metric=metric, metric_params=params,
+                                lower_bound=lb, return_distance=True)
+    monkeypatch.delenv("WB_GPU_ARGMIN_BATCH")
+    sidx, sdist = argmin_distance(X, Y, k=4, metric=metric, metric_params=params,
+                                  lower_bound=lb, return_distance=True)
+    np.testing.assert_array_equal(idx, sidx)
+    assert np.array_equal(dist.view(np.uint64), sdist.view(np.uint64))
+    oidx, odist = O.argmin(X, Y, k=4, metric=metric, metric_params=params, lower_bound=lb)
+    np.testing.assert_array_equal(idx, oidx)
+    np.testing.assert_allclose(dist, odist, rtol=RTOL, atol=0)
+    if metric == "dtw":
+        Xd = torch.as_tensor(X, device="cuda")
+        Yd = torch.as_tensor(Y, device="cuda")
+        lbd = torch.as_tensor(lb, device="cuda")
+        monkeypatch.setenv("WB_GPU_ARGMIN_BATCH", str(7 * 150))
+        didx, ddist = argmin_distance(Xd, Yd, k=4, metric=metric, metric_params=params,
+                                      lower_bound=lbd, return_distance=True)
+        np.testing.assert_array_equal(didx.cpu().numpy(), idx)
+        assert np.array_equal(ddist.cpu().numpy().view(np.uint64), dist.view(np.uint64))

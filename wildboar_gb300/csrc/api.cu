@@ -612,8 +612,13 @@ extern "C" int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_
     ElasticJob J;
     WB_TRY(metric_fields(metric, params, xl, yl, true, J));
     Workspace ws(s);
-    const size_t pairs = (size_t)x->n * y->n;
-    SeriesSet probeR{nullptr, 0, x->n, xl}, probeC{nullptr, 0, y->n, yl};
+    // Queries go in batches whose (distance, key) matrices stay within 2 GiB:
+    // the reference keeps O(k) per query, so the whole (nx, ny) matrix is
+    // never needed at once (every query's candidate loop is independent).
+    const int64_t budget = argmin_pair_budget();
+    const int64_t batch = std::max<int64_t>(1, std::min<int64_t>(x->n, budget / y->n));
+    const size_t bpairs = (size_t)batch * y->n;
+    SeriesSet probeR{nullptr, 0, batch, xl}, probeC{nullptr, 0, y->n, yl};
     ElasticJob probe = J;
     probe.rows = probeR;
     probe.cols = probeC;
@@ -629,100 +634,114 @@ extern "C" int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_
     // early-abandoned chunks of candidates (argmin_ea.cu) where the metric
     // and band allow them: chunk sizes double from a first chunk that gives
     // every lane a few pairs, so the k-th distances tighten early
-    std::vector<int64_t> chunks;
-    size_t ea_ring_bytes = 0;
-    {
-        ElasticJob ea = probe;
-        ea.all_zero = derivative(metric) && std::min(xl, yl) < 3;
-        if (!argmin_ea_disabled() && argmin_ea_supported(ea)) {
-            ea_ring_bytes = argmin_ea_ring_bytes(ea);
-            // (rounded down: the first chunk abandons nothing, so its pairs
-            // take equally long and should fill whole rounds of lanes)
-            int64_t c = std::max<int64_t>(64, 4 * argmin_ea_lanes(ea) / x->n);
-            if (argmin_ea_first_chunk() > 0) c = argmin_ea_first_chunk();
-            if (!argmin_ea_chunked(ea)) c = y->n;  // one chunk without a bound
-            for (int64_t a = 0; a < y->n; c *= 2) {
-                chunks.push_back(a);
-                a = std::min<int64_t>(y->n, a + c);
-            }
-            chunks.push_back(y->n);
+    ElasticJob ea = probe;
+    ea.all_zero = derivative(metric) && std::min(xl, yl) < 3;
+    const bool use_ea = !argmin_ea_disabled() && argmin_ea_supported(ea);
+    const size_t ea_ring_bytes = use_ea ? argmin_ea_ring_bytes(ea) : 0;
+    constexpr int kMaxChunks = 64;  // doubling chunks of at most 2^31 candidates
+    auto schedule = [&](int64_t nq) {
+        std::vector<int64_t> chunks;
+        int64_t c = std::max<int64_t>(64, 4 * argmin_ea_lanes(ea) / nq);
+        if (argmin_ea_first_chunk() > 0) c = argmin_ea_first_chunk();
+        if (!argmin_ea_chunked(ea)) c = y->n;  // one chunk without a bound
+        for (int64_t a = 0; a < y->n; c *= 2) {
+            chunks.push_back(a);
+            a = std::min<int64_t>(y->n, a + c);
         }
-    }
-    const bool use_ea = !chunks.empty();
-    size_t need = stage_bytes(x) + stage_bytes(y) +
-                  table_bytes(metric, params, probeR, probeC, x->n, y->n, xl, yl) +
-                  (use_ea ? 0 : elastic_workspace_bytes(probe)) + 2 * align256(pairs * 8) +
-                  2 * align256((size_t)x->n * k * 8) +
-                  (lower_bound && !out_on_device ? align256(pairs * 8) : 0) +
-                  (out_on_device ? 0 : 2 * align256((size_t)x->n * k * 8)) +
-                  (use_ea ? 2 * align256((size_t)x->n * 8) + align256(chunks.size() * 8) +
-                                ea_ring_bytes
-                          : 0);
-    WB_TRY(ws.reserve(need));
+        chunks.push_back(y->n);
+        return chunks;
+    };
+    const size_t fixed = stage_bytes(x) + stage_bytes(y) +
+                         table_bytes(metric, params, SeriesSet{nullptr, 0, x->n, xl}, probeC,
+                                     x->n, y->n, xl, yl) +
+                         (out_on_device ? 0 : 2 * align256((size_t)x->n * k * 8));
+    const size_t per_batch =
+        (use_ea ? 0 : elastic_workspace_bytes(probe)) + 2 * align256(bpairs * 8) +
+        2 * align256((size_t)batch * k * 8) +
+        (lower_bound && !out_on_device ? align256(bpairs * 8) : 0) +
+        (use_ea ? 2 * align256((size_t)batch * 8) + align256(kMaxChunks * 8) + ea_ring_bytes
+                : 0);
+    WB_TRY(ws.reserve(fixed + per_batch));
     WB_TRY(stage(x, dim, ws, J.rows));
     WB_TRY(stage(y, dim, ws, J.cols));
     WB_TRY(build_tables(metric, params, J, ws, false, xl, yl));
-    WB_TAKE(D, double, ws, pairs);
-    WB_TAKE(K, double, ws, pairs);
-    J.out = D;
-    J.out_ld = y->n;
-    J.key = metric == WB_EUCLIDEAN ? nullptr : K;
-    J.mode = PM_ALL;
+    int64_t *hidx_all = out_on_device ? indices : ws.take<int64_t>((size_t)x->n * k);
+    double *hdist_all = out_on_device ? distances : ws.take<double>((size_t)x->n * k);
+    if (!hidx_all || !hdist_all) return fail(WB_ENOMEM, "workspace reservation exceeded");
     int never_push = 0;
     if (derivative(metric) && std::min(xl, yl) < 3) never_push = 1;
-    if (!never_push && !use_ea) WB_TRY(launch_elastic(J, ws, nullptr));
+    const size_t batch_mark = ws.mark();
+    if (use_ea) timer_begin("argmin_ea_kernel", s);
+    for (int64_t b0 = 0; b0 < x->n; b0 += batch) {
+        const int64_t nb = std::min<int64_t>(batch, x->n - b0);
+        const size_t pairs = (size_t)nb * y->n;
+        ws.rewind(batch_mark);
+        ElasticJob Jb = J;
+        Jb.rows.base = J.rows.base + b0 * J.rows.stride;
+        Jb.rows.count = nb;
+        if (J.std_rows) Jb.std_rows = J.std_rows + b0;
+        if (J.gsum_rows) Jb.gsum_rows = J.gsum_rows + b0;
+        WB_TAKE(D, double, ws, pairs);
+        WB_TAKE(K, double, ws, pairs);
+        Jb.out = D;
+        Jb.out_ld = y->n;
+        Jb.key = metric == WB_EUCLIDEAN ? nullptr : K;
+        Jb.mode = PM_ALL;
+        if (!never_push && !use_ea) WB_TRY(launch_elastic(Jb, ws, nullptr));
 
-    const double *lb = lower_bound;
-    if (lower_bound && !out_on_device) {
-        WB_TAKE(dlb, double, ws, pairs);
-        WB_CUDA(cudaMemcpyAsync(dlb, lower_bound, pairs * 8, cudaMemcpyHostToDevice, s));
-        lb = dlb;
-    }
-    ArgminJob A;
-    A.metric = metric;
-    A.nx = x->n;
-    A.ny = y->n;
-    A.k = k;
-    A.dist = D;
-    A.key = J.key;
-    A.lower_bound = lb;
-    A.xl = xl;
-    A.yl = yl;
-    A.never_push = never_push;
-    A.heap_idx = ws.take<int64_t>((size_t)x->n * k);
-    A.heap_val = ws.take<double>((size_t)x->n * k);
-    A.out_idx = out_on_device ? indices : ws.take<int64_t>((size_t)x->n * k);
-    A.out_dist = out_on_device ? distances : ws.take<double>((size_t)x->n * k);
-    if (!A.heap_idx || !A.heap_val || !A.out_idx || !A.out_dist)
-        return fail(WB_ENOMEM, "workspace reservation exceeded");
-    if (use_ea) {
-        A.state_n = ws.take<int64_t>(x->n);
-        A.state_dist = ws.take<double>(x->n);
-        auto *counters = ws.take<unsigned long long>(chunks.size());
-        double *ea_ring = ea_ring_bytes ? ws.take<double>(ea_ring_bytes / 8) : nullptr;
-        if (!A.state_n || !A.state_dist || !counters || (ea_ring_bytes && !ea_ring))
-            return fail(WB_ENOMEM, "workspace reservation exceeded");
-        WB_CUDA(cudaMemsetAsync(counters, 0, chunks.size() * 8, s));
-        WB_TRY(launch_fill(A.state_dist, HUGE_VAL, x->n, s));
-        timer_begin("argmin_ea_kernel", s);
-        for (size_t c = 0; c + 1 < chunks.size(); c++) {
-            const int64_t a = chunks[c], b = chunks[c + 1];
-            WB_TRY(launch_argmin_ea(J, metric, xl, yl, a, b - a, y->n, A.state_dist, lb,
-                                    counters + c, ea_ring, s));
-            A.j0 = a;
-            A.j1 = b;
-            A.resume = c > 0;
-            A.finish = c + 2 == chunks.size();
+        const double *lb = lower_bound ? lower_bound + (size_t)b0 * y->n : nullptr;
+        if (lower_bound && !out_on_device) {
+            WB_TAKE(dlb, double, ws, pairs);
+            WB_CUDA(cudaMemcpyAsync(dlb, lb, pairs * 8, cudaMemcpyHostToDevice, s));
+            lb = dlb;
+        }
+        ArgminJob A;
+        A.metric = metric;
+        A.nx = nb;
+        A.ny = y->n;
+        A.k = k;
+        A.dist = D;
+        A.key = Jb.key;
+        A.lower_bound = lb;
+        A.xl = xl;
+        A.yl = yl;
+        A.never_push = never_push;
+        A.heap_idx = ws.take<int64_t>((size_t)nb * k);
+        A.heap_val = ws.take<double>((size_t)nb * k);
+        A.out_idx = hidx_all + (size_t)b0 * k;
+        A.out_dist = hdist_all + (size_t)b0 * k;
+        if (!A.heap_idx || !A.heap_val) return fail(WB_ENOMEM, "workspace reservation exceeded");
+        if (use_ea && !never_push) {
+            const std::vector<int64_t> chunks = schedule(nb);
+            if ((int)chunks.size() > kMaxChunks + 1)
+                return fail(WB_EINVAL, "too many candidate chunks");
+            A.state_n = ws.take<int64_t>(nb);
+            A.state_dist = ws.take<double>(nb);
+            auto *counters = ws.take<unsigned long long>(kMaxChunks);
+            double *ea_ring = ea_ring_bytes ? ws.take<double>(ea_ring_bytes / 8) : nullptr;
+            if (!A.state_n || !A.state_dist || !counters || (ea_ring_bytes && !ea_ring))
+                return fail(WB_ENOMEM, "workspace reservation exceeded");
+            WB_CUDA(cudaMemsetAsync(counters, 0, kMaxChunks * 8, s));
+            WB_TRY(launch_fill(A.state_dist, HUGE_VAL, nb, s));
+            for (size_t c = 0; c + 1 < chunks.size(); c++) {
+                const int64_t a = chunks[c], b = chunks[c + 1];
+                WB_TRY(launch_argmin_ea(Jb, metric, xl, yl, a, b - a, y->n, A.state_dist, lb,
+                                        counters + c, ea_ring, s));
+                A.j0 = a;
+                A.j1 = b;
+                A.resume = c > 0;
+                A.finish = c + 2 == chunks.size();
+                WB_TRY(launch_argmin_replay(A, s));
+            }
+        } else {
             WB_TRY(launch_argmin_replay(A, s));
         }
-        timer_end(s);
-    } else {
-        WB_TRY(launch_argmin_replay(A, s));
     }
+    if (use_ea) timer_end(s);
     if (!out_on_device) {
-        WB_CUDA(cudaMemcpyAsync(indices, A.out_idx, (size_t)x->n * k * 8,
+        WB_CUDA(cudaMemcpyAsync(indices, hidx_all, (size_t)x->n * k * 8,
                                 cudaMemcpyDeviceToHost, s));
-        WB_CUDA(cudaMemcpyAsync(distances, A.out_dist, (size_t)x->n * k * 8,
+        WB_CUDA(cudaMemcpyAsync(distances, hdist_all, (size_t)x->n * k * 8,
                                 cudaMemcpyDeviceToHost, s));
         WB_CUDA(cudaStreamSynchronize(s));
     }

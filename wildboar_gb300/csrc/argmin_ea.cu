@@ -308,6 +308,12 @@ bool argmin_ea_disabled() {
     return e && strcmp(e, "all") == 0;
 }
 
+int64_t argmin_pair_budget() {
+    const char *e = getenv("WB_GPU_ARGMIN_BATCH");
+    const long long v = e ? atoll(e) : 0;
+    return v > 0 ? (int64_t)v : ((int64_t)1 << 27);  // 2 GiB of distances and keys
+}
+
 int64_t argmin_ea_first_chunk() {
     const char *e = getenv("WB_GPU_ARGMIN");
     if (!e) return 0;

@@ -75,6 +75,10 @@ class Workspace {
         return reinterpret_cast<T *>(p);
     }
     cudaStream_t stream() const { return stream_; }
+    // rewind to an earlier position: later takes reuse the memory, which is
+    // safe for work enqueued on this call's stream (it runs in order)
+    size_t mark() const { return arena_->used; }
+    void rewind(size_t m) { arena_->used = m; }
 
   private:
     Arena *arena_;

@@ -151,6 +151,9 @@ bool strip_forced();
 // strip form of the chunks for any band.  All forms give the same results.
 bool argmin_ea_disabled();
 int64_t argmin_ea_first_chunk();
+// pairs of one query batch of argmin_distance (WB_GPU_ARGMIN_BATCH=<pairs>
+// overrides the 2^27 default, for tests of the batching)
+int64_t argmin_pair_budget();
 size_t strip_workspace_bytes(const ElasticJob &J, bool fp32);
 int launch_strip(const ElasticJob &J, Workspace &ws, bool fp32);
 
