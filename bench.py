@@ -443,6 +443,72 @@ def bench_subsequence_elastic(args, dev, flush):
                       f"fragments) x {X.shape[0]} series, T={T}, float64", **res}
 
 
+def bench_subsequence_search(args, dev, flush):
+    """The subsequence search functions on 2,000 random-walk series of length
+    1,024: argmin_subsequence_distance (one length-64 query per series, taken
+    from it plus N(0, 1) noise, k=5), distance_profile and subsequence_match
+    (one length-64 pattern against every series).  End-to-end host timings of
+    the public calls (they return host arrays).  CPU: the oracle on all host
+    threads on a row sample."""
+    from oracle import oracle as O
+    from wildboar_gb300.distance import (argmin_subsequence_distance, distance_profile,
+                                         subsequence_match)
+
+    rng = np.random.default_rng(3)
+    n, T, L = 2000, 1024, 64
+    X = np.cumsum(rng.standard_normal((n, T)), axis=1)
+    starts = 100 + (np.arange(n) % 500)
+    Yq = np.stack([X[i, starts[i]:starts[i] + L] + rng.standard_normal(L) for i in range(n)])
+    pat = X[7, 300:300 + L].copy()
+    n_threads = os.cpu_count() or 1
+    rows = 32
+
+    def host_ms(fn, reps=3):
+        fn()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            out = fn()
+            ts.append((time.perf_counter() - t0) * 1e3)
+        return statistics.median(ts), out
+
+    res = {"config": f"{n} series, T={T}, queries / pattern of length {L}, float64"}
+    for metric, params in (("dtw", {"r": 0.1}), ("scaled_euclidean", {})):
+        ms, (idx, dist) = host_ms(lambda: argmin_subsequence_distance(
+            Yq, X, k=5, metric=metric, metric_params=params, return_distance=True))
+        t0 = time.perf_counter()
+        oi, od = O.argmin_subsequence(Yq[:rows], X[:rows], k=5, metric=metric,
+                                      metric_params=params, n_threads=n_threads)
+        cpu_ms = (time.perf_counter() - t0) * 1e3 * n / rows
+        res[f"argmin_subsequence_{metric}"] = {
+            "ms": ms, "exact_on_sample": bool(np.array_equal(idx[:rows], oi)),
+            "cpu_oracle_ms_extrapolated": cpu_ms,
+            "cpu_oracle": {"cores": n_threads, "kind": "port",
+                           "sample": f"{rows} pairs, scaled to {n}"}}
+    for metric, params in (("euclidean", {}), ("dtw", {"r": 0.1})):
+        ms, prof = host_ms(lambda: distance_profile(pat, X, metric=metric,
+                                                    metric_params=params))
+        t0 = time.perf_counter()
+        od, _ = O.subsequence_matches([pat] * rows, X[:rows], np.inf, metric=metric,
+                                      metric_params=params, transient=True,
+                                      n_threads=n_threads)
+        cpu_ms = (time.perf_counter() - t0) * 1e3 * n / rows
+        prof = np.asarray(prof)
+        res[f"distance_profile_{metric}"] = {
+            "ms": ms, "windows": int(prof.size),
+            "max_rel_err_on_sample": float(np.nanmax(np.abs(prof[:rows] - od[:, :prof.shape[1]]) /
+                                                     np.maximum(np.abs(od[:, :prof.shape[1]]),
+                                                                1e-300))),
+            "cpu_oracle_ms_extrapolated": cpu_ms}
+    thr = 12.0
+    ms, (midx, mdist) = host_ms(lambda: subsequence_match(
+        pat, X, thr, metric="dtw", metric_params={"r": 0.1}, return_distance=True))
+    res["subsequence_match_dtw"] = {
+        "ms": ms, "threshold": thr,
+        "matches": int(sum(0 if m is None else len(m) for m in midx))}
+    return res
+
+
 def c6_data(n_series=4096, L=256, K=32, seed=5):
     """KMeans / barycenter inputs: float64 series from 32 sine / random-walk
     prototypes + N(0, 0.1), the prototype labels."""
@@ -847,6 +913,8 @@ def run_gpu(args):
             forms["argmin_knn"] = bench_argmin(args, dev, flush)
         if args.only in ("", "subseq_elastic"):
             forms["subsequence_elastic"] = bench_subsequence_elastic(args, dev, flush)
+        if args.only in ("", "subseq_search"):
+            forms["subsequence_search"] = bench_subsequence_search(args, dev, flush)
         if rank == 0:
             print(json.dumps({"forms": forms}), flush=True)
         return
@@ -951,6 +1019,7 @@ def run_gpu(args):
         forms["ucr_lower_bounds"] = bench_ucr(args, dev, flush)
         forms["argmin_knn"] = bench_argmin(args, dev, flush)
         forms["subsequence_elastic"] = bench_subsequence_elastic(args, dev, flush)
+        forms["subsequence_search"] = bench_subsequence_search(args, dev, flush)
         forms["both_beat_fp64_drop_in"] = bool(
             forms["batched_fp32"]["gcups"] > value and forms["fwd_bwd_fp32"]["gcups"] > value)
     line = {
@@ -1004,7 +1073,8 @@ def main():
                     help="only the FP32 forms (profiling captures)")
     ap.add_argument("--only", default="", choices=["", "batched", "fwdbwd", "subseq", "euclid",
                                                      "precision", "barycenter", "ucr",
-                                                     "argmin", "subseq_elastic"],
+                                                     "argmin", "subseq_elastic",
+                                                     "subseq_search"],
                     help="with --skip-fp64: run one form only")
     ap.add_argument("--c6-series", type=int, default=4096)
     ap.add_argument("--c7-series", type=int, default=200,

@@ -302,3 +302,24 @@ def test_argmin_subsequence_long_scan_vs_oracle(monkeypatch, metric, params, sca
                                               scale=scale, return_distance=True)
     np.testing.assert_array_equal(idx, fidx)
     assert np.array_equal(np.asarray(dist).view(np.uint64), np.asarray(fdist).view(np.uint64))
+
+
+def test_transient_statistics_square_like_the_compiled_reference():
+    # _ts_view_update_statistics squares with `v ** 2`, which the C compiler
+    # folds to v * v; a libm pow may round differently for large values.  The
+    # scaled searches must match the oracle (gcc -O2, the same folding) bit
+    # for bit on such data.
+    rng = np.random.default_rng(71)
+    X = np.cumsum(rng.standard_normal((200, 260)), axis=1) * 1e6
+    Y = [rng.standard_normal(int(L)) * 1e6 for L in rng.integers(10, 60, size=200)]
+    idx, dist = argmin_subsequence_distance(Y, X, k=3, metric="scaled_euclidean",
+                                            return_distance=True)
+    oi, od = O.argmin_subsequence(Y, X, k=3, metric="scaled_euclidean")
+    np.testing.assert_array_equal(idx, oi)
+    assert np.array_equal(np.asarray(dist).view(np.uint64), od.view(np.uint64))
+    y = Y[0]
+    dp = distance_profile(y, X[:20], metric="scaled_euclidean")
+    od2, _ = O.subsequence_matches([y] * 20, X[:20], np.inf, metric="scaled_euclidean",
+                                   transient=True)
+    got = np.asarray(dp)
+    np.testing.assert_allclose(got, od2[:, :got.shape[1]], rtol=RTOL, atol=0)

@@ -97,6 +97,22 @@ def _transient_stats(s):
     return mean, (math.sqrt(var) if var > 1e-13 else 0.0)
 
 
+def _transient_stats_rows(S, lens):
+    """_transient_stats of rows S[i, :lens[i]] at once: np.cumsum sums left to
+    right like the reference's loop, and the square is v * v, which is what
+    ``current_value ** 2`` (Cython's pow(v, 2.0), folded by the C compiler)
+    computes -- a correctly rounded pow(v, 2) gives the same value."""
+    S = np.ascontiguousarray(S, dtype=np.float64)
+    lens = np.asarray(lens, dtype=np.int64)
+    rows = np.arange(S.shape[0])
+    ex = np.cumsum(S, axis=1)[rows, lens - 1]
+    ex2 = np.cumsum(S * S, axis=1)[rows, lens - 1]
+    mean = ex / lens
+    var = ex2 / lens - mean * mean
+    std = np.where(var > 1e-13, np.sqrt(np.where(var > 1e-13, var, 0.0)), 0.0)
+    return mean, std
+
+
 def _profile_raw(shapelets, X, dim, metric, transient=False):
     """(raw, key, lengths) of every window, pair i = (shapelets[i], x[i]).
 
@@ -106,9 +122,10 @@ def _profile_raw(shapelets, X, dim, metric, transient=False):
     packed, offs, lens, means, stds = _pack_shapelets(
         shapelets, metric.scaled or getattr(metric, "needs_std", False))
     if transient and means is not None:
-        st = [_transient_stats(s) for s in shapelets]
-        means = np.array([a for a, _ in st])
-        stds = np.array([b for _, b in st])
+        pad = np.zeros((len(shapelets), int(max(len(s) for s in shapelets))))
+        for i, sh in enumerate(shapelets):
+            pad[i, :len(sh)] = sh
+        means, stds = _transient_stats_rows(pad, [len(sh) for sh in shapelets])
     n = len(shapelets)
     T = X.shape[-1]
     ld = int(T - lens.min() + 1)
@@ -491,9 +508,7 @@ def argmin_subsequence_distance(y, x, *, dim=0, k=1, metric="euclidean", metric_
     n = S.shape[0]
     means = stds = None
     if scale:
-        st = [_transient_stats(S[i, : y_len[i]]) for i in range(n)]
-        means = np.array([a for a, _ in st])
-        stds = np.array([b for _, b in st])
+        means, stds = _transient_stats_rows(S, y_len)
     indices = np.zeros((n, k), dtype=np.int64)
     distances = np.zeros((n, k))
     sx = X.series()
