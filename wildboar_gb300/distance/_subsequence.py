@@ -84,24 +84,13 @@ def _check_option(options, key, name):
     raise ValueError(msg)
 
 
-def _transient_stats(s):
-    """Mean and std of a subsequence as _ts_view_update_statistics computes
-    them (distance/_cdistance.pyx:167-185): sequential sums, libm pow, std 0
-    when the variance is <= 1e-13."""
-    ex = ex2 = 0.0
-    for v in s.tolist():
-        ex += v
-        ex2 += math.pow(v, 2.0)
-    mean = ex / len(s)
-    var = ex2 / len(s) - mean * mean
-    return mean, (math.sqrt(var) if var > 1e-13 else 0.0)
-
-
 def _transient_stats_rows(S, lens):
-    """_transient_stats of rows S[i, :lens[i]] at once: np.cumsum sums left to
-    right like the reference's loop, and the square is v * v, which is what
-    ``current_value ** 2`` (Cython's pow(v, 2.0), folded by the C compiler)
-    computes -- a correctly rounded pow(v, 2) gives the same value."""
+    """Mean and std of the rows S[i, :lens[i]] as _ts_view_update_statistics
+    computes them (distance/_cdistance.pyx:167-185): sequential sums (np.cumsum
+    adds left to right like the reference's loop), std 0 when the variance is
+    <= 1e-13.  The square is v * v: ``current_value ** 2`` is Cython's
+    pow(v, 2.0), which the C compiler folds to v * v (a libm pow may round
+    differently for large values)."""
     S = np.ascontiguousarray(S, dtype=np.float64)
     lens = np.asarray(lens, dtype=np.int64)
     rows = np.arange(S.shape[0])
@@ -111,6 +100,13 @@ def _transient_stats_rows(S, lens):
     var = ex2 / lens - mean * mean
     std = np.where(var > 1e-13, np.sqrt(np.where(var > 1e-13, var, 0.0)), 0.0)
     return mean, std
+
+
+def _transient_stats(s):
+    """_transient_stats_rows of one subsequence: (mean, std) as floats."""
+    s = np.asarray(s, dtype=np.float64).ravel()
+    mean, std = _transient_stats_rows(s[None, :], [s.shape[0]])
+    return float(mean[0]), float(std[0])
 
 
 def _profile_raw(shapelets, X, dim, metric, transient=False):

@@ -14,7 +14,7 @@ import numpy as np
 
 from .. import _lib
 from ._distance import _as_input, check_metric, check_subsequence_metric
-from ._subsequence import _transient_stats
+from ._subsequence import _transient_stats_rows
 
 _vp = ctypes.c_void_p
 _i64 = ctypes.c_int64
@@ -83,9 +83,10 @@ def subsequence_distance_views(x, views, target=None, *, dim=0, metric="euclidea
     Metric_ = check_subsequence_metric(metric)
     m = Metric_(**(metric_params or {}))
     host = X.arr.detach().cpu().numpy() if X.device else X.arr
-    stats = [_transient_stats(host[v[0], v[1], v[2]:v[2] + v[3]]) for v in views]
-    means = np.array([a for a, _ in stats])
-    stds = np.array([b for _, b in stats])
+    pad = np.zeros((views.shape[0], int(views[:, 3].max()) if views.shape[0] else 1))
+    for i, v in enumerate(views):
+        pad[i, :v[3]] = host[v[0], v[1], v[2]:v[2] + v[3]]
+    means, stds = _transient_stats_rows(pad, views[:, 3])
     vs = [np.ascontiguousarray(views[:, k]) for k in range(4)]
     dev = T.device
     if dev:
