@@ -57,7 +57,9 @@ static idx_t compute_r(idx_t length, double r)
     return (idx_t)(v > 1.0 ? v : 1.0);
 }
 
-/* fast_mean_std: utils/_stats.pyx:22-42 (ex2 accumulates libm pow(x, 2.0)) */
+/* fast_mean_std: utils/_stats.pyx:22-42.  ex2 accumulates pow(x, 2.0), the
+ * call Cython emits for `x ** 2`; gcc -O2 folds it into x * x here as in the
+ * reference's own build. */
 static void fast_mean_std(const double *x, idx_t n, double *mean, double *std)
 {
     double ex = 0, ex2 = 0;

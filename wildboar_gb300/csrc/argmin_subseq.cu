@@ -14,7 +14,8 @@
 // the reference's pushes and heap exactly.
 //
 // Scaled: the subsequence is z-normalised with its own statistics (computed
-// on the host with libm pow, as fast_mean_std does) and every window with the
+// on the host, sequential sums of v and v * v, as the compiled fast_mean_std
+// does) and every window with the
 // IncStats mean / std sequence of its series (utils/_stats.pyx:45-93), which a
 // prepass reproduces per series; normalised windows (or their slopes for the
 // derivative metrics) are materialised per batch of pairs.
@@ -54,7 +55,8 @@ struct ArgminSubseqJob {
     int no_abandon = 0;           // evaluate every window in full (WB_GPU_ARGMIN=all)
 };
 
-// fast_mean_std, utils/_stats.pyx:22-42 (x*x where the reference calls pow)
+// fast_mean_std, utils/_stats.pyx:22-42 (x*x: the reference's pow(x, 2.0) is
+// folded into a multiplication by its C compiler)
 __device__ __forceinline__ double row_std(const double *x, int n) {
     double ex = 0, ex2 = 0;
     for (int i = 0; i < n; i++) {
