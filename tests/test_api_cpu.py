@@ -211,3 +211,25 @@ def test_sharded_requires_process_group():
 
     with pytest.raises(ValueError):
         sharded.shard_bounds(3, -1, 2)
+
+
+def test_transient_statistics_match_the_oracle_bitwise():
+    # the host helper of the subsequence searches against the oracle's C
+    # fast_mean_std (gcc -O2: pow(v, 2.0) folded into v * v, as in the
+    # reference's build), on ragged rows with large values and constant rows
+    from oracle import oracle as O
+    from wildboar_gb300.distance._subsequence import _transient_stats_rows
+
+    rng = np.random.default_rng(5)
+    n, width = 400, 90
+    lens = rng.integers(1, width + 1, size=n)
+    S = np.zeros((n, width))
+    for i in range(n):
+        S[i, :lens[i]] = rng.standard_normal(lens[i]) * rng.choice([1e-9, 1.0, 1e6, 3e12])
+    S[5, :lens[5]] = 2.5          # constant: std 0
+    S[6, :lens[6]] = 0.0
+    mean, std = _transient_stats_rows(S, lens)
+    for i in range(n):
+        om, os_ = O.fast_mean_std(S[i, :lens[i]])
+        assert np.float64(om).view(np.uint64) == mean[i].view(np.uint64), i
+        assert np.float64(os_).view(np.uint64) == std[i].view(np.uint64), i
