@@ -430,11 +430,13 @@ __device__ double rec_twe(R ring, int P, const double *__restrict__ X, int n,
         for (int j = js; j < je; j++) {
             double up = ring.ld(q);
             const double yj = ldg(Y + j);
-            double del_x = (up + dxi) + pen;
             const double dyj = DYTAB ? ldg(dY + j) : fabs(yp - yj);
-            double del_y = (left + dyj) + pen;
+            // min((up + dxi) + pen, (left + dyj) + pen) equals
+            // min(up + dxi, left + dyj) + pen exactly (rounding is monotone and
+            // the same operand is added last): one addition fewer per cell
+            double del = nn_min(up + dxi, left + dyj) + pen;
             double match = ((upleft + fabs(xi - yj)) + fabs(xp - yp)) + ldg(stab + abs(i - j));
-            double nv = nn_min(nn_min(del_x, del_y), match);
+            double nv = nn_min(del, match);
             ring.st(q, nv);
             rmin = nn_min(rmin, nv);
             upleft = up;

@@ -219,8 +219,14 @@ __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
             const V e = A::add(lf, msm_cost<A>(ycf, Rw.xf[k], ypf, C.c));
             nv = A::vmin(A::vmin(a, b), e);
         } else {  // K_TWE
-            const V del_x = A::add(A::add(up, Rw.rx[k]), C.pen);
-            const V del_y = A::add(A::add(lf, colv), C.pen);
+            V del;
+            if constexpr (is_f64<A>()) {
+                // min((up + dx) + pen, (lf + dy) + pen) == min(up + dx, lf + dy) + pen
+                // exactly (monotone rounding, the same operand added last)
+                del = A::add(A::vmin(A::add(up, Rw.rx[k]), A::add(lf, colv)), C.pen);
+            } else {
+                del = A::vmin(A::add(A::add(up, Rw.rx[k]), C.pen), A::add(A::add(lf, colv), C.pen));
+            }
             E st;
             if constexpr (is_f64<A>())
                 st = __ldg(C.stab + ((!MASK || k < valid) ? abs(d) : 0));
@@ -229,7 +235,7 @@ __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
             const V match = A::add(
                 A::add(A::add(dg, A::absv(A::sub(Rw.x[k], yc))), A::absv(A::sub(Rw.px[k], yp))),
                 st);
-            nv = A::vmin(A::vmin(del_x, del_y), match);
+            nv = A::vmin(del, match);
         }
         if (MASK) {
             if (d > hi) {
