@@ -218,10 +218,14 @@ __device__ double rec_edr(R ring, int P, const double *__restrict__ X, int n,
         for (int j = js; j < je; j++) {
             double up = ring.ld(q);
             const long long vb = abs_bits(xi - ldg(Y + j));  // |x - y| as bits
-            double a = diag + (vb < eb ? 0.0 : 1.0);
-            // min(up + 1, left + 1) == min(up, left) + 1 exactly (rounding is
-            // monotone and the same operand is added): one addition fewer
-            double nv = nn_min(a, nn_min(up, left) + 1.0);
+            // The three moves add 0 or 1 to diag, 1 to up and left.  Rounding is
+            // monotone, so min(a + 1, b + 1) == min(a, b) + 1 exactly: a match
+            // gives min(diag, min(up, left) + 1), a mismatch
+            // min(diag, up, left) + 1 -- one addition per cell either way.
+            const bool match = vb < eb;
+            const double mul = nn_min(up, left);
+            const double r = (match ? mul : nn_min(diag, mul)) + 1.0;
+            double nv = match ? nn_min(diag, r) : r;
             ring.st(q, nv);
             rmin = nn_min(rmin, nv);
             diag = up;

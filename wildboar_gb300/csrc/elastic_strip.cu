@@ -198,10 +198,13 @@ __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
         } else if constexpr (KIND == K_EDR) {
             const E v = A::absv(A::sub(Rw.x[k], yc));
             if constexpr (is_f64<A>()) {
-                // the comparison on the integer pipe; min(up + 1, left + 1) ==
-                // min(up, left) + 1 exactly (monotone rounding, same operand)
-                const V a = A::add(dg, abs_bits(A::sub(Rw.x[k], yc)) < C.eb ? 0.0 : 1.0);
-                nv = A::vmin(a, A::add(A::vmin(up, lf), 1.0));
+                // the comparison on the integer pipe; min(a + 1, b + 1) ==
+                // min(a, b) + 1 exactly (monotone rounding): a match gives
+                // min(dg, min(up, lf) + 1), a mismatch min(dg, up, lf) + 1
+                const bool match = abs_bits(A::sub(Rw.x[k], yc)) < C.eb;
+                const V mul = A::vmin(up, lf);
+                const V r = A::add(match ? mul : A::vmin(dg, mul), 1.0);
+                nv = match ? A::vmin(dg, r) : r;
             } else {
                 const V a = A::add(dg, v < C.eps ? A::el(0.0) : A::el(1.0));
                 const V b = A::add(up, A::el(1.0));
