@@ -174,17 +174,11 @@ __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
         } else if constexpr (KIND == K_ADTW || KIND == K_ADTW_ANY) {
             const E v = A::sub(Rw.x[k], yc);
             V mv;
-            if constexpr (is_f64<A>()) {
-                // min(up + p, left + p) == min(up, left) + p exactly (monotone
-                // rounding, same operand): one addition fewer per cell
-                if constexpr (KIND == K_ADTW) mv = A::vmin(A::add(A::vmin(up, lf), C.pen), dg);
-                else mv = A::vmin_any(A::add(A::vmin_any(up, lf), C.pen), dg);
-            } else {
-                const V a = A::add(up, C.pen);
-                const V l = A::add(lf, C.pen);
-                if constexpr (KIND == K_ADTW) mv = A::vmin(A::vmin(a, l), dg);
-                else mv = A::vmin_any(A::vmin_any(a, l), dg);
-            }
+            // min(up + p, left + p) == min(up, left) + p (monotone rounding, the
+            // same operand): one (compensated) addition fewer per cell; exact in
+            // FP64, within the compensated form's error in FP32
+            if constexpr (KIND == K_ADTW) mv = A::vmin(A::add(A::vmin(up, lf), C.pen), dg);
+            else mv = A::vmin_any(A::add(A::vmin_any(up, lf), C.pen), dg);
             nv = A::add(mv, A::mul(v, v));
         } else if constexpr (KIND == K_LCSS || KIND == K_WLCSS) {
             const E v = A::absv(A::sub(Rw.x[k], yc));
@@ -206,10 +200,12 @@ __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
                 const V r = A::add(match ? mul : A::vmin(dg, mul), 1.0);
                 nv = match ? A::vmin(dg, r) : r;
             } else {
-                const V a = A::add(dg, v < C.eps ? A::el(0.0) : A::el(1.0));
-                const V b = A::add(up, A::el(1.0));
-                const V cc = A::add(lf, A::el(1.0));
-                nv = A::vmin(A::vmin(a, b), cc);
+                // the same one-addition form (edit counts are small integers,
+                // exact in FP32)
+                const bool match = v < C.eps;
+                const V mul = A::vmin(up, lf);
+                const V r = A::add(match ? mul : A::vmin(dg, mul), A::el(1.0));
+                nv = match ? A::vmin(dg, r) : r;
             }
         } else if constexpr (KIND == K_ERP) {
             const V a = A::add(dg, A::absv(A::sub(Rw.x[k], yc)));
@@ -222,14 +218,9 @@ __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
             const V e = A::add(lf, msm_cost<A>(ycf, Rw.xf[k], ypf, C.c));
             nv = A::vmin(A::vmin(a, b), e);
         } else {  // K_TWE
-            V del;
-            if constexpr (is_f64<A>()) {
-                // min((up + dx) + pen, (lf + dy) + pen) == min(up + dx, lf + dy) + pen
-                // exactly (monotone rounding, the same operand added last)
-                del = A::add(A::vmin(A::add(up, Rw.rx[k]), A::add(lf, colv)), C.pen);
-            } else {
-                del = A::vmin(A::add(A::add(up, Rw.rx[k]), C.pen), A::add(A::add(lf, colv), C.pen));
-            }
+            // min((up + dx) + pen, (lf + dy) + pen) == min(up + dx, lf + dy) + pen
+            // (monotone rounding, the same operand added last): exact in FP64
+            const V del = A::add(A::vmin(A::add(up, Rw.rx[k]), A::add(lf, colv)), C.pen);
             E st;
             if constexpr (is_f64<A>())
                 st = __ldg(C.stab + ((!MASK || k < valid) ? abs(d) : 0));
