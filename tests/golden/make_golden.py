@@ -523,6 +523,24 @@ def main():
              "mapping": dtw_mapping(ha, hc, r=r),
              "walign": np.where(wmask, wal, 0.0)})
 
+    # argmin over long candidate lists: the reference's abandoning and heap over
+    # hundreds of candidates, with near matches late in the scan
+    LONG = [("dtw", {"r": 0.1}, 64), ("dtw", {"r": 1.0}, 170), ("wdtw", {"g": 0.05}, 64),
+            ("adtw", {"p": 0.5, "r": 0.2}, 64), ("edr", {}, 64), ("erp", {"g": 0.1}, 64),
+            ("msm", {"c": 0.5}, 64), ("twe", {"penalty": 0.5, "stiffness": 0.01}, 64),
+            ("lcss", {"epsilon": 0.5}, 64), ("ddtw", {"r": 0.3}, 64)]
+    for ci, (metric, params, L) in enumerate(LONG):
+        Q = _walk(rng, (12, L))
+        C = _walk(rng, (400, L))
+        for t, q in enumerate((2, 5, 9)):
+            C[300 + 30 * t] = Q[q] + 0.02 * rng.standard_normal(L)
+        for k in (1, 5):
+            idx, dist = argmin_distance(Q, C, k=k, metric=metric, metric_params=params,
+                                        return_distance=True)
+            add(f"argmin_long_k{k}_{metric}_{ci}", "argmin", {"x": Q, "y": C},
+                {"metric": metric, "metric_params": params, "k": k},
+                {"idx": idx, "dist": dist})
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"reference_version": getattr(wildboar, "__version__", "?"),

@@ -297,3 +297,22 @@ def test_argmin_query_batches(monkeypatch, metric, params, first):
                                       lower_bound=lbd, return_distance=True)
         np.testing.assert_array_equal(didx.cpu().numpy(), idx)
         assert np.array_equal(ddist.cpu().numpy().view(np.uint64), dist.view(np.uint64))
+
+
+def _golden_argmin_cases():
+    from tests import _golden
+    return [c for c in _golden.cases("argmin") if c["name"].startswith("argmin_long_")]
+
+
+@pytest.mark.parametrize("case", _golden_argmin_cases(), ids=lambda c: c["name"])
+@pytest.mark.parametrize("first", ["3", "40", "all"])
+def test_argmin_long_golden_chunked(monkeypatch, case, first):
+    # the reference's own outputs over 400 candidates (golden fixtures),
+    # through forced small chunks, larger chunks and the all-pairs form
+    a = case["args"]
+    inp = case["inputs"]
+    monkeypatch.setenv("WB_GPU_ARGMIN", first)
+    idx, dist = argmin_distance(inp["x"], inp["y"], k=a["k"], metric=a["metric"],
+                                metric_params=a.get("metric_params"), return_distance=True)
+    np.testing.assert_array_equal(idx, case["outputs"]["idx"])
+    np.testing.assert_allclose(dist, case["outputs"]["dist"], rtol=RTOL, atol=0)
