@@ -233,3 +233,37 @@ def test_transient_statistics_match_the_oracle_bitwise():
         om, os_ = O.fast_mean_std(S[i, :lens[i]])
         assert np.float64(om).view(np.uint64) == mean[i].view(np.uint64), i
         assert np.float64(os_).view(np.uint64) == std[i].view(np.uint64), i
+
+
+@pytest.mark.parametrize("mid", [0, 1, 2, 5, 6, 7, 8, 9, 10, 11, 33])
+@pytest.mark.parametrize("threshold", [0.5, 3.0, float("inf")])
+def test_subsequence_match_filter_all_pairs_at_once(mid, threshold):
+    # the vectorised post-filter of subsequence_match against the per-pair
+    # filter it replaces, on synthetic (raw, key) profiles with ragged lengths
+    from wildboar_gb300.distance import _subsequence as S
+
+    rng = np.random.default_rng(mid + int(threshold) if threshold < 1e9 else mid + 99)
+    T, n = 60, 9
+    lens = rng.integers(3, 20, size=n)
+    ld = int(T - lens.min() + 1)
+    raw = np.abs(rng.standard_normal((n, ld))) * 4
+    key = raw * rng.uniform(0.2, 1.5, size=raw.shape)
+    if mid == 5:
+        raw -= 1.0  # adtw may go negative
+    for i in range(n):
+        raw[i, T - lens[i] + 1:] = np.nan
+        key[i, T - lens[i] + 1:] = np.nan
+    got_i, got_d = S._matches_from_profile(mid, raw, key, lens, T, threshold)
+    for i in range(n):
+        L = int(lens[i])
+        nwin = T - L + 1
+        r, k = raw[i, :nwin], key[i, :nwin]
+        d = S._distances(mid, r, L)
+        keep = S._match_mask(mid, r, k, d, L, T, threshold)
+        idx = np.flatnonzero(keep)
+        if idx.size == 0:
+            assert got_i[i] is None and got_d[i] is None
+        else:
+            np.testing.assert_array_equal(got_i[i], idx)
+            assert np.array_equal(got_d[i].view(np.uint64),
+                                  np.asarray(d[keep], dtype=np.double).view(np.uint64))

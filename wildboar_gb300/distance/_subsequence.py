@@ -173,26 +173,44 @@ def _match_mask(metric_id, raw, key, dist, L, T, t):
         return ~(key > t) & (raw <= t)
 
 
-def _matches(shapelets, X, dim, metric, threshold):
-    """Per pair: (indices, distances) arrays or None, as _subsequence_match."""
-    raw, key, lens = _profile_raw(shapelets, X, dim, metric)
-    T = X.shape[-1]
-    mid = metric.metric_id
+def _matches_from_profile(mid, raw, key, lens, T, threshold):
+    """Per pair: (indices, distances) arrays or None, from every window's raw
+    value and abandon key; all pairs at once (a pair's windows past its last
+    one are excluded explicitly)."""
+    n, ld = raw.shape
+    lens = np.asarray(lens, dtype=np.int64)
+    Lc = lens.astype(np.float64)[:, None]
+    d = _distances(mid, raw, Lc)
+    if mid == _EDR:
+        keep = _match_mask_edr(raw, key, d, Lc, T, threshold)
+    else:
+        keep = _match_mask(mid, raw, key, d, Lc, T, threshold)
+    keep &= np.arange(ld)[None, :] < (T - lens + 1)[:, None]
+    rows, cols = np.nonzero(keep)
+    vals = d[rows, cols]
+    bounds = np.searchsorted(rows, np.arange(n + 1))
     out_i, out_d = [], []
-    for i in range(len(shapelets)):
-        L = int(lens[i])
-        nwin = T - L + 1
-        r, k = raw[i, :nwin], key[i, :nwin]
-        d = _distances(mid, r, L)
-        keep = _match_mask(mid, r, k, d, L, T, threshold)
-        idx = np.flatnonzero(keep).astype(np.intp)
-        if idx.size == 0:
+    for i in range(n):
+        a, b = bounds[i], bounds[i + 1]
+        if a == b:
             out_i.append(None)
             out_d.append(None)
         else:
-            out_i.append(idx)
-            out_d.append(np.asarray(d[keep], dtype=np.double))
+            out_i.append(cols[a:b].astype(np.intp))
+            out_d.append(np.asarray(vals[a:b], dtype=np.double))
     return out_i, out_d
+
+
+def _match_mask_edr(raw, key, dist, L, T, t):
+    """_match_mask for edr with per-row lengths L (an (n, 1) array)."""
+    with np.errstate(invalid="ignore"):
+        return ~(key > t * np.maximum(L, T)) & (dist <= t)
+
+
+def _matches(shapelets, X, dim, metric, threshold):
+    """Per pair: (indices, distances) arrays or None, as _subsequence_match."""
+    raw, key, lens = _profile_raw(shapelets, X, dim, metric)
+    return _matches_from_profile(metric.metric_id, raw, key, lens, X.shape[-1], threshold)
 
 
 def _any_in_exclude(lst, i, exclude):
