@@ -267,3 +267,18 @@ def test_subsequence_match_filter_all_pairs_at_once(mid, threshold):
             np.testing.assert_array_equal(got_i[i], idx)
             assert np.array_equal(got_d[i].view(np.uint64),
                                   np.asarray(d[keep], dtype=np.double).view(np.uint64))
+
+
+def test_shapelet_statistics_grouped_by_length_bitwise():
+    # ScaledSubsequenceMetric.from_array takes np.mean / np.std per shapelet;
+    # the host computes them once per distinct length over stacked rows
+    from wildboar_gb300.distance._distance import _shapelet_stats
+
+    rng = np.random.default_rng(8)
+    shp = [np.cumsum(rng.standard_normal(int(L))) * rng.choice([1e-6, 1.0, 1e7])
+           for L in rng.integers(1, 300, size=700)]
+    lens = np.array([len(s) for s in shp])
+    mean, std = _shapelet_stats(shp, lens)
+    for i, s in enumerate(shp):
+        assert np.mean(s).view(np.uint64) == mean[i].view(np.uint64), i
+        assert np.std(s).view(np.uint64) == std[i].view(np.uint64), i

@@ -436,6 +436,47 @@ def _is_arraylike(x):
     return hasattr(x, "__len__") or hasattr(x, "shape") or hasattr(x, "__array__")
 
 
+_GROUPED_STATS_OK = None
+
+
+def _grouped_stats_ok():
+    """Whether np.mean / np.std over the rows of a stacked (count, L) array
+    give, bit for bit, the values of one call per row (numpy reduces every
+    contiguous row with the same pairwise sum); checked once per process."""
+    global _GROUPED_STATS_OK
+    if _GROUPED_STATS_OK is None:
+        rng = np.random.default_rng(12345)
+        ok = True
+        for L in (1, 7, 8, 9, 16, 33, 100, 128, 129, 300):
+            A = rng.standard_normal((5, L)) * 1e3 + 7.0
+            m, sd = np.mean(A, axis=1), np.std(A, axis=1)
+            for i in range(5):
+                ok &= bool(np.mean(A[i]).view(np.uint64) == m[i].view(np.uint64))
+                ok &= bool(np.std(A[i]).view(np.uint64) == sd[i].view(np.uint64))
+        _GROUPED_STATS_OK = ok
+    return _GROUPED_STATS_OK
+
+
+def _shapelet_stats(shapelets, lens):
+    """np.mean / np.std of every shapelet (ScaledSubsequenceMetric.from_array,
+    distance/_cdistance.pyx:453-467), one reduction per distinct length."""
+    n = len(shapelets)
+    # other dtypes reduce in their own precision: keep one call per shapelet
+    all_f64 = all(getattr(s, "dtype", None) == np.float64 for s in shapelets)
+    if n < 64 or not all_f64 or not _grouped_stats_ok():
+        means = np.array([np.mean(s) for s in shapelets], dtype=np.float64)
+        stds = np.array([np.std(s) for s in shapelets], dtype=np.float64)
+        return means, stds
+    means = np.empty(n)
+    stds = np.empty(n)
+    for L in np.unique(lens):
+        rows = np.flatnonzero(lens == L)
+        A = np.stack([np.ravel(shapelets[i]) for i in rows])
+        means[rows] = np.mean(A, axis=1)
+        stds[rows] = np.std(A, axis=1)
+    return means, stds
+
+
 def _pack_shapelets(shapelets, scaled):
     lens = np.array([s.shape[0] for s in shapelets], dtype=np.int64)
     offs = np.zeros(len(shapelets), dtype=np.int64)
@@ -445,8 +486,7 @@ def _pack_shapelets(shapelets, scaled):
                                   dtype=np.float64)
     if scaled:
         # ScaledSubsequenceMetric.from_array: distance/_cdistance.pyx:453-467
-        means = np.array([np.mean(s) for s in shapelets], dtype=np.float64)
-        stds = np.array([np.std(s) for s in shapelets], dtype=np.float64)
+        means, stds = _shapelet_stats(shapelets, lens)
         stds[stds <= 1e-13] = 0.0
     else:
         means = stds = None
