@@ -457,9 +457,10 @@ def _grouped_stats_ok():
     return _GROUPED_STATS_OK
 
 
-def _shapelet_stats(shapelets, lens):
+def _shapelet_stats(shapelets, lens, packed=None, offs=None):
     """np.mean / np.std of every shapelet (ScaledSubsequenceMetric.from_array,
-    distance/_cdistance.pyx:453-467), one reduction per distinct length."""
+    distance/_cdistance.pyx:453-467), one reduction per distinct length (rows
+    gathered from the packed float64 copy when it is given)."""
     n = len(shapelets)
     # other dtypes reduce in their own precision: keep one call per shapelet
     all_f64 = all(getattr(s, "dtype", None) == np.float64 for s in shapelets)
@@ -471,7 +472,10 @@ def _shapelet_stats(shapelets, lens):
     stds = np.empty(n)
     for L in np.unique(lens):
         rows = np.flatnonzero(lens == L)
-        A = np.stack([np.ravel(shapelets[i]) for i in rows])
+        if packed is not None:
+            A = packed[offs[rows][:, None] + np.arange(L)[None, :]]
+        else:
+            A = np.stack([np.ravel(shapelets[i]) for i in rows])
         means[rows] = np.mean(A, axis=1)
         stds[rows] = np.std(A, axis=1)
     return means, stds
@@ -486,7 +490,7 @@ def _pack_shapelets(shapelets, scaled):
                                   dtype=np.float64)
     if scaled:
         # ScaledSubsequenceMetric.from_array: distance/_cdistance.pyx:453-467
-        means, stds = _shapelet_stats(shapelets, lens)
+        means, stds = _shapelet_stats(shapelets, lens, packed, offs)
         stds[stds <= 1e-13] = 0.0
     else:
         means = stds = None
