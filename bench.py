@@ -43,9 +43,9 @@ WORKLOAD = {
 }
 FP64_OPS_PER_CELL = 3  # v = x - y, v * v, min + v*v (mins run on the integer pipe)
 # DRAM bytes (read + write) of one launch of the headline kernel at 2000 x 2000,
-# L = 512, from one ncu capture of `python bench.py --no-cpu --no-forms --steps 2
-# --warmup 3` (dram__bytes_read.sum 17.12 MB + dram__bytes_write.sum 10.75 KB;
-# profiles/elastic_pairs_dtw_f64_2000x2000_L512.md).  The 32 MB output is still in
+# L = 512, from one earlier ncu capture of `python bench.py --no-cpu --no-forms
+# --steps 2 --warmup 3` (dram__bytes_read.sum 17.12 MB + dram__bytes_write.sum
+# 10.75 KB); it is not measured in the timed run.  The 32 MB output is still in
 # L2 when the kernel ends.
 HEADLINE_DRAM_BYTES = 17.12e6 + 10.75e3
 
@@ -122,7 +122,7 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_reference(X, Y, wl, budget_s=15.0, n_threads=None):
+def cpu_reference(X, Y, wl, budget_s=15.0, n_threads=None, return_rows=False):
     """The reference algorithm (oracle restatement) on the host cores, bounded."""
     from oracle import oracle as O
 
@@ -139,14 +139,15 @@ def cpu_reference(X, Y, wl, budget_s=15.0, n_threads=None):
     rows = max(n_threads, (rows // n_threads) * n_threads)
     rows = min(rows, X.shape[0])
     t0 = time.perf_counter()
-    O.pairwise(X[:rows], Y, metric=wl["metric"], metric_params=wl["params"],
-               n_threads=n_threads)
+    ref = O.pairwise(X[:rows], Y, metric=wl["metric"], metric_params=wl["params"],
+                     n_threads=n_threads)
     dt = time.perf_counter() - t0
     cells = rows * Y.shape[0] * cells_pair
-    return {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": n_threads, "kind": "port",
-            "sample": f"{rows} x {Y.shape[0]} pairs of the workload "
-                      f"({cells:.3e} cells, {dt:.2f} s), oracle/wb_oracle.c with "
-                      f"{n_threads} threads"}
+    res = {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": n_threads, "kind": "port",
+           "sample": f"{rows} x {Y.shape[0]} pairs of the workload "
+                     f"({cells:.3e} cells, {dt:.2f} s), oracle/wb_oracle.c with "
+                     f"{n_threads} threads"}
+    return (res, ref) if return_rows else res
 
 
 def run_reference(args):
@@ -1000,14 +1001,23 @@ def run_gpu(args):
         # measured for the default 2000 x 2000 workload only
         "traffic": HEADLINE_DRAM_BYTES if (wl["nx"], wl["ny"]) == (2000, 2000) else None,
         "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+        "traffic_source": "one earlier ncu capture of this workload, not measured in this run",
         "algorithmic_bytes": int(X.nbytes + Y.nbytes + wl["nx"] * wl["ny"] * 8),
         "kernel": "elastic_pairs_kernel<K_DTW>",
         "kernel_ms": k_avg,
         "ops_per_cell": FP64_OPS_PER_CELL,
     }
     cpu = None
+    parity = None
     if world == 1 and not args.no_cpu:
-        cpu = cpu_reference(X, Y, wl, budget_s=args.cpu_budget)
+        cpu, ref_rows = cpu_reference(X, Y, wl, budget_s=args.cpu_budget, return_rows=True)
+        # the headline output against the oracle on the same rows
+        got = np.asarray(out)[: ref_rows.shape[0]]
+        rel = np.abs(got - ref_rows) / np.maximum(np.abs(ref_rows), 1e-300)
+        parity = {"rows": int(ref_rows.shape[0]), "cols": int(ref_rows.shape[1]),
+                  "max_rel_err": float(rel.max()),
+                  "bit_exact": bool(np.array_equal(got, ref_rows)),
+                  "against": "oracle rows of the cpu_baseline sample"}
     forms = {}
     if not args.no_forms:
         forms["batched_fp32"] = bench_batched(args, dev, flush)
@@ -1020,8 +1030,22 @@ def run_gpu(args):
         forms["argmin_knn"] = bench_argmin(args, dev, flush)
         forms["subsequence_elastic"] = bench_subsequence_elastic(args, dev, flush)
         forms["subsequence_search"] = bench_subsequence_search(args, dev, flush)
-        forms["both_beat_fp64_drop_in"] = bool(
-            forms["batched_fp32"]["gcups"] > value and forms["fwd_bwd_fp32"]["gcups"] > value)
+    targets = None
+    if forms:
+        bt, fb = forms["batched_fp32"], forms["fwd_bwd_fp32"]
+        targets = {
+            "fp64_drop_in_gcups": value,
+            "batched_fp32_gcups": bt["gcups"],
+            "batched_fp32_max_rel_err_vs_fp64": bt["max_rel_err_vs_fp64"],
+            "batched_fp32_over_fp64": bt["gcups"] / value,
+            "fwd_bwd_fp32_gcups": fb["gcups"],
+            "fwd_bwd_fp32_max_rel_err_vs_fp64": fb["max_rel_err_vs_fp64"],
+            "fwd_bwd_fp32_over_fp64": fb["gcups"] / value,
+            "both_beat_fp64_drop_in": bool(bt["gcups"] > value and fb["gcups"] > value),
+        }
+        # the bulky per-form records go on their own line before the headline
+        if rank == 0:
+            print(json.dumps({"forms": forms}), flush=True)
     line = {
         "metric": "DTW cell-updates/s (GCUPS), plain FP64 drop-in",
         "value": value,
@@ -1043,7 +1067,8 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
-        "forms": forms,
+        "parity_on_sample": parity,
+        "targets": targets,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
