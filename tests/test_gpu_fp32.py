@@ -83,6 +83,79 @@ def test_paired_ragged_batch_vs_oracle():
     np.testing.assert_allclose(got, want, rtol=DIST_RTOL, atol=1e-9)
 
 
+TILES = [(8, 128), (16, 256), (24, 128), (32, 64)]
+
+
+@pytest.mark.parametrize("tile", TILES, ids=lambda t: f"s{t[0]}-b{t[1]}")
+def test_ragged_batch_tiles_vs_oracle(tile):
+    # ragged lengths from 1 to L on both sides, so the lanes of a warp mix
+    # both orientations (n < m, n > m) and single-element series
+    rng = np.random.default_rng(17)
+    n, d, L = 240, 2, 300
+    x, lx = _ragged(rng, n, d, L, 1, L)
+    y, ly = _ragged(rng, n, d, L, 1, L)
+    plan = B.plan_pairs(torch.as_tensor(x, device="cuda"), torch.as_tensor(y, device="cuda"),
+                        0.1, tune=False, tile=tile)
+    got = B.combine_dims(plan, B.run_plan(plan)).cpu().numpy()
+    want = np.zeros(n)
+    for i in range(n):
+        acc = 0.0
+        for k in range(d):
+            acc += O.distance_1d(x[i, k, : lx[i, k]].astype(np.float64),
+                                 y[i, k, : ly[i, k]].astype(np.float64), metric="dtw",
+                                 metric_params={"r": 0.1})
+        want[i] = acc / d
+    np.testing.assert_allclose(got, want, rtol=DIST_RTOL, atol=1e-9)
+
+
+@pytest.mark.parametrize("r", [0.0, 0.1, 1.0])
+@pytest.mark.parametrize("lx,ly", [(64, 64), (130, 41), (41, 130), (1, 50), (50, 1)])
+@pytest.mark.parametrize("strip", [8, 24])
+@pytest.mark.parametrize("g", [None, 0.1])
+def test_grid_shapes_vs_fp64_oracle(r, lx, ly, strip, g):
+    rng = np.random.default_rng(lx * 1000 + ly)
+    X = _walk(rng, (21, lx))
+    Y = _walk(rng, (7, ly))
+    xt = torch.as_tensor(X, device="cuda")
+    yt = torch.as_tensor(Y, device="cuda")
+    w = None if g is None else B.logistic_weights(max(lx, ly), g, "cuda")
+    got = B.dtw32(xt, yt, r=r, weights=w, strip=strip).view(7, 21).t().cpu().numpy()
+    metric, params = ("dtw", {"r": r}) if g is None else ("wdtw", {"r": r, "g": g})
+    want = O.pairwise(X.astype(np.float64), Y.astype(np.float64), metric=metric,
+                      metric_params=params)
+    np.testing.assert_allclose(got, want, rtol=DIST_RTOL, atol=1e-9)
+
+
+def test_ragged_wdtw_batch_vs_oracle():
+    # one side of every pair has the full length L, so the oracle's weights
+    # (length max(n, m) of the pair) are the kernel's table of length L; the
+    # other side is ragged, on x for half the pairs and on y for the rest
+    rng = np.random.default_rng(23)
+    n, L = 160, 120
+    x, lx = _ragged(rng, n, 1, L, 2, L)
+    y, ly = _ragged(rng, n, 1, L, 2, L)
+    full_x = rng.random(n) < 0.5
+    for i in range(n):
+        if full_x[i]:
+            x[i, 0] = _walk(rng, (L,))
+            lx[i, 0] = L
+        else:
+            y[i, 0] = _walk(rng, (L,))
+            ly[i, 0] = L
+    w = B.logistic_weights(L, 0.05, "cuda")
+    xt = torch.as_tensor(x[:, 0].copy(), device="cuda")
+    yt = torch.as_tensor(y[:, 0].copy(), device="cuda")
+    xl, yl = B.series_lengths(xt), B.series_lengths(yt)
+    item = B.bucket_order(xl, yl, 0.2, transpose=False).to(torch.int32).contiguous()
+    got = B.dtw32(xt, yt, r=0.2, x_lengths=xl, y_lengths=yl, item_x=item, item_y=item,
+                  weights=w, strip=8).cpu().numpy()
+    for t, i in enumerate(item.cpu().numpy()):
+        want = O.distance_1d(x[i, 0, : lx[i, 0]].astype(np.float64),
+                             y[i, 0, : ly[i, 0]].astype(np.float64), metric="wdtw",
+                             metric_params={"r": 0.2, "g": 0.05})
+        assert abs(got[t] - want) <= DIST_RTOL * want, (t, got[t], want)
+
+
 def test_batched_graph_replay_matches_direct():
     rng = np.random.default_rng(8)
     x, _ = _ragged(rng, 200, 2, 150, 20, 150)

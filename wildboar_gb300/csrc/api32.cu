@@ -52,7 +52,8 @@ int dtw32_plan(const wb_dtw32 *q, bool backward, Dtw32Job &J, size_t &bytes) {
     J.weights = q->weights;
     J.grid = grid;
     J.block = block;
-    J.ring_cols = q->y_len + 1;
+    // the forward puts the longer series of a dtw item on the columns
+    J.ring_cols = (backward ? q->y_len : std::max(q->x_len, q->y_len)) + 1;
     const int64_t nth = (int64_t)grid * block;
     size_t ring_bytes = align256((size_t)J.ring_cols * nth * sizeof(float2));
     size_t dir_bytes = 0;

@@ -105,7 +105,19 @@ __device__ __forceinline__ void strip_column(HL (&P)[S], HL bup, HL bdiag, float
         float cst = __fmul_rn(vv, vv);
         if (W) cst = __fmul_rn(cst, w[(!MASK || k < valid) ? abs(d) : 0]);
         if (MASK) cst = ((unsigned)(d - lo) < width) ? cst : WB_FINF;
-        const HL nv = add_c(best, cst);
+        HL nv;
+        if (DIRS) {
+            nv = add_c(best, cst);
+        } else {
+            // Fast2Sum: exact when best.h >= cst; otherwise (a partial sum
+            // smaller than the next cost, near the start of a path) the error
+            // term is off by at most half an ulp of the new partial sum, and
+            // such steps at least double it, so they add at most one unit
+            // roundoff of the path cost in all
+            const float sh = __fadd_rn(best.h, cst);
+            const float err = __fsub_rn(cst, __fsub_rn(sh, best.h));
+            nv = HL{sh, __fadd_rn(best.l, err)};
+        }
         if (DIRS) word |= (uint32_t)dir << (2 * k);
         dg = lf;
         up = nv;
@@ -209,6 +221,132 @@ __device__ HL sweep(const Item &it, const float *__restrict__ w, float2 *ring, i
     return result;
 }
 
+// The forward sweep of the 32 lanes of a warp with warp-uniform loop bounds:
+// every strip runs over the union of the lanes' column ranges, so lanes whose
+// items differ in shape never diverge; a lane's cells outside its own band
+// (or past its own series) get an infinite cost on the masked path.  Columns
+// where every row of every lane's strip is in band take the mask-free path.
+// Called by all 32 lanes; `active` lanes return the (hi, lo) cost of their
+// cell (n-1, m-1), the others run masked and return +inf.
+template <int S, bool W>
+__device__ HL sweep_uniform(Item it, bool active, const float *__restrict__ w, float2 *ring,
+                            int64_t nth) {
+    const unsigned FULL = 0xffffffffu;
+    if (!active) it.n = it.m = 0;
+    if (!W && it.n > it.m) {
+        // dtw: rows are the shorter series (the transposed problem has the
+        // same band, the same costs and the same minima), so the lanes of a
+        // warp, sorted by the shorter length, have their bands in the same
+        // columns
+        const float *tp = it.X;
+        it.X = it.Y;
+        it.Y = tp;
+        const int tn = it.n;
+        it.n = it.m;
+        it.m = tn;
+        it.mx = imax(0, it.m - it.n) + it.r;
+        it.mn = imax(0, it.n - it.m);
+    }
+    const float *__restrict__ X = it.X;
+    const float *__restrict__ Y = it.Y;
+    const int n = it.n, m = it.m, r = it.r, mx = it.mx, mn = it.mn;
+    const float qnan = __int_as_float(0x7fc00000);
+    // row 0: cumulative, weight index j-1 for j >= 1
+    const int lim = active ? imin(m, mx) : 0;
+    const int lim_w = __reduce_max_sync(FULL, lim);
+    HL acc = hl_inf();
+    const float x0 = active ? X[0] : qnan;
+    for (int c = 0; c < lim_w; c++) {
+        if (c < lim) {
+            const float v = __fsub_rn(x0, Y[c]);
+            float cc = __fmul_rn(v, v);
+            if (W) cc = __fmul_rn(cc, w[c > 0 ? c - 1 : 0]);
+            acc = c == 0 ? HL{cc, 0.0f} : add_c(acc, cc);
+            ring[(int64_t)c * nth] = make_float2(acc.h, acc.l);
+        }
+    }
+    HL result = acc;
+    int pstart = 0, pend = lim;
+    const int lo = -(mn + r - 1);
+    const int hi = mx - 1;
+    const unsigned width = (unsigned)(hi - lo + 1);
+    const int n_w = __reduce_max_sync(FULL, n);
+    for (int i0 = 1; i0 < n_w; i0 += S) {
+        const int rows = imax(0, imin(S, n - i0));
+        float xr[S];
+#pragma unroll
+        for (int k = 0; k < S; k++) xr[k] = (k < rows) ? X[i0 + k] : qnan;
+        int cstart = imax(0, i0 - mn - r + 1);
+        int cend = imin(m, i0 + rows - 1 + mx);
+        if (rows == 0) {
+            cstart = 0x7fffffff;
+            cend = 0;
+        }
+        // columns where every row of a full strip is in band
+        int bstart = 0x7fffffff, bend = 0;
+        if (rows == S) {
+            bstart = imax(cstart, i0 + S - 1 + lo);
+            bend = imin(cend, i0 + hi + 1);
+        }
+        const int cs_w = __reduce_min_sync(FULL, cstart);
+        const int ce_w = __reduce_max_sync(FULL, cend);
+        const int bs_w = __reduce_max_sync(FULL, bstart);
+        const int be_w = __reduce_min_sync(FULL, bend);
+        HL P[S];
+#pragma unroll
+        for (int k = 0; k < S; k++) P[k] = hl_inf();
+        HL bdiag = hl_inf();
+        if (cs_w - 1 >= pstart && cs_w - 1 < pend) {
+            const float2 t2 = ring[(int64_t)(cs_w - 1) * nth];
+            bdiag = HL{t2.x, t2.y};
+        }
+        auto load_up = [&](int c) {
+            HL b = hl_inf();
+            if (c >= pstart && c < pend) {
+                const float2 t2 = ring[(int64_t)c * nth];
+                b = HL{t2.x, t2.y};
+            }
+            return b;
+        };
+        // a lane reads y only inside its own series
+        auto load_y = [&](int c) { return c < m ? Y[c] : 0.0f; };
+        HL nb0 = load_up(cs_w), nb1 = load_up(cs_w + 1);
+        float ny0 = load_y(cs_w), ny1 = load_y(cs_w + 1);
+        const bool last = rows > 0 && (i0 + rows == n);
+        const int krow = rows - 1;
+        for (int c = cs_w; c < ce_w; c++) {
+            const HL bup = nb0;
+            const float yc = ny0;
+            nb0 = nb1;
+            ny0 = ny1;
+            nb1 = load_up(c + 2);
+            ny1 = load_y(c + 2);
+            uint32_t word = 0;
+            if (c >= bs_w && c < be_w) {
+                strip_column<S, W, false, false>(P, bup, bdiag, yc, xr, c - i0, lo, width, w,
+                                                 rows, word);
+            } else {
+                // past the lane's series end every row is out of band
+                const unsigned wid = c < m ? width : 0u;
+                strip_column<S, W, false, true>(P, bup, bdiag, yc, xr, c - i0, lo, wid, w,
+                                                rows, word);
+            }
+            if (last && c == m - 1) {
+#pragma unroll
+                for (int k = 0; k < S; k++)
+                    if (k <= krow) result = P[k];
+            }
+            ring[(int64_t)c * nth] = make_float2(P[S - 1].h, P[S - 1].l);
+            bdiag = bup;
+        }
+        if (rows > 0) {
+            pstart = cstart;
+            pend = cend;
+        }
+    }
+    return active ? result : hl_inf();
+}
+
 __device__ __forceinline__ int64_t take_items(unsigned long long *q, int lane) {
     unsigned long long base = 0;
     if (lane == 0) base = atomicAdd(q, 32ull);
@@ -225,17 +363,22 @@ __global__ void __launch_bounds__(256) dtw32_forward_kernel(const Dtw32Job J) {
         const int64_t base = take_items(J.queue, lane);
         if (base >= J.n_items) break;
         const int64_t t = base + lane;
+        Item it{};
+        bool active = false;
         if (t < J.n_items) {
-            Item it = load_item(J, t);
-            double res;
-            if (it.n < 1 || it.m < 1 || it.m >= J.ring_cols) {
-                res = __longlong_as_double(0x7ff8000000000000LL);  // NaN: empty series
-                if (J.out_cost) J.out_cost[t] = res;
-            } else {
-                HL h = sweep<S, W, false>(it, J.weights, ring, nth, nullptr);
-                double cost = (double)h.h + (double)h.l;
+            it = load_item(J, t);
+            active = !(it.n < 1 || it.m < 1 || it.m >= J.ring_cols);
+        }
+        // all 32 lanes sweep together (warp-uniform bounds)
+        const HL h = sweep_uniform<S, W>(it, active, J.weights, ring, nth);
+        if (t < J.n_items) {
+            double res = __longlong_as_double(0x7ff8000000000000LL);  // NaN: empty series
+            if (active) {
+                const double cost = (double)h.h + (double)h.l;
                 if (J.out_cost) J.out_cost[t] = cost;
                 res = sqrt(cost);
+            } else if (J.out_cost) {
+                J.out_cost[t] = res;
             }
             J.out[t] = res;
         }
@@ -350,8 +493,8 @@ static int launch_fwd(const Dtw32Job &J, cudaStream_t s) {
 int dtw32_forward(const Dtw32Job &J, int strip, cudaStream_t s) {
     if (J.n_items == 0) return WB_OK;
     WB_CUDA(cudaMemsetAsync(J.queue, 0, sizeof(unsigned long long), s));
-    timer_begin("dtw32_forward_kernel", s);
     int st;
+    timer_begin("dtw32_forward_kernel", s);
     switch (strip) {
         case 4: st = launch_fwd<4>(J, s); break;
         case 8: st = launch_fwd<8>(J, s); break;

@@ -170,7 +170,7 @@ class Autotuner:
         torch = _torch()
         name = torch.cuda.get_device_name(device)
         bucket = 1 << max(int(max_len) - 1, 1).bit_length()
-        return f"{name}|L<={bucket}|r={r:g}|w={int(bool(weighted))}"
+        return f"v2|{name}|L<={bucket}|r={r:g}|w={int(bool(weighted))}"
 
     def pick(self, x, y, *, r, x_lengths, y_lengths, item_x, item_y, weights=None,
              sample=16384, reps=2):
@@ -188,19 +188,18 @@ class Autotuner:
             sx, sy = item_x, item_y
         best = None
         out = torch.empty(sx.numel(), dtype=torch.float64, device=x.device)
-        for strip in STRIPS:
-            for block in BLOCKS:
-                kw = dict(r=r, x_lengths=x_lengths, y_lengths=y_lengths, item_x=sx,
-                          item_y=sy, weights=weights, strip=strip, block=block)
-                dtw32(x, y, out=out, **kw)  # warm-up (workspace growth)
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                for _ in range(reps):
-                    dtw32(x, y, out=out, **kw)
-                torch.cuda.synchronize()
-                dt = (time.perf_counter() - t0) / reps
-                if best is None or dt < best[0]:
-                    best = (dt, strip, block)
+        for strip, block in [(s_, b_) for s_ in STRIPS for b_ in BLOCKS]:
+            kw = dict(r=r, x_lengths=x_lengths, y_lengths=y_lengths, item_x=sx,
+                      item_y=sy, weights=weights, strip=strip, block=block)
+            dtw32(x, y, out=out, **kw)  # warm-up (workspace growth)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                dtw32(x, y, out=out, **kw)
+            torch.cuda.synchronize()
+            dt = (time.perf_counter() - t0) / reps
+            if best is None or dt < best[0]:
+                best = (dt, strip, block)
         with self.lock:
             tab = self._load()
             tab[k] = {"strip": best[1], "block": best[2], "sample_s": best[0]}
@@ -209,6 +208,8 @@ class Autotuner:
 
 
 AUTOTUNER = Autotuner()
+# configuration without autotuning: (strip, block)
+DEFAULT_TILE = (24, 128)
 
 
 # --------------------------------------------------------------------------
@@ -235,24 +236,28 @@ def band_cost(n, m, r):
     return torch.where((n > 0) & (m > 0), cells, torch.zeros_like(cells))
 
 
-def bucket_order(n, m, r):
+def bucket_order(n, m, r, transpose=True):
     """Processing order of the items.
 
-    A lane's work is (number of 32-row strips) x (columns per strip, the band
-    width min(m, |m - n| + 2r)).  Items are sorted by strip count, then by
-    band width, both descending: the 32 consecutive items a warp takes share
-    their strip count and have nearly equal band widths (little SIMT
-    divergence), and the persistent queue ends on the smallest problems.
-    Measured on the 65,536 x 3 ragged batch (lengths U{32..2048}, r = 0.1):
-    1271 GCUPS against 1055 for a bucketing by (n / 32, (m - n) / 16) ranked
-    by mean cost.
+    The 32 lanes of a warp sweep their items together over the union of their
+    column ranges, so neighbours in this order should have their bands in the
+    same columns.  A lane's rows are the shorter series when the kernel
+    transposes (dtw: ``transpose=True``), else x; its work is (number of
+    32-row strips) x (band width min(m, |m - n| + 2r)).  Items are sorted by
+    strip count, then by band width, both descending (without transposition
+    the orientation n > m comes first, as it places the band on the other
+    side of the diagonal); the persistent queue ends on the smallest
+    problems.
     """
     torch = _torch()
     n = n.long()
     m = m.long()
     w = torch.clamp(torch.floor(torch.minimum(n, m).double() * r), min=1).long()
-    cols = torch.minimum(m, (m - n).abs() + 2 * w).clamp(0, 8191)
-    key = ((n - 2).clamp(min=0) // 32) * 8192 + cols
+    cols = torch.minimum(torch.maximum(n, m), (m - n).abs() + 2 * w).clamp(0, 8191)
+    rows = torch.minimum(n, m) if transpose else n
+    key = ((rows - 2).clamp(min=0) // 32) * 8192 + cols
+    if not transpose:
+        key = key + (n > m).long() * (1 << 40)
     return torch.argsort(key, descending=True, stable=True)
 
 
@@ -272,7 +277,7 @@ def plan_pairs(x, y, r, *, tune=True, weights=None, tile=None):
     xl = series_lengths(xf)
     yl = series_lengths(yf)
     cost = band_cost(xl, yl, r)
-    order = bucket_order(xl, yl, r).to(torch.int32)
+    order = bucket_order(xl, yl, r, transpose=weights is None).to(torch.int32)
     item = order.contiguous()
     plan = {"xf": xf, "yf": yf, "xl": xl, "yl": yl, "item_x": item, "item_y": item,
             "order": order.long(), "N": N, "d": d, "r": float(r), "weights": weights,
@@ -284,7 +289,7 @@ def plan_pairs(x, y, r, *, tune=True, weights=None, tile=None):
             xf, yf, r=r, x_lengths=xl, y_lengths=yl, item_x=item, item_y=item,
             weights=weights)
     else:
-        plan["strip"], plan["block"] = 16, 128
+        plan["strip"], plan["block"] = DEFAULT_TILE
     return plan
 
 
