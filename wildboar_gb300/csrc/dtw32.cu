@@ -105,20 +105,71 @@ __device__ __forceinline__ void strip_column(HL (&P)[S], HL bup, HL bdiag, float
         float cst = __fmul_rn(vv, vv);
         if (W) cst = __fmul_rn(cst, w[(!MASK || k < valid) ? abs(d) : 0]);
         if (MASK) cst = ((unsigned)(d - lo) < width) ? cst : WB_FINF;
-        HL nv;
-        if (DIRS) {
-            nv = add_c(best, cst);
-        } else {
-            // Fast2Sum: exact when best.h >= cst; otherwise (a partial sum
-            // smaller than the next cost, near the start of a path) the error
-            // term is off by at most half an ulp of the new partial sum, and
-            // such steps at least double it, so they add at most one unit
-            // roundoff of the path cost in all
-            const float sh = __fadd_rn(best.h, cst);
-            const float err = __fsub_rn(cst, __fsub_rn(sh, best.h));
-            nv = HL{sh, __fadd_rn(best.l, err)};
-        }
+        const HL nv = add_c(best, cst);
         if (DIRS) word |= (uint32_t)dir << (2 * k);
+        dg = lf;
+        up = nv;
+        P[k] = nv;
+    }
+}
+
+// (x0 - y)^2 and (x1 - y)^2 as one packed f32x2 subtraction and one packed
+// multiplication (each half rounded as the scalar operation would be)
+__device__ __forceinline__ void sqdiff2(float x0, float x1, float y, float &c0, float &c1) {
+    asm("{\n\t.reg .b64 pa, pb;\n\t"
+        "mov.b64 pa, {%2, %3};\n\t"
+        "mov.b64 pb, {%4, %4};\n\t"
+        "sub.rn.f32x2 pa, pa, pb;\n\t"
+        "mul.rn.f32x2 pa, pa, pa;\n\t"
+        "mov.b64 {%0, %1}, pa;\n\t}"
+        : "=f"(c0), "=f"(c1)
+        : "f"(x0), "f"(x1), "f"(y));
+}
+
+// Bits k (k < 32) with 0 <= e - k < width: the strip rows in band at a
+// column, e = c - i0 - lo.
+__device__ __forceinline__ unsigned band_bits(int e, int width) {
+    const unsigned upper = e < 0 ? 0u : (e >= 31 ? 0xffffffffu : (0xffffffffu >> (31 - e)));
+    const int lb = e - width + 1;
+    const unsigned lower = lb <= 0 ? 0u : (lb >= 32 ? 0xffffffffu : ((1u << lb) - 1u));
+    return upper & ~lower;
+}
+
+// One column of a strip in the forward sweep (no traceback directions):
+// the minimum of the three hi parts with the lo of a candidate holding it
+// (left, then up, then diag on equal hi), Fast2Sum for the new partial sum.
+// With MASK, rows whose bit of M is clear are out of band (infinite cost).
+template <int S, bool W, bool MASK>
+__device__ __forceinline__ void fwd_column(HL (&P)[S], HL bup, HL bdiag, float yc,
+                                           const float (&xr)[S], int d0, unsigned M,
+                                           const float *__restrict__ w, int valid) {
+    HL dg = bdiag;  // cell (i0 + k - 1, c - 1)
+    HL up = bup;    // cell (i0 + k - 1, c)
+    float cpair[2];
+#pragma unroll
+    for (int k = 0; k < S; k++) {
+        float cst;
+        if (W) {
+            const float vv = __fsub_rn(xr[k], yc);
+            cst = __fmul_rn(__fmul_rn(vv, vv), w[(!MASK || k < valid) ? abs(d0 - k) : 0]);
+        } else {
+            if ((k & 1) == 0) sqdiff2(xr[k], xr[k + 1], yc, cpair[0], cpair[1]);
+            cst = cpair[k & 1];
+        }
+        if (MASK) cst = ((M >> k) & 1u) ? cst : WB_FINF;
+        const HL lf = P[k];
+        HL best;
+        asm("min.f32 %0, %1, %2, %3;" : "=f"(best.h) : "f"(dg.h), "f"(up.h), "f"(lf.h));
+        best.l = (up.h == best.h) ? up.l : dg.l;
+        best.l = (lf.h == best.h) ? lf.l : best.l;
+        // Fast2Sum: exact when best.h >= cst; otherwise (a partial sum
+        // smaller than the next cost, near the start of a path) the error
+        // term is off by at most half an ulp of the new partial sum, and such
+        // steps at least double it, so they add at most one unit roundoff of
+        // the path cost in all
+        const float sh = __fadd_rn(best.h, cst);
+        const float err = __fsub_rn(cst, __fsub_rn(sh, best.h));
+        const HL nv{sh, __fadd_rn(best.l, err)};
         dg = lf;
         up = nv;
         P[k] = nv;
@@ -321,15 +372,12 @@ __device__ HL sweep_uniform(Item it, bool active, const float *__restrict__ w, f
             ny0 = ny1;
             nb1 = load_up(c + 2);
             ny1 = load_y(c + 2);
-            uint32_t word = 0;
             if (c >= bs_w && c < be_w) {
-                strip_column<S, W, false, false>(P, bup, bdiag, yc, xr, c - i0, lo, width, w,
-                                                 rows, word);
+                fwd_column<S, W, false>(P, bup, bdiag, yc, xr, c - i0, 0u, w, rows);
             } else {
                 // past the lane's series end every row is out of band
-                const unsigned wid = c < m ? width : 0u;
-                strip_column<S, W, false, true>(P, bup, bdiag, yc, xr, c - i0, lo, wid, w,
-                                                rows, word);
+                const unsigned M = c < m ? band_bits(c - i0 - lo, (int)width) : 0u;
+                fwd_column<S, W, true>(P, bup, bdiag, yc, xr, c - i0, M, w, rows);
             }
             if (last && c == m - 1) {
 #pragma unroll
