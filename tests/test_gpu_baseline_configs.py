@@ -138,10 +138,11 @@ def test_c4_slice_ragged_batch_vs_fp64_oracle():
     np.testing.assert_allclose(got, want, rtol=1e-5, atol=0)
 
 
-def _near_tie(al, path, rel=2e-5):
+def _near_tie(al, path, rel=1e-9):
     """True if some step of the optimal path had a competing predecessor whose
-    cumulative cost is within `rel` of the chosen one (float32 partial sums
-    may then pick the other, equally optimal, step)."""
+    cumulative cost is within `rel` of the chosen one (dtw is not
+    differentiable at a tie, and the compensated float32 costs resolve
+    differences down to about 1e-12 of the path cost)."""
     for a, b in path:
         if a == 0 or b == 0:
             continue
@@ -173,7 +174,7 @@ def test_c5_slice_gradient_vs_alignment_path():
                 # pair whose path passes a near-tie is left out of the check
                 gw[i, j] = 0.0
             paths[i, j] = (np.sqrt(al[-1, -1]), path)
-    assert np.count_nonzero(gw) >= 2
+    assert np.count_nonzero(gw) >= nx * nc // 2
     xt = torch.as_tensor(X, device="cuda").requires_grad_(True)
     ct = torch.as_tensor(C, device="cuda").requires_grad_(True)
     D = AG.dtw_matrix(xt, ct, r)

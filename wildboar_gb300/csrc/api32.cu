@@ -4,6 +4,8 @@
 // the job's size, so a call can be captured in a CUDA graph after a warm-up.
 
 #include <algorithm>
+#include <cmath>
+#include <cstdlib>
 
 #include "dtw32.cuh"
 
@@ -23,15 +25,45 @@ int dtw32_plan(const wb_dtw32 *q, bool backward, Dtw32Job &J, size_t &bytes) {
     const int strip = backward ? 16 : (q->strip ? q->strip : 16);
     if (strip != 4 && strip != 8 && strip != 16 && strip != 24 && strip != 32)
         return fail(WB_EINVAL, "strip must be one of 4, 8, 16, 24, 32");
-    const int block = q->block ? q->block : 128;
+    int block = q->block ? q->block : 128;
     if (block % 32 || block < 32 || block > 256)
         return fail(WB_EINVAL, "block must be a multiple of 32 in [32, 256]");
     const DeviceInfo &dev = device_info();
+    // the longer series of a dtw item goes on the columns, the shorter on the
+    // rows; wdtw keeps x on the rows
+    const int cols_max = std::max(q->x_len, q->y_len);
+    const int rows_max = q->weights ? q->x_len : std::min(q->x_len, q->y_len);
+    J.ring_cols = cols_max + 1;
+    // backward geometry: strips of 16 rows cut into segments of K strips; the
+    // direction words of one segment (K strips x at most cols_max columns) and
+    // one checkpoint row per segment boundary per resident thread
+    size_t per_thread = (size_t)J.ring_cols * sizeof(float2);
+    if (backward) {
+        const int64_t strips = rows_max > 1 ? (rows_max - 2) / 16 + 1 : 0;
+        int64_t K = std::max<int64_t>(strips, 1);
+        if (K > 64 || K * cols_max * 4 > (64 << 10)) {
+            K = (int64_t)std::ceil(std::sqrt(2.0 * (double)strips));
+            K = std::min<int64_t>(std::max<int64_t>(K, 1), 64);
+        }
+        J.seg_strips = (int)K;
+        J.n_ckpt = strips > 0 ? (int)((strips + K - 1) / K - 1) : 0;
+        J.dir_words = (K * cols_max + 7) / 8 * 8;  // whole 8-word groups
+        per_thread += (size_t)J.dir_words * sizeof(uint32_t) +
+                      (size_t)J.n_ckpt * J.ring_cols * sizeof(float2);
+        block = 128;  // the backward kernel's block size
+    }
     int grid = q->grid;
     if (grid <= 0) {
         int nb = dtw32_blocks_per_sm(strip, q->weights != nullptr, backward, block);
         if (nb < 1) nb = 1;
         grid = nb * dev.sm_count;
+        if (backward) {
+            // resident threads bounded by the backward workspace budget
+            const char *env = getenv("WB_GPU_BWD_WORKSPACE_MB");
+            const double mb = env ? atof(env) : 8192.0;
+            const int64_t cap = (int64_t)(mb * 1048576.0 / ((double)per_thread * block));
+            grid = (int)std::max<int64_t>(1, std::min<int64_t>(grid, cap));
+        }
         int64_t need = (q->n_items + block - 1) / block;
         if (need < grid) grid = (int)std::max<int64_t>(need, 1);
     }
@@ -52,22 +84,12 @@ int dtw32_plan(const wb_dtw32 *q, bool backward, Dtw32Job &J, size_t &bytes) {
     J.weights = q->weights;
     J.grid = grid;
     J.block = block;
-    // the forward puts the longer series of a dtw item on the columns
-    J.ring_cols = (backward ? q->y_len : std::max(q->x_len, q->y_len)) + 1;
     const int64_t nth = (int64_t)grid * block;
     size_t ring_bytes = align256((size_t)J.ring_cols * nth * sizeof(float2));
     size_t dir_bytes = 0;
     if (backward) {
-        int64_t words;
-        if (!q->x_lengths && !q->y_lengths) {
-            int r = compute_r(std::min(q->x_len, q->y_len), q->r);
-            words = dtw32_dir_words(q->x_len, q->y_len, r);
-        } else {
-            int64_t strips = q->x_len > 1 ? (q->x_len - 2) / 16 + 1 : 0;
-            words = strips * q->y_len + 1;
-        }
-        J.dir_words = words;
-        dir_bytes = align256((size_t)words * nth * sizeof(uint32_t));
+        dir_bytes = align256((size_t)J.dir_words * nth * sizeof(uint32_t)) +
+                    align256((size_t)std::max(J.n_ckpt, 1) * J.ring_cols * nth * sizeof(float2));
     }
     bytes = ring_bytes + dir_bytes + 256;
     return WB_OK;
@@ -81,7 +103,8 @@ int dtw32_take(Workspace &ws, Dtw32Job &J, bool backward) {
     if (!J.ring || !J.queue) return fail(WB_ENOMEM, "workspace reservation exceeded");
     if (backward) {
         J.dirs = ws.take<uint32_t>((size_t)J.dir_words * nth);
-        if (!J.dirs) return fail(WB_ENOMEM, "workspace reservation exceeded");
+        J.ckpt = ws.take<float2>((size_t)std::max(J.n_ckpt, 1) * J.ring_cols * nth);
+        if (!J.dirs || !J.ckpt) return fail(WB_ENOMEM, "workspace reservation exceeded");
     }
     return WB_OK;
 }

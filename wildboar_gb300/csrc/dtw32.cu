@@ -73,46 +73,6 @@ __device__ __forceinline__ Item load_item(const Dtw32Job &J, int64_t t) {
     return it;
 }
 
-// One column of a strip, updated in place: on entry P[k] holds cell
-// (i0 + k, c - 1), on exit cell (i0 + k, c).  With MASK, out-of-band cells get
-// an infinite cost (their hi is +inf and no in-band cell picks it); without,
-// every row of the strip is known to be in band for this column.  Rows past
-// the series end (k >= valid) carry NaN x values: their cells are NaN, valid
-// rows (which only look upward) never read them, and they read weight 0 so
-// that |c - i| never runs past the weight table.
-template <int S, bool W, bool DIRS, bool MASK>
-__device__ __forceinline__ void strip_column(HL (&P)[S], HL bup, HL bdiag, float yc,
-                                             const float (&xr)[S], int d0, int lo,
-                                             unsigned width, const float *__restrict__ w,
-                                             int valid, uint32_t &word) {
-    HL dg = bdiag;  // cell (i0 + k - 1, c - 1)
-    HL up = bup;    // cell (i0 + k - 1, c)
-#pragma unroll
-    for (int k = 0; k < S; k++) {
-        const HL lf = P[k];
-        HL best = dg;
-        int dir = 0;
-        if (up.h < best.h) {
-            best = up;
-            dir = 1;
-        }
-        if (lf.h < best.h) {
-            best = lf;
-            dir = 2;
-        }
-        const int d = d0 - k;  // c - i
-        float vv = __fsub_rn(xr[k], yc);
-        float cst = __fmul_rn(vv, vv);
-        if (W) cst = __fmul_rn(cst, w[(!MASK || k < valid) ? abs(d) : 0]);
-        if (MASK) cst = ((unsigned)(d - lo) < width) ? cst : WB_FINF;
-        const HL nv = add_c(best, cst);
-        if (DIRS) word |= (uint32_t)dir << (2 * k);
-        dg = lf;
-        up = nv;
-        P[k] = nv;
-    }
-}
-
 // (x0 - y)^2 and (x1 - y)^2 as one packed f32x2 subtraction and one packed
 // multiplication (each half rounded as the scalar operation would be)
 __device__ __forceinline__ void sqdiff2(float x0, float x1, float y, float &c0, float &c1) {
@@ -174,102 +134,6 @@ __device__ __forceinline__ void fwd_column(HL (&P)[S], HL bup, HL bdiag, float y
         up = nv;
         P[k] = nv;
     }
-}
-
-// One forward sweep; returns the (hi, lo) cost of cell (n-1, m-1).
-template <int S, bool W, bool DIRS>
-__device__ HL sweep(const Item &it, const float *__restrict__ w, float2 *ring, int64_t nth,
-                    uint32_t *dirs) {
-    const float *__restrict__ X = it.X;
-    const float *__restrict__ Y = it.Y;
-    const int n = it.n, m = it.m, r = it.r, mx = it.mx, mn = it.mn;
-    // row 0: cumulative, weight index j-1 for j >= 1
-    const float x0 = X[0];
-    float v = __fsub_rn(x0, Y[0]);
-    float c0 = __fmul_rn(v, v);
-    if (W) c0 = __fmul_rn(c0, w[0]);
-    HL acc{c0, 0.0f};
-    ring[0] = make_float2(acc.h, acc.l);
-    const int lim = imin(m, mx);
-    for (int c = 1; c < lim; c++) {
-        v = __fsub_rn(x0, Y[c]);
-        float cc = __fmul_rn(v, v);
-        if (W) cc = __fmul_rn(cc, w[c - 1]);
-        acc = add_c(acc, cc);
-        ring[(int64_t)c * nth] = make_float2(acc.h, acc.l);
-    }
-    HL result = acc;
-    int pstart = 0, pend = lim;
-    int64_t wofs = 0;
-    // in band iff lo <= c - i <= hi
-    const int lo = -(mn + r - 1);
-    const int hi = mx - 1;
-    const unsigned width = (unsigned)(hi - lo + 1);
-    const float qnan = __int_as_float(0x7fc00000);
-    for (int i0 = 1; i0 < n; i0 += S) {
-        const int rows = imin(S, n - i0);
-        float xr[S];
-#pragma unroll
-        for (int k = 0; k < S; k++) xr[k] = (k < rows) ? X[i0 + k] : qnan;
-        const int cstart = imax(0, i0 - mn - r + 1);
-        const int cend = imin(m, i0 + rows - 1 + mx);
-        // columns where every row of a full strip is in band
-        int bstart = cend, bend = cend;
-        if (rows == S) {
-            bstart = imax(cstart, i0 + S - 1 + lo);
-            bend = imin(cend, i0 + hi + 1);
-            if (bstart >= bend) bstart = bend = cend;
-        }
-        HL P[S];
-#pragma unroll
-        for (int k = 0; k < S; k++) P[k] = hl_inf();
-        HL bdiag = hl_inf();
-        if (cstart - 1 >= pstart && cstart - 1 < pend) {
-            float2 t2 = ring[(int64_t)(cstart - 1) * nth];
-            bdiag = HL{t2.x, t2.y};
-        }
-        // loads run two columns ahead of their use
-        auto load_up = [&](int c) {
-            HL b = hl_inf();
-            if (c < cend && c < pend) {
-                float2 t2 = ring[(int64_t)c * nth];
-                b = HL{t2.x, t2.y};
-            }
-            return b;
-        };
-        auto load_y = [&](int c) { return c < cend ? Y[c] : 0.0f; };
-        HL nb0 = load_up(cstart), nb1 = load_up(cstart + 1);
-        float ny0 = load_y(cstart), ny1 = load_y(cstart + 1);
-        const bool last = (i0 + rows == n);
-        const int krow = rows - 1;
-        for (int c = cstart; c < cend; c++) {
-            const HL bup = nb0;
-            const float yc = ny0;
-            nb0 = nb1;
-            ny0 = ny1;
-            nb1 = load_up(c + 2);
-            ny1 = load_y(c + 2);
-            uint32_t word = 0;
-            if (c >= bstart && c < bend)
-                strip_column<S, W, DIRS, false>(P, bup, bdiag, yc, xr, c - i0, lo, width, w,
-                                                rows, word);
-            else
-                strip_column<S, W, DIRS, true>(P, bup, bdiag, yc, xr, c - i0, lo, width, w,
-                                               rows, word);
-            if (DIRS) dirs[(wofs + (c - cstart)) * nth] = word;
-            if (last && c == m - 1) {
-#pragma unroll
-                for (int k = 0; k < S; k++)
-                    if (k <= krow) result = P[k];
-            }
-            ring[(int64_t)c * nth] = make_float2(P[S - 1].h, P[S - 1].l);
-            bdiag = bup;
-        }
-        pstart = cstart;
-        pend = cend;
-        wofs += cend - cstart;
-    }
-    return result;
 }
 
 // The forward sweep of the 32 lanes of a warp with warp-uniform loop bounds:
@@ -433,100 +297,416 @@ __global__ void __launch_bounds__(256) dtw32_forward_kernel(const Dtw32Job J) {
     }
 }
 
-constexpr int kGradStrip = 16;
+// ---------------------------------------------------------------------------
+// Backward.
+//
+// A warp takes 32 consecutive items and sweeps them together in strips of 16
+// rows (one 32-bit word of 2-bit directions per strip column) over rows
+// 1..n-1, with warp-uniform column bounds as in the forward and dtw items
+// transposed so that rows are the shorter series.  The predecessor of a cell
+// is the one with the smallest compensated value (hi - hi') + (lo - lo'),
+// ties in dtw_mapping's order (diag, up, left; distance/dtw.py:362-426), so
+// the path is the one the FP64 reference takes except at exact ties.
+//
+// Memory: the strips of an item are cut into segments of K strips.  Items of
+// one segment store all their directions and walk back directly.  Longer
+// items first sweep the strips once without directions, saving the bottom
+// row of every segment but the last (a checkpoint of the band boundary);
+// then, from the last segment to the first, each segment is recomputed from
+// the checkpoint above it with its directions and the path is walked through
+// its rows.  Per resident thread this holds K strips of direction words, the
+// checkpoints and one working row, instead of the directions of the whole
+// band.
+//
+// Gradients are added in the kernel (atomically) to per-series rows:
+//   dD/dr_i += g / D * sum_{j:(i,j) on path} w (r_i - c_j)
+//   dD/dc_j -= g / D * sum_{i:(i,j) on path} w (r_i - c_j)
+// (r the row series, c the column series, w the wdtw weight of the cell;
+// cells of row 0 use the row-0 weight index j - 1 of the forward).
 
-__host__ __device__ int64_t dtw32_dir_words(int n, int m, int band_r) {
-    // strips of 16 rows over rows 1..n-1, each covering at most
-    // (|m - n| + 2 r - 1) + 15 columns, clipped to m
-    int64_t strips = (n > 1) ? (n - 2) / kGradStrip + 1 : 0;
-    int64_t cols = (int64_t)(m > n ? m - n : n - m) + 2 * (int64_t)band_r - 1 + kGradStrip - 1;
-    if (cols > m) cols = m;
-    return strips * cols + 1;
+constexpr int kGradStrip = 16;      // rows per strip (2-bit words of 32 bits)
+constexpr int kMaxSegStrips = 64;   // strips per segment (shared-memory tables)
+constexpr int kBwdBlock = 128;      // threads per block of the backward kernel
+
+// (a.h + a.l) < (b.h + b.l) for the compensated pairs of two cumulative costs,
+// as (a.h - b.h) < (b.l - a.l): the hi difference of close values is exact
+// (Sterbenz) and the comparison of the two rounded differences has the sign
+// of the exact compensated difference.  An unreachable cell (+inf, 0) is never
+// preferred to a finite one; two of them compare false (NaN difference).
+__device__ __forceinline__ bool hl_less(HL a, HL b) {
+    return __fsub_rn(a.h, b.h) < __fsub_rn(b.l, a.l);
+}
+
+// Direction words are stored in groups of 8 consecutive words of one thread
+// (one 32-byte sector): word w of thread g at ((w / 8) * nth + g) * 8 + w % 8,
+// so a path walked left or diagonally reads words of one cached sector.
+__device__ __forceinline__ int64_t dir_index(int64_t w, int64_t g, int64_t nth) {
+    return (((w >> 3) * nth + g) << 3) + (w & 7);
+}
+
+// One column of a backward strip: Fast2Sum accumulation, the predecessor by
+// compensated comparison, its 2-bit code (0 diag, 1 up, 2 left) per row into
+// `word`.  With MASK, rows whose bit of M is clear are out of band and hold
+// (+inf, 0).
+template <bool W, bool MASK>
+__device__ __forceinline__ void bwd_column(HL (&P)[kGradStrip], HL bup, HL bdiag, float yc,
+                                           const float (&xr)[kGradStrip], int d0, unsigned M,
+                                           const float *__restrict__ w, int valid,
+                                           uint32_t &word) {
+    HL dg = bdiag;
+    HL up = bup;
+    float cpair[2];
+#pragma unroll
+    for (int k = 0; k < kGradStrip; k++) {
+        const HL lf = P[k];
+        HL best = dg;
+        uint32_t dir = 0;
+        if (hl_less(up, best)) {
+            best = up;
+            dir = 1;
+        }
+        if (hl_less(lf, best)) {
+            best = lf;
+            dir = 2;
+        }
+        float cst;
+        if (W) {
+            const float vv = __fsub_rn(xr[k], yc);
+            cst = __fmul_rn(__fmul_rn(vv, vv), w[(!MASK || k < valid) ? abs(d0 - k) : 0]);
+        } else {
+            if ((k & 1) == 0) sqdiff2(xr[k], xr[k + 1], yc, cpair[0], cpair[1]);
+            cst = cpair[k & 1];
+        }
+        // Fast2Sum (see fwd_column)
+        const float sh = __fadd_rn(best.h, cst);
+        HL nv{sh, __fadd_rn(best.l, __fsub_rn(cst, __fsub_rn(sh, best.h)))};
+        if (MASK && !((M >> k) & 1u)) nv = hl_inf();
+        word |= dir << (2 * k);
+        dg = lf;
+        up = nv;
+        P[k] = nv;
+    }
+}
+
+// Per-lane geometry of a backward item (rows: r series, columns: c series).
+struct BwdItem {
+    const float *R = nullptr, *C = nullptr;
+    float *GR = nullptr, *GC = nullptr;  // gradient rows of the r and c series
+    int n = 0, m = 0, r = 1, mx = 0, mn = 0, lo = 0;
+    int width = 0;
+    int nstrips = 0;                     // strips over rows 1..n-1
+};
+
+// own column range [cs, ce) of strip s (s = -1: row 0, columns [0, lim))
+__device__ __forceinline__ void bwd_range(const BwdItem &B, int s, int &cs, int &ce) {
+    if (B.n < 1 || s >= B.nstrips) {
+        cs = 0x7fffffff;
+        ce = 0;
+        return;
+    }
+    if (s < 0) {
+        cs = 0;
+        ce = imin(B.m, B.mx);
+        return;
+    }
+    const int i0 = 1 + s * kGradStrip;
+    const int rows = imin(kGradStrip, B.n - i0);
+    cs = imax(0, i0 - B.mn - B.r + 1);
+    ce = imin(B.m, i0 + rows - 1 + B.mx);
+}
+
+// Row 0 of every lane into `ring` (warp-uniform loop); lanes with n == 1 get
+// their cost of cell (0, m-1) in `result`.
+template <bool W>
+__device__ void bwd_row0(const BwdItem &B, const float *__restrict__ w, float2 *ring,
+                         int64_t nth, HL &result) {
+    int cs, lim;
+    bwd_range(B, -1, cs, lim);
+    const int lim_w = __reduce_max_sync(0xffffffffu, lim);
+    HL acc = hl_inf();
+    const float x0 = B.n > 0 ? B.R[0] : 0.0f;
+    for (int c = 0; c < lim_w; c++) {
+        if (c < lim) {
+            const float v = __fsub_rn(x0, B.C[c]);
+            float cc = __fmul_rn(v, v);
+            if (W) cc = __fmul_rn(cc, w[c > 0 ? c - 1 : 0]);
+            acc = c == 0 ? HL{cc, 0.0f} : add_c(acc, cc);
+            ring[(int64_t)c * nth] = make_float2(acc.h, acc.l);
+        }
+    }
+    if (B.n == 1) result = acc;
+}
+
+// Strips [s0, s1) of every lane with warp-uniform column bounds.  The row above
+// strip s0 is read from `src`; each strip's bottom row goes to `ring`, the last
+// one's to `last_dst` when it is set.  With DIRS, the direction words of the
+// strips go to dirs[(base + c - cs_w) * nth] and (cs_w, base) of each strip to
+// the warp's tables; returns false (for every lane) if the words would not fit
+// in dir_words.  A lane whose last strip is in the range gets its cost of cell
+// (n-1, m-1) in `result`.
+template <bool W, bool DIRS>
+__device__ bool bwd_strips(const BwdItem &B, int s0, int s1, const float2 *src, float2 *ring,
+                           float2 *last_dst, uint32_t *dirs, int64_t dir_words, int *tab_cs,
+                           int *tab_base, uint32_t *stage, int64_t gtid, int64_t nth,
+                           const float *__restrict__ w, HL &result) {
+    constexpr int S = kGradStrip;
+    const unsigned FULL = 0xffffffffu;
+    const float qnan = __int_as_float(0x7fc00000);
+    const int lane = threadIdx.x & 31;
+    int pstart, pend;
+    bwd_range(B, s0 - 1, pstart, pend);
+    int64_t base = 0;
+    for (int s = s0; s < s1; s++) {
+        const int i0 = 1 + s * S;
+        const int rows = imax(0, imin(S, B.n - i0));
+        float xr[S];
+#pragma unroll
+        for (int k = 0; k < S; k++) xr[k] = (k < rows) ? B.R[i0 + k] : qnan;
+        int cstart, cend;
+        bwd_range(B, s, cstart, cend);
+        int bstart = 0x7fffffff, bend = 0;
+        if (rows == S) {
+            bstart = imax(cstart, i0 + S - 1 + B.lo);
+            bend = imin(cend, i0 + (B.mx - 1) + 1);
+        }
+        const int cs_w = __reduce_min_sync(FULL, cstart);
+        const int ce_w = __reduce_max_sync(FULL, cend);
+        const int bs_w = __reduce_max_sync(FULL, bstart);
+        const int be_w = __reduce_min_sync(FULL, bend);
+        if (ce_w <= cs_w) continue;  // no lane has rows here
+        if (DIRS) {
+            if (base + (ce_w - cs_w) > dir_words) return false;
+            if (lane == 0) {
+                tab_cs[s - s0] = cs_w;
+                tab_base[s - s0] = (int)base;
+            }
+        }
+        const float2 *in = (s == s0) ? src : ring;
+        float2 *out = (s == s1 - 1 && last_dst) ? last_dst : ring;
+        HL P[S];
+#pragma unroll
+        for (int k = 0; k < S; k++) P[k] = hl_inf();
+        auto load_up = [&](int c) {
+            HL b = hl_inf();
+            if (c >= pstart && c < pend) {
+                const float2 t2 = in[(int64_t)c * nth];
+                b = HL{t2.x, t2.y};
+            }
+            return b;
+        };
+        auto load_y = [&](int c) { return c < B.m ? B.C[c] : 0.0f; };
+        HL bdiag = load_up(cs_w - 1);
+        HL nb0 = load_up(cs_w), nb1 = load_up(cs_w + 1);
+        float ny0 = load_y(cs_w), ny1 = load_y(cs_w + 1);
+        const bool last = rows > 0 && (i0 + rows == B.n);
+        const int krow = rows - 1;
+        for (int c = cs_w; c < ce_w; c++) {
+            const HL bup = nb0;
+            const float yc = ny0;
+            nb0 = nb1;
+            ny0 = ny1;
+            nb1 = load_up(c + 2);
+            ny1 = load_y(c + 2);
+            uint32_t word = 0;
+            if (c >= bs_w && c < be_w) {
+                bwd_column<W, false>(P, bup, bdiag, yc, xr, c - i0, 0u, w, rows, word);
+            } else {
+                const unsigned M = c < B.m ? band_bits(c - i0 - B.lo, B.width) : 0u;
+                bwd_column<W, true>(P, bup, bdiag, yc, xr, c - i0, M, w, rows, word);
+            }
+            if (DIRS) {
+                // stage the word; a full group of 8 (or the strip's last
+                // column) goes out as two 16-byte stores
+                const int64_t wi = base + (c - cs_w);
+                stage[(wi & 7) * 33] = word;
+                if ((wi & 7) == 7 || c == ce_w - 1) {
+                    uint4 *dst = reinterpret_cast<uint4 *>(dirs + dir_index(wi & ~(int64_t)7, gtid, nth));
+                    dst[0] = make_uint4(stage[0], stage[33], stage[66], stage[99]);
+                    dst[1] = make_uint4(stage[132], stage[165], stage[198], stage[231]);
+                }
+            }
+            if (last && c == B.m - 1) {
+#pragma unroll
+                for (int k = 0; k < S; k++)
+                    if (k == krow) result = P[k];
+            }
+            out[(int64_t)c * nth] = make_float2(P[S - 1].h, P[S - 1].l);
+            bdiag = bup;
+        }
+        base += ce_w - cs_w;
+        if (rows > 0) {
+            pstart = cstart;
+            pend = cend;
+        }
+    }
+    return true;
+}
+
+// Walk of one lane through the rows of segment g (strips [g K, (g+1) K), and
+// row 0 when g == 0), from (i, j) upward, adding the gradient of every row and
+// column the path leaves.  Returns with i below the segment (or done).
+template <bool W>
+__device__ void bwd_walk(const BwdItem &B, int g, int K, const uint32_t *dirs,
+                         const int *tab_cs, const int *tab_base, int64_t gtid, int64_t nth,
+                         const float *__restrict__ w, float sc, int &i, int &j, float &gr,
+                         float &gc, bool &done) {
+    const int first_row = g == 0 ? 0 : 1 + g * K * kGradStrip;
+    while (!done && i >= first_row) {
+        const float vv = __fsub_rn(B.R[i], B.C[j]);
+        float d = vv;
+        if (W) d = __fmul_rn(w[i == 0 ? imax(j - 1, 0) : abs(i - j)], vv);
+        gr = __fadd_rn(gr, d);
+        gc = __fadd_rn(gc, d);
+        if (i == 0 && j == 0) {
+            atomicAdd(B.GR, sc * gr);
+            atomicAdd(B.GC, -(sc * gc));
+            done = true;
+            break;
+        }
+        uint32_t move;
+        if (i == 0) {
+            move = 2;
+        } else if (j == 0) {
+            move = 1;
+        } else {
+            const int s = (i - 1) / kGradStrip;
+            const int loc = s - g * K;
+            const uint32_t word =
+                dirs[dir_index((int64_t)tab_base[loc] + (j - tab_cs[loc]), gtid, nth)];
+            move = (word >> (2 * ((i - 1) - s * kGradStrip))) & 3u;
+        }
+        if (move != 2) {  // leaving row i
+            atomicAdd(B.GR + i, sc * gr);
+            gr = 0.0f;
+            i -= 1;
+        }
+        if (move != 1) {  // leaving column j
+            atomicAdd(B.GC + j, -(sc * gc));
+            gc = 0.0f;
+            j -= 1;
+        }
+    }
 }
 
 template <bool W>
-__global__ void __launch_bounds__(256) dtw32_backward_kernel(const Dtw32Job J) {
+__global__ void __launch_bounds__(kBwdBlock) dtw32_backward_kernel(const Dtw32Job J) {
     constexpr int S = kGradStrip;
+    __shared__ int tab_cs_all[kBwdBlock / 32][kMaxSegStrips];
+    __shared__ int tab_base_all[kBwdBlock / 32][kMaxSegStrips];
+    // per lane 8 staged direction words, stride 33 words between slots so the
+    // lanes of a warp hit different banks
+    __shared__ uint32_t stage_all[kBwdBlock * 33 / 4 + 8 * 33];
+    const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    int *tab_cs = tab_cs_all[wid];
+    int *tab_base = tab_base_all[wid];
     const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nth = (int64_t)gridDim.x * blockDim.x;
     float2 *ring = J.ring + gtid;
-    uint32_t *dirs = J.dirs + gtid;
+    float2 *ckpt = J.ckpt ? J.ckpt + gtid : nullptr;
+    const int64_t slot = (int64_t)J.ring_cols * nth;  // elements per checkpoint row
+    uint32_t *dirs = J.dirs;
+    uint32_t *stage = stage_all + (threadIdx.x >> 5) * (32 * 8 + 8) + (threadIdx.x & 31);
+    const int K = J.seg_strips;
+    const float *__restrict__ w = J.weights;
+    const float qnan = __int_as_float(0x7fc00000);
     for (;;) {
         const int64_t base = take_items(J.queue, lane);
         if (base >= J.n_items) break;
         const int64_t t = base + lane;
-        if (t >= J.n_items) continue;
-        Item it = load_item(J, t);
-        float *GX = J.grad_x + t * J.gx_stride;
-        float *GY = J.grad_y + t * J.gy_stride;
-        const double g = J.grad_out ? J.grad_out[t] : 1.0;
-        if (it.n < 1 || it.m < 1 || it.m >= J.ring_cols || g == 0.0 ||
-            dtw32_dir_words(it.n, it.m, it.r) > J.dir_words) {
-            for (int i = 0; i < J.x_len; i++) GX[i] = 0.0f;
-            for (int j = 0; j < J.y_len; j++) GY[j] = 0.0f;
-            continue;
-        }
-        HL h = sweep<S, W, true>(it, J.weights, ring, nth, dirs);
-        const double D = sqrt((double)h.h + (double)h.l);
-        const float sc = D > 0.0 ? (float)(g / D) : 0.0f;
-        const float *X = it.X;
-        const float *Y = it.Y;
-        const int n = it.n, m = it.m, r = it.r, mn = it.mn;
-        for (int i = n; i < J.x_len; i++) GX[i] = 0.0f;
-        for (int j = m; j < J.y_len; j++) GY[j] = 0.0f;
-        // strip bookkeeping for the walk (rows 1..n-1 in strips of S)
-        auto strip_cols = [&](int s) {
-            int i0 = 1 + s * S;
-            int rows = imin(S, n - i0);
-            int cs = imax(0, i0 - mn - r + 1);
-            int ce = imin(m, i0 + rows - 1 + it.mx);
-            return ce - cs;
-        };
-        int64_t total = 0;
-        const int nstrips = n > 1 ? (n - 2) / S + 1 : 0;
-        for (int s = 0; s < nstrips; s++) total += strip_cols(s);
-        int s = nstrips - 1;
-        int64_t wofs = s >= 0 ? total - strip_cols(s) : 0;
-        int i = n - 1, j = m - 1;
-        float gx = 0.0f, gy = 0.0f;
-        const int max_steps = n + m;
-        for (int step = 0; step < max_steps; step++) {
-            const float vv = __fsub_rn(X[i], Y[j]);
-            const float gc = W ? __fmul_rn(J.weights[abs(i - j)], vv) : vv;
-            gx = __fadd_rn(gx, gc);
-            gy = __fadd_rn(gy, gc);
-            if (i == 0 && j == 0) break;
-            int move;
-            if (i == 0) {
-                move = 2;
-            } else if (j == 0) {
-                move = 1;
+        BwdItem B;
+        double g = 0.0;
+        bool bad = false;
+        if (t < J.n_items) {
+            Item it = load_item(J, t);
+            int64_t cx, cy;
+            if (J.item_x) {
+                cx = J.item_x[t];
+                cy = J.item_y[t];
             } else {
-                const int i0 = 1 + s * S;
-                const int cs = imax(0, i0 - mn - r + 1);
-                const uint32_t word = dirs[(wofs + (j - cs)) * nth];
-                move = (word >> (2 * (i - i0))) & 3u;
+                cy = t / J.nx;
+                cx = t - cy * J.nx;
             }
-            if (move != 2) {  // leaving row i
-                GX[i] = sc * gx;
-                gx = 0.0f;
-            }
-            if (move != 1) {  // leaving column j
-                GY[j] = -(sc * gy);
-                gy = 0.0f;
-            }
-            if (move != 2) {
-                i -= 1;
-                if (i >= 1 && i < 1 + s * S) {
-                    s -= 1;
-                    wofs -= strip_cols(s);
+            float *gx = J.grad_x + cx * J.gx_stride;
+            float *gy = J.grad_y + cy * J.gy_stride;
+            g = J.grad_out ? J.grad_out[t] : 1.0;
+            if (it.n >= 1 && it.m >= 1 && g != 0.0) {
+                if (!W && it.n > it.m) {  // rows: the shorter series (dtw)
+                    B.R = it.Y;
+                    B.C = it.X;
+                    B.GR = gy;
+                    B.GC = gx;
+                    B.n = it.m;
+                    B.m = it.n;
+                } else {
+                    B.R = it.X;
+                    B.C = it.Y;
+                    B.GR = gx;
+                    B.GC = gy;
+                    B.n = it.n;
+                    B.m = it.m;
+                }
+                B.r = it.r;
+                B.mx = imax(0, B.m - B.n) + B.r;
+                B.mn = imax(0, B.n - B.m);
+                B.lo = -(B.mn + B.r - 1);
+                B.width = (B.mx - 1) - B.lo + 1;
+                B.nstrips = B.n > 1 ? (B.n - 2) / S + 1 : 0;
+                if (B.m >= J.ring_cols) {
+                    bad = true;
+                    B.n = B.m = B.nstrips = 0;
                 }
             }
-            if (move != 1) j -= 1;
+            if (bad) {  // longer than the planned rows: NaN gradients, never zeros
+                for (int i = 0; i < it.n; i++) atomicAdd(gx + i, qnan);
+                for (int j = 0; j < it.m; j++) atomicAdd(gy + j, qnan);
+            }
         }
-        GX[0] = sc * gx;
-        GY[0] = -(sc * gy);
+        const int nstr_w = __reduce_max_sync(FULL, B.nstrips);
+        const int nseg_w = nstr_w > 0 ? (nstr_w + K - 1) / K : 1;
+        const bool fits = nseg_w - 1 <= J.n_ckpt;
+        HL result = hl_inf();
+        bool ok = fits;
+        // pass 1: checkpoints at the segment boundaries (multi-segment items)
+        if (ok && nseg_w > 1) {
+            HL dummy = hl_inf();
+            bwd_row0<W>(B, w, ring, nth, dummy);
+            for (int sg = 0; sg + 1 < nseg_w && ok; sg++) {
+                const float2 *src = sg == 0 ? ring : ckpt + (int64_t)(sg - 1) * slot;
+                ok = bwd_strips<W, false>(B, sg * K, (sg + 1) * K, src, ring,
+                                          ckpt + (int64_t)sg * slot, nullptr, 0, tab_cs,
+                                          tab_base, stage, gtid, nth, w, dummy);
+            }
+        }
+        // pass 2: segments from the last, each recomputed with its directions,
+        // then the walk through its rows
+        const int g_last = B.nstrips > 0 ? (B.nstrips - 1) / K : 0;
+        int i = B.n - 1, j = B.m - 1;
+        float gr = 0.0f, gcol = 0.0f, sc = 0.0f;
+        bool done = B.n < 1;
+        for (int sg = nseg_w - 1; sg >= 0 && ok; sg--) {
+            if (sg == 0) bwd_row0<W>(B, w, ring, nth, result);
+            const float2 *src = sg == 0 ? ring : ckpt + (int64_t)(sg - 1) * slot;
+            ok = bwd_strips<W, true>(B, sg * K, imin((sg + 1) * K, nstr_w), src, ring, nullptr,
+                                     dirs, J.dir_words, tab_cs, tab_base, stage, gtid, nth, w,
+                                     result);
+            if (!ok) break;
+            __syncwarp();
+            if (!done && sg <= g_last) {
+                if (sg == g_last) {
+                    const double D = sqrt((double)result.h + (double)result.l);
+                    sc = D > 0.0 ? (float)(g / D) : 0.0f;
+                }
+                bwd_walk<W>(B, sg, K, dirs, tab_cs, tab_base, gtid, nth, w, sc, i, j, gr, gcol,
+                            done);
+            }
+            __syncwarp();
+        }
+        if (!ok && B.n >= 1) {  // workspace too small for this warp's items
+            for (int a = 0; a < B.n; a++) atomicAdd(B.GR + a, qnan);
+            for (int b = 0; b < B.m; b++) atomicAdd(B.GC + b, qnan);
+        }
     }
 }
 
@@ -559,8 +739,8 @@ int dtw32_backward(const Dtw32Job &J, cudaStream_t s) {
     if (J.n_items == 0) return WB_OK;
     WB_CUDA(cudaMemsetAsync(J.queue, 0, sizeof(unsigned long long), s));
     timer_begin("dtw32_backward_kernel", s);
-    if (J.weights) dtw32_backward_kernel<true><<<J.grid, J.block, 0, s>>>(J);
-    else dtw32_backward_kernel<false><<<J.grid, J.block, 0, s>>>(J);
+    if (J.weights) dtw32_backward_kernel<true><<<J.grid, kBwdBlock, 0, s>>>(J);
+    else dtw32_backward_kernel<false><<<J.grid, kBwdBlock, 0, s>>>(J);
     timer_end(s);
     WB_LAUNCH_CHECK("dtw32_backward_kernel");
     return WB_OK;

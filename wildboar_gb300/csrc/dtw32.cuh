@@ -31,22 +31,24 @@ struct Dtw32Job {
     double *out_cost = nullptr;   // optional per item: hi + lo (squared distance)
     // backward
     const double *grad_out = nullptr;  // per item upstream gradient of the distance
-    float *grad_x = nullptr;      // per item, x_len floats (row i of item t at t * gx_stride)
+    float *grad_x = nullptr;      // per x series (series s at s * gx_stride), accumulated
     int64_t gx_stride = 0;
-    float *grad_y = nullptr;
+    float *grad_y = nullptr;      // per y series, accumulated
     int64_t gy_stride = 0;
     // scratch
     float2 *ring = nullptr;       // [column][thread] (hi, lo) boundary rows
-    int ring_cols = 0;            // columns per thread (max y length + 1)
+    int ring_cols = 0;            // columns per thread (longest series + 1)
     uint32_t *dirs = nullptr;     // [word][thread] direction words (backward)
     int64_t dir_words = 0;        // words per thread
+    float2 *ckpt = nullptr;       // [slot][column][thread] segment checkpoints (backward)
+    int n_ckpt = 0;               // checkpoint rows per thread
+    int seg_strips = 1;           // strips per segment (backward)
     unsigned long long *queue = nullptr;  // work counter (persistent kernel)
     int grid = 0, block = 0;
 };
 
 int dtw32_forward(const Dtw32Job &J, int strip, cudaStream_t s);
 int dtw32_backward(const Dtw32Job &J, cudaStream_t s);
-__host__ __device__ int64_t dtw32_dir_words(int n, int m, int band_r);
 int dtw32_blocks_per_sm(int strip, bool weighted, bool backward, int block);
 int launch_grid_to_matrix(const double *in, int64_t nx, int64_t ny, int upper, double *out,
                           cudaStream_t s);

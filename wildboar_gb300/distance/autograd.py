@@ -1,20 +1,26 @@
-"""Differentiable dtw / wdtw: a torch.autograd.Function over the FP32 kernels.
+"""Differentiable dtw / wdtw: torch.autograd.Functions over the FP32 kernels.
 
 ``dtw_matrix(x, y, r)`` returns the (n_x, n_y) matrix of dtw distances
 (wildboar's ``pairwise_distance(x, y, metric="dtw", metric_params={"r": r})``)
-as a differentiable float64 tensor.  Its backward recomputes every pair's
-forward with a 2-bit direction per band cell and walks the optimal path back
-(dtw_mapping's tie order: diag, up, left -- distance/dtw.py:362-426), giving
+as a differentiable float64 tensor; ``paired_dtw(x, y, r)`` the distances of
+the pairs (x[i], y[i]) of a NaN-padded ragged batch (``paired_distance`` with
+``dim="mean"``).  Their backward (wb_dtw32_backward) recomputes the forward
+with a 2-bit direction per band cell, checkpointing the band boundary every K
+strips for long series, and walks the optimal path back (dtw_mapping's tie
+order: diag, up, left -- distance/dtw.py:362-426), adding in the kernel
 
     dD/dx_i =  sum_{j: (i, j) on the path} w_{|i-j|} (x_i - y_j) / D
     dD/dy_j = -sum_{i: (i, j) on the path} w_{|i-j|} (x_i - y_j) / D
 
-the gradient of D = sqrt(sum over the path of w (x_i - y_j)^2) with the path
-fixed (dtw is differentiable wherever the optimal path is unique).
+to one gradient row per series: the gradient of D = sqrt(sum over the path
+of w (x_i - y_j)^2) with the path fixed (dtw is differentiable wherever the
+optimal path is unique).  Workspace per resident thread: the direction words
+of one segment and one checkpoint row per segment boundary (bounded in total
+by ``WB_GPU_BWD_WORKSPACE_MB``, default 8192).
 
-``barycenter_kmeans`` uses it for DTW-barycenter updates: Adam on the centroids
-with a soft assignment of every series to every centroid, so every pair takes
-part in the backward.
+``barycenter_kmeans`` uses ``dtw_matrix`` for DTW-barycenter updates: Adam on
+the centroids with a soft assignment of every series to every centroid, so
+every pair takes part in the backward.
 """
 
 import ctypes
@@ -47,17 +53,61 @@ class DTWMatrix(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad):
         x, y = ctx.saved_tensors
-        nx, ny = x.shape[0], y.shape[0]
+        # items are t = j * nx + i: the upstream gradient in that order
         g = grad.t().contiguous().to(torch.float64).reshape(-1)
-        gx = torch.empty((ny * nx, x.shape[1]), dtype=torch.float32, device=x.device)
-        gy = torch.empty((ny * nx, y.shape[1]), dtype=torch.float32, device=x.device)
+        gx = torch.zeros_like(x)
+        gy = torch.zeros_like(y)
         job = _job(x, y, ctx.r, ctx.weights)
         _lib.check(_lib.lib().wb_dtw32_backward(
             ctypes.byref(job), g.data_ptr(), gx.data_ptr(), x.shape[1], gy.data_ptr(),
             y.shape[1], _b._stream()))
-        grad_x = gx.view(ny, nx, x.shape[1]).sum(dim=0) if ctx.needs_input_grad[0] else None
-        grad_y = gy.view(ny, nx, y.shape[1]).sum(dim=1) if ctx.needs_input_grad[1] else None
-        return grad_x, grad_y, None, None
+        return (gx if ctx.needs_input_grad[0] else None,
+                gy if ctx.needs_input_grad[1] else None, None, None)
+
+
+class PairedDTW(torch.autograd.Function):
+    """dtw of the pairs of a ragged batch; see ``paired_dtw``."""
+
+    @staticmethod
+    def forward(ctx, x, y, r, tile):
+        plan = _b.plan_pairs(x.detach(), y.detach(), r, tune=False, tile=tile)
+        items = _b.run_plan(plan)
+        ctx.plan = plan
+        ctx.shape = x.shape
+        return _b.combine_dims(plan, items)
+
+    @staticmethod
+    def backward(ctx, grad):
+        plan = ctx.plan
+        N, d, L = ctx.shape
+        # the pair distance is the mean over dims: each (pair, dim) item gets
+        # grad / d; items run in the plan's (sorted) order
+        g = (grad.to(torch.float64) / d).repeat_interleave(d)[plan["order"]].contiguous()
+        gx = torch.zeros((N * d, L), dtype=torch.float32, device=grad.device)
+        gy = torch.zeros_like(gx)
+        job = _b.make_job(plan["xf"], plan["yf"], r=plan["r"], x_lengths=plan["xl"],
+                          y_lengths=plan["yl"], item_x=plan["item_x"],
+                          item_y=plan["item_y"], weights=plan["weights"])
+        _lib.check(_lib.lib().wb_dtw32_backward(
+            ctypes.byref(job), g.data_ptr(), gx.data_ptr(), L, gy.data_ptr(), L,
+            _b._stream()))
+        return gx.view(N, d, L), gy.view(N, d, L), None, None
+
+
+def paired_dtw(x, y, r=1.0, *, tile=None):
+    """Differentiable dtw of the pairs (x[i], y[i]) of a NaN-padded batch.
+
+    x, y: (N, L) or (N, d, L) float32 CUDA tensors; a series ends at its first
+    NaN.  Returns the (N,) float64 distances (mean over dims), differentiable
+    with respect to x and y (gradients are 0 on the padding).
+    """
+    if x.dtype != torch.float32 or y.dtype != torch.float32:
+        raise ValueError("paired_dtw works on float32 CUDA tensors")
+    squeeze = x.dim() == 2
+    if squeeze:
+        x = x.unsqueeze(1)
+        y = y.unsqueeze(1)
+    return PairedDTW.apply(x.contiguous(), y.contiguous(), float(r), tile)
 
 
 def dtw_matrix(x, y, r=1.0, *, g=None):
