@@ -260,6 +260,31 @@ int wb_pairwise_distance_fp32(const wb_series *x, const wb_series *y, int64_t di
                               int32_t metric, const wb_params *params, double *out,
                               int32_t out_on_device, void *stream);
 
+/*
+ * Distance profile with dilation and / or padding (distance_profile,
+ * distance/_distance.py:1560-1619; _dilated_distance_profile,
+ * distance/_cdistance.pyx:804-933, 1809-1841): out (x.n, T + 2 padding -
+ * (L - 1) dilation) where output position p compares the samples of x[i, dim]
+ * at a dilation stride with the values of y[i] (one dim, L values) by the
+ * pairwise metric's early-abandoning distance with an infinite threshold,
+ * divided by (float) k / (float) L when padding leaves only k < L samples.
+ * scale != 0 z-normalises every window by its own mean and variance over L
+ * (variance <= 1e-13 -> std 1); y is given already scaled.
+ */
+int wb_dilated_profile(const wb_series *y, const wb_series *x, int64_t dim, int32_t metric,
+                       const wb_params *params, int64_t dilation, int64_t padding,
+                       int32_t scale, double *out, int32_t out_on_device, void *stream);
+
+/*
+ * The "mass" distance profile (ScaledMassSubsequenceMetric,
+ * distance/_mass.pyx:35-240): z-normalised euclidean distance of y[i, 0] at
+ * every window of x[i, 0] by the MASS formula, with the windows' IncStats
+ * mean / std and the exact dot products in place of the reference's
+ * pocketfft cross-correlation (equal up to that rounding).  out (x.n, T - L + 1).
+ */
+int wb_mass_profile(const wb_series *y, const wb_series *x, double *out, int32_t out_on_device,
+                    void *stream);
+
 /* valid length of each float32 series: index of its first NaN (padding or
  * end-of-series marker, utils/variable_len.py:66-115), else L */
 int wb_series_lengths_f32(const float *x, int64_t n_series, int64_t stride, int32_t L,

@@ -84,6 +84,9 @@ def lib():
                                  ctypes.c_int, pp, i64, dp, ip, dp, ctypes.c_int]
         L.wbo_subsequence.argtypes = [dp, ip, ip, dp, dp, i64, dp, i64, i64, i64, i64,
                                       ctypes.c_int, pp, dp, ip, ctypes.c_int]
+        L.wbo_dilated_profile.argtypes = [dp, i64, dp, i64, i64, i64, i64, ctypes.c_int, pp,
+                                          i64, i64, ctypes.c_int, dp]
+        L.wbo_cumulative_mean_std.argtypes = [dp, i64, i64, dp, dp]
         L.wbo_distance_1d.argtypes = [dp, i64, dp, i64, ctypes.c_int, pp]
         L.wbo_distance_1d.restype = ctypes.c_double
         L.wbo_fast_mean_std.argtypes = [dp, i64, dp, dp]
@@ -669,3 +672,82 @@ def dtw_average_ssg(X, *, r=1.0, g=None, init, sample_weight=None, max_epoch=50,
         else:
             n_stable += 1
     return best_mean, min_cost
+
+
+def dilated_profile(y, x, *, dilation=1, padding=0, dim=0, metric="euclidean",
+                    metric_params=None, scale=False):
+    """distance_profile with dilation / padding (distance/_distance.py:1560-1619,
+    _cdistance.pyx:804-933, 1809-1841): y (n, L) one subsequence per sample,
+    x (n, d, T) or (n, T).  "mass" and "scaled_*" metrics run their unscaled
+    pairwise metric on z-normalised windows.  Positions the reference leaves
+    unwritten (an infinite distance) are NaN."""
+    Y = np.ascontiguousarray(np.atleast_2d(np.asarray(y, dtype=np.float64)))
+    X = np.asarray(x, dtype=np.float64)
+    if X.ndim == 2:
+        X = X[:, None, :]
+    X = np.ascontiguousarray(X)
+    L = Y.shape[1]
+    if padding == "same":
+        padding = ((L - 1) * dilation + 1) // 2
+    if metric == "mass":
+        metric = "scaled_euclidean"
+    scale = metric.startswith("scaled_") or scale
+    if metric.startswith("scaled_"):
+        metric = metric[7:]
+    if scale:
+        std = np.std(Y, axis=-1, keepdims=True)
+        mean = np.mean(Y, axis=-1, keepdims=True)
+        std[std < 1e-13] = 1
+        Y = np.ascontiguousarray((Y - mean) / std)
+    n, d, T = X.shape
+    out = np.empty((n, T + 2 * padding - ((L - 1) * dilation + 1) + 1))
+    p = make_params(metric, metric_params)
+    rc = lib().wbo_dilated_profile(_dp(Y), L, _dp(X), n, d, T, dim, METRIC_IDS[metric],
+                                   ctypes.byref(p), dilation, padding, 1 if scale else 0,
+                                   _dp(out))
+    if rc != 0:
+        raise ValueError("invalid dilation / padding")
+    return out
+
+
+def mass_profile(y, x):
+    """The "mass" distance profile (ScaledMassSubsequenceMetric,
+    distance/_mass.pyx:35-240 with cumulative_mean_std, utils/_stats.pyx:95-111,
+    and the transient statistics of _cdistance.pyx:167-185): y (n, L), x
+    (n, T) (dim 0).  The cross-correlation is numpy's FFT of the zero-padded
+    reversed subsequence times the series, as the reference does with its
+    vendored pocketfft."""
+    Y = np.atleast_2d(np.asarray(y, dtype=np.float64))
+    X = np.asarray(x, dtype=np.float64)
+    if X.ndim == 3:
+        X = X[:, 0, :]
+    X = np.atleast_2d(X)
+    n, T = X.shape
+    L = Y.shape[1]
+    nw = T - L + 1
+    out = np.empty((n, nw))
+    eps = 1e-10
+    for i in range(n):
+        yi = np.ascontiguousarray(Y[i])
+        ex = np.cumsum(yi)[-1]
+        ex2 = np.cumsum(yi * yi)[-1]
+        mu = ex / L
+        var = ex2 / L - mu * mu
+        sd = math.sqrt(var) if var > 1e-13 else 0.0
+        mt = np.empty(nw)
+        st = np.empty(nw)
+        xi = np.ascontiguousarray(X[i])
+        lib().wbo_cumulative_mean_std(_dp(xi), T, L, _dp(mt), _dp(st))
+        yb = np.zeros(T, dtype=complex)
+        yb[:L] = yi[::-1]
+        qt = np.fft.ifft(np.fft.fft(xi.astype(complex)) * np.fft.fft(yb)).real[L - 1:]
+        for w in range(nw):
+            zx, zy = st[w] <= eps, sd <= eps
+            if zx != zy:
+                out[i, w] = math.sqrt(L)
+            elif zx:
+                out[i, w] = 0.0
+            else:
+                z = 2 * (L - (qt[w] - L * mt[w] * mu) / (st[w] * sd))
+                out[i, w] = 0.0 if z < eps else math.sqrt(z)
+    return out

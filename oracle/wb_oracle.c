@@ -1242,6 +1242,109 @@ double wbo_distance_1d(const double *x, idx_t xl, const double *y, idx_t yl, int
     return d;
 }
 
+/* _dilated_distance_profile with dilated_distance_profile /
+ * scaled_dilated_distance_profile (distance/_cdistance.pyx:804-933,
+ * 1809-1841): S (n, L) kernels (scaled by the caller when `scaled`), X
+ * (n, xd, T); out (n, T + 2 padding - (L - 1) dilation).  Positions where the
+ * metric's _eadistance returns false (an infinite distance) are NAN here; the
+ * reference leaves them unwritten. */
+int wbo_dilated_profile(const double *S, idx_t L, const double *X, idx_t n, idx_t xd,
+                        idx_t T, idx_t dim, int metric, const wbo_params *p, idx_t dilation,
+                        idx_t padding, int scaled, double *out)
+{
+    idx_t input_size = T + 2 * padding;
+    idx_t kernel_size = (L - 1) * dilation + 1;
+    if (dilation < 1 || padding < 0 || kernel_size > input_size) return -1;
+    idx_t output_size = input_size - kernel_size + 1;
+    double *xb = malloc(sizeof(double) * (size_t)L);
+    double *kb = malloc(sizeof(double) * (size_t)L);
+    wbo_metric M = {0};
+    M.id = metric;
+    M.p = *p;
+    /* Metric.reset(X, X): weights sized from the series length */
+    metric_reset(&M, X, n, xd, T, X, n, xd, T);
+    wbo_scratch s;
+    scratch_init(&s, imax(L, T));
+    for (idx_t i = 0; i < n; i++) {
+        const double *x = X + (i * xd + dim) * T;
+        const double *kernel = S + i * L;
+        for (idx_t o = 0; o < output_size; o++) {
+            idx_t padding_offset = padding - o;
+            idx_t kernel_offset, input_offset;
+            if (padding_offset > 0) {
+                if (padding_offset % dilation == 0)
+                    kernel_offset = padding_offset;
+                else
+                    kernel_offset = padding_offset + dilation - (padding_offset % dilation);
+                input_offset = kernel_offset - padding_offset;
+            } else {
+                kernel_offset = 0;
+                input_offset = -padding_offset;
+            }
+            idx_t conv = imin(T, input_offset + kernel_size - imax(0, padding_offset)) -
+                         input_offset;
+            idx_t k = 0;
+            double mean = 0, std = 0;
+            for (idx_t j = 0; j < conv; j += dilation) {
+                double v = x[input_offset + j];
+                xb[k] = v;
+                kb[k] = kernel[(j + kernel_offset) / dilation];
+                mean += v;
+                std += v * v;
+                k++;
+            }
+            if (scaled) {
+                mean = mean / L;
+                std = std / L - mean * mean;
+                if (std > 1e-13) std = sqrt(std);
+                else std = 1;
+                for (idx_t j = 0; j < k; j++) xb[j] = (xb[j] - mean) / std;
+            }
+            double md = INF;
+            if (metric_call(&M, &s, xb, k, -1, kb, k, -1, 0, 1, &md))
+                out[i * output_size + o] = md / (double)((float)k / (float)L);
+            else
+                out[i * output_size + o] = NAN;
+        }
+    }
+    scratch_free(&s);
+    metric_free(&M);
+    free(xb);
+    free(kb);
+    return 0;
+}
+
+/* cumulative_mean_std (utils/_stats.pyx:95-111): IncStats mean and std of
+ * every window of length L of x (n_windows = T - L + 1) */
+void wbo_cumulative_mean_std(const double *x, idx_t T, idx_t L, double *mean, double *std)
+{
+    double m = 0, ns = 0, ssq = 0;
+    for (idx_t i = 0; i < T; i++) {
+        double v = x[i], next_m;
+        ns += 1.0;
+        next_m = m + (v - m) / ns;
+        ssq += (v - m) * (v - next_m);
+        m = next_m;
+        if (i >= L - 1) {
+            double var = ns <= 1 ? 0 : ssq / ns;
+            if (var < 1e-13) var = 0.0;
+            mean[i - (L - 1)] = m;
+            std[i - (L - 1)] = sqrt(var);
+            double u = x[i - (L - 1)];
+            if (ns == 1.0) {
+                ns = 0.0;
+                m = 0.0;
+                ssq = 0.0;
+            } else {
+                double old_m = (ns * m - u) / (ns - 1.0);
+                ssq -= (u - m) * (u - old_m);
+                m = old_m;
+                ns -= 1.0;
+            }
+        }
+    }
+}
+
 /* fast_mean_std, exported for tests */
 void wbo_fast_mean_std(const double *x, idx_t n, double *mean, double *std)
 {

@@ -541,6 +541,49 @@ def main():
                 {"metric": metric, "metric_params": params, "k": k},
                 {"idx": idx, "dist": dist})
 
+    # distance profile with dilation / padding (distance/_distance.py:1560-1619,
+    # _cdistance.pyx:804-933): pairwise metrics on the gathered windows,
+    # "mass" / "scaled_*" on z-normalised windows, partial windows rescaled
+    TD = _walk(rng, (3, 70))
+    QD = _walk(rng, (3, 9))
+    for metric, params in (("euclidean", {}), ("mass", {}), ("scaled_euclidean", {}),
+                           ("dtw", {"r": 0.3}), ("scaled_dtw", {"r": 0.5}),
+                           ("wdtw", {"g": 0.1}), ("ddtw", {}), ("wddtw", {"g": 0.2}),
+                           ("lcss", {"epsilon": 0.7}),
+                           ("edr", {}), ("erp", {"g": 0.2}), ("msm", {}), ("twe", {}),
+                           ("adtw", {"p": 0.5})):
+        for dil, pad in ((1, 3), (2, 0), (2, "same"), (3, 6)):
+            dp = distance_profile(QD, TD, metric=metric, metric_params=params,
+                                  dilation=dil, padding=pad)
+            add(f"dprofile_{metric}_{tagof(params)}_d{dil}_p{pad}", "dilated_profile",
+                {"x": TD, "y": QD},
+                {"metric": metric, "metric_params": params, "dilation": dil,
+                 "padding": pad}, {"d": dp})
+    # scale=True with a plain metric on 3-d input (dim 0: for dim > 0 the
+    # reference reads the one-dim subsequence array at S[i, dim], past its end),
+    # and one subsequence broadcast against one series
+    TD3 = _walk(rng, (2, 3, 40))
+    QD3 = _walk(rng, (2, 7))
+    dp = distance_profile(QD3, TD3, metric="dtw", metric_params={"r": 0.2}, dilation=2,
+                          padding=4, dim=0, scale=True)
+    add("dprofile_dtw_scale_3d", "dilated_profile", {"x": TD3, "y": QD3},
+        {"metric": "dtw", "metric_params": {"r": 0.2}, "dilation": 2, "padding": 4,
+         "dim": 0, "scale": True}, {"d": dp})
+    dp = distance_profile(QD[0], TD[1], metric="euclidean", dilation=4, padding="same")
+    add("dprofile_euclidean_1d_same", "dilated_profile", {"x": TD[1], "y": QD[0]},
+        {"metric": "euclidean", "metric_params": {}, "dilation": 4, "padding": "same"},
+        {"d": dp})
+    # the default "mass" profile (dilation 1, no padding): z-normalised
+    # euclidean by an FFT cross-correlation; a constant stretch of series 1 and
+    # a constant subsequence reach the zero-variance branches
+    TM = _walk(rng, (4, 120))
+    TM[1, 30:75] = 3.0
+    for L in (5, 16, 40):
+        QM = _walk(rng, (4, L))
+        QM[2] = 1.0
+        dp = distance_profile(QM, TM)
+        add(f"mass_L{L}", "mass_profile", {"x": TM, "y": QM}, {}, {"d": dp})
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"reference_version": getattr(wildboar, "__version__", "?"),

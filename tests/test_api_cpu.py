@@ -202,8 +202,6 @@ def test_subsequence_search_validation():
         distance_profile(X[:2, :10], X)
     with pytest.raises(ValueError, match="larger than input"):
         distance_profile(np.zeros(40), X, metric="euclidean")
-    with pytest.raises(NotImplementedError):
-        distance_profile(X[0, :5], X)  # the FFT 'mass' metric
 
 
 def test_sharded_requires_process_group():
@@ -282,3 +280,25 @@ def test_shapelet_statistics_grouped_by_length_bitwise():
     for i, s in enumerate(shp):
         assert np.mean(s).view(np.uint64) == mean[i].view(np.uint64), i
         assert np.std(s).view(np.uint64) == std[i].view(np.uint64), i
+
+
+def test_distance_profile_parameter_validation():
+    # @validate_params of distance_profile (distance/_distance.py:1460-1476) and
+    # the checks of its body (:1561-1581); all raise before any device call
+    from wildboar_gb300.distance import InvalidParameterError, distance_profile
+
+    y, x = np.arange(5.0), np.cumsum(np.ones((2, 30)), axis=1)
+    with pytest.raises(InvalidParameterError, match="'dilation' parameter"):
+        distance_profile(y, x, dilation=0)
+    with pytest.raises(InvalidParameterError, match="'padding' parameter"):
+        distance_profile(y, x, padding=-1)
+    with pytest.raises(InvalidParameterError, match="'padding' parameter"):
+        distance_profile(y, x, padding="valid")
+    with pytest.raises(InvalidParameterError, match="'metric' parameter"):
+        distance_profile(y, x, metric="wlcss")
+    with pytest.raises(ValueError, match="only supported for odd"):
+        distance_profile(np.arange(4.0), x, padding="same")
+    with pytest.raises(ValueError, match="larger than input"):
+        distance_profile(np.arange(9.0), x[:, :5], dilation=2, padding=1)
+    with pytest.raises(NotImplementedError, match="pointwise"):
+        distance_profile(y, x, metric="scaled_manhattan", dilation=2)

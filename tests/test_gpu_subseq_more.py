@@ -9,6 +9,7 @@ machines), indices and match sets exact.
 """
 
 import math
+import zlib
 
 import numpy as np
 import pytest
@@ -71,6 +72,61 @@ def test_argmin_subsequence_golden(case):
                                             scale=a["scale"], return_distance=True)
     np.testing.assert_array_equal(idx, case["outputs"]["idx"])
     np.testing.assert_allclose(dist, case["outputs"]["dist"], rtol=RTOL, atol=0)
+
+
+@_cases("dilated_profile")
+def test_dilated_profile_golden(case):
+    a = case["args"]
+    inp = case["inputs"]
+    dp = distance_profile(inp["y"], inp["x"], metric=a["metric"],
+                          metric_params=a.get("metric_params"), dilation=a["dilation"],
+                          padding=a["padding"], dim=a.get("dim", 0),
+                          scale=a.get("scale", False))
+    want = case["outputs"]["d"]
+    assert dp.shape == want.shape
+    np.testing.assert_allclose(dp, want, rtol=RTOL, atol=0)
+
+
+# the reference's MASS cross-correlation is a pocketfft product, the kernel's
+# an exact dot product: the profiles agree to the FFT's rounding
+MASS_ATOL = 1e-8
+
+
+@_cases("mass_profile")
+def test_mass_profile_golden(case):
+    inp = case["inputs"]
+    dp = distance_profile(inp["y"], inp["x"])
+    want = case["outputs"]["d"]
+    assert dp.shape == want.shape
+    np.testing.assert_allclose(dp, want, rtol=0, atol=MASS_ATOL)
+
+
+@pytest.mark.parametrize("metric,params", [("euclidean", {}), ("mass", {}), ("dtw", {"r": 0.2}),
+                                           ("scaled_msm", {}), ("wdtw", {"g": 0.1}),
+                                           ("edr", {}), ("twe", {})])
+@pytest.mark.parametrize("dilation,padding", [(1, 4), (3, 0), (2, "same"), (5, 17)])
+def test_dilated_profile_vs_oracle(metric, params, dilation, padding):
+    rng = np.random.default_rng(zlib.crc32(repr((metric, dilation, padding)).encode()))
+    X = np.cumsum(rng.standard_normal((6, 2, 300)), axis=-1)
+    Y = np.cumsum(rng.standard_normal((6, 11)), axis=-1)
+    want = O.dilated_profile(Y, X, dilation=dilation, padding=padding, dim=1, metric=metric,
+                             metric_params=params)
+    got = distance_profile(Y, X, dilation=dilation, padding=padding, dim=1, metric=metric,
+                           metric_params=params)
+    np.testing.assert_allclose(got, want, rtol=RTOL, atol=0)
+    # device inputs give the same host profile
+    got_d = distance_profile(Y, torch.as_tensor(X, device="cuda"), dilation=dilation,
+                             padding=padding, dim=1, metric=metric, metric_params=params)
+    np.testing.assert_array_equal(got_d, got)
+
+
+def test_mass_profile_vs_oracle():
+    rng = np.random.default_rng(31)
+    X = np.cumsum(rng.standard_normal((5, 500)), axis=-1)
+    Y = np.cumsum(rng.standard_normal((5, 37)), axis=-1)
+    X[3, 100:200] = -2.0
+    np.testing.assert_allclose(distance_profile(Y, X), O.mass_profile(Y, X), rtol=0,
+                               atol=MASS_ATOL)
 
 
 @_cases("distance_profile")

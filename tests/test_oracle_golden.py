@@ -93,6 +93,13 @@ def run_oracle(case):
         d, _ = O.subsequence_matches([q] * X.shape[0], X, math.inf, metric=metric,
                                      metric_params=params, transient=True)
         return {"d": np.squeeze(d[:, : X.shape[2] - q.shape[0] + 1])}
+    if kind == "dilated_profile":
+        d = O.dilated_profile(np.atleast_2d(inp["y"]), _ts(inp["x"]), dilation=a["dilation"],
+                              padding=a["padding"], dim=a.get("dim", 0), metric=metric,
+                              metric_params=params, scale=a.get("scale", False))
+        return {"d": np.squeeze(d)}
+    if kind == "mass_profile":
+        return {"d": np.squeeze(O.mass_profile(inp["y"], _ts(inp["x"])))}
     if kind in ("subsequence_match", "paired_subsequence_match"):
         X = _ts(inp["x"])
         if kind == "subsequence_match":
@@ -197,7 +204,10 @@ ORACLE_KINDS = {"pairwise", "singleton", "paired", "argmin", "subsequence", "ali
 ORACLE_KINDS |= {"argmin_subsequence", "distance_profile", "subsequence_match",
                  "paired_subsequence_match"}
 ORACLE_KINDS |= {"dtw_average", "kmeans", "knn", "kneighbors", "lb_keogh", "lb_kim",
-                 "dtw_helpers"}
+                 "dtw_helpers", "dilated_profile", "mass_profile"}
+# the reference's MASS takes its cross-correlation from its vendored pocketfft,
+# the oracle from numpy's FFT: the profiles agree to the FFT's rounding
+FFT_ATOL = 1e-9
 CASES = [c for c in _golden.cases() if c["kind"] in ORACLE_KINDS]
 
 
@@ -246,6 +256,8 @@ def test_oracle_matches_reference(case):
         if want.dtype.kind in "iu":
             keep = want >= 0  # -1: the reference leaves the index unset
             np.testing.assert_array_equal(g[keep], want[keep])
+        elif case["kind"] == "mass_profile":
+            np.testing.assert_allclose(g, want, rtol=0, atol=FFT_ATOL)
         elif EXACT:
             np.testing.assert_array_equal(g, want)
         else:

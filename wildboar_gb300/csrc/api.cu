@@ -1205,6 +1205,134 @@ extern "C" int wb_paired_subsequence_distance(
                         out_dist, out_idx, out_on_device, stream_, true);
 }
 
+// ---------------------------------------------------------------------------
+// distance profiles outside the subsequence scans
+
+extern "C" int wb_dilated_profile(const wb_series *y, const wb_series *x, int64_t dim,
+                                  int32_t metric, const wb_params *params, int64_t dilation,
+                                  int64_t padding, int32_t scale, double *out,
+                                  int32_t out_on_device, void *stream_) {
+    WB_TRY(check_series(y, "y"));
+    WB_TRY(check_series(x, "x"));
+    if (!params) return fail(WB_EINVAL, "params is NULL");
+    WB_TRY(check_dim(x, dim));
+    if (!is_elastic(metric) && metric != WB_EUCLIDEAN)
+        return fail(WB_EUNSUPPORTED, "unsupported metric id " + std::to_string(metric));
+    if (dilation < 1) return fail(WB_EINVAL, "dilation must be >= 1");
+    if (padding < 0) return fail(WB_EINVAL, "padding must be >= 0");
+    if (y->n != x->n) return fail(WB_EINVAL, "y and x must have the same number of samples.");
+    const int L = (int)y->n_timestep, T = (int)x->n_timestep;
+    const int64_t ks = (int64_t)(L - 1) * dilation + 1;
+    const int64_t input_size = T + 2 * padding;
+    if (L < 1 || ks > input_size)
+        return fail(WB_EINVAL, "subsequence in y is larger than input in x.");
+    const int64_t n = x->n;
+    const int out_size = (int)(input_size - ks + 1);
+    if (n == 0) return WB_OK;
+    if (!out) return fail(WB_EINVAL, "out is NULL");
+    cudaStream_t s = (cudaStream_t)stream_;
+    // window size k of every output position (_cdistance.pyx:832-852);
+    // positions of equal k form runs
+    std::vector<int> kk(out_size);
+    for (int p = 0; p < out_size; p++) {
+        const int64_t po = padding - p;
+        int64_t ko = 0, io;
+        if (po > 0) {
+            ko = po % dilation == 0 ? po : po + dilation - po % dilation;
+            io = ko - po;
+        } else {
+            io = -po;
+        }
+        const int64_t conv = std::min<int64_t>(T, io + ks - std::max<int64_t>(0, po)) - io;
+        kk[p] = conv > 0 ? (int)((conv + dilation - 1) / dilation) : 0;
+    }
+    // workspace: staged inputs, the largest run's windows and distances, the
+    // metric tables at the largest k, the output
+    int64_t max_run = 0;
+    for (int p = 0; p < out_size;) {
+        int q = p;
+        while (q < out_size && kk[q] == kk[p]) q++;
+        max_run = std::max<int64_t>(max_run, q - p);
+        p = q;
+    }
+    const int64_t rows_max = n * max_run;
+    ElasticJob J0;
+    WB_TRY(metric_fields(metric, params, L, L, true, J0));
+    SeriesSet probeR{nullptr, 0, rows_max, L}, probeC{nullptr, 0, rows_max, L};
+    ElasticJob probe = J0;
+    probe.rows = probeR;
+    probe.cols = probeC;
+    probe.mode = PM_PAIRED;
+    size_t need = stage_bytes(x) + stage_bytes(y) + 2 * align256((size_t)rows_max * L * 8) +
+                  align256((size_t)rows_max * 8) +
+                  table_bytes(metric, params, probeR, probeC, rows_max, rows_max, L, L) +
+                  align256((size_t)std::max(T, 1) * 8) + elastic_workspace_bytes(probe) +
+                  align256((size_t)n * out_size * 8);
+    Workspace ws(s);
+    WB_TRY(ws.reserve(need));
+    SeriesSet sx, sy;
+    WB_TRY(stage(x, dim, ws, sx));
+    // the subsequences have one dim (the reference reads y[i, dim], past the
+    // end of y for dim > 0)
+    WB_TRY(stage(y, 0, ws, sy));
+    double *dout = out_on_device ? out : ws.take<double>((size_t)n * out_size);
+    WB_TAKE(xw, double, ws, (size_t)rows_max * L);
+    WB_TAKE(kw, double, ws, (size_t)rows_max * L);
+    WB_TAKE(dist, double, ws, (size_t)rows_max);
+    if (!dout) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    const size_t mark = ws.mark();
+    for (int p = 0; p < out_size;) {
+        int q = p;
+        while (q < out_size && kk[q] == kk[p]) q++;
+        const int k = kk[p], np = q - p;
+        const int64_t rows = n * np;
+        ws.rewind(mark);
+        WB_TRY(launch_dilated_gather(sx.base, n, sx.stride, T, sy.base, sy.stride, L,
+                                     (int)dilation, (int)padding, p, np, k, scale, xw, kw, s));
+        // metric._eadistance(x window, k, kernel, k): the window is the
+        // recurrence's rows; weights sized from the series length T as in
+        // Metric.reset(X, X)
+        ElasticJob J;
+        WB_TRY(metric_fields(metric, params, k, k, true, J));
+        J.rows = SeriesSet{xw, k, rows, k};
+        J.cols = SeriesSet{kw, k, rows, k};
+        WB_TRY(build_tables(metric, params, J, ws, false, T, T));
+        J.out = dist;
+        J.out_ld = 0;
+        J.mode = PM_PAIRED;
+        WB_TRY(launch_elastic(J, ws, nullptr));
+        WB_TRY(launch_dilated_scatter(dist, n, p, np, k, L, dout, out_size, s));
+        p = q;
+    }
+    return finish_host_copy(out, dout, (size_t)n * out_size * sizeof(double), out_on_device, s);
+}
+
+extern "C" int wb_mass_profile(const wb_series *y, const wb_series *x, double *out,
+                               int32_t out_on_device, void *stream_) {
+    WB_TRY(check_series(y, "y"));
+    WB_TRY(check_series(x, "x"));
+    if (y->n != x->n) return fail(WB_EINVAL, "y and x must have the same number of samples.");
+    const int L = (int)y->n_timestep, T = (int)x->n_timestep;
+    if (L < 1 || L > T) return fail(WB_EINVAL, "subsequence in y is larger than input in x.");
+    const int64_t n = x->n;
+    const int nwin = T - L + 1;
+    if (n == 0) return WB_OK;
+    if (!out) return fail(WB_EINVAL, "out is NULL");
+    cudaStream_t s = (cudaStream_t)stream_;
+    Workspace ws(s);
+    WB_TRY(ws.reserve(stage_bytes(x) + stage_bytes(y) + 3 * align256((size_t)n * nwin * 8)));
+    SeriesSet sx, sy;
+    // _DistanceProfile reads x[i, 0] and y[i, 0] (distance/_cdistance.pyx:1680-1699)
+    WB_TRY(stage(x, 0, ws, sx));
+    WB_TRY(stage(y, 0, ws, sy));
+    WB_TAKE(mt, double, ws, (size_t)n * nwin);
+    WB_TAKE(st, double, ws, (size_t)n * nwin);
+    double *dout = out_on_device ? out : ws.take<double>((size_t)n * nwin);
+    if (!dout) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    WB_TRY(launch_mass_profile(sx.base, n, sx.stride, T, sy.base, sy.stride, L, mt, st, dout, s));
+    return finish_host_copy(out, dout, (size_t)n * nwin * sizeof(double), out_on_device, s);
+}
+
 extern "C" const char *wb_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" int32_t wb_version(void) { return 1; }

@@ -49,4 +49,14 @@ int launch_subseq(const SubseqJob &J, bool scaled, Workspace &ws);
 int launch_subseq_profile(const SubseqJob &J, bool scaled, Workspace &ws, double *raw,
                           int64_t ld);
 
+// profile.cu: dilated / padded distance profile windows and the MASS profile
+int launch_dilated_gather(const double *x, int64_t n, int64_t x_stride, int T, const double *y,
+                          int64_t y_stride, int L, int dilation, int padding, int p0, int np,
+                          int k, int scale, double *xw, double *kw, cudaStream_t s);
+int launch_dilated_scatter(const double *d, int64_t n, int p0, int np, int k, int L,
+                           double *out, int64_t out_ld, cudaStream_t s);
+int launch_mass_profile(const double *x, int64_t n, int64_t x_stride, int T, const double *y,
+                        int64_t y_stride, int L, double *mean_tab, double *std_tab,
+                        double *out, cudaStream_t s);
+
 }  // namespace wb

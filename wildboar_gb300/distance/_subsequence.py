@@ -22,12 +22,25 @@ import numpy as np
 
 from .. import _lib
 from ._distance import (
+    InvalidParameterError,
     _as_input,
+    _device_of,
+    _empty,
+    _stream,
     _format_return,
     _pack_shapelets,
     _validate_subsequence,
+    check_metric,
     check_subsequence_metric,
 )
+
+_P = ctypes.POINTER
+_lib.declare("wb_dilated_profile", [_P(_lib.Series), _P(_lib.Series), ctypes.c_int64,
+                                    ctypes.c_int32, _P(_lib.Params), ctypes.c_int64,
+                                    ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p,
+                                    ctypes.c_int32, ctypes.c_void_p])
+_lib.declare("wb_mass_profile", [_P(_lib.Series), _P(_lib.Series), ctypes.c_void_p,
+                                 ctypes.c_int32, ctypes.c_void_p])
 from ._metrics import check_scalar
 
 _SQRT = {0, 1, 2, 3, 4, 5, 32, 33}      # euclidean, dtw family, scaled_euclidean / dtw
@@ -271,14 +284,69 @@ def _jagged(lst):
     return arr
 
 
+# the metric names distance_profile accepts (the reference's
+# _SUBSEQUENCE_METRICS keys, distance/_distance.py:149-183); the pointwise
+# metrics among them (normalized_euclidean, manhattan, minkowski, chebyshev,
+# cosine, angular and their scaled_ forms) are not provided here
+_PROFILE_METRIC_NAMES = (
+    "euclidean", "scaled_euclidean", "normalized_euclidean", "adtw", "scaled_adtw", "wdtw",
+    "scaled_wdtw", "ddtw", "scaled_ddtw", "wddtw", "scaled_wddtw", "dtw", "scaled_dtw",
+    "lcss", "scaled_lcss", "edr", "scaled_edr", "twe", "scaled_twe", "msm", "scaled_msm",
+    "erp", "scaled_erp", "mass", "manhattan", "scaled_manhattan", "minkowski",
+    "scaled_minkowski", "chebyshev", "scaled_chebyshev", "cosine", "scaled_cosine",
+    "angular", "scaled_angular")
+
+
+def _validate_profile_params(dilation, padding, dim, metric):
+    # @validate_params of distance/_distance.py:1460-1476
+    if not (callable(metric) or (isinstance(metric, str) and metric in _PROFILE_METRIC_NAMES)):
+        opts = ", ".join(repr(m) for m in _PROFILE_METRIC_NAMES)
+        raise InvalidParameterError(
+            "The 'metric' parameter of distance_profile must be a callable or a str among "
+            f"{{{opts}}}. Got {metric!r} instead.")
+    if not (isinstance(dilation, numbers.Integral) and not isinstance(dilation, bool)) or \
+            dilation < 1:
+        raise InvalidParameterError(
+            "The 'dilation' parameter of distance_profile must be an int in the range "
+            f"[1, inf). Got {dilation!r} instead.")
+    if not ((isinstance(padding, numbers.Integral) and not isinstance(padding, bool)
+             and padding >= 0) or padding == "same"):
+        raise InvalidParameterError(
+            "The 'padding' parameter of distance_profile must be an int in the range "
+            f"[0, inf) or a str among {{'same'}}. Got {padding!r} instead.")
+    if not (isinstance(dim, numbers.Integral) and not isinstance(dim, bool)) or dim < 0:
+        raise InvalidParameterError(
+            "The 'dim' parameter of distance_profile must be an int in the range [0, inf). "
+            f"Got {dim!r} instead.")
+
+
+def _profile_device_call(entry, Y, X, out_shape, *args):
+    """One profile entry point; the result is a host array like the other
+    profile paths."""
+    dev = _device_of(X, Y)
+    out = _empty(dev, out_shape)
+    sy, sx = Y.series(), X.series()
+    st = getattr(_lib.lib(), entry)(ctypes.byref(sy), ctypes.byref(sx), *args,
+                                    _lib.ptr(out), 1 if dev is not None else 0,
+                                    _stream(X, Y))
+    _lib.check(st)
+    return out.cpu().numpy() if dev is not None else out
+
+
 def distance_profile(y, x, *, dilation=1, padding=0, dim=0, metric="mass",
                      metric_params=None, scale=False, n_jobs=None):
     """Distance of the subsequence(s) y at every time point of x.
 
-    Mirrors distance/_distance.py:1477-1620 for dilation 1 and no padding
-    (the SubsequenceMetric profile); the dilated / padded path and the FFT
-    'mass' metric are not provided.
+    Mirrors distance/_distance.py:1477-1620.  Dilation 1 without padding runs
+    the SubsequenceMetric profile; the default metric "mass" is the
+    z-normalised euclidean profile of the MASS formula, evaluated with exact
+    dot products where the reference uses a pocketfft cross-correlation
+    (wb_mass_profile: equal up to the FFT's rounding).  Dilation or padding
+    runs _dilated_distance_profile (distance/_cdistance.pyx:1809-1841) with the
+    pairwise metric ("mass" and "scaled_*" metrics become their unscaled
+    pairwise metric on z-normalised windows; wb_dilated_profile).
     """
+    _validate_profile_params(dilation, padding, dim, metric)
     y = np.asarray(y, dtype=float).squeeze()
     xa = x
     if not _lib.is_torch_cuda(x):
@@ -290,34 +358,65 @@ def distance_profile(y, x, *, dilation=1, padding=0, dim=0, metric="mass",
     if y.ndim == 1 and xdim != 1:
         y = np.broadcast_to(y, shape=(xa.shape[0], y.shape[0]))
     X = _as_input(xa)
-    y2 = np.atleast_2d(y)
-    if y2.shape[1] > X.shape[-1]:
+    y2 = np.ascontiguousarray(np.atleast_2d(y))
+    L = y2.shape[1]
+    shapelet_size = (L - 1) * dilation + 1
+    if padding == "same":
+        if L % 2 == 0:
+            raise ValueError("padding='same' is only supported for odd subsequence length")
+        padding = shapelet_size // 2
+    if shapelet_size > X.shape[-1] + 2 * padding:
         raise ValueError("subsequence in y is larger than input in x.")
     if y2.shape[0] != X.shape[0]:
         raise ValueError("y and x must have the same number of samples.")
     if dim >= X.shape[1]:
         raise ValueError(f"The parameter dim must be dim ({dim}) < n_dims ({X.shape[1]})")
-    if dilation != 1 or padding != 0:
-        raise NotImplementedError("only dilation=1 and padding=0 are provided")
-    if metric == "mass":
-        raise NotImplementedError("the 'mass' metric is not provided; use "
-                                  "metric='scaled_euclidean'")
-    Metric_ = check_subsequence_metric(metric, scale=scale)
     metric_params = metric_params if metric_params is not None else {}
+    base = metric[7:] if isinstance(metric, str) and metric.startswith("scaled_") else metric
+    if base in ("normalized_euclidean", "manhattan", "minkowski", "chebyshev", "cosine",
+                "angular"):
+        raise NotImplementedError(
+            f"the pointwise metric {metric!r} is not provided by wildboar_gb300")
+    if dilation == 1 and padding == 0:
+        if metric == "mass":
+            Y = _as_input(y2)
+            dp = _profile_device_call("wb_mass_profile", Y, X,
+                                      (X.shape[0], X.shape[-1] - L + 1))
+            return np.squeeze(dp)
+        Metric_ = check_subsequence_metric(metric, scale=scale)
+        m = Metric_(**metric_params)
+        shapelets = [np.ascontiguousarray(r, dtype=float) for r in y2]
+        # _DistanceProfile reads y[i, 0] and x[i, 0] whatever dim is
+        # (distance/_cdistance.pyx:1680-1699)
+        raw, key, lens = _profile_raw(shapelets, X, 0, m, transient=True)
+        nwin = X.shape[-1] - L + 1
+        dp = _distances(m.metric_id, raw[:, :nwin], float(L))
+        if m.metric_id == _SCALED_DTW:
+            # the profile is scaled_dtw_matches with an infinite threshold over
+            # a profile of ones: windows it does not keep stay 1
+            keep = _match_mask(m.metric_id, raw[:, :nwin], key[:, :nwin], dp, float(L),
+                               X.shape[-1], math.inf)
+            dp = np.where(keep, dp, 1.0)
+        return np.squeeze(dp)
+    # distance/_distance.py:1590-1616
+    if metric == "mass":
+        metric = "scaled_euclidean"
+    scale = (isinstance(metric, str) and metric.startswith("scaled_")) or scale
+    if isinstance(metric, str) and metric.startswith("scaled_"):
+        metric = metric[7:]
+    Metric_ = check_metric(metric)
     m = Metric_(**metric_params)
-    shapelets = [np.ascontiguousarray(r, dtype=float) for r in y2]
-    # _DistanceProfile reads y[i, 0] and x[i, 0] whatever dim is
-    # (distance/_cdistance.pyx:1680-1699)
-    raw, key, lens = _profile_raw(shapelets, X, 0, m, transient=True)
-    nwin = X.shape[-1] - y2.shape[1] + 1
-    dp = _distances(m.metric_id, raw[:, :nwin], float(y2.shape[1]))
-    if m.metric_id == _SCALED_DTW:
-        # the profile is scaled_dtw_matches with an infinite threshold over a
-        # profile of ones: windows it does not keep stay 1
-        L = float(y2.shape[1])
-        keep = _match_mask(m.metric_id, raw[:, :nwin], key[:, :nwin], dp, L,
-                           X.shape[-1], math.inf)
-        dp = np.where(keep, dp, 1.0)
+    if scale:
+        std = np.std(y2, axis=-1, keepdims=True)
+        mean = np.mean(y2, axis=-1, keepdims=True)
+        std[std < 1e-13] = 1  # EPSILON of distance/_cdistance.pxd
+        y2 = (y2 - mean) / std
+    Y = _as_input(np.ascontiguousarray(y2))
+    out_size = X.shape[-1] + 2 * padding - shapelet_size + 1
+    p = m.params()
+    dp = _profile_device_call("wb_dilated_profile", Y, X, (X.shape[0], out_size), dim,
+                              m.metric_id, ctypes.byref(p), dilation, padding,
+                              1 if scale else 0)
     return np.squeeze(dp)
 
 
