@@ -261,6 +261,22 @@ int wb_pairwise_distance_fp32(const wb_series *x, const wb_series *y, int64_t di
                               int32_t out_on_device, void *stream);
 
 /*
+ * wb_subsequence_profile for WB_SCALED_EUCLIDEAN with the reference's
+ * threshold stop: the sum of window w of pair i stops before the first term
+ * at which it is >= stop_sq[i] (host array of m values), as
+ * inner_scaled_euclidean_distance breaks on the squared threshold inside
+ * scaled_euclidean_distance_matches (distance/_metric.pyx:625-651, 798-860).
+ * A window then matches threshold t iff out_raw <= t^2 with distance
+ * sqrt(out_raw): a partial sum equal to t^2 matches with that distance, and
+ * t = 0 matches every window with distance 0, as in the reference.
+ */
+int wb_subsequence_profile_stop(const double *shapelets, const int64_t *offsets,
+                                const int64_t *lengths, const double *means,
+                                const double *stds, int64_t m, const wb_series *x, int64_t dim,
+                                const double *stop_sq, double *out_raw, int64_t ld,
+                                int32_t out_on_device, void *stream);
+
+/*
  * Distance profile with dilation and / or padding (distance_profile,
  * distance/_distance.py:1560-1619; _dilated_distance_profile,
  * distance/_cdistance.pyx:804-933, 1809-1841): out (x.n, T + 2 padding -

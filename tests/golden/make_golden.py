@@ -584,6 +584,27 @@ def main():
         dp = distance_profile(QM, TM)
         add(f"mass_L{L}", "mass_profile", {"x": TM, "y": QM}, {}, {"d": dp})
 
+    # scaled_euclidean matching stops a window's sum at the first term where it
+    # is >= t^2 and keeps the window if that partial sum is <= t^2
+    # (distance/_metric.pyx:625-651, 798-860): with t = 0 every window matches
+    # with distance 0; one series holds an exact copy of the subsequence
+    TZ = _walk(rng, (3, 40))
+    qz = TZ[1, 5:14].copy()
+    for t in (0.0, 0.5):
+        res = subsequence_match(qz, TZ, threshold=t, metric="scaled_euclidean",
+                                return_distance=True)
+        add(f"match_scaled_euclidean_t{t}", "subsequence_match", {"x": TZ, "y": qz},
+            {"metric": "scaled_euclidean", "metric_params": {},
+             "kw": {"threshold": t}}, flat(res))
+    shpz = [TZ[i, 2 + i:10 + i].copy() for i in range(3)]
+    res = paired_subsequence_match(shpz, TZ, threshold=0.0, metric="scaled_euclidean",
+                                   return_distance=True)
+
+    add("paired_match_scaled_euclidean_t0", "paired_subsequence_match",
+        {"x": TZ, "shapelets": np.concatenate(shpz), "lengths": np.array([8, 8, 8])},
+        {"metric": "scaled_euclidean", "metric_params": {}, "kw": {"threshold": 0.0}},
+        flat(res))
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"reference_version": getattr(wildboar, "__version__", "?"),

@@ -70,6 +70,8 @@ def _declare(L):
                                                  i32, P(Params), i32, i64, vp, vp, i32, vp]
     L.wb_subsequence_profile.argtypes = [vp, vp, vp, vp, vp, i64, P(Series), i64, i32,
                                          P(Params), vp, vp, i64, i32, i32, vp]
+    L.wb_subsequence_profile_stop.argtypes = [vp, vp, vp, vp, vp, i64, P(Series), i64, vp,
+                                              vp, i64, i32, vp]
     L.wb_last_error.restype = ctypes.c_char_p
     L.wb_version.restype = i32
     L.wb_release_workspace.argtypes = [vp]

@@ -992,7 +992,8 @@ static int subseq_entry(const double *shapelets, const int64_t *offsets, const i
                         int64_t dim, int32_t metric, const wb_params *params, double *out_dist,
                         int64_t *out_idx, int32_t out_on_device, void *stream_, bool paired,
                         double *prof_raw = nullptr, double *prof_key = nullptr,
-                        int64_t prof_ld = 0, int std_as_given = 0) {
+                        int64_t prof_ld = 0, int std_as_given = 0,
+                        const double *stop_sq = nullptr) {
     WB_TRY(check_series(x, "x"));
     const bool profile = prof_raw != nullptr;
     if (paired && m != x->n)
@@ -1080,6 +1081,7 @@ static int subseq_entry(const double *shapelets, const int64_t *offsets, const i
     J.paired = paired ? 1 : 0;
     J.std_as_given = std_as_given;
     J.total_values = total;
+    if (stop_sq && !profile) return fail(WB_EINVAL, "stop values apply to profiles only");
     J.win_stride = (int)x->n_timestep;
     J.chunk = kScaledTileChunk;
     Workspace ws(s);
@@ -1087,12 +1089,18 @@ static int subseq_entry(const double *shapelets, const int64_t *offsets, const i
                   align256(group_len.size() * 4) +
                   (dev_in ? 0 : align256(total * 8) + 2 * align256(m * 8) + 2 * align256(m * 8)) +
                   (out_on_device ? 0 : 2 * align256(n_out * 8)) +
-                  align256(ch_first.size() * 8) + 2 * align256(ch_first.size() * 4);
+                  align256(ch_first.size() * 8) + 2 * align256(ch_first.size() * 4) +
+                  (stop_sq ? align256(m * 8) : 0);
     J.x.count = x->n;
     J.x.len = (int)x->n_timestep;
     need += subseq_workspace_bytes(J, scaled);
     WB_TRY(ws.reserve(need));
     WB_TRY(stage(x, dim, ws, J.x));
+    if (stop_sq) {
+        WB_TAKE(dstop, double, ws, m);
+        WB_CUDA(cudaMemcpyAsync(dstop, stop_sq, m * 8, cudaMemcpyHostToDevice, s));
+        J.stop_sq = dstop;
+    }
     if (dev_in) {
         J.shapelets = shapelets;
         J.offsets = offsets;
@@ -1194,6 +1202,20 @@ extern "C" int wb_subsequence_profile(const double *shapelets, const int64_t *of
     return subseq_entry(shapelets, offsets, lengths, means, stds, m, x, dim, metric, params,
                         nullptr, nullptr, out_on_device, stream_, true, out_raw, out_key, ld,
                         std_as_given ? 1 : 0);
+}
+
+extern "C" int wb_subsequence_profile_stop(const double *shapelets, const int64_t *offsets,
+                                           const int64_t *lengths, const double *means,
+                                           const double *stds, int64_t m, const wb_series *x,
+                                           int64_t dim, const double *stop_sq,
+                                           double *out_raw, int64_t ld, int32_t out_on_device,
+                                           void *stream_) {
+    if (!out_raw) return fail(WB_EINVAL, "out_raw is NULL");
+    if (!stop_sq) return fail(WB_EINVAL, "stop_sq is NULL");
+    wb_params p{};
+    return subseq_entry(shapelets, offsets, lengths, means, stds, m, x, dim,
+                        WB_SCALED_EUCLIDEAN, &p, nullptr, nullptr, out_on_device, stream_,
+                        true, out_raw, nullptr, ld, 0, stop_sq);
 }
 
 extern "C" int wb_paired_subsequence_distance(

@@ -473,7 +473,9 @@ __global__ void subseq_profile_kernel(const SubseqJob J, const double *norm,
         if (SCALED) {
             const double mean = mean_tab[i * J.win_stride + w];
             const double sd = std_tab[i * J.win_stride + w];
+            const double stop = J.stop_sq ? J.stop_sq[i] : __longlong_as_double(0x7ff0000000000000LL);
             for (int k = 0; k < L; k++) {
+                if (dist >= stop) break;
                 double x = __ldg(S + k);
                 x = x - (__ldg(T + w + k) - mean) / sd;
                 dist = dist + x * x;

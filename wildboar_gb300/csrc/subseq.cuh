@@ -31,6 +31,10 @@ struct SubseqJob {
     // window-stat tables one row per series at its shapelet's length
     int paired = 0;
     int std_as_given = 0;  // a zero std divides as is (distance profile's transient stats)
+    // scaled profile only: per pair, stop a window's sum once it reaches this
+    // value (checked before each term, as scaled_euclidean_distance_matches
+    // does with the squared threshold, distance/_metric.pyx:625-651, 798-860)
+    const double *stop_sq = nullptr;
     // FP32 pre-filter of the minimum scans (set by launch_subseq)
     const float *shp_f32 = nullptr;      // packed shapelets (z-normalised when scaled)
     const float *shp_absmax = nullptr;   // (m,) max |value| of each shapelet, rounded up

@@ -122,11 +122,13 @@ def _transient_stats(s):
     return float(mean[0]), float(std[0])
 
 
-def _profile_raw(shapelets, X, dim, metric, transient=False):
+def _profile_raw(shapelets, X, dim, metric, transient=False, stop_sq=None):
     """(raw, key, lengths) of every window, pair i = (shapelets[i], x[i]).
 
     raw / key are (n, ld) float64 numpy arrays, NaN past a pair's windows.
     transient: the distance profile's shapelet statistics, zero std kept.
+    stop_sq (scaled_euclidean): each window's sum stops once it reaches
+    stop_sq, as the reference's matching scan does (wb_subsequence_profile_stop).
     """
     packed, offs, lens, means, stds = _pack_shapelets(
         shapelets, metric.scaled or getattr(metric, "needs_std", False))
@@ -146,10 +148,18 @@ def _profile_raw(shapelets, X, dim, metric, transient=False):
     arr = np.ascontiguousarray(arr, dtype=np.float64)
     sx = _lib.series_from_numpy(arr)
     p = metric.params() if hasattr(metric, "params") else _lib.Params()
-    st = _lib.lib().wb_subsequence_profile(
-        _lib.ptr(packed), _lib.ptr(offs), _lib.ptr(lens), _lib.ptr(means), _lib.ptr(stds),
-        n, ctypes.byref(sx), dim, metric.metric_id, ctypes.byref(p), _lib.ptr(raw),
-        _lib.ptr(key), ld, 1 if transient else 0, 0, None)
+    if stop_sq is not None:
+        stop = np.full(n, float(stop_sq))
+        st = _lib.lib().wb_subsequence_profile_stop(
+            _lib.ptr(packed), _lib.ptr(offs), _lib.ptr(lens), _lib.ptr(means),
+            _lib.ptr(stds), n, ctypes.byref(sx), dim, _lib.ptr(stop), _lib.ptr(raw), ld, 0,
+            None)
+        key[:] = np.nan
+    else:
+        st = _lib.lib().wb_subsequence_profile(
+            _lib.ptr(packed), _lib.ptr(offs), _lib.ptr(lens), _lib.ptr(means), _lib.ptr(stds),
+            n, ctypes.byref(sx), dim, metric.metric_id, ctypes.byref(p), _lib.ptr(raw),
+            _lib.ptr(key), ld, 1 if transient else 0, 0, None)
     _lib.check(st)
     return raw, key, lens
 
@@ -222,7 +232,12 @@ def _match_mask_edr(raw, key, dist, L, T, t):
 
 def _matches(shapelets, X, dim, metric, threshold):
     """Per pair: (indices, distances) arrays or None, as _subsequence_match."""
-    raw, key, lens = _profile_raw(shapelets, X, dim, metric)
+    stop = None
+    if metric.metric_id == 32 and math.isfinite(threshold):
+        # scaled_euclidean_distance_matches stops a window's sum at the first
+        # term where it is >= t^2 and keeps it if that partial sum is <= t^2
+        stop = threshold * threshold
+    raw, key, lens = _profile_raw(shapelets, X, dim, metric, stop_sq=stop)
     return _matches_from_profile(metric.metric_id, raw, key, lens, X.shape[-1], threshold)
 
 
