@@ -42,6 +42,7 @@ WORKLOAD = {
     "params": {"r": 0.1},
 }
 FP64_OPS_PER_CELL = 3  # v = x - y, v * v, min + v*v (mins run on the integer pipe)
+FP64_OPS_PER_SM_CLK = 2  # GB300 FP64 pipe (ncu sm__inst_executed_pipe_fp64 / pipe activity)
 # DRAM bytes (read + write) of one launch of the headline kernel at 2000 x 2000,
 # L = 512, from one earlier ncu capture of `python bench.py --no-cpu --no-forms
 # --steps 2 --warmup 3` (dram__bytes_read.sum 17.12 MB + dram__bytes_write.sum
@@ -988,16 +989,26 @@ def run_gpu(args):
         return
 
     # roofline of the recurrence kernel: FP64 ops per launch / launch time
-    fp64_peak = _lib.alu_probe(_lib.WB_F64, 4096)
+    probe_peak = _lib.alu_probe(_lib.WB_F64, 4096)
     kms = [k for k in kern_ms if k > 0]
     k_avg = sum(kms) / len(kms) if kms else t_step
     achieved = FP64_OPS_PER_CELL * cells / (k_avg * 1e-3)
+    # the FP64 pipe issues 2 operations per clock per SM (ncu: the probe kernel
+    # keeps the pipe 84.2 % busy at 0.0526 FP64 warp-instructions per
+    # SM-cycle), times the SM count and the median SM clock sampled during the
+    # timed region
+    clk = clocks.summary()
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    pipe_peak = FP64_OPS_PER_SM_CLK * torch.cuda.get_device_properties(dev).multi_processor_count \
+        * sm_mhz * 1e6
     roofline = {
         "bound": "fp64",
         "achieved": achieved / 1e12,
-        "peak": fp64_peak / 1e12,
-        "unit": "TFLOP/s (FP64 add+mul, peak measured by wb_alu_probe in this run)",
-        "frac": achieved / fp64_peak,
+        "peak": pipe_peak / 1e12,
+        "unit": "TFLOP/s (FP64 pipe: 2 ops/clk/SM x SMs x the median SM clock of the run)",
+        "frac": achieved / pipe_peak,
+        "probe_peak": probe_peak / 1e12,
+        "frac_of_probe": achieved / probe_peak,
         # measured for the default 2000 x 2000 workload only
         "traffic": HEADLINE_DRAM_BYTES if (wl["nx"], wl["ny"]) == (2000, 2000) else None,
         "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",

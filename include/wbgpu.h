@@ -301,6 +301,21 @@ int wb_dilated_profile(const wb_series *y, const wb_series *x, int64_t dim, int3
 int wb_mass_profile(const wb_series *y, const wb_series *x, double *out, int32_t out_on_device,
                     void *stream);
 
+/*
+ * Host-side fault injection for testing the error paths (no counterpart in
+ * the reference, whose metrics report failures only as -1 from reset,
+ * distance/_elastic.pyx:2224-2225).  Arms one fault that fires once:
+ * site 1 = the next device-workspace reservation returns WB_ENOMEM, 2 = the
+ * next kernel launch check returns WB_ECUDA (the kernel itself runs), 3 =
+ * the next bounded-wait status read (tensor-core euclidean) returns
+ * WB_ETIMEOUT; skip = matching events let through first; site 0 disarms.
+ * The environment variable WB_GPU_INJECT_FAULT=reserve|launch|wait[:skip]
+ * arms the same fault when the library is first used.  No device code is
+ * made to fail: the host takes the error path the real failure would take,
+ * and the library stays usable for the next call.
+ */
+int wb_inject_fault(int32_t site, int64_t skip);
+
 /* valid length of each float32 series: index of its first NaN (padding or
  * end-of-series marker, utils/variable_len.py:66-115), else L */
 int wb_series_lengths_f32(const float *x, int64_t n_series, int64_t stride, int32_t L,

@@ -72,6 +72,7 @@ def _declare(L):
                                          P(Params), vp, vp, i64, i32, i32, vp]
     L.wb_subsequence_profile_stop.argtypes = [vp, vp, vp, vp, vp, i64, P(Series), i64, vp,
                                               vp, i64, i32, vp]
+    L.wb_inject_fault.argtypes = [i32, i64]
     L.wb_last_error.restype = ctypes.c_char_p
     L.wb_version.restype = i32
     L.wb_release_workspace.argtypes = [vp]
@@ -140,6 +141,14 @@ def check(status):
     if status == WB_ETIMEOUT:
         raise TimeoutError(msg)
     raise RuntimeError(msg)
+
+
+FAULT_NONE, FAULT_RESERVE, FAULT_LAUNCH, FAULT_WAIT = 0, 1, 2, 3
+
+
+def inject_fault(site, skip=0):
+    """Arm a host-side fault that fires once (wb_inject_fault); site 0 disarms."""
+    check(lib().wb_inject_fault(int(site), int(skip)))
 
 
 def launch_count():

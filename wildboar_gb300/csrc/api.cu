@@ -9,8 +9,10 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <numeric>
 #include <vector>
 
@@ -40,6 +42,41 @@ int cuda_fail(cudaError_t e, const char *what) {
 }
 
 void count_launch(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// Armed fault: the site, and how many matching events pass before it fires
+// (once).  WB_GPU_INJECT_FAULT="reserve|launch|wait[:skip]" arms it when the
+// library is first used; wb_inject_fault arms or clears it at run time.
+static std::mutex g_inject_mu;
+static int g_inject_site = INJ_NONE;
+static int64_t g_inject_skip = 0;
+static bool g_inject_env_read = false;
+
+static void inject_from_env() {
+    if (g_inject_env_read) return;
+    g_inject_env_read = true;
+    const char *e = getenv("WB_GPU_INJECT_FAULT");
+    if (!e || !*e) return;
+    std::string v(e);
+    std::string name = v.substr(0, v.find(':'));
+    int64_t skip = 0;
+    if (v.find(':') != std::string::npos) skip = atoll(v.c_str() + v.find(':') + 1);
+    if (name == "reserve") g_inject_site = INJ_RESERVE;
+    else if (name == "launch") g_inject_site = INJ_LAUNCH;
+    else if (name == "wait") g_inject_site = INJ_WAIT;
+    g_inject_skip = skip;
+}
+
+bool injected(int site) {
+    std::lock_guard<std::mutex> g(g_inject_mu);
+    inject_from_env();
+    if (g_inject_site != site) return false;
+    if (g_inject_skip > 0) {
+        g_inject_skip--;
+        return false;
+    }
+    g_inject_site = INJ_NONE;
+    return true;
+}
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
@@ -91,6 +128,8 @@ Workspace::Workspace(cudaStream_t stream)
 Workspace::~Workspace() { arena_->used = 0; }
 
 int Workspace::reserve(size_t bytes) {
+    if (injected(INJ_RESERVE))
+        return fail(WB_ENOMEM, "cannot allocate device workspace (injected fault)");
     bytes = align256(bytes) + 4096;
     if (bytes > arena_->cap) {
         if (arena_->base) {
@@ -1353,6 +1392,16 @@ extern "C" int wb_mass_profile(const wb_series *y, const wb_series *x, double *o
     if (!dout) return fail(WB_ENOMEM, "workspace reservation exceeded");
     WB_TRY(launch_mass_profile(sx.base, n, sx.stride, T, sy.base, sy.stride, L, mt, st, dout, s));
     return finish_host_copy(out, dout, (size_t)n * nwin * sizeof(double), out_on_device, s);
+}
+
+extern "C" int wb_inject_fault(int32_t site, int64_t skip) {
+    if (site < INJ_NONE || site > INJ_WAIT) return fail(WB_EINVAL, "unknown fault site");
+    if (skip < 0) return fail(WB_EINVAL, "skip must be >= 0");
+    std::lock_guard<std::mutex> g(g_inject_mu);
+    g_inject_env_read = true;  // an explicit setting replaces the environment's
+    g_inject_site = site;
+    g_inject_skip = skip;
+    return WB_OK;
 }
 
 extern "C" const char *wb_last_error(void) { return g_last_error.c_str(); }

@@ -29,11 +29,19 @@ void timer_end(cudaStream_t s);
         if (e_ != cudaSuccess) return ::wb::cuda_fail(e_, #call); \
     } while (0)
 
+// Host-side fault injection (wb_inject_fault, WB_GPU_INJECT_FAULT): a
+// matching site returns its error as if the CUDA call or the wait had failed;
+// nothing on the device faults.
+enum InjectSite { INJ_NONE = 0, INJ_RESERVE = 1, INJ_LAUNCH = 2, INJ_WAIT = 3 };
+bool injected(int site);
+
 #define WB_LAUNCH_CHECK(what)                               \
     do {                                                    \
         ::wb::count_launch();                               \
         cudaError_t e_ = cudaGetLastError();                \
         if (e_ != cudaSuccess) return ::wb::cuda_fail(e_, what); \
+        if (::wb::injected(::wb::INJ_LAUNCH))               \
+            return ::wb::fail(WB_ECUDA, std::string(what) + ": injected launch failure"); \
     } while (0)
 
 #define WB_TAKE(var, T, ws, count)                                           \

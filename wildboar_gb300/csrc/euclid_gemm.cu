@@ -477,7 +477,8 @@ int euclid_tc(const double *x, int64_t sx, int M, const double *y, int64_t sy, i
     int herr = 0;
     WB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     WB_CUDA(cudaStreamSynchronize(s));
-    if (herr) return fail(WB_ETIMEOUT, "euclid_tc_kernel: a pipeline wait gave up");
+    if (herr || injected(INJ_WAIT))
+        return fail(WB_ETIMEOUT, "euclid_tc_kernel: a pipeline wait gave up");
     return WB_OK;
 }
 
