@@ -326,14 +326,18 @@ int wb_series_lengths_f32(const float *x, int64_t n_series, int64_t stride, int3
  * wb_pairwise_distance for callers that cannot have the library allocate
  * device memory (memory budgeted up front, or no device-synchronising
  * cudaMalloc/cudaFree allowed in their loop): x, y (or NULL for the singleton
- * path) and out must be device memory; nothing is allocated.  The recurrence
- * scratch lives in a static 64 MiB device array (wb_noalloc_scratch_bytes())
- * that every GPU loading the library keeps until exit; a band ring that does
- * not fit in it is rejected with WB_EINVAL.  Metrics: euclidean, dtw, wdtw,
- * adtw, lcss, wlcss, edr (explicit epsilon), msm; others give
- * WB_EUNSUPPORTED.  All calls share the array: calls that overlap on the GPU
- * race.  The first call on a device looks the array up; make it before any
- * stream capture.
+ * path) and out must be device memory; nothing is allocated.  Bands whose ring
+ * fits in shared memory run on the shared-memory kernel with no scratch; wider
+ * ones keep their rings in a static 64 MiB device array
+ * (wb_noalloc_scratch_bytes()) that every GPU loading the library keeps until
+ * exit; a band ring that does not fit in it is rejected with WB_EINVAL.
+ * Metrics: euclidean, dtw, wdtw, adtw, lcss, wlcss, edr (explicit epsilon),
+ * msm; others give WB_EUNSUPPORTED.  All calls share the array: calls that
+ * overlap on the GPU race.  The first call on a device looks the array up;
+ * make it before any stream capture, and do not reset the device afterwards.
+ * wdtw and wlcss copy their weight table from pageable host memory, which
+ * waits for the stream, on every call, and are refused (WB_EUNSUPPORTED)
+ * while the stream is being captured.
  */
 int wb_pairwise_distance_noalloc(const wb_series *x, const wb_series *y, int64_t dim,
                                  int32_t metric, const wb_params *params, double *out,

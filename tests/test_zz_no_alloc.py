@@ -2,10 +2,12 @@
 
 The no-allocation entry point exists for callers that cannot let a library
 allocate device memory (memory reserved and accounted up front, or a loop in
-which a device-synchronising cudaMalloc/cudaFree is not allowed).  Its scratch
-is a static device array, so this file checks that two calls in a row -- the
-second reusing the array the first one left behind -- give the same results
-as the allocating entry point, and that oversize problems are rejected.
+which a device-synchronising cudaMalloc/cudaFree is not allowed).  Bands that
+fit in shared memory need no scratch; wider ones use a static device array,
+so this file checks that two calls in a row -- the second reusing the array
+the first one left behind -- give bit for bit the results of the allocating
+entry point, on narrow and wide bands, univariate and multivariate input, and
+that oversize problems and unsupported metrics are rejected.
 It runs last (file name) and does not depend on any other test.
 """
 
@@ -24,7 +26,6 @@ if not torch.cuda.is_available():  # pragma: no cover
 
 from wildboar_gb300 import _build, _lib  # noqa: E402
 
-RTOL = 1e-12
 
 _build.build()
 L = _lib.lib()
@@ -35,7 +36,7 @@ L.wb_pairwise_distance_noalloc.argtypes = [
 L.wb_noalloc_scratch_bytes.restype = ctypes.c_int64
 
 IDS = {"euclidean": 0, "dtw": 1, "wdtw": 2, "adtw": 5, "lcss": 6, "wlcss": 7, "edr": 8,
-       "msm": 10}
+       "erp": 9, "msm": 10, "twe": 11}
 
 
 def _params(**kw):
@@ -55,7 +56,7 @@ def _series(t):
     return _lib.series_from_torch(t.contiguous()), t
 
 
-def _both(X, Y, metric, **kw):
+def _both(X, Y, metric, dim=0, **kw):
     sx, X3 = _series(X)
     sy, Y3 = (None, None) if Y is None else _series(Y)
     ny = X.shape[0] if Y is None else Y.shape[0]
@@ -63,13 +64,13 @@ def _both(X, Y, metric, **kw):
     stream = torch.cuda.current_stream().cuda_stream
     ref = torch.zeros((X.shape[0], ny), dtype=torch.float64, device="cuda")
     st = L.wb_pairwise_distance(ctypes.byref(sx), None if sy is None else ctypes.byref(sy),
-                                0, IDS[metric], ctypes.byref(p), ref.data_ptr(), 1, stream)
+                                dim, IDS[metric], ctypes.byref(p), ref.data_ptr(), 1, stream)
     _lib.check(st)
     outs = []
     for _ in range(2):
         out = torch.full((X.shape[0], ny), -1.0, dtype=torch.float64, device="cuda")
         st = L.wb_pairwise_distance_noalloc(
-            ctypes.byref(sx), None if sy is None else ctypes.byref(sy), 0, IDS[metric],
+            ctypes.byref(sx), None if sy is None else ctypes.byref(sy), dim, IDS[metric],
             ctypes.byref(p), out.data_ptr(), stream)
         _lib.check(st)
         outs.append(out)
@@ -88,6 +89,9 @@ CASES = [
     ("edr", (14, 15, 88, 88), {"r": 0.2, "epsilon": 0.4}),
     ("msm", (22, 19, 77, 77), {"r": 0.15, "c": 0.5}),
     ("euclidean", (31, 29, 64, 64), {}),
+    # a band ring too wide for shared memory: the static array
+    ("dtw", (7, 5, 3000, 3000), {"r": 1.0}),
+    ("wdtw", (6, 4, 2600, 2600), {"r": 1.0, "g": 0.01}),
 ]
 
 
@@ -99,7 +103,7 @@ def test_noalloc_matches_allocating_entry(metric, shape, params):
     Y = torch.as_tensor(np.cumsum(rng.standard_normal((ny, ly)), axis=1), device="cuda")
     ref, outs = _both(X, Y, metric, **params)
     for out in outs:
-        np.testing.assert_allclose(out, ref, rtol=RTOL, atol=0)
+        np.testing.assert_array_equal(out, ref)
 
 
 def test_noalloc_singleton_path():
@@ -107,8 +111,38 @@ def test_noalloc_singleton_path():
     X = torch.as_tensor(np.cumsum(rng.standard_normal((37, 70)), axis=1), device="cuda")
     ref, outs = _both(X, None, "dtw", r=0.2)
     for out in outs:
-        np.testing.assert_allclose(out, ref, rtol=RTOL, atol=0)
+        np.testing.assert_array_equal(out, ref)
         assert np.all(np.diag(out) == 0.0)
+
+
+def test_noalloc_multivariate_dim():
+    # (n, 3, L) input, dim 2: series start at dim * L with stride 3 L
+    rng = np.random.default_rng(6)
+    X = torch.as_tensor(np.cumsum(rng.standard_normal((19, 3, 80)), axis=-1), device="cuda")
+    Y = torch.as_tensor(np.cumsum(rng.standard_normal((11, 3, 80)), axis=-1), device="cuda")
+    for metric, params in (("dtw", {"r": 0.1}), ("msm", {"r": 0.3})):
+        ref, outs = _both(X, Y, metric, dim=2, **params)
+        for out in outs:
+            np.testing.assert_array_equal(out, ref)
+    # dim 2 of the input is not dim 0
+    ref0, _ = _both(X, Y, "dtw", dim=0, r=0.1)
+    assert not np.array_equal(ref0, ref)
+
+
+@pytest.mark.parametrize("metric,params,status,text", [
+    ("erp", {"g": 0.1}, "WB_EUNSUPPORTED", b"not provided without allocation"),
+    ("twe", {}, "WB_EUNSUPPORTED", b"not provided without allocation"),
+    ("edr", {}, "WB_EINVAL", b"explicit edr epsilon"),
+])
+def test_noalloc_rejects_metrics_that_need_tables(metric, params, status, text):
+    X = torch.zeros((3, 1, 16), dtype=torch.float64, device="cuda")
+    sx, _ = _series(X)
+    out = torch.empty((3, 3), dtype=torch.float64, device="cuda")
+    p = _params(**params)
+    st = L.wb_pairwise_distance_noalloc(ctypes.byref(sx), ctypes.byref(sx), 0, IDS[metric],
+                                        ctypes.byref(p), out.data_ptr(), None)
+    assert st == getattr(_lib, status)
+    assert text in L.wb_last_error()
 
 
 def test_noalloc_rejects_oversize_and_host_inputs():

@@ -83,6 +83,9 @@ int launch_elastic(const ElasticJob &job, Workspace &ws, size_t *ring_bytes_quer
 // fits.  WB_EINVAL when not even one block's rings fit.
 int launch_elastic_external_ring(const ElasticJob &job, double *ring, size_t ring_bytes,
                                  cudaStream_t s);
+// The shared-memory ring kernels (and the tiled euclidean kernel) without any
+// workspace; WB_EUNSUPPORTED when the band ring does not fit in shared memory.
+int launch_elastic_shared_ring(const ElasticJob &job, cudaStream_t s);
 size_t elastic_workspace_bytes(const ElasticJob &job);
 
 // elastic subsequence distance (one warp per (series, shapelet), one lane per

@@ -516,6 +516,44 @@ int launch_shapelet_slopes(const double *shp, const int64_t *off, const int64_t 
     return WB_OK;
 }
 
+// The shared-memory ring form of launch_elastic, which needs no workspace:
+// WB_EUNSUPPORTED when the job's band ring does not fit in shared memory (the
+// tiled euclidean kernel needs none either).
+int launch_elastic_shared_ring(const ElasticJob &J, cudaStream_t s) {
+    if (J.rows.count == 0 || J.cols.count == 0) return WB_OK;
+    if (J.kind == K_EUCLID && J.mode != PM_PAIRED && J.key == nullptr &&
+        J.rows.len == J.cols.len)
+        return launch_euclid_tiled(J, s);
+    const ElasticPlan pl = plan_elastic(J);
+    if (pl.gring) return fail(WB_EUNSUPPORTED, "band ring does not fit in shared memory");
+    const size_t smem = (size_t)pl.P * kThreads * sizeof(double);
+    switch (J.kind) {
+#define WB_SHR_CASE(K)                                                                   \
+    case K: {                                                                            \
+        auto kfn = elastic_pairs_kernel<K, false>;                                       \
+        WB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                                     (int)smem));                                        \
+        kfn<<<pl.grid, kThreads, smem, s>>>(J, nullptr, pl.P);                            \
+        break;                                                                           \
+    }
+        WB_SHR_CASE(K_DTW)
+        WB_SHR_CASE(K_WDTW)
+        WB_SHR_CASE(K_ADTW)
+        WB_SHR_CASE(K_ADTW_ANY)
+        WB_SHR_CASE(K_LCSS)
+        WB_SHR_CASE(K_WLCSS)
+        WB_SHR_CASE(K_EDR)
+        WB_SHR_CASE(K_ERP)
+        WB_SHR_CASE(K_MSM)
+        WB_SHR_CASE(K_TWE)
+        WB_SHR_CASE(K_EUCLID)
+#undef WB_SHR_CASE
+        default: return fail(WB_EINVAL, "unknown elastic kernel");
+    }
+    WB_LAUNCH_CHECK("elastic_pairs_kernel");
+    return WB_OK;
+}
+
 int launch_elastic_external_ring(const ElasticJob &J, double *ring, size_t ring_bytes,
                                  cudaStream_t s) {
     if (J.rows.count == 0 || J.cols.count == 0) return WB_OK;

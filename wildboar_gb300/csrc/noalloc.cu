@@ -19,7 +19,16 @@
 //
 // Set-up: the first call on a device, with that device current, looks up the
 // array's device address with cudaGetSymbolAddress and caches it per device;
-// make that first call before any stream capture begins.
+// make that first call before any stream capture begins.  The cached address
+// belongs to the device context the library first saw: a cudaDeviceReset after
+// that call is not supported (a new context may place the array elsewhere).
+//
+// A band ring that fits in shared memory runs on the shared-memory kernel and
+// touches no scratch at all; only wider bands use the static array.  wdtw and
+// wlcss upload their weight table from pageable host memory, a copy the CUDA
+// driver orders with the stream's earlier work before it returns: those two
+// metrics wait for the stream on every call and are refused while the stream
+// is being captured.
 
 #include <algorithm>
 #include <mutex>
@@ -139,6 +148,12 @@ extern "C" int wb_pairwise_distance_noalloc(const wb_series *x, const wb_series 
     char *scratch = static_cast<char *>(base);
     size_t avail = kStaticScratchBytes;
     if (weights) {
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        WB_CUDA(cudaStreamIsCapturing(s, &cap));
+        if (cap != cudaStreamCaptureStatusNone)
+            return fail(WB_EUNSUPPORTED, "wdtw / wlcss upload a weight table from host "
+                                         "memory and cannot run while the stream is "
+                                         "captured");
         // WeightedDtwMetric.reset: w[i] = 1 / (1 + exp(-g (i - n/2))), n = max width
         const int64_t nw = std::max(xl, yl);
         const size_t wbytes = align256((size_t)nw * sizeof(double));
@@ -148,10 +163,10 @@ extern "C" int wb_pairwise_distance_noalloc(const wb_series *x, const wb_series 
         std::vector<double> w((size_t)nw);
         for (int64_t i = 0; i < nw; i++)
             w[i] = 1.0 / (1.0 + std::exp(-params->g * ((double)i - (double)nw / 2.0)));
+        // a copy from pageable memory returns once the driver holds the data,
+        // so the vector may go out of scope afterwards
         WB_CUDA(cudaMemcpyAsync(scratch, w.data(), nw * sizeof(double),
                                 cudaMemcpyHostToDevice, s));
-        // the host vector must outlive the copy
-        WB_CUDA(cudaStreamSynchronize(s));
         J.weights = reinterpret_cast<const double *>(scratch);
         scratch += wbytes;
         avail -= wbytes;
@@ -171,6 +186,8 @@ extern "C" int wb_pairwise_distance_noalloc(const wb_series *x, const wb_series 
     J.out_ld = yy->n;
     J.mode = y ? PM_ALL : PM_UPPER;
     if (!y) WB_CUDA(cudaMemsetAsync(out, 0, (size_t)x->n * x->n * sizeof(double), s));
+    const int st = launch_elastic_shared_ring(J, s);
+    if (st != WB_EUNSUPPORTED) return st;
     return launch_elastic_external_ring(J, reinterpret_cast<double *>(scratch), avail, s);
 }
 

@@ -447,7 +447,7 @@ def _grouped_stats_ok():
     if _GROUPED_STATS_OK is None:
         rng = np.random.default_rng(12345)
         ok = True
-        for L in (1, 7, 8, 9, 16, 33, 100, 128, 129, 300):
+        for L in (1, 7, 8, 9, 16, 33, 100, 128, 129, 300, 513, 1024, 4097):
             A = rng.standard_normal((5, L)) * 1e3 + 7.0
             m, sd = np.mean(A, axis=1), np.std(A, axis=1)
             for i in range(5):
