@@ -3,25 +3,30 @@
 //
 // One thread per (x, y) problem, persistent: warps take 32 consecutive items
 // at a time from an atomic counter, so a batch sorted by cost keeps the 32
-// lanes of a warp on problems of similar size.  A thread sweeps its band in
-// strips of S rows: the S cells of one column live in registers as (hi, lo)
+// lanes of a warp on problems of similar size.  dtw items are transposed so
+// that the rows of the recurrence are the shorter series (wdtw keeps x on the
+// rows: its row-0 weight index makes it asymmetric).  A thread sweeps its band
+// in strips of S rows: the S cells of one column live in registers as (hi, lo)
 // float pairs, the previous strip's bottom row is read from, and the strip's
 // own bottom row written to, a ring in global memory laid out
-// [column][thread] (coalesced when the lanes of a warp sweep the same column).
+// [column][thread].  The loop bounds of every strip are the union of the 32
+// lanes' column ranges, so lanes never diverge on ragged shapes; cells outside
+// a lane's own band take the masked path with an infinite cost.
 //
-// Arithmetic: the cost (x_i - y_j)^2 (times the wdtw weight) is FP32; every
-// accumulation is a TwoSum, whose exact rounding error goes into the lo part,
-// so the cumulative cost carries ~48 bits.  The minimum picks the candidate
-// with the smallest hi in the dtw_mapping order (diag, up, left; distance/
-// dtw.py:362-426), which also gives the traceback direction.  The final
-// distance sqrt(hi + lo) is formed in FP64.  Band, row-0 weights and
-// out-of-band +inf follow dtw_distance (distance/_elastic.pyx:869-940).
+// Arithmetic: the cost (x_i - y_j)^2 (times the wdtw weight) is FP32 (two
+// columns' differences and squares as packed f32x2 operations, each half
+// rounded as the scalar operation); the minimum of the three hi parts is one
+// 3-input min, the lo of a candidate holding it comes with it, and the new
+// partial sum is a Fast2Sum of (minimum, cost), whose error term is exact
+// when the minimum is at least the cost and within one rounding of the sum
+// otherwise, so the cumulative cost carries ~48 bits.  The final distance
+// sqrt(hi + lo) is formed in FP64.  Band, row-0 weights and out-of-band +inf
+// follow dtw_distance (distance/_elastic.pyx:869-940).
 //
-// Backward: the same sweep stores a 2-bit direction per cell (one 32-bit word
-// per strip column for S = 16), then the thread walks the optimal path back
-// from (n-1, m-1) and writes d dist / d x_i and d dist / d y_j:
-// dD/dx_i = sum_{j:(i,j) on path} w_{|i-j|} (x_i - y_j) / D, dD/dy_j the
-// negative column sums (D = sqrt of the path cost).
+// Backward (second half of the file): checkpointed recomputation with 2-bit
+// traceback directions and an in-kernel walk of the optimal path that adds
+// dD/dx_i = sum_{j:(i,j) on path} w_{|i-j|} (x_i - y_j) / D and the negative
+// column sums dD/dy_j to per-series gradient rows (D = sqrt of the path cost).
 
 #include "dtw32.cuh"
 
