@@ -13,12 +13,13 @@ if not torch.cuda.is_available():  # pragma: no cover
 from oracle import oracle as O  # noqa: E402
 from wildboar_gb300.distance import precision as P  # noqa: E402
 
-# 3xTF32 products with FP32 tensor-core accumulation (four K quarters added in
-# FP64): the squared distance carries an error of a few 1e-6 of
-# |x|^2 + |y|^2 (cancellation makes that larger relative to d^2 for close
-# pairs).  Bars: |d2_tc - d2| <= 1e-5 (|x|^2 + |y|^2) and 1e-4 relative on d
-# for pairs whose d^2 is at least 5% of |x|^2 + |y|^2.
-NORM_TOL = 1e-5
+# 3xTF32 products of the series centred on their means, accumulated in FP32
+# in tensor memory (one accumulator over the whole length): the squared
+# distance carries an error of ~1e-5 of |x|^2 + |y|^2 at length 1000
+# (cancellation makes that larger relative to d^2 for close pairs).  Bars:
+# |d2_tc - d2| <= 2e-5 (|x|^2 + |y|^2) and 1e-4 relative on d for pairs whose
+# d^2 is at least 5% of |x|^2 + |y|^2.
+NORM_TOL = 2e-5
 TC_RTOL = 1e-4
 
 
@@ -63,3 +64,20 @@ def test_dtw_fp32_precision_form():
                       Y.astype(np.float32).astype(np.float64), metric="dtw",
                       metric_params={"r": 0.1})
     np.testing.assert_allclose(got, want, rtol=1e-5)
+
+
+def test_euclidean_tc_offset_series():
+    # series far from zero: centring keeps the error relative to the centred
+    # magnitudes, so distances stay accurate although |x|^2 + |y|^2 >> d^2
+    rng = np.random.default_rng(4)
+    X = np.cumsum(rng.standard_normal((200, 300)), axis=1) + 1000.0
+    Y = np.cumsum(rng.standard_normal((260, 300)), axis=1) + 990.0
+    got = P.pairwise_euclidean_tc(torch.as_tensor(X, device="cuda"),
+                                  torch.as_tensor(Y, device="cuda")).cpu().numpy()
+    want = np.sqrt(((X[:, None, :] - Y[None, :, :]) ** 2).sum(-1))
+    Xc = X - X.mean(1, keepdims=True)
+    Yc = Y - Y.mean(1, keepdims=True)
+    scale = (Xc * Xc).sum(1)[:, None] + (Yc * Yc).sum(1)[None, :]
+    assert np.max(np.abs(got ** 2 - want ** 2) / scale) <= NORM_TOL
+    far = want ** 2 >= 0.05 * scale
+    np.testing.assert_allclose(got[far], want[far], rtol=TC_RTOL)
