@@ -322,25 +322,32 @@ def bench_fwd_bwd(args, dev, flush):
         losses.append(step())
     torch.cuda.synchronize()
     adam_s = time.perf_counter() - t0
+    # errors against FP64 of the plain forward and of the forward that keeps
+    # the directions (the one inside the step)
     D = AG.dtw_matrix(x[:16], c.detach(), r).detach().cpu().numpy()
+    Dk = AG.dtw_matrix(x[:16], c, r).detach().cpu().numpy()
     Cn = c.detach().cpu().numpy().astype(np.float64)
-    err = 0.0
+    err = err_k = 0.0
     for i in range(16):
         for k in range(K):
             want = O.distance_1d(X[i].astype(np.float64), Cn[k], metric="dtw",
                                  metric_params={"r": r})
             err = max(err, abs(D[i, k] - want) / want)
+            err_k = max(err_k, abs(Dk[i, k] - want) / want)
     return {
         "gcups": 2 * cells_fwd / (ms * 1e-3) / 1e9,
         "ms_per_step": ms,
         "forward_gcups": cells_fwd / (ms_fwd * 1e-3) / 1e9,
         "cells_per_step": 2 * cells_fwd,
         "config": f"{N} x {K} centroids, L={L}, r={r}, float32; step = forward + "
-                  "backward (recompute + path traceback, all pairs) + Adam",
+                  "backward (path traceback, all pairs) + Adam",
+        "backward": ("directions kept by the forward, walk only" if AG.keeps_directions(x, c, r)
+                     else "checkpointed recompute + walk"),
         "adam_steps": args.c5_adam_steps,
         "adam_total_s": adam_s,
         "loss_first_last": [float(losses[0].detach()), float(losses[-1].detach())],
         "max_rel_err_vs_fp64": err,
+        "max_rel_err_vs_fp64_step_forward": err_k,
     }
 
 

@@ -237,6 +237,24 @@ int wb_dtw32_distance(const wb_dtw32 *job, double *out, double *out_cost, void *
 int wb_dtw32_backward(const wb_dtw32 *job, const double *grad_out, float *grad_x,
                       int64_t gx_stride, float *grad_y, int64_t gy_stride, void *stream);
 
+/*
+ * Kept directions (no counterpart in the reference): the forward of a
+ * differentiable call may store the 2-bit traceback directions of every item
+ * (the sweep the backward would otherwise recompute), so that the backward
+ * only walks the paths.  wb_dtw32_keep_bytes gives the buffer size for a job
+ * (-1 for an invalid job); wb_dtw32_distance_keep computes out / out_cost like
+ * wb_dtw32_distance (predecessors chosen by compensated comparison, as in the
+ * backward) and fills the buffer; wb_dtw32_backward_keep adds the gradients
+ * of wb_dtw32_backward from that buffer and the distances `dist` of the same
+ * forward.  The job must be the same in both calls.
+ */
+int64_t wb_dtw32_keep_bytes(const wb_dtw32 *job);
+int wb_dtw32_distance_keep(const wb_dtw32 *job, double *out, double *out_cost, void *keep,
+                           int64_t keep_bytes, void *stream);
+int wb_dtw32_backward_keep(const wb_dtw32 *job, const double *dist, const double *grad_out,
+                           float *grad_x, int64_t gx_stride, float *grad_y, int64_t gy_stride,
+                           const void *keep, int64_t keep_bytes, void *stream);
+
 /* Full-series euclidean distance matrix on the tensor cores (precision form,
  * no counterpart in the reference, whose EuclideanMetric sums in FP64 on the
  * CPU, distance/_metric.pyx:381-409): out[i, j] = sqrt(|x_i|^2 + |y_j|^2 -

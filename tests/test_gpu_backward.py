@@ -7,7 +7,9 @@ implied by the reference's dtw_alignment + dtw_mapping path
 differences of the FP64 distance, on pairs whose optimal path has no near-tie
 (a step where another predecessor's cumulative cost is within 1e-9 relative:
 dtw is not differentiable there).  Series of 600 and 2048 points take the
-checkpointed path (several segments of strips per item).
+checkpointed path (several segments of strips per item).  dtw_matrix keeps
+the forward's directions when they fit the workspace budget; a small budget
+forces the recompute path, and both give the same distances and gradients.
 """
 
 import os
@@ -133,9 +135,11 @@ def test_paired_gradient_vs_finite_differences_long():
     assert checked >= 24
 
 
-def test_matrix_gradient_multisegment_vs_alignment_path():
+def test_matrix_gradient_multisegment_vs_alignment_path(monkeypatch):
     # 600 points: 38 strips of 16 rows, more direction words than one segment
-    # holds, so the backward checkpoints and recomputes segments
+    # holds, so the backward checkpoints and recomputes segments (a budget
+    # below the kept directions' 2.9 MB keeps the forward from storing them)
+    monkeypatch.setenv("WB_GPU_BWD_WORKSPACE_MB", "2")
     rng = np.random.default_rng(600)
     L, r = 600, 0.2
     X = np.stack([_walk(rng, L) for _ in range(3)])
@@ -181,3 +185,46 @@ def test_small_workspace_budget_gives_the_same_gradients(monkeypatch):
     np.testing.assert_allclose(gx1, gx0, rtol=0, atol=1e-6)
     np.testing.assert_allclose(gy1, gy0, rtol=0, atol=1e-6)
     assert os.environ["WB_GPU_BWD_WORKSPACE_MB"] == "0.01"
+
+
+@pytest.mark.parametrize("lx,ly,g", [(300, 300, None), (300, 180, None), (140, 260, 0.05)])
+def test_kept_directions_match_the_recompute_path(monkeypatch, lx, ly, g):
+    # 40 x 9 pairs: the kept directions take 3.6-8.8 MB (12 batches of 32
+    # items); a 2 MB budget sends the same call through the recompute path
+    rng = np.random.default_rng(lx * 3 + ly)
+    X = np.stack([_walk(rng, lx) for _ in range(40)])
+    Y = np.stack([_walk(rng, ly) for _ in range(9)])
+    gw = torch.as_tensor(rng.standard_normal((40, 9)), device="cuda")
+
+    def run():
+        xt = torch.as_tensor(X, device="cuda").requires_grad_(True)
+        yt = torch.as_tensor(Y, device="cuda").requires_grad_(True)
+        D = AG.dtw_matrix(xt, yt, 0.2, g=g)
+        (D * gw).sum().backward()
+        return (D.detach().cpu().numpy(), xt.grad.cpu().numpy(), yt.grad.cpu().numpy())
+
+    d_keep, gx_keep, gy_keep = run()
+    monkeypatch.setenv("WB_GPU_BWD_WORKSPACE_MB", "2")
+    d_rec, gx_rec, gy_rec = run()
+    metric = "dtw" if g is None else "wdtw"
+    params = {"r": 0.2} if g is None else {"r": 0.2, "g": g}
+    want = O.pairwise(X.astype(np.float64), Y.astype(np.float64), metric=metric,
+                      metric_params=params)
+    np.testing.assert_allclose(d_keep, want, rtol=1e-5)
+    np.testing.assert_allclose(d_keep, d_rec, rtol=1e-6)
+    # same directions and paths; only the order of the gradient atomics differs
+    np.testing.assert_allclose(gx_keep, gx_rec, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(gy_keep, gy_rec, rtol=1e-5, atol=1e-6)
+    assert np.count_nonzero(gx_keep) > 0.9 * gx_keep.size
+
+
+def test_no_kept_directions_without_grad():
+    # under no_grad (or with no input requiring a gradient) the plain forward runs
+    rng = np.random.default_rng(8)
+    X = torch.as_tensor(np.stack([_walk(rng, 64) for _ in range(5)]), device="cuda")
+    Y = torch.as_tensor(np.stack([_walk(rng, 64) for _ in range(3)]), device="cuda")
+    D0 = AG.dtw_matrix(X, Y, 0.3)
+    assert not D0.requires_grad
+    with torch.no_grad():
+        D1 = AG.dtw_matrix(X.clone().requires_grad_(True), Y, 0.3)
+    np.testing.assert_array_equal(D0.cpu().numpy(), D1.cpu().numpy())

@@ -109,6 +109,54 @@ int dtw32_take(Workspace &ws, Dtw32Job &J, bool backward) {
     return WB_OK;
 }
 
+// Geometry of the kept directions of a job: per batch of 32 items the two
+// strip tables and 32 lanes x cap words, cap = every strip of the longest
+// rows over the longest columns (whole groups of 8).
+static int keep_geometry(const wb_dtw32 *q, DirKeep &D, int64_t &total) {
+    if (!q) return fail(WB_EINVAL, "job is NULL");
+    if (q->x_len < 1 || q->y_len < 1) return fail(WB_EINVAL, "x_len and y_len must be >= 1");
+    if (q->n_items < 0) return fail(WB_EINVAL, "negative number of items");
+    const int64_t cols_max = std::max(q->x_len, q->y_len);
+    const int64_t rows_max = q->weights ? q->x_len : std::min(q->x_len, q->y_len);
+    const int64_t strips = rows_max > 1 ? (rows_max - 2) / 16 + 1 : 0;
+    D.max_strips = (int)std::max<int64_t>(strips, 1);
+    D.cap = (std::max<int64_t>(strips * cols_max, 8) + 7) / 8 * 8;
+    D.tab_bytes = (int64_t)align256((size_t)2 * D.max_strips * sizeof(int));
+    D.batch_bytes = D.tab_bytes + 32 * D.cap * (int64_t)sizeof(uint32_t);
+    total = (q->n_items + 31) / 32 * D.batch_bytes;
+    return WB_OK;
+}
+
+// A planned job for the kept-direction kernels (128-thread blocks, grid by
+// their occupancy); the ring only for the forward.
+static int prepare_keep(const wb_dtw32 *q, bool walk, void *keep, int64_t keep_bytes,
+                        Workspace &ws, Dtw32Job &J, DirKeep &D) {
+    if (q && (!q->x || !q->y)) return fail(WB_EINVAL, "x and y must be device pointers");
+    int64_t total = 0;
+    WB_TRY(keep_geometry(q, D, total));
+    if (!keep || keep_bytes < total) return fail(WB_EINVAL, "kept-direction buffer too small");
+    D.base = static_cast<unsigned char *>(keep);
+    size_t bytes = 0;
+    WB_TRY(dtw32_plan(q, false, J, bytes));
+    J.block = 128;
+    int nb = dtw32_keep_blocks_per_sm(walk, q->weights != nullptr);
+    if (nb < 1) nb = 1;
+    int grid = nb * device_info().sm_count;
+    const int64_t need = (q->n_items + J.block - 1) / J.block;
+    if (need < grid) grid = (int)std::max<int64_t>(need, 1);
+    J.grid = grid;
+    const int64_t nth = (int64_t)grid * J.block;
+    const size_t ring_bytes = walk ? 0 : align256((size_t)J.ring_cols * nth * sizeof(float2));
+    WB_TRY(ws.reserve(ring_bytes + 512));
+    if (!walk) {
+        J.ring = ws.take<float2>((size_t)J.ring_cols * nth);
+        if (!J.ring) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    }
+    J.queue = ws.take<unsigned long long>(1);
+    if (!J.queue) return fail(WB_ENOMEM, "workspace reservation exceeded");
+    return WB_OK;
+}
+
 static int prepare32(const wb_dtw32 *q, bool backward, Workspace &ws, Dtw32Job &J) {
     if (q && (!q->x || !q->y)) return fail(WB_EINVAL, "x and y must be device pointers");
     size_t bytes = 0;
@@ -150,6 +198,48 @@ extern "C" int wb_dtw32_backward(const wb_dtw32 *q, const double *grad_out, floa
     J.grad_y = grad_y;
     J.gy_stride = gy_stride;
     return dtw32_backward(J, s);
+}
+
+extern "C" int64_t wb_dtw32_keep_bytes(const wb_dtw32 *q) {
+    DirKeep D;
+    int64_t total = 0;
+    if (keep_geometry(q, D, total) != WB_OK) return -1;
+    return total;
+}
+
+extern "C" int wb_dtw32_distance_keep(const wb_dtw32 *q, double *out, double *out_cost,
+                                      void *keep, int64_t keep_bytes, void *stream_) {
+    if (!out) return fail(WB_EINVAL, "out is NULL");
+    cudaStream_t s = (cudaStream_t)stream_;
+    Workspace ws(s);
+    Dtw32Job J;
+    DirKeep D;
+    WB_TRY(prepare_keep(q, false, keep, keep_bytes, ws, J, D));
+    J.out = out;
+    J.out_cost = out_cost;
+    return dtw32_keep_forward(J, D, s);
+}
+
+extern "C" int wb_dtw32_backward_keep(const wb_dtw32 *q, const double *dist,
+                                      const double *grad_out, float *grad_x, int64_t gx_stride,
+                                      float *grad_y, int64_t gy_stride, const void *keep,
+                                      int64_t keep_bytes, void *stream_) {
+    if (!q) return fail(WB_EINVAL, "job is NULL");
+    if (!dist) return fail(WB_EINVAL, "dist is NULL");
+    if (!grad_x || !grad_y) return fail(WB_EINVAL, "gradient outputs are NULL");
+    if (gx_stride < q->x_len || gy_stride < q->y_len)
+        return fail(WB_EINVAL, "gradient strides must cover x_len / y_len");
+    cudaStream_t s = (cudaStream_t)stream_;
+    Workspace ws(s);
+    Dtw32Job J;
+    DirKeep D;
+    WB_TRY(prepare_keep(q, true, const_cast<void *>(keep), keep_bytes, ws, J, D));
+    J.grad_out = grad_out;
+    J.grad_x = grad_x;
+    J.gx_stride = gx_stride;
+    J.grad_y = grad_y;
+    J.gy_stride = gy_stride;
+    return dtw32_keep_walk(J, D, dist, s);
 }
 
 extern "C" int wb_series_lengths_f32(const float *x, int64_t n_series, int64_t stride,

@@ -444,16 +444,17 @@ __device__ void bwd_row0(const BwdItem &B, const float *__restrict__ w, float2 *
 
 // Strips [s0, s1) of every lane with warp-uniform column bounds.  The row above
 // strip s0 is read from `src`; each strip's bottom row goes to `ring`, the last
-// one's to `last_dst` when it is set.  With DIRS, the direction words of the
-// strips go to dirs[(base + c - cs_w) * nth] and (cs_w, base) of each strip to
-// the warp's tables; returns false (for every lane) if the words would not fit
+// one's to `last_dst` when it is set (ring rows have stride nth).  With DIRS,
+// the direction words of the strips go to word base + c - cs_w of thread
+// dir_g of dir_n (dir_index) and (cs_w, base) of each strip to the warp's
+// tables; returns false (for every lane) if the words would not fit
 // in dir_words.  A lane whose last strip is in the range gets its cost of cell
 // (n-1, m-1) in `result`.
 template <bool W, bool DIRS>
 __device__ bool bwd_strips(const BwdItem &B, int s0, int s1, const float2 *src, float2 *ring,
                            float2 *last_dst, uint32_t *dirs, int64_t dir_words, int *tab_cs,
-                           int *tab_base, uint32_t *stage, int64_t gtid, int64_t nth,
-                           const float *__restrict__ w, HL &result) {
+                           int *tab_base, uint32_t *stage, int64_t dir_g, int64_t dir_n,
+                           int64_t nth, const float *__restrict__ w, HL &result) {
     constexpr int S = kGradStrip;
     const unsigned FULL = 0xffffffffu;
     const float qnan = __int_as_float(0x7fc00000);
@@ -525,7 +526,7 @@ __device__ bool bwd_strips(const BwdItem &B, int s0, int s1, const float2 *src, 
                 const int64_t wi = base + (c - cs_w);
                 stage[(wi & 7) * 33] = word;
                 if ((wi & 7) == 7 || c == ce_w - 1) {
-                    uint4 *dst = reinterpret_cast<uint4 *>(dirs + dir_index(wi & ~(int64_t)7, gtid, nth));
+                    uint4 *dst = reinterpret_cast<uint4 *>(dirs + dir_index(wi & ~(int64_t)7, dir_g, dir_n));
                     dst[0] = make_uint4(stage[0], stage[33], stage[66], stage[99]);
                     dst[1] = make_uint4(stage[132], stage[165], stage[198], stage[231]);
                 }
@@ -593,9 +594,60 @@ __device__ void bwd_walk(const BwdItem &B, int g, int K, const uint32_t *dirs,
     }
 }
 
+// The backward geometry of item t (nothing for t >= n_items, an empty series
+// or a zero upstream gradient): dtw items transposed so that the rows are the
+// shorter series; an item longer than the planned rows gets NaN gradients,
+// never zeros.  g: the upstream gradient of the item.
+__device__ __forceinline__ void bwd_setup(const Dtw32Job &J, int64_t t, BwdItem &B, double &g) {
+    constexpr int S = kGradStrip;
+    const float qnan = __int_as_float(0x7fc00000);
+    g = 0.0;
+    if (t >= J.n_items) return;
+    Item it = load_item(J, t);
+    int64_t cx, cy;
+    if (J.item_x) {
+        cx = J.item_x[t];
+        cy = J.item_y[t];
+    } else {
+        cy = t / J.nx;
+        cx = t - cy * J.nx;
+    }
+    float *gx = J.grad_x ? J.grad_x + cx * J.gx_stride : nullptr;
+    float *gy = J.grad_y ? J.grad_y + cy * J.gy_stride : nullptr;
+    g = J.grad_out ? J.grad_out[t] : 1.0;
+    if (it.n < 1 || it.m < 1 || g == 0.0) return;
+    if (it.m >= J.ring_cols || it.n >= J.ring_cols) {
+        if (gx)
+            for (int i = 0; i < it.n; i++) atomicAdd(gx + i, qnan);
+        if (gy)
+            for (int j = 0; j < it.m; j++) atomicAdd(gy + j, qnan);
+        return;
+    }
+    if (!J.weights && it.n > it.m) {  // rows: the shorter series (dtw)
+        B.R = it.Y;
+        B.C = it.X;
+        B.GR = gy;
+        B.GC = gx;
+        B.n = it.m;
+        B.m = it.n;
+    } else {
+        B.R = it.X;
+        B.C = it.Y;
+        B.GR = gx;
+        B.GC = gy;
+        B.n = it.n;
+        B.m = it.m;
+    }
+    B.r = it.r;
+    B.mx = imax(0, B.m - B.n) + B.r;
+    B.mn = imax(0, B.n - B.m);
+    B.lo = -(B.mn + B.r - 1);
+    B.width = (B.mx - 1) - B.lo + 1;
+    B.nstrips = B.n > 1 ? (B.n - 2) / S + 1 : 0;
+}
+
 template <bool W>
 __global__ void __launch_bounds__(kBwdBlock) dtw32_backward_kernel(const Dtw32Job J) {
-    constexpr int S = kGradStrip;
     __shared__ int tab_cs_all[kBwdBlock / 32][kMaxSegStrips];
     __shared__ int tab_base_all[kBwdBlock / 32][kMaxSegStrips];
     // per lane 8 staged direction words, stride 33 words between slots so the
@@ -622,52 +674,7 @@ __global__ void __launch_bounds__(kBwdBlock) dtw32_backward_kernel(const Dtw32Jo
         const int64_t t = base + lane;
         BwdItem B;
         double g = 0.0;
-        bool bad = false;
-        if (t < J.n_items) {
-            Item it = load_item(J, t);
-            int64_t cx, cy;
-            if (J.item_x) {
-                cx = J.item_x[t];
-                cy = J.item_y[t];
-            } else {
-                cy = t / J.nx;
-                cx = t - cy * J.nx;
-            }
-            float *gx = J.grad_x + cx * J.gx_stride;
-            float *gy = J.grad_y + cy * J.gy_stride;
-            g = J.grad_out ? J.grad_out[t] : 1.0;
-            if (it.n >= 1 && it.m >= 1 && g != 0.0) {
-                if (!W && it.n > it.m) {  // rows: the shorter series (dtw)
-                    B.R = it.Y;
-                    B.C = it.X;
-                    B.GR = gy;
-                    B.GC = gx;
-                    B.n = it.m;
-                    B.m = it.n;
-                } else {
-                    B.R = it.X;
-                    B.C = it.Y;
-                    B.GR = gx;
-                    B.GC = gy;
-                    B.n = it.n;
-                    B.m = it.m;
-                }
-                B.r = it.r;
-                B.mx = imax(0, B.m - B.n) + B.r;
-                B.mn = imax(0, B.n - B.m);
-                B.lo = -(B.mn + B.r - 1);
-                B.width = (B.mx - 1) - B.lo + 1;
-                B.nstrips = B.n > 1 ? (B.n - 2) / S + 1 : 0;
-                if (B.m >= J.ring_cols) {
-                    bad = true;
-                    B.n = B.m = B.nstrips = 0;
-                }
-            }
-            if (bad) {  // longer than the planned rows: NaN gradients, never zeros
-                for (int i = 0; i < it.n; i++) atomicAdd(gx + i, qnan);
-                for (int j = 0; j < it.m; j++) atomicAdd(gy + j, qnan);
-            }
-        }
+        bwd_setup(J, t, B, g);
         const int nstr_w = __reduce_max_sync(FULL, B.nstrips);
         const int nseg_w = nstr_w > 0 ? (nstr_w + K - 1) / K : 1;
         const bool fits = nseg_w - 1 <= J.n_ckpt;
@@ -681,7 +688,7 @@ __global__ void __launch_bounds__(kBwdBlock) dtw32_backward_kernel(const Dtw32Jo
                 const float2 *src = sg == 0 ? ring : ckpt + (int64_t)(sg - 1) * slot;
                 ok = bwd_strips<W, false>(B, sg * K, (sg + 1) * K, src, ring,
                                           ckpt + (int64_t)sg * slot, nullptr, 0, tab_cs,
-                                          tab_base, stage, gtid, nth, w, dummy);
+                                          tab_base, stage, gtid, nth, nth, w, dummy);
             }
         }
         // pass 2: segments from the last, each recomputed with its directions,
@@ -694,8 +701,8 @@ __global__ void __launch_bounds__(kBwdBlock) dtw32_backward_kernel(const Dtw32Jo
             if (sg == 0) bwd_row0<W>(B, w, ring, nth, result);
             const float2 *src = sg == 0 ? ring : ckpt + (int64_t)(sg - 1) * slot;
             ok = bwd_strips<W, true>(B, sg * K, imin((sg + 1) * K, nstr_w), src, ring, nullptr,
-                                     dirs, J.dir_words, tab_cs, tab_base, stage, gtid, nth, w,
-                                     result);
+                                     dirs, J.dir_words, tab_cs, tab_base, stage, gtid, nth, nth,
+                                     w, result);
             if (!ok) break;
             __syncwarp();
             if (!done && sg <= g_last) {
@@ -713,6 +720,140 @@ __global__ void __launch_bounds__(kBwdBlock) dtw32_backward_kernel(const Dtw32Jo
             for (int b = 0; b < B.m; b++) atomicAdd(B.GC + b, qnan);
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Kept directions: when the direction words of every item fit the workspace
+// budget, the forward of a differentiable call stores them (the backward's
+// sweep, run once) and the backward only walks the paths.  One region per
+// batch of 32 consecutive items (the items a warp takes together): the
+// strip tables (cs_w, base) of the batch's sweep, then 32 lanes x cap words
+// grouped 8 per lane as in the recompute path.
+
+__device__ __forceinline__ void keep_region(const DirKeep &D, int64_t base, int *&tab_cs,
+                                            int *&tab_base, uint32_t *&words) {
+    unsigned char *reg = D.base + (base >> 5) * D.batch_bytes;
+    tab_cs = reinterpret_cast<int *>(reg);
+    tab_base = tab_cs + D.max_strips;
+    words = reinterpret_cast<uint32_t *>(reg + D.tab_bytes);
+}
+
+// The sweep with directions of every item into its batch region, and the
+// distance sqrt(hi + lo) of the same sweep (compensated predecessor choice).
+template <bool W>
+__global__ void __launch_bounds__(kBwdBlock) dtw32_keep_forward_kernel(const Dtw32Job J,
+                                                                      const DirKeep D) {
+    __shared__ uint32_t stage_all[kBwdBlock * 33 / 4 + 8 * 33];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    float2 *ring = J.ring + gtid;
+    uint32_t *stage = stage_all + (threadIdx.x >> 5) * (32 * 8 + 8) + lane;
+    const float *__restrict__ w = J.weights;
+    for (;;) {
+        const int64_t base = take_items(J.queue, lane);
+        if (base >= J.n_items) break;
+        const int64_t t = base + lane;
+        BwdItem B;
+        double g = 0.0;
+        bwd_setup(J, t, B, g);
+        int *tab_cs, *tab_base;
+        uint32_t *words;
+        keep_region(D, base, tab_cs, tab_base, words);
+        const int nstr_w = __reduce_max_sync(FULL, B.nstrips);
+        HL result = hl_inf();
+        bwd_row0<W>(B, w, ring, nth, result);
+        bool ok = true;
+        if (nstr_w > 0)
+            ok = bwd_strips<W, true>(B, 0, nstr_w, ring, ring, nullptr, words, D.cap, tab_cs,
+                                     tab_base, stage, lane, 32, nth, w, result);
+        if (t < J.n_items) {
+            double res = __longlong_as_double(0x7ff8000000000000LL);  // NaN: empty or unplanned
+            if (ok && B.n >= 1) {
+                const double cost = (double)result.h + (double)result.l;
+                if (J.out_cost) J.out_cost[t] = cost;
+                res = sqrt(cost);
+            } else if (J.out_cost) {
+                J.out_cost[t] = res;
+            }
+            J.out[t] = res;
+        }
+    }
+}
+
+// The backward from kept directions: each lane walks its item's path with the
+// distance of the kept forward (dist[t]) and adds the gradients as the
+// recompute path does.
+template <bool W>
+__global__ void __launch_bounds__(kBwdBlock) dtw32_keep_walk_kernel(const Dtw32Job J,
+                                                                   const DirKeep D,
+                                                                   const double *dist) {
+    const int lane = threadIdx.x & 31;
+    const float *__restrict__ w = J.weights;
+    for (;;) {
+        const int64_t base = take_items(J.queue, lane);
+        if (base >= J.n_items) break;
+        const int64_t t = base + lane;
+        BwdItem B;
+        double g = 0.0;
+        bwd_setup(J, t, B, g);
+        int *tab_cs, *tab_base;
+        uint32_t *words;
+        keep_region(D, base, tab_cs, tab_base, words);
+        int i = B.n - 1, j = B.m - 1;
+        float gr = 0.0f, gcol = 0.0f, sc = 0.0f;
+        bool done = B.n < 1;
+        if (!done) {
+            const double Dv = dist[t];
+            // a NaN distance (an item the forward could not sweep) gives NaN
+            // gradients, never zeros
+            sc = (Dv > 0.0 || Dv != Dv) ? (float)(g / Dv) : 0.0f;
+        }
+        bwd_walk<W>(B, 0, 1, words, tab_cs, tab_base, lane, 32, w, sc, i, j, gr, gcol, done);
+    }
+}
+
+int dtw32_keep_forward(const Dtw32Job &J, const DirKeep &D, cudaStream_t s) {
+    if (J.n_items == 0) return WB_OK;
+    WB_CUDA(cudaMemsetAsync(J.queue, 0, sizeof(unsigned long long), s));
+    timer_begin("dtw32_keep_forward_kernel", s);
+    if (J.weights) dtw32_keep_forward_kernel<true><<<J.grid, kBwdBlock, 0, s>>>(J, D);
+    else dtw32_keep_forward_kernel<false><<<J.grid, kBwdBlock, 0, s>>>(J, D);
+    timer_end(s);
+    WB_LAUNCH_CHECK("dtw32_keep_forward_kernel");
+    return WB_OK;
+}
+
+int dtw32_keep_walk(const Dtw32Job &J, const DirKeep &D, const double *dist, cudaStream_t s) {
+    if (J.n_items == 0) return WB_OK;
+    WB_CUDA(cudaMemsetAsync(J.queue, 0, sizeof(unsigned long long), s));
+    timer_begin("dtw32_keep_walk_kernel", s);
+    if (J.weights) dtw32_keep_walk_kernel<true><<<J.grid, kBwdBlock, 0, s>>>(J, D, dist);
+    else dtw32_keep_walk_kernel<false><<<J.grid, kBwdBlock, 0, s>>>(J, D, dist);
+    timer_end(s);
+    WB_LAUNCH_CHECK("dtw32_keep_walk_kernel");
+    return WB_OK;
+}
+
+int dtw32_keep_blocks_per_sm(bool walk, bool weighted) {
+    int nb = 0;
+    cudaError_t e;
+    if (walk)
+        e = weighted ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                           &nb, dtw32_keep_walk_kernel<true>, kBwdBlock, 0)
+                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                           &nb, dtw32_keep_walk_kernel<false>, kBwdBlock, 0);
+    else
+        e = weighted ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                           &nb, dtw32_keep_forward_kernel<true>, kBwdBlock, 0)
+                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                           &nb, dtw32_keep_forward_kernel<false>, kBwdBlock, 0);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return nb;
 }
 
 template <int S>

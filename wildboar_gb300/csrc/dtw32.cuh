@@ -47,7 +47,21 @@ struct Dtw32Job {
     int grid = 0, block = 0;
 };
 
+// Kept directions of a differentiable call (see dtw32.cu): one region of
+// batch_bytes per batch of 32 consecutive items, the two strip tables
+// (max_strips ints each, tab_bytes in all) first, then 32 lanes x cap words.
+struct DirKeep {
+    unsigned char *base = nullptr;
+    int64_t batch_bytes = 0;
+    int64_t tab_bytes = 0;
+    int64_t cap = 0;       // direction words per lane (multiple of 8)
+    int max_strips = 0;
+};
+
 int dtw32_forward(const Dtw32Job &J, int strip, cudaStream_t s);
+int dtw32_keep_forward(const Dtw32Job &J, const DirKeep &D, cudaStream_t s);
+int dtw32_keep_walk(const Dtw32Job &J, const DirKeep &D, const double *dist, cudaStream_t s);
+int dtw32_keep_blocks_per_sm(bool walk, bool weighted);
 int dtw32_backward(const Dtw32Job &J, cudaStream_t s);
 int dtw32_blocks_per_sm(int strip, bool weighted, bool backward, int block);
 int launch_grid_to_matrix(const double *in, int64_t nx, int64_t ny, int upper, double *out,

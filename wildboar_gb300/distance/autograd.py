@@ -18,12 +18,21 @@ optimal path is unique).  Workspace per resident thread: the direction words
 of one segment and one checkpoint row per segment boundary (bounded in total
 by ``WB_GPU_BWD_WORKSPACE_MB``, default 8192).
 
+When an input of ``dtw_matrix`` requires a gradient and the direction words of
+all its pairs fit that budget (``wb_dtw32_keep_bytes``), the forward runs the
+sweep with directions once and keeps them (wb_dtw32_distance_keep); the
+backward then only walks the paths (wb_dtw32_backward_keep) instead of
+recomputing the sweep.  The distances of that forward choose predecessors by
+compensated comparison, like the backward; they agree with the plain forward
+to a few float32 ulps of the path cost.
+
 ``barycenter_kmeans`` uses ``dtw_matrix`` for DTW-barycenter updates: Adam on
 the centroids with a soft assignment of every series to every centroid, so
 every pair takes part in the backward.
 """
 
 import ctypes
+import os
 
 import torch
 
@@ -35,16 +44,42 @@ def _job(x, y, r, weights):
     return _b.make_job(x, y, r=r, weights=weights, strip=16, block=128)
 
 
+def _workspace_budget():
+    return float(os.environ.get("WB_GPU_BWD_WORKSPACE_MB", "8192")) * 1048576.0
+
+
+def keeps_directions(x, y, r=1.0, *, g=None):
+    """Whether a differentiable ``dtw_matrix(x, y, r, g=g)`` keeps the
+    forward's directions (they fit ``WB_GPU_BWD_WORKSPACE_MB``)."""
+    weights = None
+    if g is not None:
+        weights = _b.logistic_weights(max(x.shape[1], y.shape[1]), g, x.device)
+    job = _job(x.detach().contiguous(), y.detach().contiguous(), float(r), weights)
+    nbytes = _lib.lib().wb_dtw32_keep_bytes(ctypes.byref(job))
+    return 0 <= nbytes <= _workspace_budget()
+
+
 class DTWMatrix(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, x, y, r, weights):
+    def forward(ctx, x, y, r, weights, keep_dirs):
         x = x.contiguous()
         y = y.contiguous()
         out = torch.empty(x.shape[0] * y.shape[0], dtype=torch.float64, device=x.device)
         job = _job(x, y, r, weights)
-        _lib.check(_lib.lib().wb_dtw32_distance(ctypes.byref(job), out.data_ptr(), None,
-                                                _b._stream()))
-        ctx.save_for_backward(x, y)
+        keep = None
+        if keep_dirs:
+            nbytes = _lib.lib().wb_dtw32_keep_bytes(ctypes.byref(job))
+            if 0 <= nbytes <= _workspace_budget():
+                keep = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=x.device)
+        if keep is not None:
+            _lib.check(_lib.lib().wb_dtw32_distance_keep(
+                ctypes.byref(job), out.data_ptr(), None, keep.data_ptr(), keep.numel(),
+                _b._stream()))
+        else:
+            _lib.check(_lib.lib().wb_dtw32_distance(ctypes.byref(job), out.data_ptr(), None,
+                                                    _b._stream()))
+        ctx.save_for_backward(x, y, out)
+        ctx.keep = keep
         ctx.r = r
         ctx.weights = weights
         # items are t = j * nx + i: reshape to (ny, nx) and transpose
@@ -52,17 +87,23 @@ class DTWMatrix(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, grad):
-        x, y = ctx.saved_tensors
+        x, y, out = ctx.saved_tensors
         # items are t = j * nx + i: the upstream gradient in that order
         g = grad.t().contiguous().to(torch.float64).reshape(-1)
         gx = torch.zeros_like(x)
         gy = torch.zeros_like(y)
         job = _job(x, y, ctx.r, ctx.weights)
-        _lib.check(_lib.lib().wb_dtw32_backward(
-            ctypes.byref(job), g.data_ptr(), gx.data_ptr(), x.shape[1], gy.data_ptr(),
-            y.shape[1], _b._stream()))
+        if ctx.keep is not None:
+            keep, ctx.keep = ctx.keep, None
+            _lib.check(_lib.lib().wb_dtw32_backward_keep(
+                ctypes.byref(job), out.data_ptr(), g.data_ptr(), gx.data_ptr(), x.shape[1],
+                gy.data_ptr(), y.shape[1], keep.data_ptr(), keep.numel(), _b._stream()))
+        else:
+            _lib.check(_lib.lib().wb_dtw32_backward(
+                ctypes.byref(job), g.data_ptr(), gx.data_ptr(), x.shape[1], gy.data_ptr(),
+                y.shape[1], _b._stream()))
         return (gx if ctx.needs_input_grad[0] else None,
-                gy if ctx.needs_input_grad[1] else None, None, None)
+                gy if ctx.needs_input_grad[1] else None, None, None, None)
 
 
 class PairedDTW(torch.autograd.Function):
@@ -122,7 +163,9 @@ def dtw_matrix(x, y, r=1.0, *, g=None):
     weights = None
     if g is not None:
         weights = _b.logistic_weights(max(x.shape[1], y.shape[1]), g, x.device)
-    return DTWMatrix.apply(x, y, float(r), weights)
+    # keep the directions only when a backward can follow
+    keep_dirs = torch.is_grad_enabled() and (x.requires_grad or y.requires_grad)
+    return DTWMatrix.apply(x, y, float(r), weights, keep_dirs)
 
 
 def soft_assignment_loss(D, temperature=1.0):

@@ -58,6 +58,10 @@ _lib.declare("wb_dtw32_backward", [_P(Dtw32), _vp, _vp, ctypes.c_int64, _vp, cty
                                    _vp])
 _lib.declare("wb_series_lengths_f32", [_vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
                                        _vp, _vp])
+_lib.declare("wb_dtw32_keep_bytes", [_P(Dtw32)], ctypes.c_int64)
+_lib.declare("wb_dtw32_distance_keep", [_P(Dtw32), _vp, _vp, _vp, ctypes.c_int64, _vp])
+_lib.declare("wb_dtw32_backward_keep", [_P(Dtw32), _vp, _vp, _vp, ctypes.c_int64, _vp,
+                                        ctypes.c_int64, _vp, ctypes.c_int64, _vp])
 
 STRIPS = (4, 8, 16, 24, 32)
 BLOCKS = (64, 128, 256)
