@@ -91,6 +91,23 @@ __device__ __forceinline__ void sqdiff2(float x0, float x1, float y, float &c0, 
         : "f"(x0), "f"(x1), "f"(y));
 }
 
+// two floats as one packed f32x2 operand (adjacent registers)
+__device__ __forceinline__ uint64_t pack2(float a, float b) {
+    uint64_t p;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(p) : "f"(a), "f"(b));
+    return p;
+}
+
+// (x0 - y)^2 and (x1 - y)^2 from the packed pairs x2 = {x0, x1}, y2 = {y, y}
+__device__ __forceinline__ void sqdiff2p(uint64_t x2, uint64_t y2, float &c0, float &c1) {
+    asm("{\n\t.reg .b64 pa;\n\t"
+        "sub.rn.f32x2 pa, %2, %3;\n\t"
+        "mul.rn.f32x2 pa, pa, pa;\n\t"
+        "mov.b64 {%0, %1}, pa;\n\t}"
+        : "=f"(c0), "=f"(c1)
+        : "l"(x2), "l"(y2));
+}
+
 // Bits k (k < 32) with 0 <= e - k < width: the strip rows in band at a
 // column, e = c - i0 - lo.
 __device__ __forceinline__ unsigned band_bits(int e, int width) {
@@ -103,26 +120,31 @@ __device__ __forceinline__ unsigned band_bits(int e, int width) {
 // One column of a strip in the forward sweep (no traceback directions):
 // the minimum of the three hi parts with the lo of a candidate holding it
 // (left, then up, then diag on equal hi), Fast2Sum for the new partial sum.
-// With MASK, rows whose bit of M is clear are out of band (infinite cost).
+// The column reads the previous column's cells from Pin and writes its own
+// to Pout (two register sets alternating between columns, so no cell value
+// has to be copied to free its register).  With MASK, rows whose bit of M
+// is clear are out of band (infinite cost).
 template <int S, bool W, bool MASK>
-__device__ __forceinline__ void fwd_column(HL (&P)[S], HL bup, HL bdiag, float yc,
-                                           const float (&xr)[S], int d0, unsigned M,
+__device__ __forceinline__ void fwd_column(const HL (&Pin)[S], HL (&Pout)[S], HL bup,
+                                           HL bdiag, float yc, const float (&xr)[S],
+                                           const uint64_t (&xr2)[S / 2], int d0, unsigned M,
                                            const float *__restrict__ w, int valid) {
-    HL dg = bdiag;  // cell (i0 + k - 1, c - 1)
-    HL up = bup;    // cell (i0 + k - 1, c)
     float cpair[2];
+    const uint64_t yp = W ? 0ull : pack2(yc, yc);
 #pragma unroll
     for (int k = 0; k < S; k++) {
+        if (!W && (k & 1) == 0) sqdiff2p(xr2[k / 2], yp, cpair[0], cpair[1]);
+        const HL dg = k == 0 ? bdiag : Pin[k - 1];  // cell (i0 + k - 1, c - 1)
+        const HL up = k == 0 ? bup : Pout[k - 1];   // cell (i0 + k - 1, c)
+        const HL lf = Pin[k];                       // cell (i0 + k, c - 1)
         float cst;
         if (W) {
             const float vv = __fsub_rn(xr[k], yc);
             cst = __fmul_rn(__fmul_rn(vv, vv), w[(!MASK || k < valid) ? abs(d0 - k) : 0]);
         } else {
-            if ((k & 1) == 0) sqdiff2(xr[k], xr[k + 1], yc, cpair[0], cpair[1]);
             cst = cpair[k & 1];
         }
         if (MASK) cst = ((M >> k) & 1u) ? cst : WB_FINF;
-        const HL lf = P[k];
         HL best;
         asm("min.f32 %0, %1, %2, %3;" : "=f"(best.h) : "f"(dg.h), "f"(up.h), "f"(lf.h));
         best.l = (up.h == best.h) ? up.l : dg.l;
@@ -134,10 +156,7 @@ __device__ __forceinline__ void fwd_column(HL (&P)[S], HL bup, HL bdiag, float y
         // the path cost in all
         const float sh = __fadd_rn(best.h, cst);
         const float err = __fsub_rn(cst, __fsub_rn(sh, best.h));
-        const HL nv{sh, __fadd_rn(best.l, err)};
-        dg = lf;
-        up = nv;
-        P[k] = nv;
+        Pout[k] = HL{sh, __fadd_rn(best.l, err)};
     }
 }
 
@@ -196,6 +215,9 @@ __device__ HL sweep_uniform(Item it, bool active, const float *__restrict__ w, f
         float xr[S];
 #pragma unroll
         for (int k = 0; k < S; k++) xr[k] = (k < rows) ? X[i0 + k] : qnan;
+        uint64_t xr2[S / 2];
+#pragma unroll
+        for (int k = 0; k < S / 2; k++) xr2[k] = W ? 0ull : pack2(xr[2 * k], xr[2 * k + 1]);
         int cstart = imax(0, i0 - mn - r + 1);
         int cend = imin(m, i0 + rows - 1 + mx);
         if (rows == 0) {
@@ -212,7 +234,7 @@ __device__ HL sweep_uniform(Item it, bool active, const float *__restrict__ w, f
         const int ce_w = __reduce_max_sync(FULL, cend);
         const int bs_w = __reduce_max_sync(FULL, bstart);
         const int be_w = __reduce_min_sync(FULL, bend);
-        HL P[S];
+        HL P[S], Q[S];
 #pragma unroll
         for (int k = 0; k < S; k++) P[k] = hl_inf();
         HL bdiag = hl_inf();
@@ -234,7 +256,8 @@ __device__ HL sweep_uniform(Item it, bool active, const float *__restrict__ w, f
         float ny0 = load_y(cs_w), ny1 = load_y(cs_w + 1);
         const bool last = rows > 0 && (i0 + rows == n);
         const int krow = rows - 1;
-        for (int c = cs_w; c < ce_w; c++) {
+        // column c from the cells of column c - 1 (Pin) into Pout
+        auto column = [&](int c, const HL(&Pin)[S], HL(&Pout)[S]) {
             const HL bup = nb0;
             const float yc = ny0;
             nb0 = nb1;
@@ -242,20 +265,50 @@ __device__ HL sweep_uniform(Item it, bool active, const float *__restrict__ w, f
             nb1 = load_up(c + 2);
             ny1 = load_y(c + 2);
             if (c >= bs_w && c < be_w) {
-                fwd_column<S, W, false>(P, bup, bdiag, yc, xr, c - i0, 0u, w, rows);
+                fwd_column<S, W, false>(Pin, Pout, bup, bdiag, yc, xr, xr2, c - i0, 0u, w,
+                                        rows);
             } else {
                 // past the lane's series end every row is out of band
                 const unsigned M = c < m ? band_bits(c - i0 - lo, (int)width) : 0u;
-                fwd_column<S, W, true>(P, bup, bdiag, yc, xr, c - i0, M, w, rows);
+                fwd_column<S, W, true>(Pin, Pout, bup, bdiag, yc, xr, xr2, c - i0, M, w,
+                                       rows);
             }
             if (last && c == m - 1) {
 #pragma unroll
                 for (int k = 0; k < S; k++)
-                    if (k <= krow) result = P[k];
+                    if (k <= krow) result = Pout[k];
             }
-            ring[(int64_t)c * nth] = make_float2(P[S - 1].h, P[S - 1].l);
+            ring[(int64_t)c * nth] = make_float2(Pout[S - 1].h, Pout[S - 1].l);
             bdiag = bup;
+        };
+        int c = cs_w;
+        for (; c + 1 < ce_w; c += 2) {
+            if (c >= bs_w && c + 1 < be_w) {
+                // two band-interior columns as one straight-line block, so
+                // the cells of column c + 1 can issue beside those of c
+                const HL bup0 = nb0, bup1 = nb1;
+                const float y0 = ny0, y1 = ny1;
+                nb0 = load_up(c + 2);
+                nb1 = load_up(c + 3);
+                ny0 = load_y(c + 2);
+                ny1 = load_y(c + 3);
+                fwd_column<S, W, false>(P, Q, bup0, bdiag, y0, xr, xr2, c - i0, 0u, w, rows);
+                fwd_column<S, W, false>(Q, P, bup1, bup0, y1, xr, xr2, c + 1 - i0, 0u, w,
+                                        rows);
+                if (last && (c == m - 1 || c + 1 == m - 1)) {
+#pragma unroll
+                    for (int k = 0; k < S; k++)
+                        if (k <= krow) result = c == m - 1 ? Q[k] : P[k];
+                }
+                ring[(int64_t)c * nth] = make_float2(Q[S - 1].h, Q[S - 1].l);
+                ring[(int64_t)(c + 1) * nth] = make_float2(P[S - 1].h, P[S - 1].l);
+                bdiag = bup1;
+            } else {
+                column(c, P, Q);
+                column(c + 1, Q, P);
+            }
         }
+        if (c < ce_w) column(c, P, Q);
         if (rows > 0) {
             pstart = cstart;
             pend = cend;
