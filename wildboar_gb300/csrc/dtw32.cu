@@ -404,19 +404,24 @@ __device__ __forceinline__ int64_t dir_index(int64_t w, int64_t g, int64_t nth) 
 
 // One column of a backward strip: Fast2Sum accumulation, the predecessor by
 // compensated comparison, its 2-bit code (0 diag, 1 up, 2 left) per row into
-// `word`.  With MASK, rows whose bit of M is clear are out of band and hold
-// (+inf, 0).
+// `word`.  Reads the previous column from Pin and writes Pout (register sets
+// alternating between columns, as in fwd_column).  With MASK, rows whose bit
+// of M is clear are out of band and hold (+inf, 0).
 template <bool W, bool MASK>
-__device__ __forceinline__ void bwd_column(HL (&P)[kGradStrip], HL bup, HL bdiag, float yc,
-                                           const float (&xr)[kGradStrip], int d0, unsigned M,
-                                           const float *__restrict__ w, int valid,
+__device__ __forceinline__ void bwd_column(const HL (&Pin)[kGradStrip], HL (&Pout)[kGradStrip],
+                                           HL bup, HL bdiag, float yc,
+                                           const float (&xr)[kGradStrip],
+                                           const uint64_t (&xr2)[kGradStrip / 2], int d0,
+                                           unsigned M, const float *__restrict__ w, int valid,
                                            uint32_t &word) {
-    HL dg = bdiag;
-    HL up = bup;
     float cpair[2];
+    const uint64_t yp = W ? 0ull : pack2(yc, yc);
 #pragma unroll
     for (int k = 0; k < kGradStrip; k++) {
-        const HL lf = P[k];
+        if (!W && (k & 1) == 0) sqdiff2p(xr2[k / 2], yp, cpair[0], cpair[1]);
+        const HL dg = k == 0 ? bdiag : Pin[k - 1];
+        const HL up = k == 0 ? bup : Pout[k - 1];
+        const HL lf = Pin[k];
         HL best = dg;
         uint32_t dir = 0;
         if (hl_less(up, best)) {
@@ -432,7 +437,6 @@ __device__ __forceinline__ void bwd_column(HL (&P)[kGradStrip], HL bup, HL bdiag
             const float vv = __fsub_rn(xr[k], yc);
             cst = __fmul_rn(__fmul_rn(vv, vv), w[(!MASK || k < valid) ? abs(d0 - k) : 0]);
         } else {
-            if ((k & 1) == 0) sqdiff2(xr[k], xr[k + 1], yc, cpair[0], cpair[1]);
             cst = cpair[k & 1];
         }
         // Fast2Sum (see fwd_column)
@@ -440,9 +444,7 @@ __device__ __forceinline__ void bwd_column(HL (&P)[kGradStrip], HL bup, HL bdiag
         HL nv{sh, __fadd_rn(best.l, __fsub_rn(cst, __fsub_rn(sh, best.h)))};
         if (MASK && !((M >> k) & 1u)) nv = hl_inf();
         word |= dir << (2 * k);
-        dg = lf;
-        up = nv;
-        P[k] = nv;
+        Pout[k] = nv;
     }
 }
 
@@ -542,7 +544,10 @@ __device__ bool bwd_strips(const BwdItem &B, int s0, int s1, const float2 *src, 
         }
         const float2 *in = (s == s0) ? src : ring;
         float2 *out = (s == s1 - 1 && last_dst) ? last_dst : ring;
-        HL P[S];
+        uint64_t xr2[S / 2];
+#pragma unroll
+        for (int k = 0; k < S / 2; k++) xr2[k] = W ? 0ull : pack2(xr[2 * k], xr[2 * k + 1]);
+        HL P[S], Q[S];
 #pragma unroll
         for (int k = 0; k < S; k++) P[k] = hl_inf();
         auto load_up = [&](int c) {
@@ -559,7 +564,22 @@ __device__ bool bwd_strips(const BwdItem &B, int s0, int s1, const float2 *src, 
         float ny0 = load_y(cs_w), ny1 = load_y(cs_w + 1);
         const bool last = rows > 0 && (i0 + rows == B.n);
         const int krow = rows - 1;
-        for (int c = cs_w; c < ce_w; c++) {
+        // the column's direction word into the stage; a full group of 8 (or
+        // the strip's last column) goes out as two 16-byte stores
+        auto put_word = [&](int c, uint32_t word) {
+            if (DIRS) {
+                const int64_t wi = base + (c - cs_w);
+                stage[(wi & 7) * 33] = word;
+                if ((wi & 7) == 7 || c == ce_w - 1) {
+                    uint4 *dst = reinterpret_cast<uint4 *>(
+                        dirs + dir_index(wi & ~(int64_t)7, dir_g, dir_n));
+                    dst[0] = make_uint4(stage[0], stage[33], stage[66], stage[99]);
+                    dst[1] = make_uint4(stage[132], stage[165], stage[198], stage[231]);
+                }
+            }
+        };
+        // column c from the cells of column c - 1 (Pin) into Pout
+        auto column = [&](int c, const HL(&Pin)[S], HL(&Pout)[S]) {
             const HL bup = nb0;
             const float yc = ny0;
             nb0 = nb1;
@@ -568,30 +588,52 @@ __device__ bool bwd_strips(const BwdItem &B, int s0, int s1, const float2 *src, 
             ny1 = load_y(c + 2);
             uint32_t word = 0;
             if (c >= bs_w && c < be_w) {
-                bwd_column<W, false>(P, bup, bdiag, yc, xr, c - i0, 0u, w, rows, word);
+                bwd_column<W, false>(Pin, Pout, bup, bdiag, yc, xr, xr2, c - i0, 0u, w, rows,
+                                     word);
             } else {
                 const unsigned M = c < B.m ? band_bits(c - i0 - B.lo, B.width) : 0u;
-                bwd_column<W, true>(P, bup, bdiag, yc, xr, c - i0, M, w, rows, word);
+                bwd_column<W, true>(Pin, Pout, bup, bdiag, yc, xr, xr2, c - i0, M, w, rows,
+                                    word);
             }
-            if (DIRS) {
-                // stage the word; a full group of 8 (or the strip's last
-                // column) goes out as two 16-byte stores
-                const int64_t wi = base + (c - cs_w);
-                stage[(wi & 7) * 33] = word;
-                if ((wi & 7) == 7 || c == ce_w - 1) {
-                    uint4 *dst = reinterpret_cast<uint4 *>(dirs + dir_index(wi & ~(int64_t)7, dir_g, dir_n));
-                    dst[0] = make_uint4(stage[0], stage[33], stage[66], stage[99]);
-                    dst[1] = make_uint4(stage[132], stage[165], stage[198], stage[231]);
-                }
-            }
+            put_word(c, word);
             if (last && c == B.m - 1) {
 #pragma unroll
                 for (int k = 0; k < S; k++)
-                    if (k == krow) result = P[k];
+                    if (k == krow) result = Pout[k];
             }
-            out[(int64_t)c * nth] = make_float2(P[S - 1].h, P[S - 1].l);
+            out[(int64_t)c * nth] = make_float2(Pout[S - 1].h, Pout[S - 1].l);
             bdiag = bup;
+        };
+        int c = cs_w;
+        for (; c + 1 < ce_w; c += 2) {
+            if (c >= bs_w && c + 1 < be_w) {
+                // two band-interior columns as one straight-line block
+                const HL bup0 = nb0, bup1 = nb1;
+                const float y0 = ny0, y1 = ny1;
+                nb0 = load_up(c + 2);
+                nb1 = load_up(c + 3);
+                ny0 = load_y(c + 2);
+                ny1 = load_y(c + 3);
+                uint32_t w0 = 0, w1 = 0;
+                bwd_column<W, false>(P, Q, bup0, bdiag, y0, xr, xr2, c - i0, 0u, w, rows, w0);
+                bwd_column<W, false>(Q, P, bup1, bup0, y1, xr, xr2, c + 1 - i0, 0u, w, rows,
+                                     w1);
+                put_word(c, w0);
+                put_word(c + 1, w1);
+                if (last && (c == B.m - 1 || c + 1 == B.m - 1)) {
+#pragma unroll
+                    for (int k = 0; k < S; k++)
+                        if (k == krow) result = c == B.m - 1 ? Q[k] : P[k];
+                }
+                out[(int64_t)c * nth] = make_float2(Q[S - 1].h, Q[S - 1].l);
+                out[(int64_t)(c + 1) * nth] = make_float2(P[S - 1].h, P[S - 1].l);
+                bdiag = bup1;
+            } else {
+                column(c, P, Q);
+                column(c + 1, Q, P);
+            }
         }
+        if (c < ce_w) column(c, P, Q);
         base += ce_w - cs_w;
         if (rows > 0) {
             pstart = cstart;
@@ -603,15 +645,24 @@ __device__ bool bwd_strips(const BwdItem &B, int s0, int s1, const float2 *src, 
 
 // Walk of one lane through the rows of segment g (strips [g K, (g+1) K), and
 // row 0 when g == 0), from (i, j) upward, adding the gradient of every row and
-// column the path leaves.  Returns with i below the segment (or done).
+// column the path leaves.  Returns with i below the segment (or done).  The
+// walk keeps in registers the 8-word group (one 32-byte sector) of direction
+// words it reads from, the strip's table entries and the current r_i and c_j,
+// so a step that stays in the group (a move up, or left within 8 columns)
+// issues no dependent load.
 template <bool W>
-__device__ void bwd_walk(const BwdItem &B, int g, int K, const uint32_t *dirs,
-                         const int *tab_cs, const int *tab_base, int64_t gtid, int64_t nth,
-                         const float *__restrict__ w, float sc, int &i, int &j, float &gr,
-                         float &gc, bool &done) {
+__device__ __forceinline__ void bwd_walk(const BwdItem &B, int g, int K, const uint32_t *dirs,
+                                         const int *tab_cs, const int *tab_base, int64_t gtid,
+                                         int64_t nth, const float *__restrict__ w, float sc,
+                                         int &i, int &j, float &gr, float &gc, bool &done) {
     const int first_row = g == 0 ? 0 : 1 + g * K * kGradStrip;
-    while (!done && i >= first_row) {
-        const float vv = __fsub_rn(B.R[i], B.C[j]);
+    if (done || i < first_row) return;
+    int cur_s = -1, tcs = 0, tbase = 0;
+    int64_t cur_grp = -1;
+    uint4 ga = make_uint4(0, 0, 0, 0), gb = ga;
+    float ri = B.R[i], cj = B.C[j];
+    while (true) {
+        const float vv = __fsub_rn(ri, cj);
         float d = vv;
         if (W) d = __fmul_rn(w[i == 0 ? imax(j - 1, 0) : abs(i - j)], vv);
         gr = __fadd_rn(gr, d);
@@ -620,7 +671,7 @@ __device__ void bwd_walk(const BwdItem &B, int g, int K, const uint32_t *dirs,
             atomicAdd(B.GR, sc * gr);
             atomicAdd(B.GC, -(sc * gc));
             done = true;
-            break;
+            return;
         }
         uint32_t move;
         if (i == 0) {
@@ -629,9 +680,25 @@ __device__ void bwd_walk(const BwdItem &B, int g, int K, const uint32_t *dirs,
             move = 1;
         } else {
             const int s = (i - 1) / kGradStrip;
-            const int loc = s - g * K;
-            const uint32_t word =
-                dirs[dir_index((int64_t)tab_base[loc] + (j - tab_cs[loc]), gtid, nth)];
+            if (s != cur_s) {
+                const int loc = s - g * K;
+                tcs = tab_cs[loc];
+                tbase = tab_base[loc];
+                cur_s = s;
+            }
+            const int64_t widx = (int64_t)tbase + (j - tcs);
+            const int64_t grp = widx >> 3;
+            if (grp != cur_grp) {
+                const uint4 *src = reinterpret_cast<const uint4 *>(dirs + dir_index(grp << 3, gtid, nth));
+                ga = src[0];
+                gb = src[1];
+                cur_grp = grp;
+            }
+            const int e = (int)(widx & 7);
+            const uint4 h = (e & 4) ? gb : ga;
+            const uint32_t lo2 = (e & 2) ? h.z : h.x;
+            const uint32_t hi2 = (e & 2) ? h.w : h.y;
+            const uint32_t word = (e & 1) ? hi2 : lo2;
             move = (word >> (2 * ((i - 1) - s * kGradStrip))) & 3u;
         }
         if (move != 2) {  // leaving row i
@@ -644,6 +711,9 @@ __device__ void bwd_walk(const BwdItem &B, int g, int K, const uint32_t *dirs,
             gc = 0.0f;
             j -= 1;
         }
+        if (i < first_row) return;
+        if (move != 2) ri = B.R[i];
+        if (move != 1) cj = B.C[j];
     }
 }
 
