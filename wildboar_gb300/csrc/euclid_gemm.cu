@@ -429,9 +429,11 @@ struct SplitSide {
     float *sum;
 };
 
-// rows 0 .. A.rows_p - 1 of the launch are A's, the next B.rows_p are B's
+// rows 0 .. A.rows_p - 1 of the launch are A's, the next B.rows_p are B's;
+// the first thread also clears the GEMM's wait-status word
 template <int KR>
-__global__ void tf32_split_kernel(SplitSide A, SplitSide B, int K, int Kp) {
+__global__ void tf32_split_kernel(SplitSide A, SplitSide B, int K, int Kp, int *err) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *err = 0;
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -499,13 +501,24 @@ __global__ void tf32_split_kernel(SplitSide A, SplitSide B, int K, int Kp) {
     }
 }
 
-static void launch_split(const SplitSide &A, const SplitSide &B, int K, int Kp, cudaStream_t s) {
+static void launch_split(const SplitSide &A, const SplitSide &B, int K, int Kp, int *err,
+                         cudaStream_t s) {
     const int64_t rows = (int64_t)A.rows_p + B.rows_p;
     const int grid = (int)std::min<int64_t>((int64_t)device_info().sm_count * 8, (rows + 7) / 8);
     if (Kp <= 32 * 32)
-        tf32_split_kernel<32><<<grid, 256, 0, s>>>(A, B, K, Kp);
+        tf32_split_kernel<32><<<grid, 256, 0, s>>>(A, B, K, Kp, err);
     else
-        tf32_split_kernel<0><<<grid, 256, 0, s>>>(A, B, K, Kp);
+        tf32_split_kernel<0><<<grid, 256, 0, s>>>(A, B, K, Kp, err);
+}
+
+// a pinned host word per thread for the status read-back (allocated once)
+static int *pinned_status() {
+    thread_local int *p = nullptr;
+    if (!p && cudaMallocHost(&p, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        p = nullptr;
+    }
+    return p;
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point
@@ -566,9 +579,8 @@ int euclid_tc(const double *x, int64_t sx, int M, const double *y, int64_t sy, i
     WB_TAKE(smx, float, ws, M);
     WB_TAKE(smy, float, ws, N);
     WB_TAKE(err, int, ws, 1);
-    WB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
     launch_split(SplitSide{x, sx, M, Mp, ahi, alo, stx, smx},
-                 SplitSide{y, sy, N, Np, bhi, blo, sty, smy}, K, Kp, s);
+                 SplitSide{y, sy, N, Np, bhi, blo, sty, smy}, K, Kp, err, s);
     WB_LAUNCH_CHECK("tf32_split_kernel");
     CUtensorMap mAh, mAl, mBh, mBl;
     WB_TRY(make_map(&mAh, ahi, Mp, Kp, kBM));
@@ -593,8 +605,10 @@ int euclid_tc(const double *x, int64_t sx, int M, const double *y, int64_t sy, i
     timer_end(s);
     WB_LAUNCH_CHECK("euclid_tc_kernel");
     int herr = 0;
-    WB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    int *ph = pinned_status();
+    WB_CUDA(cudaMemcpyAsync(ph ? ph : &herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     WB_CUDA(cudaStreamSynchronize(s));
+    if (ph) herr = *ph;
     if (herr || injected(INJ_WAIT))
         return fail(WB_ETIMEOUT, "euclid_tc_kernel: a pipeline wait gave up");
     return WB_OK;
