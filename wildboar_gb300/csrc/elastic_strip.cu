@@ -145,16 +145,19 @@ struct Rows {
     float pxf[S];         // msm x_{i-1} as float
 };
 
-// One strip column.  P[k]: cell (i0 + k, c - 1) on entry, (i0 + k, c) on exit;
-// bup = cell (i0 - 1, c), bdiag = cell (i0 - 1, c - 1).  MASK: some rows of
-// the strip are outside their band at this column or past the series end.
-template <int KIND, int S, class A, bool MASK, bool KEY = false>
-__device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
-                                       typename A::V bdiag, const Rows<S, A> &Rw,
-                                       typename A::E yc, typename A::E yp, typename A::E colv,
-                                       float ycf, float ypf, int c, int i0, int lo, int hi,
-                                       int valid, const PairCtx<A> &C,
-                                       typename A::V (&rmin)[S]) {
+// One strip column.  Pin[k]: cell (i0 + k, c - 1); Pout[k]: cell (i0 + k, c);
+// bup = cell (i0 - 1, c), bdiag = cell (i0 - 1, c - 1).  PP: Pin and Pout are
+// two register sets that alternate between columns (no cell value is copied
+// to free its register); otherwise they are the same array, updated in place.
+// MASK: some rows of the strip are outside their band at this column or past
+// the series end.
+template <int KIND, int S, class A, bool MASK, bool KEY = false, bool PP = false>
+__device__ __forceinline__ void column(const typename A::V (&Pin)[S], typename A::V (&Pout)[S],
+                                       typename A::V bup, typename A::V bdiag,
+                                       const Rows<S, A> &Rw, typename A::E yc,
+                                       typename A::E yp, typename A::E colv, float ycf,
+                                       float ypf, int c, int i0, int lo, int hi, int valid,
+                                       const PairCtx<A> &C, typename A::V (&rmin)[S]) {
     using V = typename A::V;
     using E = typename A::E;
     constexpr bool DTWF = Kt<KIND>::dtwf;
@@ -162,7 +165,11 @@ __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
     V up = bup;
 #pragma unroll
     for (int k = 0; k < S; k++) {
-        const V lf = P[k];
+        if (PP && k > 0) {
+            dg = Pin[k - 1];
+            up = Pout[k - 1];
+        }
+        const V lf = Pin[k];
         const int d = c - (i0 + k);
         V nv;
         if constexpr (KIND == K_DTW || KIND == K_WDTW) {
@@ -235,7 +242,7 @@ __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
             if (d > hi) {
                 nv = DTWF ? A::inf() : A::zero();
             } else if (d < lo) {
-                if constexpr (KIND == K_MSM) nv = (k < 2) ? bup : P[k >= 2 ? k - 2 : 0];
+                if constexpr (KIND == K_MSM) nv = (k < 2) ? bup : Pout[k >= 2 ? k - 2 : 0];
                 else nv = DTWF ? A::inf() : A::zero();
             }
         }
@@ -244,9 +251,11 @@ __device__ __forceinline__ void column(typename A::V (&P)[S], typename A::V bup,
             if (!MASK || (d >= lo && d <= hi && k < valid))
                 rmin[k] = KIND == K_ADTW_ANY ? A::vmin_any(rmin[k], nv) : A::vmin(rmin[k], nv);
         }
-        dg = lf;
-        up = nv;
-        P[k] = nv;
+        if (!PP) {
+            dg = lf;
+            up = nv;
+        }
+        Pout[k] = nv;
     }
 }
 
@@ -400,7 +409,7 @@ __device__ __forceinline__ int sweep_strip(const double *__restrict__ X, int n,
         if (bstart >= bend) bstart = bend = cend;
     }
     const bool at_boundary = (cstart == FC);
-    V P[S];
+    V P[S], Q[S];
 #pragma unroll
     for (int k = 0; k < S; k++) {
         V v;
@@ -434,7 +443,12 @@ __device__ __forceinline__ int sweep_strip(const double *__restrict__ X, int n,
     double ny0 = ld_y(cstart), ny1 = ld_y(cstart + 1);
     E yp = cstart > 0 ? A::el(__ldg(Y + cstart - 1)) : A::el(0.0);
     float ypf = cstart > 0 ? (float)__ldg(Y + cstart - 1) : 0.0f;
-    for (int c = cstart; c < cend; c++) {
+    // column c from the cells of column c - 1 (Pin) into Pout; the compensated
+    // FP32 forms alternate two register sets (PP), FP64 and msm (whose masked
+    // cells read the stale cell two rows up, and which measured slower that
+    // way) update P in place
+    constexpr bool PP = !is_f64<A>() && KIND != K_MSM;
+    auto step = [&](int c, const V(&Pin)[S], V(&Pout)[S]) {
         const V bup = nb0;
         const double ycd = ny0;
         nb0 = nb1;
@@ -447,23 +461,33 @@ __device__ __forceinline__ int sweep_strip(const double *__restrict__ X, int n,
         if constexpr (KIND == K_ERP) colv = A::el(__ldg(C.gY + c));
         if constexpr (KIND == K_TWE) colv = A::absv(A::sub(yp, yc));
         if (c >= bstart && c < bend)
-            column<KIND, S, A, false, KEY>(P, bup, bdiag, Rw, yc, yp, colv, ycf, ypf, c, i0,
-                                           lo, hi, rows, C, rmin);
+            column<KIND, S, A, false, KEY, PP>(Pin, Pout, bup, bdiag, Rw, yc, yp, colv, ycf,
+                                               ypf, c, i0, lo, hi, rows, C, rmin);
         else
-            column<KIND, S, A, true, KEY>(P, bup, bdiag, Rw, yc, yp, colv, ycf, ypf, c, i0, lo,
-                                          hi, rows, C, rmin);
+            column<KIND, S, A, true, KEY, PP>(Pin, Pout, bup, bdiag, Rw, yc, yp, colv, ycf,
+                                              ypf, c, i0, lo, hi, rows, C, rmin);
         if constexpr (KIND == K_MSM) {
-            if (c == cnext - 1) st.stale_next = P[S - 2];
+            if (c == cnext - 1) st.stale_next = Pout[S - 2];
         }
         if (last && c == m - 1) {
 #pragma unroll
             for (int k = 0; k < S; k++)
-                if (k < rows) st.result = P[k];  // ends at P[rows - 1], no indexed P
+                if (k < rows) st.result = Pout[k];  // ends at Pout[rows - 1], no indexed P
         }
-        ring[(int64_t)c * nth] = A::pack(P[S - 1]);
+        ring[(int64_t)c * nth] = A::pack(Pout[S - 1]);
         bdiag = bup;
         yp = yc;
         ypf = ycf;
+    };
+    if constexpr (PP) {
+        int c = cstart;
+        for (; c + 1 < cend; c += 2) {
+            step(c, P, Q);
+            step(c + 1, Q, P);
+        }
+        if (c < cend) step(c, P, Q);
+    } else {
+        for (int c = cstart; c < cend; c++) step(c, P, P);
     }
     st.pstart = cstart;
     st.pend = cend;
