@@ -78,19 +78,6 @@ __device__ __forceinline__ Item load_item(const Dtw32Job &J, int64_t t) {
     return it;
 }
 
-// (x0 - y)^2 and (x1 - y)^2 as one packed f32x2 subtraction and one packed
-// multiplication (each half rounded as the scalar operation would be)
-__device__ __forceinline__ void sqdiff2(float x0, float x1, float y, float &c0, float &c1) {
-    asm("{\n\t.reg .b64 pa, pb;\n\t"
-        "mov.b64 pa, {%2, %3};\n\t"
-        "mov.b64 pb, {%4, %4};\n\t"
-        "sub.rn.f32x2 pa, pa, pb;\n\t"
-        "mul.rn.f32x2 pa, pa, pa;\n\t"
-        "mov.b64 {%0, %1}, pa;\n\t}"
-        : "=f"(c0), "=f"(c1)
-        : "f"(x0), "f"(x1), "f"(y));
-}
-
 // two floats as one packed f32x2 operand (adjacent registers)
 __device__ __forceinline__ uint64_t pack2(float a, float b) {
     uint64_t p;
@@ -98,7 +85,9 @@ __device__ __forceinline__ uint64_t pack2(float a, float b) {
     return p;
 }
 
-// (x0 - y)^2 and (x1 - y)^2 from the packed pairs x2 = {x0, x1}, y2 = {y, y}
+// (x0 - y)^2 and (x1 - y)^2 from the packed pairs x2 = {x0, x1}, y2 = {y, y}:
+// one packed f32x2 subtraction and one packed multiplication (each half
+// rounded as the scalar operation would be)
 __device__ __forceinline__ void sqdiff2p(uint64_t x2, uint64_t y2, float &c0, float &c1) {
     asm("{\n\t.reg .b64 pa;\n\t"
         "sub.rn.f32x2 pa, %2, %3;\n\t"
