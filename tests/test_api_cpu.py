@@ -302,3 +302,40 @@ def test_distance_profile_parameter_validation():
         distance_profile(np.arange(9.0), x[:, :5], dilation=2, padding=1)
     with pytest.raises(NotImplementedError, match="pointwise"):
         distance_profile(y, x, metric="scaled_manhattan", dilation=2)
+
+
+def test_kept_direction_bytes_on_the_host():
+    # wb_dtw32_keep_bytes is host arithmetic (no device call): per batch of 32
+    # items the two strip tables (256-byte aligned) and 32 lanes x cap words,
+    # cap = strips of the shorter (dtw) or x (wdtw) length x the longer length,
+    # rounded to whole groups of 8
+    import ctypes
+
+    from wildboar_gb300 import _lib
+    from wildboar_gb300.distance import batched as B
+
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("libwbgpu.so is not built")
+    fn = _lib.lib().wb_dtw32_keep_bytes
+
+    def job(x_len, y_len, n_items, weighted=False):
+        j = B.Dtw32()
+        j.x_len, j.y_len, j.nx, j.ny = x_len, y_len, 1, n_items
+        j.n_items, j.r = n_items, 0.2
+        j.weights = 8 if weighted else None  # only whether it is set matters here
+        return j
+
+    def want(x_len, y_len, n_items, weighted=False):
+        rows = x_len if weighted else min(x_len, y_len)
+        strips = (rows - 2) // 16 + 1 if rows > 1 else 0
+        cap = (max(strips * max(x_len, y_len), 8) + 7) // 8 * 8
+        tab = (2 * max(strips, 1) * 4 + 255) // 256 * 256
+        return (n_items + 31) // 32 * (tab + 32 * cap * 4)
+
+    for args in ((256, 256, 131072), (300, 180, 360), (140, 260, 360, True), (1, 1, 5),
+                 (2048, 32, 33), (17, 17, 0)):
+        assert fn(ctypes.byref(job(*args))) == want(*args), args
+    # C5: 4096 x 32 pairs of length 256 keep 2.1 GB of directions
+    assert abs(fn(ctypes.byref(job(256, 256, 131072))) / 1e9 - 2.15) < 0.01
+    assert fn(ctypes.byref(job(0, 5, 3))) == -1
+    assert fn(None) == -1
