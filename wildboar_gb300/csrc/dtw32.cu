@@ -441,6 +441,7 @@ __device__ __forceinline__ void bwd_column(const HL (&Pin)[kGradStrip], HL (&Pou
 struct BwdItem {
     const float *R = nullptr, *C = nullptr;
     float *GR = nullptr, *GC = nullptr;  // gradient rows of the r and c series
+    int capR = 0, capC = 0;              // positions every gradient row has (padded lengths)
     int n = 0, m = 0, r = 1, mx = 0, mn = 0, lo = 0;
     int width = 0;
     int nstrips = 0;                     // strips over rows 1..n-1
@@ -632,6 +633,48 @@ __device__ bool bwd_strips(const BwdItem &B, int s0, int s1, const float2 *src, 
     return true;
 }
 
+// Gradients of four consecutive positions of one gradient row (positions
+// 4 g .. 4 g + 3), added with one 16-byte vector atomic when the walk leaves
+// the group: a path leaves every row and every column exactly once, in
+// decreasing order, so each position is assigned once.  Rows that are not
+// 16-byte aligned, or groups that reach past the positions every row has
+// (cap: the padded series length), take scalar atomics (positions below the
+// item's length only).
+struct GradQuad {
+    float *base;
+    int cap, len;
+    bool vec;
+    int g = -1;
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+    __device__ __forceinline__ GradQuad(float *b, int c, int l)
+        : base(b), cap(c), len(l), vec((reinterpret_cast<uintptr_t>(b) & 15) == 0) {}
+    __device__ __forceinline__ void flush() {
+        if (g < 0) return;
+        const int p0 = 4 * g;
+        if (vec && p0 + 3 < cap) {
+            atomicAdd(reinterpret_cast<float4 *>(base + p0), make_float4(s0, s1, s2, s3));
+        } else {
+            if (p0 < len) atomicAdd(base + p0, s0);
+            if (p0 + 1 < len) atomicAdd(base + p0 + 1, s1);
+            if (p0 + 2 < len) atomicAdd(base + p0 + 2, s2);
+            if (p0 + 3 < len) atomicAdd(base + p0 + 3, s3);
+        }
+        g = -1;
+    }
+    __device__ __forceinline__ void put(int idx, float v) {
+        if ((idx >> 2) != g) {
+            flush();
+            g = idx >> 2;
+            s0 = s1 = s2 = s3 = 0.0f;
+        }
+        const int u = idx & 3;
+        s0 = u == 0 ? v : s0;
+        s1 = u == 1 ? v : s1;
+        s2 = u == 2 ? v : s2;
+        s3 = u == 3 ? v : s3;
+    }
+};
+
 // Walk of one lane through the rows of segment g (strips [g K, (g+1) K), and
 // row 0 when g == 0), from (i, j) upward, adding the gradient of every row and
 // column the path leaves.  Returns with i below the segment (or done).  The
@@ -650,6 +693,7 @@ __device__ __forceinline__ void bwd_walk(const BwdItem &B, int g, int K, const u
     int64_t cur_grp = -1;
     uint4 ga = make_uint4(0, 0, 0, 0), gb = ga;
     float ri = B.R[i], cj = B.C[j];
+    GradQuad qr(B.GR, B.capR, B.n), qc(B.GC, B.capC, B.m);
     while (true) {
         const float vv = __fsub_rn(ri, cj);
         float d = vv;
@@ -657,8 +701,10 @@ __device__ __forceinline__ void bwd_walk(const BwdItem &B, int g, int K, const u
         gr = __fadd_rn(gr, d);
         gc = __fadd_rn(gc, d);
         if (i == 0 && j == 0) {
-            atomicAdd(B.GR, sc * gr);
-            atomicAdd(B.GC, -(sc * gc));
+            qr.put(0, sc * gr);
+            qc.put(0, -(sc * gc));
+            qr.flush();
+            qc.flush();
             done = true;
             return;
         }
@@ -691,16 +737,20 @@ __device__ __forceinline__ void bwd_walk(const BwdItem &B, int g, int K, const u
             move = (word >> (2 * ((i - 1) - s * kGradStrip))) & 3u;
         }
         if (move != 2) {  // leaving row i
-            atomicAdd(B.GR + i, sc * gr);
+            qr.put(i, sc * gr);
             gr = 0.0f;
             i -= 1;
         }
         if (move != 1) {  // leaving column j
-            atomicAdd(B.GC + j, -(sc * gc));
+            qc.put(j, -(sc * gc));
             gc = 0.0f;
             j -= 1;
         }
-        if (i < first_row) return;
+        if (i < first_row) {
+            qr.flush();
+            qc.flush();
+            return;
+        }
         if (move != 2) ri = B.R[i];
         if (move != 1) cj = B.C[j];
     }
@@ -740,6 +790,8 @@ __device__ __forceinline__ void bwd_setup(const Dtw32Job &J, int64_t t, BwdItem 
         B.C = it.X;
         B.GR = gy;
         B.GC = gx;
+        B.capR = J.y_len;
+        B.capC = J.x_len;
         B.n = it.m;
         B.m = it.n;
     } else {
@@ -747,6 +799,8 @@ __device__ __forceinline__ void bwd_setup(const Dtw32Job &J, int64_t t, BwdItem 
         B.C = it.Y;
         B.GR = gx;
         B.GC = gy;
+        B.capR = J.x_len;
+        B.capC = J.y_len;
         B.n = it.n;
         B.m = it.m;
     }
