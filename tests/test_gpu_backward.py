@@ -228,3 +228,39 @@ def test_no_kept_directions_without_grad():
     with torch.no_grad():
         D1 = AG.dtw_matrix(X.clone().requires_grad_(True), Y, 0.3)
     np.testing.assert_array_equal(D0.cpu().numpy(), D1.cpu().numpy())
+
+
+def test_kept_walk_with_foreign_tables_gives_nan_not_reads():
+    # a kept-direction buffer that no forward of this job filled: every strip
+    # table gives column start 0 and word base 2^30, so the first direction-word
+    # index of every walk lies outside the lane's words; the walk stops with
+    # NaN gradients at its first row and column instead of reading there
+    import ctypes
+
+    from wildboar_gb300 import _lib
+    from wildboar_gb300.distance import batched as B
+
+    rng = np.random.default_rng(9)
+    x = torch.as_tensor(np.stack([_walk(rng, 40) for _ in range(6)]), device="cuda")
+    y = torch.as_tensor(np.stack([_walk(rng, 40) for _ in range(3)]), device="cuda")
+    job = B.make_job(x, y, r=0.3, strip=16, block=128)
+    nbytes = _lib.lib().wb_dtw32_keep_bytes(ctypes.byref(job))
+    # one batch (18 items): tables of 3 strips (cs[3], base[3]) at the start
+    strips = (40 - 2) // 16 + 1
+    assert nbytes == ((2 * strips * 4 + 255) // 256 * 256
+                      + 32 * ((strips * 40 + 7) // 8 * 8) * 4)
+    host = np.zeros(nbytes, dtype=np.uint8)
+    tables = host[:2 * strips * 4].view(np.int32)
+    tables[:strips] = 0
+    tables[strips:] = 1 << 30
+    keep = torch.as_tensor(host, device="cuda")
+    dist = torch.ones(job.n_items, dtype=torch.float64, device="cuda")
+    gx = torch.zeros_like(x)
+    gy = torch.zeros_like(y)
+    _lib.check(_lib.lib().wb_dtw32_backward_keep(
+        ctypes.byref(job), dist.data_ptr(), None, gx.data_ptr(), 40, gy.data_ptr(), 40,
+        keep.data_ptr(), nbytes, torch.cuda.current_stream().cuda_stream))
+    gx = gx.cpu().numpy()
+    gy = gy.cpu().numpy()
+    assert np.isnan(gx[:, -1]).all() and np.isnan(gy[:, -1]).all()
+    assert np.all(gx[:, :-1] == 0) and np.all(gy[:, :-1] == 0)

@@ -681,12 +681,14 @@ struct GradQuad {
 // walk keeps in registers the 8-word group (one 32-byte sector) of direction
 // words it reads from, the strip's table entries and the current r_i and c_j,
 // so a step that stays in the group (a move up, or left within 8 columns)
-// issues no dependent load.
+// issues no dependent load.  dir_cap: the words each lane owns; an index
+// outside them ends the walk with NaN gradients.
 template <bool W>
 __device__ __forceinline__ void bwd_walk(const BwdItem &B, int g, int K, const uint32_t *dirs,
-                                         const int *tab_cs, const int *tab_base, int64_t gtid,
-                                         int64_t nth, const float *__restrict__ w, float sc,
-                                         int &i, int &j, float &gr, float &gc, bool &done) {
+                                         int64_t dir_cap, const int *tab_cs,
+                                         const int *tab_base, int64_t gtid, int64_t nth,
+                                         const float *__restrict__ w, float sc, int &i, int &j,
+                                         float &gr, float &gc, bool &done) {
     const int first_row = g == 0 ? 0 : 1 + g * K * kGradStrip;
     if (done || i < first_row) return;
     int cur_s = -1, tcs = 0, tbase = 0;
@@ -722,6 +724,17 @@ __device__ __forceinline__ void bwd_walk(const BwdItem &B, int g, int K, const u
                 cur_s = s;
             }
             const int64_t widx = (int64_t)tbase + (j - tcs);
+            if ((uint64_t)widx >= (uint64_t)dir_cap) {
+                // a word outside this lane's directions (tables that do not
+                // belong to this job): NaN gradients, no read
+                const float qn = __int_as_float(0x7fc00000);
+                qr.put(i, qn);
+                qc.put(j, qn);
+                qr.flush();
+                qc.flush();
+                done = true;
+                return;
+            }
             const int64_t grp = widx >> 3;
             if (grp != cur_grp) {
                 const uint4 *src = reinterpret_cast<const uint4 *>(dirs + dir_index(grp << 3, gtid, nth));
@@ -876,8 +889,8 @@ __global__ void __launch_bounds__(kBwdBlock) dtw32_backward_kernel(const Dtw32Jo
                     const double D = sqrt((double)result.h + (double)result.l);
                     sc = D > 0.0 ? (float)(g / D) : 0.0f;
                 }
-                bwd_walk<W>(B, sg, K, dirs, tab_cs, tab_base, gtid, nth, w, sc, i, j, gr, gcol,
-                            done);
+                bwd_walk<W>(B, sg, K, dirs, J.dir_words, tab_cs, tab_base, gtid, nth, w, sc, i,
+                            j, gr, gcol, done);
             }
             __syncwarp();
         }
@@ -976,7 +989,8 @@ __global__ void __launch_bounds__(kBwdBlock) dtw32_keep_walk_kernel(const Dtw32J
             // gradients, never zeros
             sc = (Dv > 0.0 || Dv != Dv) ? (float)(g / Dv) : 0.0f;
         }
-        bwd_walk<W>(B, 0, 1, words, tab_cs, tab_base, lane, 32, w, sc, i, j, gr, gcol, done);
+        bwd_walk<W>(B, 0, 1, words, D.cap, tab_cs, tab_base, lane, 32, w, sc, i, j, gr, gcol,
+                    done);
     }
 }
 
