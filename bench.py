@@ -1038,7 +1038,8 @@ def run_gpu(args):
                   "bit_exact": bool(np.array_equal(got, ref_rows)),
                   "against": "oracle rows of the cpu_baseline sample"}
     forms = {}
-    if not args.no_forms:
+    # the forms are single-GPU measurements: they run in the one-rank job only
+    if not args.no_forms and world == 1:
         forms["batched_fp32"] = bench_batched(args, dev, flush)
         forms["fwd_bwd_fp32"] = bench_fwd_bwd(args, dev, flush)
         forms["subsequence"] = bench_subsequence(args, dev, flush)
