@@ -86,3 +86,22 @@ def test_shim_partition_matches_python_binding(shim):
     wb, wd = nearest_pivot(x, groups, [("euclidean", {}), ("dtw", {"r": 0.2})])
     np.testing.assert_array_equal(branch, wb)
     np.testing.assert_array_equal(dist, wd)
+
+
+def test_pxd_declares_every_entry_of_the_header():
+    # every prototype of include/wbgpu.h appears in include/wbgpu.pxd with the
+    # same return type, name and parameter list (whitespace aside, "(void)"
+    # written "()" as Cython does), so compiled callers can use the whole ABI
+    import re
+
+    def norm(text):
+        return " ".join(text.split()).replace("( ", "(").replace(" )", ")")
+
+    h = open(os.path.join(ROOT, "include", "wbgpu.h")).read()
+    h = re.sub(r"/\*.*?\*/", "", h, flags=re.S)
+    protos = re.findall(r"^((?:int|int64_t|int32_t|const char \*|void)\s*\**\s*wb_\w+\s*"
+                        r"\([^;]*\));", h, flags=re.M)
+    assert len(protos) >= 38
+    pxd = norm(open(os.path.join(ROOT, "include", "wbgpu.pxd")).read())
+    missing = [p for p in protos if norm(p).replace("(void)", "()") not in pxd]
+    assert not missing, missing
