@@ -11,7 +11,9 @@
 // own bottom row written to, a ring in global memory laid out
 // [column][thread].  The loop bounds of every strip are the union of the 32
 // lanes' column ranges, so lanes never diverge on ragged shapes; cells outside
-// a lane's own band take the masked path with an infinite cost.
+// a lane's own band take the masked path with an infinite cost.  The cells of
+// a column are written to the other of two register sets, which alternate
+// between columns, so no cell value is copied to free its register.
 //
 // Arithmetic: the cost (x_i - y_j)^2 (times the wdtw weight) is FP32 (two
 // columns' differences and squares as packed f32x2 operations, each half
@@ -27,6 +29,9 @@
 // traceback directions and an in-kernel walk of the optimal path that adds
 // dD/dx_i = sum_{j:(i,j) on path} w_{|i-j|} (x_i - y_j) / D and the negative
 // column sums dD/dy_j to per-series gradient rows (D = sqrt of the path cost).
+// Kept directions (end of the file): the same sweep run once by the forward
+// of a differentiable call, its directions kept per batch of 32 items, and a
+// walk-only backward over them.
 
 #include "dtw32.cuh"
 
