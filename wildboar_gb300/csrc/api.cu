@@ -408,6 +408,7 @@ using namespace wb;
 extern "C" int wb_pairwise_distance(const wb_series *x, const wb_series *y, int64_t dim,
                                     int32_t metric, const wb_params *params, double *out,
                                     int32_t out_on_device, void *stream_) {
+    WB_TRACE();
     WB_TRY(check_series(x, "x"));
     if (y) WB_TRY(check_series(y, "y"));
     if (!params) return fail(WB_EINVAL, "params is NULL");
@@ -464,6 +465,7 @@ extern "C" int wb_pairwise_distance(const wb_series *x, const wb_series *y, int6
 extern "C" int wb_pairwise_distance_fp32(const wb_series *x, const wb_series *y, int64_t dim,
                                          int32_t metric, const wb_params *params, double *out,
                                          int32_t out_on_device, void *stream_) {
+    WB_TRACE();
     WB_TRY(check_series(x, "x"));
     if (y) WB_TRY(check_series(y, "y"));
     if (!params) return fail(WB_EINVAL, "params is NULL");
@@ -583,6 +585,7 @@ extern "C" int wb_pairwise_distance_fp32(const wb_series *x, const wb_series *y,
 extern "C" int wb_paired_distance(const wb_series *x, const wb_series *y, int64_t dim,
                                   int32_t metric, const wb_params *params, double *out,
                                   int32_t out_on_device, void *stream_) {
+    WB_TRACE();
     WB_TRY(check_series(x, "x"));
     WB_TRY(check_series(y, "y"));
     if (!params) return fail(WB_EINVAL, "params is NULL");
@@ -632,6 +635,7 @@ extern "C" int wb_argmin_distance(const wb_series *x, const wb_series *y, int64_
                                   int32_t metric, const wb_params *params, int64_t k,
                                   const double *lower_bound, int64_t *indices,
                                   double *distances, int32_t out_on_device, void *stream_) {
+    WB_TRACE();
     WB_TRY(check_series(x, "x"));
     WB_TRY(check_series(y, "y"));
     if (!params) return fail(WB_EINVAL, "params is NULL");
@@ -1224,6 +1228,7 @@ extern "C" int wb_pairwise_subsequence_distance(
     const double *means, const double *stds, int64_t m, const wb_series *x, int64_t dim,
     int32_t metric, const wb_params *params, double *out_dist, int64_t *out_idx,
     int32_t out_on_device, void *stream_) {
+    WB_TRACE();
     return subseq_entry(shapelets, offsets, lengths, means, stds, m, x, dim, metric, params,
                         out_dist, out_idx, out_on_device, stream_, false);
 }
@@ -1235,6 +1240,7 @@ extern "C" int wb_subsequence_profile(const double *shapelets, const int64_t *of
                                       double *out_raw, double *out_key, int64_t ld,
                                       int32_t std_as_given, int32_t out_on_device,
                                       void *stream_) {
+    WB_TRACE();
     if (!out_raw) return fail(WB_EINVAL, "out_raw is NULL");
     if (!out_key && metric != WB_EUCLIDEAN && metric != WB_SCALED_EUCLIDEAN)
         return fail(WB_EINVAL, "out_key is NULL");
@@ -1249,6 +1255,7 @@ extern "C" int wb_subsequence_profile_stop(const double *shapelets, const int64_
                                            int64_t dim, const double *stop_sq,
                                            double *out_raw, int64_t ld, int32_t out_on_device,
                                            void *stream_) {
+    WB_TRACE();
     if (!out_raw) return fail(WB_EINVAL, "out_raw is NULL");
     if (!stop_sq) return fail(WB_EINVAL, "stop_sq is NULL");
     wb_params p{};
@@ -1262,6 +1269,7 @@ extern "C" int wb_paired_subsequence_distance(
     const double *means, const double *stds, int64_t m, const wb_series *x, int64_t dim,
     int32_t metric, const wb_params *params, double *out_dist, int64_t *out_idx,
     int32_t out_on_device, void *stream_) {
+    WB_TRACE();
     return subseq_entry(shapelets, offsets, lengths, means, stds, m, x, dim, metric, params,
                         out_dist, out_idx, out_on_device, stream_, true);
 }
@@ -1273,6 +1281,7 @@ extern "C" int wb_dilated_profile(const wb_series *y, const wb_series *x, int64_
                                   int32_t metric, const wb_params *params, int64_t dilation,
                                   int64_t padding, int32_t scale, double *out,
                                   int32_t out_on_device, void *stream_) {
+    WB_TRACE();
     WB_TRY(check_series(y, "y"));
     WB_TRY(check_series(x, "x"));
     if (!params) return fail(WB_EINVAL, "params is NULL");
@@ -1370,6 +1379,7 @@ extern "C" int wb_dilated_profile(const wb_series *y, const wb_series *x, int64_
 
 extern "C" int wb_mass_profile(const wb_series *y, const wb_series *x, double *out,
                                int32_t out_on_device, void *stream_) {
+    WB_TRACE();
     WB_TRY(check_series(y, "y"));
     WB_TRY(check_series(x, "x"));
     if (y->n != x->n) return fail(WB_EINVAL, "y and x must have the same number of samples.");
@@ -1395,6 +1405,7 @@ extern "C" int wb_mass_profile(const wb_series *y, const wb_series *x, double *o
 }
 
 extern "C" int wb_inject_fault(int32_t site, int64_t skip) {
+    WB_TRACE();
     if (site < INJ_NONE || site > INJ_WAIT) return fail(WB_EINVAL, "unknown fault site");
     if (skip < 0) return fail(WB_EINVAL, "skip must be >= 0");
     std::lock_guard<std::mutex> g(g_inject_mu);
@@ -1411,6 +1422,7 @@ extern "C" int32_t wb_version(void) { return 1; }
 extern "C" int64_t wb_launch_count(void) { return g_launches.load(); }
 
 extern "C" int wb_release_workspace(void *stream_) {
+    WB_TRACE();
     std::lock_guard<std::mutex> g(g_arena_mu);
     for (auto it = g_arenas.begin(); it != g_arenas.end();) {
         if (stream_ == nullptr || it->first.second == (cudaStream_t)stream_) {

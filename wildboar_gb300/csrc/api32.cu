@@ -171,6 +171,7 @@ using namespace wb;
 
 extern "C" int wb_dtw32_distance(const wb_dtw32 *q, double *out, double *out_cost,
                                  void *stream_) {
+    WB_TRACE();
     if (!out) return fail(WB_EINVAL, "out is NULL");
     cudaStream_t s = (cudaStream_t)stream_;
     Workspace ws(s);
@@ -184,6 +185,7 @@ extern "C" int wb_dtw32_distance(const wb_dtw32 *q, double *out, double *out_cos
 extern "C" int wb_dtw32_backward(const wb_dtw32 *q, const double *grad_out, float *grad_x,
                                  int64_t gx_stride, float *grad_y, int64_t gy_stride,
                                  void *stream_) {
+    WB_TRACE();
     if (!q) return fail(WB_EINVAL, "job is NULL");
     if (!grad_x || !grad_y) return fail(WB_EINVAL, "gradient outputs are NULL");
     if (gx_stride < q->x_len || gy_stride < q->y_len)
@@ -201,6 +203,7 @@ extern "C" int wb_dtw32_backward(const wb_dtw32 *q, const double *grad_out, floa
 }
 
 extern "C" int64_t wb_dtw32_keep_bytes(const wb_dtw32 *q) {
+    WB_TRACE();
     DirKeep D;
     int64_t total = 0;
     if (keep_geometry(q, D, total) != WB_OK) return -1;
@@ -209,6 +212,7 @@ extern "C" int64_t wb_dtw32_keep_bytes(const wb_dtw32 *q) {
 
 extern "C" int wb_dtw32_distance_keep(const wb_dtw32 *q, double *out, double *out_cost,
                                       void *keep, int64_t keep_bytes, void *stream_) {
+    WB_TRACE();
     if (!out) return fail(WB_EINVAL, "out is NULL");
     cudaStream_t s = (cudaStream_t)stream_;
     Workspace ws(s);
@@ -224,6 +228,7 @@ extern "C" int wb_dtw32_backward_keep(const wb_dtw32 *q, const double *dist,
                                       const double *grad_out, float *grad_x, int64_t gx_stride,
                                       float *grad_y, int64_t gy_stride, const void *keep,
                                       int64_t keep_bytes, void *stream_) {
+    WB_TRACE();
     if (!q) return fail(WB_EINVAL, "job is NULL");
     if (!dist) return fail(WB_EINVAL, "dist is NULL");
     if (!grad_x || !grad_y) return fail(WB_EINVAL, "gradient outputs are NULL");
@@ -244,6 +249,7 @@ extern "C" int wb_dtw32_backward_keep(const wb_dtw32 *q, const double *dist,
 
 extern "C" int wb_series_lengths_f32(const float *x, int64_t n_series, int64_t stride,
                                      int32_t L, int32_t *lengths, void *stream_) {
+    WB_TRACE();
     if (n_series < 0 || L < 0) return fail(WB_EINVAL, "negative size");
     if (n_series > 0 && (!x || !lengths)) return fail(WB_EINVAL, "NULL pointer");
     return launch_series_lengths(x, n_series, stride, L, lengths, (cudaStream_t)stream_);

@@ -559,6 +559,7 @@ extern "C" int wb_argmin_subsequence_distance(const double *s, const int64_t *s_
                                               const wb_params *params, int32_t scaled,
                                               int64_t k, int64_t *indices, double *distances,
                                               int32_t out_on_device, void *stream) {
+    WB_TRACE();
     return wb_argmin_subsequence_impl(s, s_len, s_stride, n, s_mean, s_std, x, dim, metric,
                                       params, scaled, k, indices, distances, out_on_device,
                                       (cudaStream_t)stream);

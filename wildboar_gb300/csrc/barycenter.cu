@@ -546,6 +546,7 @@ __global__ void fill_kernel(double *p, int64_t n, double v) {
 extern "C" int wb_dtw_alignment(const double *x, int64_t n, const double *y, int64_t m, double r,
                                 const double *weights, double *out, int32_t on_device,
                                 void *stream) {
+    WB_TRACE();
     const cudaStream_t st = (cudaStream_t)stream;
     if (n < 1 || m < 1 || n > INT32_MAX / 2 || m > INT32_MAX / 2)
         return fail(WB_EINVAL, "dtw_alignment: invalid sizes");
@@ -626,6 +627,7 @@ extern "C" int wb_dtw_average_mm_step(const double *x, int64_t x_stride, int64_t
                                       int64_t n_groups, int64_t n_pairs, double r,
                                       const double *weights, const double *sample_weight,
                                       double *new_means, double *last, void *stream) {
+    WB_TRACE();
     const cudaStream_t st = (cudaStream_t)stream;
     if (n_pairs < 0 || n_groups < 0 || n_timestep < 1 || mean_len < 1)
         return fail(WB_EINVAL, "dtw_average: invalid sizes");
@@ -695,6 +697,7 @@ extern "C" int wb_dtw_average_ssg_epoch(const double *x, int64_t x_stride, int64
                                         const double *lr, int64_t n_steps, double r,
                                         const double *weights, const double *sample_weight,
                                         void *stream) {
+    WB_TRACE();
     const cudaStream_t st = (cudaStream_t)stream;
     if (n_steps < 0 || n_timestep < 1 || mean_len < 1)
         return fail(WB_EINVAL, "dtw_average: invalid sizes");
@@ -756,6 +759,7 @@ extern "C" int wb_group_mean(const double *x, int64_t x_stride, int64_t n_timest
                              const int64_t *member, const int64_t *group_start,
                              const int32_t *groups, int64_t n_groups, double *out,
                              void *stream) {
+    WB_TRACE();
     const cudaStream_t st = (cudaStream_t)stream;
     if (n_groups < 0 || n_timestep < 1 || n_timestep > INT32_MAX / 2)
         return fail(WB_EINVAL, "group_mean: invalid sizes");

@@ -106,6 +106,7 @@ extern "C" int wb_nearest_pivot(const wb_series *x, int64_t dim, int64_t n_group
                                 const int32_t *group_slot, const int32_t *slot_metric,
                                 const wb_params *slot_params, int32_t n_slots,
                                 int64_t *out_branch, double *out_dist, void *stream) {
+    WB_TRACE();
     const cudaStream_t s = (cudaStream_t)stream;
     if (!x || !x->data) return fail(WB_EINVAL, "x is NULL");
     if (x->dtype != WB_F64) return fail(WB_EINVAL, "x must be float64");
@@ -206,6 +207,7 @@ extern "C" int wb_subsequence_distance_views(const wb_series *x, const int64_t *
                                              int32_t metric, const wb_params *params,
                                              double *out_dist, int64_t *out_idx,
                                              void *stream) {
+    WB_TRACE();
     const cudaStream_t s = (cudaStream_t)stream;
     if (!x || !x->data || !target) return fail(WB_EINVAL, "x or target is NULL");
     if (x->dtype != WB_F64) return fail(WB_EINVAL, "x must be float64");

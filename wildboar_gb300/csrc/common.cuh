@@ -8,9 +8,22 @@
 #include <mutex>
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/wbgpu.h"
 
 namespace wb {
+
+// An NVTX range named after the C-ABI entry for the duration of the call, so
+// profiler timelines (nsys, ncu --nvtx) show which entry launched which
+// kernels; without an attached tool it costs one pointer test.
+struct TraceRange {
+    explicit TraceRange(const char *name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange &) = delete;
+    TraceRange &operator=(const TraceRange &) = delete;
+};
+#define WB_TRACE() ::wb::TraceRange wb_trace_range_(__func__)
 
 // ---------------------------------------------------------------------------
 // errors

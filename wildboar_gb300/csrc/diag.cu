@@ -51,12 +51,14 @@ __global__ void alu_probe_kernel(T *out, int iters, T a, T b) {
 using namespace wb;
 
 extern "C" int wb_profile_enable(int32_t on) {
+    WB_TRACE();
     g_timer.enabled = on != 0;
     g_timer.pending = false;
     return WB_OK;
 }
 
 extern "C" int wb_profile_last(double *ms) {
+    WB_TRACE();
     if (!ms) return fail(WB_EINVAL, "ms is NULL");
     *ms = -1.0;
     if (!g_timer.pending) return WB_OK;
@@ -69,6 +71,7 @@ extern "C" int wb_profile_last(double *ms) {
 }
 
 extern "C" int wb_alu_probe(int32_t dtype, int32_t iters, double *ops_per_s) {
+    WB_TRACE();
     if (!ops_per_s) return fail(WB_EINVAL, "ops_per_s is NULL");
     const DeviceInfo &dev = device_info();
     int grid = dev.sm_count * 8, block = 256;

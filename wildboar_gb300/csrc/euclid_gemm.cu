@@ -620,6 +620,7 @@ using namespace wb;
 
 extern "C" int wb_euclidean_tc(const wb_series *x, const wb_series *y, int64_t dim, double *out,
                                int32_t out_on_device, void *stream_) {
+    WB_TRACE();
     if (!x || !y) return fail(WB_EINVAL, "x and y are required");
     if (x->dtype != WB_F64 || y->dtype != WB_F64) return fail(WB_EINVAL, "float64 series expected");
     if (!x->on_device || !y->on_device)

@@ -167,6 +167,7 @@ using namespace wb;
 
 extern "C" int wb_dtw_envelope(const double *x, int64_t n, int64_t n_timestep, int64_t warp,
                                double *lower, double *upper, int32_t on_device, void *stream) {
+    WB_TRACE();
     const cudaStream_t s = (cudaStream_t)stream;
     if (n < 0 || n_timestep < 1 || n_timestep > INT32_MAX / 4)
         return fail(WB_EINVAL, "invalid sizes");
@@ -205,6 +206,7 @@ extern "C" int wb_dtw_envelope(const double *x, int64_t n, int64_t n_timestep, i
 extern "C" int wb_lb_keogh(const double *q, int64_t nq, const double *x, int64_t nx,
                            int64_t n_timestep, int64_t warp, int32_t kind, double *out,
                            int32_t on_device, void *stream) {
+    WB_TRACE();
     const cudaStream_t s = (cudaStream_t)stream;
     if (nq < 0 || nx < 0 || n_timestep < 1 || n_timestep > INT32_MAX / 4)
         return fail(WB_EINVAL, "invalid sizes");
@@ -266,6 +268,7 @@ extern "C" int wb_lb_keogh(const double *q, int64_t nq, const double *x, int64_t
 
 extern "C" int wb_lb_kim(const double *y, int64_t ny, const double *x, int64_t nx,
                          int64_t n_timestep, double *out, int32_t on_device, void *stream) {
+    WB_TRACE();
     const cudaStream_t s = (cudaStream_t)stream;
     if (ny < 0 || nx < 0 || n_timestep < 1 || n_timestep > INT32_MAX / 4)
         return fail(WB_EINVAL, "invalid sizes");
@@ -295,6 +298,7 @@ extern "C" int wb_lb_kim(const double *y, int64_t ny, const double *x, int64_t n
 extern "C" int wb_lb_keogh_terms(const double *x, const double *lower, const double *upper,
                                  int64_t n_timestep, double *cb, double *dist,
                                  int32_t on_device, void *stream) {
+    WB_TRACE();
     const cudaStream_t s = (cudaStream_t)stream;
     if (n_timestep < 1 || n_timestep > INT32_MAX / 4) return fail(WB_EINVAL, "invalid sizes");
     if (!x || !lower || !upper || !cb || !dist) return fail(WB_EINVAL, "NULL array");

@@ -85,6 +85,7 @@ extern "C" int wb_pairwise_distance_noalloc(const wb_series *x, const wb_series 
                                             int64_t dim, int32_t metric,
                                             const wb_params *params, double *out,
                                             void *stream_) {
+    WB_TRACE();
     WB_TRY(check_device_series(x, "x"));
     if (y) WB_TRY(check_device_series(y, "y"));
     if (!params) return fail(WB_EINVAL, "params is NULL");
