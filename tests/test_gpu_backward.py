@@ -264,3 +264,31 @@ def test_kept_walk_with_foreign_tables_gives_nan_not_reads():
     gy = gy.cpu().numpy()
     assert np.isnan(gx[:, -1]).all() and np.isnan(gy[:, -1]).all()
     assert np.all(gx[:, :-1] == 0) and np.all(gy[:, :-1] == 0)
+
+
+@pytest.mark.parametrize("lx,ly", [(1, 1), (1, 5), (5, 1), (2, 3), (3, 17), (17, 2)])
+def test_kept_directions_short_series(monkeypatch, lx, ly):
+    # no strip (one row), one partial strip, a single column: the kept path and
+    # the recompute path agree, distances match the oracle
+    rng = np.random.default_rng(lx * 31 + ly)
+    X = np.stack([_walk(rng, lx) for _ in range(5)])
+    Y = np.stack([_walk(rng, ly) for _ in range(4)])
+    gw = torch.as_tensor(rng.standard_normal((5, 4)), device="cuda")
+
+    def run():
+        xt = torch.as_tensor(X, device="cuda").requires_grad_(True)
+        yt = torch.as_tensor(Y, device="cuda").requires_grad_(True)
+        D = AG.dtw_matrix(xt, yt, 0.5)
+        (D * gw).sum().backward()
+        return (D.detach().cpu().numpy(), xt.grad.cpu().numpy(), yt.grad.cpu().numpy())
+
+    d_keep, gx_keep, gy_keep = run()
+    monkeypatch.setenv("WB_GPU_BWD_WORKSPACE_MB", "0.0001")
+    d_rec, gx_rec, gy_rec = run()
+    want = O.pairwise(X.astype(np.float64), Y.astype(np.float64), metric="dtw",
+                      metric_params={"r": 0.5})
+    np.testing.assert_allclose(d_keep, want, rtol=1e-5)
+    np.testing.assert_allclose(d_rec, want, rtol=1e-5)
+    np.testing.assert_allclose(gx_keep, gx_rec, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(gy_keep, gy_rec, rtol=1e-5, atol=1e-6)
+    assert np.all(np.isfinite(gx_keep)) and np.all(np.isfinite(gy_keep))
