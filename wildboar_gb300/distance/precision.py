@@ -58,7 +58,10 @@ def _as3(t):
         t = t.reshape(1, 1, -1)
     elif t.dim() == 2:
         t = t.reshape(t.shape[0], 1, t.shape[1])
-    return t.to(torch.float64).contiguous()
+    # conversions only when needed (each costs a dispatch even as a no-op)
+    if t.dtype != torch.float64:
+        t = t.to(torch.float64)
+    return t if t.is_contiguous() else t.contiguous()
 
 
 def pairwise_euclidean_tc(x, y, *, dim=0):
